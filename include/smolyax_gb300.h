@@ -1,0 +1,189 @@
+/*
+ * smolyax_gb300 -- C ABI of the GB300 (sm_103a) evaluation path of the
+ * barycentric Smolyak interpolant.
+ *
+ * Conventions
+ *  - Every pointer argument is a DEVICE pointer owned by the caller unless the
+ *    comment says "host".  The library allocates no device memory: scratch
+ *    space is passed in by the caller (`ws`, `ws_bytes`).
+ *  - `stream` is a cudaStream_t passed as void*; all work is stream-ordered and
+ *    asynchronous unless the comment says the call synchronises.
+ *  - Every entry point returns SMX_OK (0) or one of the negative SMX_ERR_*
+ *    codes below; smx_last_error_string() describes the most recent failure of
+ *    the calling thread.
+ *  - Reference citations are paths inside JoWestermann/smolyax.
+ */
+#ifndef SMOLYAX_GB300_H
+#define SMOLYAX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  SMX_OK = 0,
+  SMX_ERR_ARG = -1,        /* invalid argument (null pointer, bad size)            */
+  SMX_ERR_WORKSPACE = -2,  /* workspace too small                                   */
+  SMX_ERR_CUDA = -3,       /* a CUDA runtime call or launch failed                  */
+  SMX_ERR_DEPTH = -4,      /* enumeration deeper than SMX_MAX_DEPTH                 */
+  SMX_ERR_UNSUPPORTED = -5 /* configuration outside what the kernels support       */
+};
+
+#define SMX_MAX_DEPTH 64 /* max number of included dimensions in one DFS path */
+
+/* ---- anisotropic multi-index set Lambda_{k,t} -----------------------------------
+ * The set is built level by level, level n holding the multi-indices with n
+ * non-zero entries.  An entry of a level is (rem, start, parent, dim, deg): the
+ * remaining budget after its last inclusion, the first dimension of its
+ * continuation chain, its parent in level n-1, and its last non-zero entry
+ * (dim, deg).  `mode` selects the arithmetic and chain rule of the reference
+ * function being replaced:
+ *   SMX_MODE_NONZERO  -- subtractive budget, chain continues while k[i+1] < rem
+ *                        (indices.py:214-259 non_zero_indices_and_zetas and
+ *                        indices.py:175-211 __nodeset_cardinality_non_nested);
+ *   SMX_MODE_INDEXSET -- subtractive budget, chain continues while k[i] < rem
+ *                        (indices.py:20-69 indexset);
+ *   SMX_MODE_ADDITIVE -- `rem` holds the USED budget, inclusion test
+ *                        used + j*k[i] < t (indices.py:72-118 indexset_cardinality).
+ */
+#define SMX_MODE_NONZERO 0
+#define SMX_MODE_INDEXSET 1
+#define SMX_MODE_ADDITIVE 2
+
+/* Per entry: number of children (written to `count`) and the chain end
+ * (`term`).  Replaces the inner expansion loops of indices.py:49-67,
+ * indices.py:98-116 and indices.py:242-258. */
+int smx_lambda_count(const double* k, int d, double t, int mode, const double* rem, const int32_t* start,
+                     int64_t n, int64_t* count, int32_t* term, void* stream);
+
+/* Writes the children of every entry at offsets `offs` (exclusive scan of
+ * `count`); c_parent receives parent_base + the parent's index (global id).
+ * Same reference lines as smx_lambda_count. */
+int smx_lambda_expand(const double* k, int d, double t, int mode, const double* rem, const int32_t* start,
+                      int64_t n, const int64_t* offs, int64_t parent_base, double* c_rem, int32_t* c_start,
+                      int32_t* c_parent, int32_t* c_dim, int32_t* c_deg, void* stream);
+
+/* zeta[i] = smolyak_coefficient(k, d, rem[i], parity[i] or 0): signed count of
+ * e in {0,1}^d with nu+e in Lambda (indices.py:121-168).  `parity` may be NULL.
+ * On an enumeration deeper than SMX_MAX_DEPTH the entry's zeta is set to 0 and
+ * *flag (device int, may be NULL) is set to 1. */
+int smx_zeta(const double* k, int d, const double* rem, const int32_t* parity, int64_t n, int64_t* zeta,
+             int32_t* flag, void* stream);
+
+/* Inclusive/exclusive scan of int64 values; out[n] receives the total when
+ * `out` has n+1 slots (exclusive form).  ws >= smx_scan_workspace(n) bytes. */
+size_t smx_scan_workspace(int64_t n);
+int smx_scan_i64(const int64_t* in, int64_t* out, int64_t n, void* ws, size_t ws_bytes, void* stream);
+
+/* DFS-order ranks of all entries of a level set, i.e. the order of the
+ * reference's stack-based enumeration (indices.py:46-67, indices.py:241-258).
+ * Entries of all levels are concatenated (global ids); `first_child` and
+ * `n_child` give each entry's children range (children are written by
+ * smx_lambda_expand in dimension-ascending, degree-ascending order).
+ * smx_lambda_subtree_sizes is called level by level from the deepest level up;
+ * smx_lambda_ranks level by level from the root down, with base[root] = 0: it
+ * writes rank[e] and the first rank base[c] of every child subtree.  In
+ * SMX_MODE_NONZERO an entry precedes the children at its chain-end dimension
+ * `term`; in SMX_MODE_INDEXSET it follows all its children. */
+int smx_lambda_subtree_sizes(const int64_t* first_child, const int64_t* n_child, int64_t lvl_begin, int64_t lvl_end,
+                             int64_t* size, void* stream);
+int smx_lambda_ranks(int mode, const int32_t* term, const int32_t* dim, const int64_t* first_child,
+                     const int64_t* n_child, const int64_t* size, int64_t lvl_begin, int64_t lvl_end, int64_t* base,
+                     int64_t* rank, void* stream);
+
+/* ---- interpolation plan ------------------------------------------------------------
+ * Summands are the multi-indices with zeta != 0 and n >= 1; each summand's
+ * tensor of nodal values is stored unpadded, its active (dim, deg) pairs in
+ * ascending dim order, the last pair varying fastest; rows hold d_out values
+ * with zeta folded in.  Pairs are unique (dim, deg) combinations, deg >= 1;
+ * each owns deg+1 consecutive "value slots" (node, weight, basis value).
+ */
+typedef struct smx_plan {
+  int32_t d_in, d_out;
+  int32_t n_pairs;     /* unique (dim, deg) pairs                                  */
+  int32_t n_values;    /* V = sum over pairs of (deg + 1)                          */
+  int32_t n_summands;  /* summands with n >= 1                                     */
+  int32_t max_n;       /* max active dimensions of a summand                       */
+  int64_t n_entries;   /* R = sum over summands of prod(deg + 1)                   */
+  const int32_t* pair_dim;     /* [n_pairs]                                        */
+  const int32_t* pair_deg;     /* [n_pairs]                                        */
+  const int32_t* pair_voff;    /* [n_pairs] first value slot of the pair           */
+  const double* node;          /* [n_values] nodes of every pair                   */
+  const double* bweight;       /* [n_values] barycentric weights                   */
+  const int32_t* sum_poff;     /* [n_summands+1] offsets into sum_pairs            */
+  const int32_t* sum_pairs;    /* pair ids of each summand, ascending dim          */
+  const int64_t* sum_eoff;     /* [n_summands+1] first entry (row) of each summand */
+  const double* F64;           /* [n_entries * d_out] zeta * f(node)               */
+  const float* F32;            /* [n_entries * d_out] FP32 rounding of F64 (or NULL)*/
+  const double* offset;        /* [d_out] zeta_0 * f(zero point)                   */
+} smx_plan;
+
+/* Barycentric weights of every pair: w_b = prod_a 1/(xi_a - xi_b) with zero
+ * differences replaced by 1 (barycentric.py:13-31). */
+int smx_bary_weights(int n_pairs, const int32_t* pair_deg, const int32_t* pair_voff, const double* node,
+                     double* bweight, void* stream);
+
+/* Summand pairs and entry counts from the zeta != 0 entries: walks the parent
+ * chain of entry `ent[s]` (global ids), writes its pair ids in ascending dim
+ * order at sum_poff[s] and prod(deg+1) into n_ent[s] (replaces the block
+ * assembly of interpolation.py:168-199 with an unpadded layout). */
+int smx_plan_summands(int64_t n_sum, const int64_t* ent, const int32_t* parent, const int32_t* dim,
+                      const int32_t* deg, const int32_t* pair_base, const int32_t* sum_poff, int32_t* sum_pairs,
+                      int64_t* n_ent, void* stream);
+
+/* Per-dimension maximal degree over a set of entries (atomicMax). */
+int smx_max_degree(int64_t n, const int32_t* dim, const int32_t* deg, int32_t* maxdeg, void* stream);
+
+/* F64/F32 rows from unique function values: F64[r] = zeta(r) * fu[umap[r]]
+ * (interpolation.py:201-235, with the reference's cached f evaluations
+ * gathered on the device). */
+int smx_assemble_F(const smx_plan* plan_host, const int64_t* sum_zeta, const double* fu, const int64_t* umap,
+                   double* F64, float* F32, void* stream);
+
+/* ---- evaluation -------------------------------------------------------------------
+ * Basis table: Lt[v*P + p] = normalised barycentric basis value of slot v at
+ * point p, with the one-hot rule at exact nodes (barycentric.py:34-66 and the
+ * normalisation at barycentric.py:117).  dLt (nullable) receives the
+ * derivative of the normalised basis, NaN at exact nodes (barycentric.py:126-155,
+ * :213-219).  x is row-major [P, ldx] FP64. */
+int smx_basis_f64(const smx_plan* plan_host, const double* x, int64_t P, int64_t ldx, double* Lt, double* dLt,
+                  void* stream);
+
+/* y[p*d_out + o] = offset[o] + sum over summands of the tensor-product
+ * contraction of the summand's rows with the basis values of point p
+ * (barycentric.py:69-123, interpolation.py:264-304). */
+int smx_contract_f64(const smx_plan* plan_host, const double* Lt, int64_t P, double* y, void* stream);
+
+/* One call of the FP64 path: basis table into `ws`, then the contraction.
+ * ws_bytes must be at least smx_eval_workspace(plan, P, 64); y is FP64
+ * [P, d_out] (interpolation.py:264-304). */
+size_t smx_eval_workspace(const smx_plan* plan_host, int64_t P, int precision);
+int smx_eval(const smx_plan* plan_host, int precision, const double* x, int64_t P, int64_t ldx, void* y, void* ws,
+             size_t ws_bytes, void* stream);
+
+/* Full Jacobian J[(p*d_out + o)*d_in + j] (dense, zero outside active
+ * dimensions), FP64 (barycentric.py:158-229, interpolation.py:306-345). */
+size_t smx_jacobian_workspace(const smx_plan* plan_host, int64_t P);
+int smx_jacobian(const smx_plan* plan_host, const double* x, int64_t P, int64_t ldx, double* J, void* ws,
+                 size_t ws_bytes, void* stream);
+
+/* Integral: Q[o] = offset[o] + sum_r qw(r) F64[r, o] with qw the product of
+ * the pairs' quadrature weights `qnode` ([n_values], host-computed rule
+ * weights) (interpolation.py:347-390). */
+size_t smx_integral_workspace(const smx_plan* plan_host);
+int smx_integral(const smx_plan* plan_host, const double* qnode, double* Q, void* ws, size_t ws_bytes, void* stream);
+
+/* Human-readable description of the last error on this thread (host string). */
+const char* smx_last_error_string(void);
+
+/* Library version string (host). */
+const char* smx_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SMOLYAX_GB300_H */

@@ -1,0 +1,320 @@
+r"""Barycentric Smolyak interpolant on the GPU (mirrors ``src/smolyax/interpolation.py``).
+
+$I^{\Lambda_{k,t}}[f] = \sum_{\nu\in\Lambda} \zeta_{\Lambda,\nu} I^\nu[f]$.  Set-up
+(``set_f``) builds the index set, the Smolyak coefficients and the summand
+layout on the device, calls the user function at every interpolation node on
+the host (the reference's f-evaluation cache format is kept), and gathers the
+nodal values into an unpadded device array.  Evaluation, gradient and
+integral run as hand-written sm_103a kernels through the C ABI.
+"""
+from __future__ import annotations
+
+import math
+from typing import Callable, Sequence, Union
+
+import numpy as np
+import torch
+
+from . import _capi as capi
+from . import indices
+from . import nodes as _nodes
+from ._capi import call, ptr
+
+ArrayLike = Union[np.ndarray, torch.Tensor]
+
+
+def _stream():
+    return capi.stream_ptr(torch.cuda.current_stream())
+
+
+class Plan:
+    """Device arrays of one interpolant plus the C struct that points at them."""
+
+    def __init__(self):
+        self.keep = {}
+        self.c = capi.SmxPlan()
+
+    def set(self, name, tensor):
+        self.keep[name] = tensor
+        if hasattr(self.c, name):
+            setattr(self.c, name, None if tensor is None else tensor.data_ptr())
+
+    def ref(self):
+        import ctypes
+
+        return ctypes.byref(self.c)
+
+
+class SmolyakBarycentricInterpolator:
+    r"""Smolyak operator for $f:\mathbb R^{d_{in}}\to\mathbb R^{d_{out}}$ (``interpolation.py:15-113``).
+
+    Same keyword-only constructor as the reference.  Results are torch tensors
+    on the CUDA device; inputs may be numpy arrays or torch tensors.
+    """
+
+    @property
+    def d_in(self) -> int:
+        return self._d_in
+
+    @property
+    def d_out(self) -> int:
+        return self._d_out
+
+    @property
+    def n_f_evals(self) -> int:
+        return self._n_f_evals
+
+    @property
+    def n_f_evals_new(self) -> int:
+        return self._n_f_evals_new
+
+    def __init__(self, *, d_out: int, node_gen: _nodes.Generator, k: Sequence[float], t: float,
+                 f: Callable = None, n_inputs: int = None, memory_limit: float = 4.0) -> None:
+        self._d_in = len(k)
+        self._d_out = int(d_out)
+        self._node_gen = node_gen
+        self._is_nested = node_gen.is_nested
+        self._k = np.asarray(k, dtype=np.float64)
+        self._t = float(t)
+        self._memory_limit = float(memory_limit)
+        self._n_inputs = n_inputs
+        self._plan = None
+        self._n_f_evals = indices.nodeset_cardinality(self._k, self._t, nested=self._is_nested)
+        self._n_f_evals_new = 0
+        if f is not None:
+            self.set_f(f=f)
+
+    # ------------------------------------------------------------------ set-up
+    def set_f(self, *, f: Callable, f_evals: dict = None) -> dict:
+        """Evaluate (or reuse) f at the interpolation nodes and build the device plan
+        (``interpolation.py:115-239``).  Returns the updated f-evaluation dictionary."""
+        if f_evals is None:
+            f_evals = {}
+        dev = indices.device()
+        st = _stream()
+        gen = self._node_gen
+        d, d_out = self._d_in, self._d_out
+        zero = np.array([g(0)[0] for g in gen])
+
+        tree = indices.LambdaTree(self._k, self._t, capi.SMX_MODE_NONZERO)
+        zeta = tree.zeta()
+        rank = tree.rank()
+        level = tree.level_of()
+        # summands: zeta != 0 and n >= 1, in the reference's emission order
+        sel = torch.nonzero((zeta != 0) & (level >= 1)).flatten()
+        ent = sel[torch.argsort(rank[sel])].contiguous()
+        n_sum = int(ent.shape[0])
+        zeta0 = int(zeta[0].item())
+
+        # offset: zeta_0 * f(zero point)   (interpolation.py:151-166)
+        if self._is_nested:
+            cache0 = f_evals
+        else:
+            cache0 = f_evals.get((), {})
+        if zeta0 != 0:
+            if () not in cache0:
+                cache0[()] = f(zero.copy())
+                self._n_f_evals_new += 1
+            if not self._is_nested:
+                f_evals[()] = cache0
+            offset = zeta0 * self._as_out(cache0[()])
+        else:
+            offset = np.zeros(d_out)
+
+        # pairs: every (dim, deg) with 1 <= deg <= maxdeg(dim)
+        maxdeg = torch.zeros(d, dtype=torch.int32, device=dev)
+        call("smx_max_degree", tree.size, ptr(tree.dim), ptr(tree.deg), ptr(maxdeg), st)
+        maxdeg_h = maxdeg.cpu().numpy().astype(np.int64)
+        pair_base_h = np.concatenate([[0], np.cumsum(maxdeg_h)[:-1]]).astype(np.int32)
+        n_pairs = int(maxdeg_h.sum())
+        pair_dim_h = np.repeat(np.arange(d, dtype=np.int32), maxdeg_h)
+        pair_deg_h = (np.arange(n_pairs) - np.repeat(pair_base_h, maxdeg_h) + 1).astype(np.int32)
+        pair_voff_h = np.concatenate([[0], np.cumsum(pair_deg_h + 1)[:-1]]).astype(np.int32)
+        n_values = int((pair_deg_h + 1).sum())
+        node_h = np.empty(n_values)
+        for u in range(n_pairs):
+            g = int(pair_deg_h[u])
+            node_h[pair_voff_h[u] : pair_voff_h[u] + g + 1] = np.asarray(gen[int(pair_dim_h[u])](g), dtype=float)
+
+        P = Plan()
+        T = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+        P.set("pair_dim", T(pair_dim_h, torch.int32))
+        P.set("pair_deg", T(pair_deg_h, torch.int32))
+        P.set("pair_voff", T(pair_voff_h, torch.int32))
+        P.set("node", T(node_h, torch.float64))
+        bw = torch.empty(n_values, dtype=torch.float64, device=dev)
+        call("smx_bary_weights", n_pairs, ptr(P.keep["pair_deg"]), ptr(P.keep["pair_voff"]), ptr(P.keep["node"]),
+             ptr(bw), st)
+        P.set("bweight", bw)
+
+        # summand layout
+        lvl_sum = level[ent]
+        sum_poff = torch.zeros(n_sum + 1, dtype=torch.int32, device=dev)
+        if n_sum:
+            sum_poff[1:] = torch.cumsum(lvl_sum, 0).to(torch.int32)
+        n_pair_tot = int(sum_poff[-1].item()) if n_sum else 0
+        sum_pairs = torch.empty(max(n_pair_tot, 1), dtype=torch.int32, device=dev)
+        n_ent = torch.empty(max(n_sum, 1), dtype=torch.int64, device=dev)
+        pair_base = T(pair_base_h, torch.int32)
+        call("smx_plan_summands", n_sum, ptr(ent), ptr(tree.parent), ptr(tree.dim), ptr(tree.deg), ptr(pair_base),
+             ptr(sum_poff), ptr(sum_pairs), ptr(n_ent), st)
+        sum_eoff = torch.empty(n_sum + 1, dtype=torch.int64, device=dev)
+        ws = torch.empty(capi.size("smx_scan_workspace", n_sum), dtype=torch.uint8, device=dev)
+        call("smx_scan_i64", ptr(n_ent), ptr(sum_eoff), n_sum, ptr(ws), ws.numel(), st)
+        R = int(sum_eoff[-1].item())
+        P.set("sum_poff", sum_poff)
+        P.set("sum_pairs", sum_pairs)
+        P.set("sum_eoff", sum_eoff)
+
+        # nodal values: host calls of f with the reference's cache keys, device gather
+        fu, umap = self._evaluate_nodes(f, f_evals, zero, sum_poff.cpu().numpy(), sum_pairs.cpu().numpy(),
+                                        pair_dim_h, pair_deg_h, pair_voff_h, node_h, R)
+        F64 = torch.empty(max(R * d_out, 1), dtype=torch.float64, device=dev)
+        F32 = torch.empty(max(R * d_out, 1), dtype=torch.float32, device=dev)
+        P.set("F64", F64)
+        P.set("F32", F32)
+        P.set("offset", T(offset, torch.float64))
+        c = P.c
+        c.d_in, c.d_out = d, d_out
+        c.n_pairs, c.n_values, c.n_summands = n_pairs, n_values, n_sum
+        c.max_n = int(lvl_sum.max().item()) if n_sum else 0
+        c.n_entries = R
+        if R:
+            fu_d = T(fu, torch.float64)
+            umap_d = T(umap, torch.int64)
+            call("smx_assemble_F", P.ref(), ptr(zeta[ent].contiguous()), ptr(fu_d), ptr(umap_d), ptr(F64), ptr(F32),
+                 st)
+        P.keep["sum_zeta"] = zeta[ent].contiguous()
+        P.keep["ent"] = ent
+        self._plan = P
+        self._tree = tree
+        self._maxdeg = maxdeg_h
+        if self._n_inputs is not None:
+            _ = self(torch.rand(self._n_inputs, d, dtype=torch.float64, device=dev))
+        return f_evals
+
+    def _as_out(self, v):
+        return np.broadcast_to(np.asarray(v, dtype=float), (self._d_out,)).astype(float)
+
+    def _evaluate_nodes(self, f, f_evals, zero, sum_poff, sum_pairs, pdim, pdeg, pvoff, node, R):
+        """Unique function values and the row -> value map (``interpolation.py:201-228``)."""
+        nested = self._is_nested
+        keys = {}
+        vals = []
+        umap = np.empty(R, dtype=np.int64)
+        r = 0
+        n_sum = len(sum_poff) - 1
+        for s in range(n_sum):
+            prs = sum_pairs[sum_poff[s] : sum_poff[s + 1]]
+            dims = [int(pdim[u]) for u in prs]
+            degs = [int(pdeg[u]) for u in prs]
+            offs = [int(pvoff[u]) for u in prs]
+            if nested:
+                cache = f_evals
+                ukey = None
+            else:
+                nu = tuple(zip(dims, degs))
+                cache = f_evals.get(nu, {})
+                ukey = nu
+            n = len(dims)
+            mu = [0] * n
+            K = int(np.prod([g + 1 for g in degs]))
+            for _ in range(K):
+                key = tuple((dims[i], mu[i]) for i in range(n) if mu[i] > 0)
+                if key not in cache:
+                    x = zero.copy()
+                    for i in range(n):
+                        x[dims[i]] = node[offs[i] + mu[i]]
+                    cache[key] = f(x)
+                    self._n_f_evals_new += 1
+                gk = (ukey, key)
+                idx = keys.get(gk)
+                if idx is None:
+                    idx = len(vals)
+                    keys[gk] = idx
+                    vals.append(self._as_out(cache[key]))
+                umap[r] = idx
+                r += 1
+                for i in range(n - 1, -1, -1):
+                    mu[i] += 1
+                    if mu[i] <= degs[i]:
+                        break
+                    mu[i] = 0
+            if not nested:
+                f_evals[ukey] = cache
+        fu = np.array(vals, dtype=float).reshape(-1, self._d_out) if vals else np.zeros((1, self._d_out))
+        return fu, umap
+
+    # ------------------------------------------------------------------ evaluation
+    def _validate_input(self, x: ArrayLike) -> torch.Tensor:
+        """``interpolation.py:253-262``: set-up check, host->device, 1-D promotion."""
+        assert self._plan is not None, "The operator has not yet been set up for a target function via `set_f`."
+        dev = indices.device()
+        if isinstance(x, torch.Tensor):
+            x = x.to(device=dev, dtype=torch.float64)
+        else:
+            x = torch.as_tensor(np.asarray(x, dtype=np.float64), device=dev)
+        if tuple(x.shape) == (self._d_in,):
+            x = x[None, :]
+        assert x.shape[1] == self._d_in, f"{x.shape[1]} != {self._d_in}"
+        self._n_inputs = int(x.shape[0])
+        return x.contiguous()
+
+    def _chunk(self, bytes_per_point):
+        lim = max(1, int(self._memory_limit * 1024**3 // max(1, bytes_per_point)))
+        return lim
+
+    def __call__(self, x: ArrayLike) -> torch.Tensor:
+        """Evaluate the interpolant at points x, shape (n_points, d_in) or (d_in,) -> (n_points, d_out)."""
+        x = self._validate_input(x)
+        Pn = int(x.shape[0])
+        y = torch.empty(Pn, self._d_out, dtype=torch.float64, device=x.device)
+        if Pn == 0:
+            return y
+        st = _stream()
+        pl = self._plan
+        per_point = capi.size("smx_eval_workspace", pl.ref(), 1, 64)
+        step = self._chunk(per_point)
+        for p0 in range(0, Pn, step):
+            p1 = min(Pn, p0 + step)
+            ws = torch.empty(capi.size("smx_eval_workspace", pl.ref(), p1 - p0, 64), dtype=torch.uint8, device=x.device)
+            call("smx_eval", pl.ref(), 64, ptr(x[p0:p1]), p1 - p0, self._d_in, ptr(y[p0:p1]), ptr(ws), ws.numel(), st)
+        return y
+
+    def gradient(self, x: ArrayLike) -> torch.Tensor:
+        """Jacobian of the interpolant at x: (n_points, d_out, d_in) (``interpolation.py:306-345``)."""
+        x = self._validate_input(x)
+        Pn = int(x.shape[0])
+        J = torch.empty(Pn, self._d_out, self._d_in, dtype=torch.float64, device=x.device)
+        if Pn == 0:
+            return J
+        st = _stream()
+        pl = self._plan
+        per_point = capi.size("smx_jacobian_workspace", pl.ref(), 1)
+        step = self._chunk(per_point)
+        for p0 in range(0, Pn, step):
+            p1 = min(Pn, p0 + step)
+            ws = torch.empty(capi.size("smx_jacobian_workspace", pl.ref(), p1 - p0), dtype=torch.uint8,
+                             device=x.device)
+            call("smx_jacobian", pl.ref(), ptr(x[p0:p1]), p1 - p0, self._d_in, ptr(J[p0:p1]), ptr(ws), ws.numel(), st)
+        return J
+
+    def integral(self) -> torch.Tensor:
+        """Integral of the interpolant, shape (d_out,) (``interpolation.py:347-390``)."""
+        assert self._plan is not None, "The operator has not yet been set up for a target function via `set_f`."
+        pl = self._plan
+        dev = indices.device()
+        c = pl.c
+        if "qnode" not in pl.keep:
+            pdim = pl.keep["pair_dim"].cpu().numpy()
+            pdeg = pl.keep["pair_deg"].cpu().numpy()
+            pvoff = pl.keep["pair_voff"].cpu().numpy()
+            q = np.zeros(max(c.n_values, 1))
+            for u in range(c.n_pairs):
+                g = int(pdeg[u])
+                q[pvoff[u] : pvoff[u] + g + 1] = self._node_gen[int(pdim[u])].get_quadrature_weights(g)
+            pl.keep["qnode"] = torch.as_tensor(q, device=dev)
+        Q = torch.empty(self._d_out, dtype=torch.float64, device=dev)
+        ws = torch.empty(capi.size("smx_integral_workspace", pl.ref()), dtype=torch.uint8, device=dev)
+        call("smx_integral", pl.ref(), ptr(pl.keep["qnode"]), ptr(Q), ptr(ws), ws.numel(), _stream())
+        return Q

@@ -1,0 +1,130 @@
+"""FP64 path on the GPU against the reference's outputs (golden vectors).
+
+Tolerance: 1e-12 relative for values (the reference's own FP64 evaluation
+differs from ours only by summation order); gradients 1e-10 relative with an
+absolute floor, NaN exactly where the reference has NaN.
+"""
+import numpy as np
+import pytest
+
+import functions as fns
+import golden_io as gio
+from gpu_helpers import assert_close_nan, product_generator, rel_err
+
+pytestmark = pytest.mark.gpu
+
+INTERP = gio.load("interp_small.npz")
+CFG = gio.load("interp_configs.npz")
+
+
+def _interp(**kw):
+    from smolyax_gb300 import SmolyakBarycentricInterpolator
+
+    return SmolyakBarycentricInterpolator(**kw)
+
+
+@pytest.mark.parametrize("name", [str(n) for n in INTERP["names"]])
+def test_small_cases(name):
+    z = INTERP
+    spec, k, t, d_out, f = gio.small_case(z, name)
+    ip = _interp(node_gen=product_generator(spec, len(k)), k=k, t=t, d_out=d_out, f=f)
+    x = z[name + "/x"]
+    y = ip(x).cpu().numpy()
+    np.testing.assert_allclose(y, z[name + "/y"], rtol=1e-12, atol=1e-13)
+    g = ip.gradient(x[:-1]).cpu().numpy()
+    assert_close_nan(g, z[name + "/grad"], rtol=1e-10, atol=1e-11)
+    np.testing.assert_allclose(ip.integral().cpu().numpy(), z[name + "/integral"], rtol=1e-12, atol=1e-12)
+    assert (ip.n_f_evals, ip.n_f_evals_new) == tuple(int(v) for v in z[name + "/n_f_evals"])
+
+
+def test_config1_full():
+    from smolyax_gb300 import nodes
+
+    d = 10
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    ip = _interp(node_gen=nodes.Leja(dim=d), k=k, t=8.831421, d_out=1, f=fns.rational(d, seed=0))
+    x = np.random.default_rng(1).uniform(-1, 1, (10000, d))
+    assert rel_err(ip(x).cpu().numpy(), CFG["cfg1/y"]) < 1e-12
+    assert rel_err(ip.gradient(x[:64]).cpu().numpy(), CFG["cfg1/grad"], 1e-8) < 1e-10
+    np.testing.assert_allclose(ip.integral().cpu().numpy(), CFG["cfg1/integral"], rtol=1e-12)
+    assert (ip.n_f_evals, ip.n_f_evals_new) == tuple(int(v) for v in CFG["cfg1/n_f_evals"])
+
+
+def test_config2_subset():
+    from smolyax_gb300 import nodes
+
+    d = 1000
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    ip = _interp(node_gen=nodes.Leja(dim=d), k=k, t=8.224520, d_out=1, f=fns.rational(d, seed=0))
+    x = np.random.default_rng(1).uniform(-1, 1, (256, d))
+    np.testing.assert_allclose([x.sum(), (x * x).sum()], CFG["cfg2/x_checksum"], rtol=1e-14)
+    assert rel_err(ip(x).cpu().numpy(), CFG["cfg2/y"]) < 1e-12
+    assert rel_err(ip.gradient(x[:4]).cpu().numpy(), CFG["cfg2/grad"], 1e-8) < 1e-10
+    np.testing.assert_allclose(ip.integral().cpu().numpy(), CFG["cfg2/integral"], rtol=1e-12)
+    assert (ip.n_f_evals, ip.n_f_evals_new) == tuple(int(v) for v in CFG["cfg2/n_f_evals"])
+
+
+def test_config4_subset():
+    from smolyax_gb300 import nodes
+
+    d = 200
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    ip = _interp(node_gen=nodes.Leja(dim=d), k=k, t=7.853604, d_out=64, f=fns.rational_vec(d, 64, seed=0))
+    x = np.random.default_rng(1).uniform(-1, 1, (64, d))
+    assert rel_err(ip(x).cpu().numpy(), CFG["cfg4/y"]) < 1e-12
+    assert rel_err(ip.gradient(x[:3]).cpu().numpy(), CFG["cfg4/grad"], 1e-8) < 1e-10
+    np.testing.assert_allclose(ip.integral().cpu().numpy(), CFG["cfg4/integral"], rtol=1e-12)
+
+
+@pytest.mark.parametrize("tag,t", [("cfg3alt", 7.723434), ("cfg3", 9.464636)])
+def test_config3_gauss_hermite(tag, t):
+    from smolyax_gb300 import nodes
+
+    d = 100
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    ip = _interp(node_gen=nodes.GaussHermite(dim=d), k=k, t=t, d_out=8, f=fns.exponential(d, 8, seed=0))
+    x = np.random.default_rng(1).normal(size=(32, d))
+    assert rel_err(ip(x).cpu().numpy(), CFG[tag + "/y"]) < 1e-12
+    np.testing.assert_allclose(ip.integral().cpu().numpy(), CFG[tag + "/integral"], rtol=1e-11)
+    assert (ip.n_f_evals, ip.n_f_evals_new) == tuple(int(v) for v in CFG[tag + "/n_f_evals"])
+    if tag == "cfg3alt":
+        assert rel_err(ip.gradient(x[:2]).cpu().numpy(), CFG[tag + "/grad"], 1e-8) < 1e-10
+
+
+def test_f_evals_reuse_and_shapes():
+    from smolyax_gb300 import nodes
+
+    d = 3
+    k = [1.0, 1.3, 2.0]
+    f = lambda x: np.array([np.cos(x[0]) * x[1] + x[2] ** 2, x[0]])
+    ip = _interp(node_gen=nodes.Leja(dim=d), k=k, t=4.0, d_out=2)
+    fe = ip.set_f(f=f)
+    assert ip.n_f_evals_new == ip.n_f_evals == len(fe)
+    ip2 = _interp(node_gen=nodes.Leja(dim=d), k=k, t=4.0, d_out=2)
+    ip2.set_f(f=f, f_evals=fe)
+    assert ip2.n_f_evals_new == 0
+    x = np.array([0.1, -0.2, 0.3])
+    assert tuple(ip(x).shape) == (1, 2)
+    assert tuple(ip(np.zeros((0, d))).shape) == (0, 2)
+    np.testing.assert_array_equal(ip(x).cpu().numpy(), ip2(x).cpu().numpy())
+    # non-nested cache layout: one dictionary per multi-index
+    gh = _interp(node_gen=nodes.GaussHermite(dim=d), k=k, t=4.0, d_out=2)
+    fe2 = gh.set_f(f=f)
+    assert all(isinstance(v, dict) for v in fe2.values())
+    assert sum(len(v) for v in fe2.values()) == gh.n_f_evals_new
+
+
+def test_constant_only_and_chunking():
+    from smolyax_gb300 import nodes
+
+    ip = _interp(node_gen=nodes.Leja(dim=2), k=[1.0, 2.0], t=0.5, d_out=1, f=lambda x: np.array([3.0]))
+    np.testing.assert_array_equal(ip(np.ones((5, 2))).cpu().numpy(), 3.0)
+    np.testing.assert_array_equal(ip.gradient(np.ones((2, 2))).cpu().numpy(), 0.0)
+    d = 5
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    f = fns.rational(d, seed=3)
+    a = _interp(node_gen=nodes.Leja(dim=d), k=k, t=6.0, d_out=1, f=f)
+    b = _interp(node_gen=nodes.Leja(dim=d), k=k, t=6.0, d_out=1, f=f, memory_limit=1e-6)
+    x = np.random.default_rng(2).uniform(-1, 1, (999, d))
+    np.testing.assert_array_equal(a(x).cpu().numpy(), b(x).cpu().numpy())
+    np.testing.assert_array_equal(a(x).cpu().numpy(), a(x).cpu().numpy())
