@@ -1,0 +1,321 @@
+"""Benchmark: high-dimensional scalar interpolation on one GB300.
+
+Workload (the reference's headline configuration for this metric): Leja nodes
+on [-1, 1]^1000, d_out = 1, k_j = log((2+j)/log 2), t = 8.224520 (|Lambda| =
+9999), f(x) = 1/(1 + w.x) with w_j = U(0,1)/(j+1)^2 rescaled to sum 0.5
+(seed 0), 1e5 query points U[-1,1]^1000.  The mixed-precision evaluation
+(orthogonal-polynomial form, FP32) is the headline; the FP64 path (the
+reference's combination sum) is timed beside it, together with the error of
+the FP32 values against the FP64 ones.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Rank 0 prints one JSON line.  With N > 1 (torchrun), every rank evaluates its
+own 1e5 points (replicas; the path has no exchange step) and the time is the
+max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+D_IN, T_THR, D_OUT, POINTS = 1000, 8.224520, 1, 100_000
+METRIC = "interpolant evals/sec (points x d_out) mixed-precision vs FP64 on 1 GB300 at <=1e-6 rel err; p99"
+WORKLOAD = "Leja d_in=1000 d_out=1 |Lambda|=9999 (t=8.224520) rational f, 1e5 points U[-1,1]^1000"
+
+
+def target(d, seed=0):
+    rng = np.random.default_rng(seed)
+    w = rng.uniform(0, 1, d) / (np.arange(d) + 1) ** 2
+    w *= 0.5 / w.sum()
+
+    def f(x):
+        x = np.asarray(x, dtype=float)
+        return np.atleast_1d(1.0 / (1.0 + x @ w))
+
+    return f
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            pk = json.load(fh)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the FP32 evaluator from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "spectral_eval_cfg2.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_full_size:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            parts = [p.strip() for p in ln.split(",")]
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except (ValueError, IndexError):
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_reference_rate(points, threads, seconds=12.0, seed=1):
+    """The oracle port (numpy restatement of the reference's JAX path) on host cores.
+
+    Evaluates chunks of the workload's points on a thread pool until about
+    `seconds` of wall time have passed; returns (evals/s, points evaluated)."""
+    import concurrent.futures as cf
+
+    from oracle import interp as ointerp
+
+    k = np.log((2 + np.arange(D_IN)) / np.log(2))
+    ip = ointerp.OracleInterpolant(rules=[("leja", None)] * D_IN, k=k, t=T_THR, d_out=D_OUT, f=target(D_IN),
+                                   nested=True)
+    rng = np.random.default_rng(seed)
+    chunk = 64
+    done = 0
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        while time.perf_counter() - t0 < seconds and done < points:
+            xs = [rng.uniform(-1, 1, (chunk, D_IN)) for _ in range(threads)]
+            list(ex.map(lambda a: ip(a, pchunk=chunk, zchunk=512), xs))
+            done += chunk * threads
+    dt = time.perf_counter() - t0
+    return done * D_OUT / dt, done
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    per_step = []
+    sample_pts = 0
+    for i in range(args.warmup + args.steps):
+        rate, n = cpu_reference_rate(10**9, threads, seconds=4.0, seed=100 + i)
+        if i >= args.warmup:
+            per_step.append(rate)
+            sample_pts += n
+    value = statistics.median(per_step)
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "evals/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * POINTS * D_OUT / value,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "points": POINTS, "d_in": D_IN, "d_out": D_OUT},
+        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
+                         "sample": "%d points of the workload over %d steps of ~4 s (numpy restatement of the "
+                                   "reference's evaluation; JAX is not installed)" % (sample_pts, args.steps)},
+        "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from smolyax_gb300 import SmolyakBarycentricInterpolator, nodes
+
+    world, rank, local = dist_setup()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    k = np.log((2 + np.arange(D_IN)) / np.log(2))
+    ip = SmolyakBarycentricInterpolator(node_gen=nodes.Leja(dim=D_IN), k=k, t=T_THR, d_out=D_OUT, f=target(D_IN))
+    sp = ip.spectral_plan()
+    P = args.points
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1 + rank)
+    x = torch.rand(P, D_IN, dtype=torch.float64, device=dev, generator=gen) * 2 - 1
+    y32 = torch.empty(P, D_OUT, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        barrier()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        t0 = time.perf_counter()
+        for a, b in ev:
+            a.record(stream)
+            fn()
+            b.record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+        per = [a.elapsed_time(b) for a, b in ev]
+        return per, wall
+
+    # FP64 path (the reference's combination sum)
+    fp64_steps = max(3, min(args.steps, 5))
+    per64, _ = timed(lambda: ip(x, precision="fp64"), fp64_steps, 1)
+    y64 = ip(x, precision="fp64")
+
+    # FP32 path: one kernel per step (the timed region)
+    with ClockSampler(local) as clk:
+        per32, wall32 = timed(lambda: sp.evaluate(x, y32), args.steps, max(3, args.warmup))
+    launches = args.steps  # smx_spectral_eval launches one kernel for d_out = 1
+    err = ((y32.double() - y64).abs() / y64.abs()).max().item()
+
+    # end to end through the public API with host buffers
+    xh = x.cpu().pin_memory()
+    e2e_per = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        yh = ip(xh, precision="fp32").cpu()
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_per.append((t1 - t0) * 1e3)
+    ms32 = statistics.mean(per32)
+    ms64 = statistics.mean(per64)
+    ms_e2e = statistics.mean(e2e_per)
+    if world > 1:
+        tmax = torch.tensor([ms32, ms_e2e, ms64], device=dev)
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        ms32, ms_e2e, ms64 = (float(v) for v in tmax.tolist())
+    if rank != 0:
+        dist.destroy_process_group() if world > 1 else None
+        return 0
+
+    c = sp.c
+    coef_bytes = (c.n_tape * (4 + 4 * D_OUT) + c.n_cold * (4 + 4 * D_OUT) + c.n_cold_groups * 12)
+    alg_bytes = P * D_IN * 8 + P * D_OUT * 4 + coef_bytes
+    achieved = alg_bytes / (ms32 * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    threads = os.cpu_count() or 1
+    cpu_rate, cpu_pts = cpu_reference_rate(10**9, threads, seconds=12.0)
+    srt = sorted(per32)
+    p99 = srt[min(len(srt) - 1, int(0.99 * len(srt)))]
+    line = {
+        "metric": METRIC,
+        "value": world * P * D_OUT / (ms32 * 1e-3),
+        "unit": "evals/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms32,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "points": P, "d_in": D_IN, "d_out": D_OUT, "lambda": 9999,
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (x is %d MB FP64)" % (P * D_IN * 8 // 2**20)},
+        "latency_ms": {"p50": statistics.median(per32), "p99": p99, "max": max(per32)},
+        "fp64": {"value": world * P * D_OUT / (ms64 * 1e-3), "ms_per_step": ms64, "steps": fp64_steps},
+        "speedup_vs_fp64": ms64 / ms32,
+        "error": {"fp32_max_rel_vs_fp64": err, "bound": 1e-6},
+        "e2e": {"value": world * P * D_OUT / (ms_e2e * 1e-3), "unit": "evals/s", "ms_per_step": ms_e2e,
+                "h2d_bytes_per_step": int(xh.numel() * 8), "d2h_bytes_per_step": int(yh.numel() * 4)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": ncu_traffic(), "algorithmic_bytes_per_launch": alg_bytes},
+        "cpu_baseline": {"value": cpu_rate, "unit": "evals/s", "cores": threads, "kind": "port",
+                         "sample": "%d points of the workload in ~12 s (numpy restatement of the reference)" % cpu_pts},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+        "wall_s_timed_region": wall32,
+    }
+    print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--points", type=int, default=POINTS)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

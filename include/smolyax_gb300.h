@@ -52,6 +52,7 @@ enum {
 #define SMX_MODE_NONZERO 0
 #define SMX_MODE_INDEXSET 1
 #define SMX_MODE_ADDITIVE 2
+#define SMX_MODE_PREORDER 3 /* ranks only: every entry before its children */
 
 /* Per entry: number of children (written to `count`) and the chain end
  * (`term`).  Replaces the inner expansion loops of indices.py:49-67,
@@ -87,7 +88,8 @@ int smx_scan_i64(const int64_t* in, int64_t* out, int64_t n, void* ws, size_t ws
  * smx_lambda_ranks level by level from the root down, with base[root] = 0: it
  * writes rank[e] and the first rank base[c] of every child subtree.  In
  * SMX_MODE_NONZERO an entry precedes the children at its chain-end dimension
- * `term`; in SMX_MODE_INDEXSET it follows all its children. */
+ * `term`; in SMX_MODE_INDEXSET it follows all its children; SMX_MODE_PREORDER
+ * places it before all its children (the order used by the FP32 evaluator). */
 int smx_lambda_subtree_sizes(const int64_t* first_child, const int64_t* n_child, int64_t lvl_begin, int64_t lvl_end,
                              int64_t* size, void* stream);
 int smx_lambda_ranks(int mode, const int32_t* term, const int32_t* dim, const int64_t* first_child,
@@ -137,11 +139,16 @@ int smx_plan_summands(int64_t n_sum, const int64_t* ent, const int32_t* parent, 
 /* Per-dimension maximal degree over a set of entries (atomicMax). */
 int smx_max_degree(int64_t n, const int32_t* dim, const int32_t* deg, int32_t* maxdeg, void* stream);
 
-/* F64/F32 rows from unique function values: F64[r] = zeta(r) * fu[umap[r]]
+/* F64/F32 rows from unique function values:
+ *   F64[r] = zeta(r) * (fu[umap[r]] - center)
  * (interpolation.py:201-235, with the reference's cached f evaluations
- * gathered on the device). */
+ * gathered on the device).  `center` (d_out values, may be NULL for zero) is
+ * a constant subtracted from every nodal value; since every tensor-product
+ * interpolant reproduces constants, the caller adds center * sum(zeta) to the
+ * offset.  Centering shrinks the summands that cancel in the combination
+ * sum and so the rounding error of the FP64 result. */
 int smx_assemble_F(const smx_plan* plan_host, const int64_t* sum_zeta, const double* fu, const int64_t* umap,
-                   double* F64, float* F32, void* stream);
+                   const double* center, double* F64, float* F32, void* stream);
 
 /* ---- evaluation -------------------------------------------------------------------
  * Basis table: Lt[v*P + p] = normalised barycentric basis value of slot v at
@@ -175,6 +182,63 @@ int smx_jacobian(const smx_plan* plan_host, const double* x, int64_t P, int64_t 
  * weights) (interpolation.py:347-390). */
 size_t smx_integral_workspace(const smx_plan* plan_host);
 int smx_integral(const smx_plan* plan_host, const double* qnode, double* Q, void* ws, size_t ws_bytes, void* stream);
+
+/* ---- mixed-precision path: orthogonal-polynomial form --------------------------------
+ * The interpolant is re-expressed as sum_{m in Lambda} c_m prod_j phi_{m_j}(z_j)
+ * with phi_n the Legendre polynomials (fam 0) or the normalised Hermite
+ * polynomials H_n / sqrt(2^n n!) (fam 1) of z_j = fam_a[j] * x_j + fam_b[j].
+ * This re-expression of the reference's combination sum (interpolation.py:
+ * 264-304 over barycentric.py:69-123) is exact in exact arithmetic; it moves
+ * the cancellation of the combination sum into an FP64 set-up step so that
+ * the evaluation can run in FP32. */
+
+/* Per pair: A = V^{-1} with V[j][m] = phi_m(z(node_j)) (FP64, row-major
+ * [m][j] at aoff[pair]); *flag != 0 on failure (degree > 23 or singular V). */
+int smx_spectral_pairs(int n_pairs, const int32_t* pair_dim, const int32_t* pair_deg, const int32_t* pair_voff,
+                       const int64_t* aoff, const double* node, const int32_t* fam, const double* fam_a,
+                       const double* fam_b, double* A, int32_t* flag, void* stream);
+
+/* Coefficients C[n_lambda * d_out] (FP64) of every entry of the index set
+ * (tree arrays of smx_lambda_*, NONZERO mode): mode products of each summand's
+ * rows with its pairs' A matrices (scratch G: n_entries * d_out doubles, ids:
+ * n_entries int32) scattered into the entries; C[root] also receives the
+ * plan's offset.  *flag = 4 if a multi-index is missing from the tree. */
+int smx_spectral_coefficients(const smx_plan* plan_host, const int64_t* aoff, const double* A,
+                              const int64_t* first_child, const int64_t* n_child, const int32_t* tdim,
+                              const int32_t* tdeg, int64_t n_lambda, double* G, int32_t* ids, double* C,
+                              int32_t* flag, void* stream);
+
+/* Evaluation layout of the orthogonal form.  "Hot" dimensions are those that
+ * occur before another dimension in some multi-index; every entry is either
+ * hot (all its dimensions hot) or cold (hot prefix + one cold last pair). */
+typedef struct smx_spectral {
+  int32_t d_in, d_out;
+  int32_t n_hot_slots;   /* basis values phi_1..phi_g of the hot dimensions      */
+  int32_t n_vp;          /* stored prefix products (slot 0 = empty prefix = 1)   */
+  int32_t n_hot_dims;
+  int32_t n_tape;        /* hot entries except the root, DFS pre-order           */
+  int32_t n_cold_groups; /* cold dimensions                                      */
+  int32_t n_cold;        /* cold entries                                         */
+  int32_t max_depth;     /* deepest hot entry (<= 8)                             */
+  const int32_t* hot_dim;   /* [n_hot_dims]                                      */
+  const int32_t* hot_deg;   /* [n_hot_dims] max degree                           */
+  const int32_t* hot_soff;  /* [n_hot_dims] first basis slot                     */
+  const int32_t* tape;      /* [n_tape] slot | depth << 16 | vp << 20 (0: none)   */
+  const float* tape_c;      /* [n_tape * d_out] FP32 coefficients                 */
+  const int32_t* cold_dim;  /* [n_cold_groups]                                   */
+  const int32_t* cold_gmax; /* [n_cold_groups] max degree of the group           */
+  const int32_t* cold_off;  /* [n_cold_groups + 1]                               */
+  const int32_t* cold_ent;  /* [n_cold] vp | degree << 24                         */
+  const float* cold_c;      /* [n_cold * d_out]                                   */
+  const float* fam_a;       /* [d_in]                                            */
+  const float* fam_b;       /* [d_in]                                            */
+  const int32_t* fam;       /* [d_in] 0 Legendre, 1 Hermite                      */
+  const float* c0;          /* [d_out] coefficient of the constant               */
+} smx_spectral;
+
+/* FP32 evaluation y[P, d_out] (x FP64 row-major, leading dimension ldx). */
+int smx_spectral_eval(const smx_spectral* plan_host, const double* x, int64_t P, int64_t ldx, float* y,
+                      void* stream);
 
 /* Human-readable description of the last error on this thread (host string). */
 const char* smx_last_error_string(void);

@@ -124,13 +124,17 @@ class OracleInterpolant:
             yield slice(z0, min(nn, z0 + zchunk))
 
     # -- barycentric.py:69-123 and interpolation.py:264-304 ---------------------------------
-    def __call__(self, x, *, pchunk=2048, zchunk=256):
+    def __call__(self, x, *, pchunk=2048, zchunk=256, dtype=np.float64):
+        """Evaluate at x.  ``dtype=np.longdouble`` evaluates the same formula in
+        extended precision (nodes, weights and basis recomputed from the FP64
+        nodes; nodal values are the FP64 data), which exposes the rounding
+        error of FP64 evaluations of the combination sum."""
         x = np.asarray(x, dtype=float)
         if x.shape == (self.d_in,):
             x = x[None, :]
         assert x.shape[1] == self.d_in
         P = x.shape[0]
-        out = np.broadcast_to(np.asarray(self.offset, dtype=float), (P, self.d_out)).copy()
+        out = np.broadcast_to(np.asarray(self.offset, dtype=float), (P, self.d_out)).astype(dtype)
         for n, blk in self.blocks.items():
             letters = string.ascii_lowercase
             fa = letters[:n]
@@ -138,34 +142,47 @@ class OracleInterpolant:
             for zs in self._block_chunks(blk, zchunk):
                 dims, degs = blk["dims"][zs], blk["degs"][zs]
                 for p0 in range(0, P, pchunk):
-                    xp = x[p0 : p0 + pchunk]
+                    xp = x[p0 : p0 + pchunk].astype(dtype)
                     bs = []
                     for s in range(n):
                         m = blk["tau"][s] + 1
-                        b = self._basis(xp[:, dims[:, s]].T, blk["nodes"][zs, s, :m], blk["weights"][zs, s, :m], degs[:, s])
+                        xi = blk["nodes"][zs, s, :m].astype(dtype)
+                        w = blk["weights"][zs, s, :m].astype(dtype)
+                        if dtype is not np.float64:
+                            w = np.zeros_like(xi)
+                            for z in range(xi.shape[0]):
+                                g = int(degs[z, s])
+                                w[z, : g + 1] = _nodes.barycentric_weights(xi[z, : g + 1], dtype=dtype)
+                        b = self._basis(xp[:, dims[:, s]].T, xi, w, degs[:, s])
                         bs.append(b / b.sum(axis=2, keepdims=True))
-                    out[p0 : p0 + pchunk] += np.einsum(sub, blk["zetas"][zs].astype(float), blk["F"][zs], *bs, optimize=True)
+                    F = blk["F"][zs].astype(dtype)
+                    out[p0 : p0 + pchunk] += np.einsum(sub, blk["zetas"][zs].astype(dtype), F, *bs, optimize=True)
         return out
 
     # -- barycentric.py:158-229 and interpolation.py:306-345 --------------------------------
-    def gradient(self, x, *, pchunk=512, zchunk=128):
+    def gradient(self, x, *, pchunk=512, zchunk=128, dtype=np.float64):
         x = np.asarray(x, dtype=float)
         if x.shape == (self.d_in,):
             x = x[None, :]
         P = x.shape[0]
-        J = np.zeros((P, self.d_out, self.d_in))
+        J = np.zeros((P, self.d_out, self.d_in), dtype=dtype)
         for n, blk in self.blocks.items():
             fa = string.ascii_lowercase[:n]
             for zs in self._block_chunks(blk, zchunk):
                 dims, degs = blk["dims"][zs], blk["degs"][zs]
-                zeta = blk["zetas"][zs].astype(float)
+                zeta = blk["zetas"][zs].astype(dtype)
                 for p0 in range(0, P, pchunk):
-                    xp = x[p0 : p0 + pchunk]
+                    xp = x[p0 : p0 + pchunk].astype(dtype)
                     bn, Bd = [], []
                     for s in range(n):
                         m = blk["tau"][s] + 1
                         xs = xp[:, dims[:, s]].T
-                        xi, w = blk["nodes"][zs, s, :m], blk["weights"][zs, s, :m]
+                        xi, w = blk["nodes"][zs, s, :m].astype(dtype), blk["weights"][zs, s, :m].astype(dtype)
+                        if dtype is not np.float64:
+                            w = np.zeros_like(xi)
+                            for z in range(xi.shape[0]):
+                                g = int(degs[z, s])
+                                w[z, : g + 1] = _nodes.barycentric_weights(xi[z, : g + 1], dtype=dtype)
                         b = self._basis(xs, xi, w, degs[:, s])
                         bnorm = b.sum(axis=2, keepdims=True)
                         db = self._basis_grad(xs, xi, w, degs[:, s])
@@ -176,26 +193,26 @@ class OracleInterpolant:
                     for s in range(n):
                         ops = [Bd[j] if j == s else bn[j] for j in range(n)]
                         sub = "z,zo" + fa + "," + ",".join("zp" + c for c in fa) + "->zpo"
-                        g = np.einsum(sub, zeta, blk["F"][zs], *ops, optimize=True)  # (Z, P, d_out)
+                        g = np.einsum(sub, zeta, blk["F"][zs].astype(dtype), *ops, optimize=True)  # (Z, P, d_out)
                         for zi in range(g.shape[0]):
                             J[p0 : p0 + pchunk, :, dims[zi, s]] += g[zi]
         return J
 
     # -- interpolation.py:347-390 -------------------------------------------------------------
-    def integral(self):
-        Q = np.broadcast_to(np.asarray(self.offset, dtype=float), (self.d_out,)).copy()
+    def integral(self, dtype=np.float64):
+        Q = np.broadcast_to(np.asarray(self.offset, dtype=float), (self.d_out,)).astype(dtype)
         for n, blk in self.blocks.items():
             nn = blk["zetas"].shape[0]
             qs = []
             for s in range(n):
-                q = np.zeros((nn, blk["tau"][s] + 1))
+                q = np.zeros((nn, blk["tau"][s] + 1), dtype=dtype)
                 for i in range(nn):
                     dim, deg = int(blk["dims"][i, s]), int(blk["degs"][i, s])
                     q[i, : deg + 1] = _nodes.rule_quadrature_weights(self.rules[dim], deg)
                 qs.append(q)
             fa = string.ascii_lowercase[:n]
             sub = "z," + ",".join("z" + c for c in fa) + ",zo" + fa + "->o"
-            Q += np.einsum(sub, blk["zetas"].astype(float), *qs, blk["F"], optimize=True)
+            Q += np.einsum(sub, blk["zetas"].astype(dtype), *qs, blk["F"].astype(dtype), optimize=True)
         return Q
 
     # -- flattened view used by tests ------------------------------------------------------------

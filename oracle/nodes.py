@@ -69,9 +69,9 @@ def rule_quadrature_weights(rule, n):
     return np.polynomial.hermite.hermgauss(n + 1)[1] / np.sqrt(np.pi)
 
 
-def barycentric_weights(nodes):
+def barycentric_weights(nodes, dtype=np.float64):
     """w_b = prod_a 1/(xi_a - xi_b), zero differences replaced by 1 (``barycentric.py:13-31``)."""
-    nodes = np.asarray(nodes, dtype=float)
+    nodes = np.asarray(nodes, dtype=dtype)
     diffs = nodes[:, None] - nodes
-    diffs = np.where(diffs == 0, 1, diffs)
-    return np.prod(1 / diffs, axis=0)
+    diffs = np.where(diffs == 0, dtype(1), diffs)
+    return np.prod(dtype(1) / diffs, axis=0)

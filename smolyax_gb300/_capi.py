@@ -16,6 +16,7 @@ SMX_OK = 0
 SMX_MODE_NONZERO = 0
 SMX_MODE_INDEXSET = 1
 SMX_MODE_ADDITIVE = 2
+SMX_MODE_PREORDER = 3
 SMX_MAX_DEPTH = 64
 
 _p = C.c_void_p
@@ -51,6 +52,36 @@ class SmxPlan(C.Structure):
     ]
 
 
+class SmxSpectral(C.Structure):
+    """Mirror of ``struct smx_spectral``."""
+
+    _fields_ = [
+        ("d_in", _i32),
+        ("d_out", _i32),
+        ("n_hot_slots", _i32),
+        ("n_vp", _i32),
+        ("n_hot_dims", _i32),
+        ("n_tape", _i32),
+        ("n_cold_groups", _i32),
+        ("n_cold", _i32),
+        ("max_depth", _i32),
+        ("hot_dim", _p),
+        ("hot_deg", _p),
+        ("hot_soff", _p),
+        ("tape", _p),
+        ("tape_c", _p),
+        ("cold_dim", _p),
+        ("cold_gmax", _p),
+        ("cold_off", _p),
+        ("cold_ent", _p),
+        ("cold_c", _p),
+        ("fam_a", _p),
+        ("fam_b", _p),
+        ("fam", _p),
+        ("c0", _p),
+    ]
+
+
 # name -> (restype, argtypes); must list every function declared in the header.
 SIGNATURES = {
     "smx_lambda_count": (_int, [_p, _int, _dbl, _int, _p, _p, _i64, _p, _p, _p]),
@@ -63,7 +94,7 @@ SIGNATURES = {
     "smx_bary_weights": (_int, [_int, _p, _p, _p, _p, _p]),
     "smx_plan_summands": (_int, [_i64, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
     "smx_max_degree": (_int, [_i64, _p, _p, _p, _p]),
-    "smx_assemble_F": (_int, [_p, _p, _p, _p, _p, _p, _p]),
+    "smx_assemble_F": (_int, [_p, _p, _p, _p, _p, _p, _p, _p]),
     "smx_basis_f64": (_int, [_p, _p, _i64, _i64, _p, _p, _p]),
     "smx_contract_f64": (_int, [_p, _p, _i64, _p, _p]),
     "smx_eval_workspace": (_sz, [_p, _i64, _int]),
@@ -72,6 +103,9 @@ SIGNATURES = {
     "smx_jacobian": (_int, [_p, _p, _i64, _i64, _p, _p, _sz, _p]),
     "smx_integral_workspace": (_sz, [_p]),
     "smx_integral": (_int, [_p, _p, _p, _p, _sz, _p]),
+    "smx_spectral_pairs": (_int, [_int, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
+    "smx_spectral_coefficients": (_int, [_p, _p, _p, _p, _p, _p, _p, _i64, _p, _p, _p, _p, _p]),
+    "smx_spectral_eval": (_int, [_p, _p, _i64, _i64, _p, _p]),
     "smx_last_error_string": (C.c_char_p, []),
     "smx_version": (C.c_char_p, []),
 }

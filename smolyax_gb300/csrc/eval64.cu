@@ -169,16 +169,29 @@ __global__ void contract64_kernel(PlanArgs a, const double* __restrict__ Lt, int
   const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (p >= P) return;
   const int nout = min(kOC, a.dout - o0);
+  // Two-level sum: summands accumulate into `blk`, which is folded into `acc`
+  // every 32 summands, so rounding grows with 32 + n_sum/32 instead of n_sum.
   double acc[kOC] = {0.0, 0.0, 0.0, 0.0};
+  double blk[kOC] = {0.0, 0.0, 0.0, 0.0};
   for (int s = 0; s < a.n_sum; ++s) {
     const int q0 = a.poff[s], n = a.poff[s + 1] - q0;
     const int64_t e0 = a.eoff[s], K = a.eoff[s + 1] - e0;
+    double one[kOC] = {0.0, 0.0, 0.0, 0.0};
     contract_summand(Lt, nullptr, -1, P, p, a.pairs + q0, n, a.pvoff, a.pdeg, a.F + e0 * a.dout, K, a.dout, o0, nout,
-                     acc);
+                     one);
+#pragma unroll
+    for (int q = 0; q < kOC; ++q) blk[q] += one[q];
+    if ((s & 31) == 31) {
+#pragma unroll
+      for (int q = 0; q < kOC; ++q) {
+        acc[q] += blk[q];
+        blk[q] = 0.0;
+      }
+    }
   }
 #pragma unroll
   for (int q = 0; q < kOC; ++q)
-    if (q < nout) y[p * a.dout + o0 + q] = a.offset[o0 + q] + acc[q];
+    if (q < nout) y[p * a.dout + o0 + q] = a.offset[o0 + q] + (acc[q] + blk[q]);
 }
 
 // Jacobian: J[p][o][dim] += derivative contraction of every summand and every
@@ -247,8 +260,9 @@ __global__ void quad_reduce_kernel(const double* __restrict__ part, int nchunks,
 
 // F rows from unique function values, zeta folded in.
 __global__ void assemble_kernel(int n_sum, const int64_t* __restrict__ eoff, const int64_t* __restrict__ zeta,
-                                const double* __restrict__ fu, const int64_t* __restrict__ umap, int dout,
-                                int64_t R, double* __restrict__ F64, float* __restrict__ F32) {
+                                const double* __restrict__ fu, const int64_t* __restrict__ umap,
+                                const double* __restrict__ center, int dout, int64_t R, double* __restrict__ F64,
+                                float* __restrict__ F32) {
   const int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (idx >= R * dout) return;
   const int64_t r = idx / dout;
@@ -258,7 +272,7 @@ __global__ void assemble_kernel(int n_sum, const int64_t* __restrict__ eoff, con
     const int mid = (lo + hi + 1) >> 1;
     if (eoff[mid] <= r) lo = mid; else hi = mid - 1;
   }
-  const double v = double(zeta[lo]) * fu[umap[r] * dout + o];
+  const double v = double(zeta[lo]) * (fu[umap[r] * dout + o] - (center ? center[o] : 0.0));
   F64[idx] = v;
   if (F32) F32[idx] = float(v);
 }
@@ -416,13 +430,13 @@ extern "C" int smx_integral(const smx_plan* pl, const double* qnode, double* Q, 
 }
 
 extern "C" int smx_assemble_F(const smx_plan* pl, const int64_t* sum_zeta, const double* fu, const int64_t* umap,
-                              double* F64, float* F32, void* stream) {
+                              const double* center, double* F64, float* F32, void* stream) {
   SMX_REQUIRE(pl != nullptr, "smx_assemble_F: null plan");
   const int64_t total = pl->n_entries * int64_t(pl->d_out);
   if (total == 0) return SMX_OK;
   SMX_REQUIRE(sum_zeta && fu && umap && F64 && pl->sum_eoff, "smx_assemble_F: null pointer");
   assemble_kernel<<<smx::grid_for(total, 256), 256, 0, smx::as_stream(stream)>>>(
-      pl->n_summands, pl->sum_eoff, sum_zeta, fu, umap, pl->d_out, pl->n_entries, F64, F32);
+      pl->n_summands, pl->sum_eoff, sum_zeta, fu, umap, center, pl->d_out, pl->n_entries, F64, F32);
   SMX_LAUNCH_CHECK("smx_assemble_F");
   return SMX_OK;
 }

@@ -183,7 +183,7 @@ __global__ void rank_kernel(int mode, const int32_t* __restrict__ term, const in
        e += int64_t(gridDim.x) * blockDim.x) {
     int64_t cur = base[e];
     const int64_t c0 = first_child[e], nc = n_child[e];
-    const int td = (mode == SMX_MODE_NONZERO) ? term[e] : 0x7fffffff;
+    const int td = (mode == SMX_MODE_NONZERO) ? term[e] : (mode == SMX_MODE_PREORDER ? -1 : 0x7fffffff);
     bool placed = false;
     int64_t c = 0;
     while (c < nc) {
@@ -281,7 +281,8 @@ extern "C" int smx_lambda_subtree_sizes(const int64_t* first_child, const int64_
 extern "C" int smx_lambda_ranks(int mode, const int32_t* term, const int32_t* dim, const int64_t* first_child,
                                 const int64_t* n_child, const int64_t* size, int64_t lvl_begin, int64_t lvl_end,
                                 int64_t* base, int64_t* rank, void* stream) {
-  SMX_REQUIRE(mode == SMX_MODE_NONZERO || mode == SMX_MODE_INDEXSET, "smx_lambda_ranks: bad mode");
+  SMX_REQUIRE(mode == SMX_MODE_NONZERO || mode == SMX_MODE_INDEXSET || mode == SMX_MODE_PREORDER,
+              "smx_lambda_ranks: bad mode");
   SMX_REQUIRE(lvl_begin >= 0 && lvl_end >= lvl_begin, "smx_lambda_ranks: bad range");
   if (lvl_end == lvl_begin) return SMX_OK;
   SMX_REQUIRE(dim && first_child && n_child && size && base && rank, "smx_lambda_ranks: null pointer");

@@ -69,7 +69,16 @@ class SmolyakBarycentricInterpolator:
         return self._n_f_evals_new
 
     def __init__(self, *, d_out: int, node_gen: _nodes.Generator, k: Sequence[float], t: float,
-                 f: Callable = None, n_inputs: int = None, memory_limit: float = 4.0) -> None:
+                 f: Callable = None, n_inputs: int = None, memory_limit: float = 4.0,
+                 precision: str = "fp64") -> None:
+        """Keyword arguments as in the reference (``interpolation.py:51-113``), plus
+        ``precision``: "fp64" (default) evaluates the reference's combination sum in
+        FP64; "fp32" evaluates the same interpolant in its orthogonal-polynomial form
+        in FP32 (coefficients computed once in FP64) and returns FP32 values."""
+        if precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32'")
+        self._precision = precision
+        self._spectral = None
         self._d_in = len(k)
         self._d_out = int(d_out)
         self._node_gen = node_gen
@@ -171,9 +180,17 @@ class SmolyakBarycentricInterpolator:
                                         pair_dim_h, pair_deg_h, pair_voff_h, node_h, R)
         F64 = torch.empty(max(R * d_out, 1), dtype=torch.float64, device=dev)
         F32 = torch.empty(max(R * d_out, 1), dtype=torch.float32, device=dev)
+        # Centering: every tensor-product interpolant reproduces constants, so
+        # sum_s zeta_s I^nu_s[f] = c * sum_s zeta_s + sum_s zeta_s I^nu_s[f - c].
+        # With c = f(zero point) (row 0 of every summand) the summands that
+        # cancel in the combination sum shrink by about an order of magnitude.
+        center = fu[umap[0]].copy() if R else np.zeros(d_out)
+        zsum = int(zeta[ent].sum().item()) if n_sum else 0
+        offset = offset + center * float(zsum)
         P.set("F64", F64)
         P.set("F32", F32)
         P.set("offset", T(offset, torch.float64))
+        P.keep["center"] = T(center, torch.float64)
         c = P.c
         c.d_in, c.d_out = d, d_out
         c.n_pairs, c.n_values, c.n_summands = n_pairs, n_values, n_sum
@@ -182,11 +199,12 @@ class SmolyakBarycentricInterpolator:
         if R:
             fu_d = T(fu, torch.float64)
             umap_d = T(umap, torch.int64)
-            call("smx_assemble_F", P.ref(), ptr(zeta[ent].contiguous()), ptr(fu_d), ptr(umap_d), ptr(F64), ptr(F32),
-                 st)
+            call("smx_assemble_F", P.ref(), ptr(zeta[ent].contiguous()), ptr(fu_d), ptr(umap_d),
+                 ptr(P.keep["center"]), ptr(F64), ptr(F32), st)
         P.keep["sum_zeta"] = zeta[ent].contiguous()
         P.keep["ent"] = ent
         self._plan = P
+        self._spectral = None
         self._tree = tree
         self._maxdeg = maxdeg_h
         if self._n_inputs is not None:
@@ -264,10 +282,25 @@ class SmolyakBarycentricInterpolator:
         lim = max(1, int(self._memory_limit * 1024**3 // max(1, bytes_per_point)))
         return lim
 
-    def __call__(self, x: ArrayLike) -> torch.Tensor:
-        """Evaluate the interpolant at points x, shape (n_points, d_in) or (d_in,) -> (n_points, d_out)."""
+    def spectral_plan(self):
+        """The FP32 orthogonal-polynomial form of this interpolant (built on first use)."""
+        assert self._plan is not None, "The operator has not yet been set up for a target function via `set_f`."
+        if self._spectral is None:
+            from .spectral import SpectralPlan
+
+            self._spectral = SpectralPlan(self)
+        return self._spectral
+
+    def __call__(self, x: ArrayLike, precision: str = None) -> torch.Tensor:
+        """Evaluate the interpolant at points x, shape (n_points, d_in) or (d_in,) -> (n_points, d_out).
+
+        ``precision`` overrides the constructor's choice for this call."""
         x = self._validate_input(x)
         Pn = int(x.shape[0])
+        if (precision or self._precision) == "fp32":
+            sp = self.spectral_plan()
+            y32 = torch.empty(Pn, self._d_out, dtype=torch.float32, device=x.device)
+            return sp.evaluate(x, y32) if Pn else y32
         y = torch.empty(Pn, self._d_out, dtype=torch.float64, device=x.device)
         if Pn == 0:
             return y

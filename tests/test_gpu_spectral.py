@@ -1,0 +1,102 @@
+"""Mixed-precision path: orthogonal-polynomial form evaluated in FP32.
+
+Pins: (1) the FP64 coefficients reproduce the FP64 combination sum (host
+evaluation of the orthogonal form, 1e-9 relative); (2) the FP32 GPU values
+against the extended-precision values of the same data, with the relative
+error bound written per workload; (3) interpolation of polynomials in the
+index set stays exact to FP32 accuracy.
+"""
+import numpy as np
+import pytest
+
+import functions as fns
+import golden_io as gio
+from gpu_helpers import product_generator, rel_err
+
+pytestmark = pytest.mark.gpu
+
+EXACT = gio.load("exact_configs.npz")
+INTERP = gio.load("interp_small.npz")
+
+
+def _interp(**kw):
+    from smolyax_gb300 import SmolyakBarycentricInterpolator
+
+    return SmolyakBarycentricInterpolator(**kw)
+
+
+def _phi(fam, z, n):
+    out = [np.ones_like(z)]
+    pm1, p = np.zeros_like(z), np.ones_like(z)
+    for m in range(n):
+        if fam == 0:
+            a, b = (2 * m + 1) / (m + 1), m / (m + 1)
+        else:
+            a, b = np.sqrt(2 / (m + 1)), np.sqrt(m / (m + 1))
+        pm1, p = p, a * z * p - b * pm1
+        out.append(p)
+    return out
+
+
+def host_orthogonal_eval(ip, x):
+    sp = ip.spectral_plan()
+    C = sp.C64.cpu().numpy()
+    tree = ip._tree
+    tuples = tree.host_tuples(np.arange(tree.size))
+    fam = sp.fam.cpu().numpy()
+    a, b = sp.fa64.cpu().numpy(), sp.fb64.cpu().numpy()
+    z = x * a + b
+    maxdeg = ip._maxdeg
+    phis = {j: _phi(fam[j], z[:, j], int(maxdeg[j])) for j in range(x.shape[1]) if maxdeg[j] > 0}
+    y = np.zeros((x.shape[0], C.shape[1]))
+    for e, nu in enumerate(tuples):
+        v = np.ones(x.shape[0])
+        for dd, g in nu:
+            v = v * phis[dd][g]
+        y += v[:, None] * C[e][None, :]
+    return y
+
+
+@pytest.mark.parametrize("name", [str(n) for n in INTERP["names"]][:8])
+def test_small_cases_fp32(name):
+    z = INTERP
+    spec, k, t, d_out, f = gio.small_case(z, name)
+    ip = _interp(node_gen=product_generator(spec, len(k)), k=k, t=t, d_out=d_out, f=f)
+    x = z[name + "/x"]
+    y64 = ip(x).cpu().numpy()
+    np.testing.assert_allclose(host_orthogonal_eval(ip, x), y64, rtol=1e-9, atol=1e-10)
+    y32 = ip(x, precision="fp32").cpu().numpy()
+    assert y32.dtype == np.float32
+    scale = max(1.0, float(np.max(np.abs(y64))))
+    assert float(np.max(np.abs(y32 - y64))) / scale < 2e-6
+
+
+CASES = {
+    # tag: (d, t, kind, d_out, f, x, bound on the max relative FP32 error)
+    "cfg1": (10, 8.831421, "leja", 1, fns.rational(10, seed=0), np.random.default_rng(1).uniform(-1, 1, (10000, 10)), 1e-6),
+    "cfg2": (1000, 8.224520, "leja", 1, fns.rational(1000, seed=0),
+             np.random.default_rng(1).uniform(-1, 1, (256, 1000)), 1e-6),
+    "cfg4": (200, 7.853604, "leja", 64, fns.rational_vec(200, 64, seed=0),
+             np.random.default_rng(1).uniform(-1, 1, (64, 200)), 2e-6),
+    "cfg3alt": (100, 7.723434, "gh", 8, fns.exponential(100, 8, seed=0),
+                np.random.default_rng(1).normal(size=(32, 100)), 1e-5),
+    "cfg3": (100, 9.464636, "gh", 8, fns.exponential(100, 8, seed=0), np.random.default_rng(1).normal(size=(32, 100)),
+             1e-5),
+}
+
+
+@pytest.mark.parametrize("tag", list(CASES))
+def test_fp32_error_bound(tag):
+    from smolyax_gb300 import nodes
+
+    d, t, kind, d_out, f, x, bound = CASES[tag]
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    gen = nodes.Leja(dim=d) if kind == "leja" else nodes.GaussHermite(dim=d)
+    ip = _interp(node_gen=gen, k=k, t=t, d_out=d_out, f=f)
+    y32 = ip(x, precision="fp32").cpu().numpy().astype(float)
+    exact = EXACT[tag + "/y"]
+    err = rel_err(y32, exact)
+    print("%s: FP32 max relative error vs FP64 exact %.3e (bound %.0e)" % (tag, err, bound))
+    assert err < bound
+    if x.shape[0] <= 256:
+        np.testing.assert_allclose(host_orthogonal_eval(ip, x[:16]), exact[:16], rtol=1e-9)
