@@ -259,8 +259,9 @@ def run_ours(args):
         dist.destroy_process_group() if world > 1 else None
         return 0
 
-    c = sp.c
-    coef_bytes = (c.n_tape * (4 + 4 * D_OUT) + c.n_cold * (4 + 4 * D_OUT) + c.n_cold_groups * 12)
+    lay = sp.layout
+    coef_bytes = int(lay["coef"].nbytes + lay["node_c"].nbytes + 8 * len(lay["cold_ab"])
+                     + 16 * (len(lay["node"]) + len(lay["cold"]) + len(lay["run"])))
     alg_bytes = P * D_IN * 8 + P * D_OUT * 4 + coef_bytes
     achieved = alg_bytes / (ms32 * 1e-3) / 1e9
     peak, peak_kind = peaks()

@@ -209,31 +209,45 @@ int smx_spectral_coefficients(const smx_plan* plan_host, const int64_t* aoff, co
                               int32_t* flag, void* stream);
 
 /* Evaluation layout of the orthogonal form.  "Hot" dimensions are those that
- * occur before another dimension in some multi-index; every entry is either
- * hot (all its dimensions hot) or cold (hot prefix + one cold last pair). */
+ * occur before another dimension in some multi-index; every entry of Lambda
+ * is either hot (all its dimensions hot) or cold (hot prefix + one cold last
+ * pair).  Per point, a row of `row` floats holds phi_g(z_d) of the hot
+ * dimensions ([0, n_hb)) and the products of the hot nodes that cold entries
+ * extend ([n_hb, n_hb + n_vp), slot n_hb = empty prefix = 1).  Sums are over
+ * runs: int4 (start slot, length, coefficient offset, degree), start and
+ * length multiples of 4, coefficients [length][dstride] contiguous; the runs
+ * of a cold group are sorted by degree. */
 typedef struct smx_spectral {
   int32_t d_in, d_out;
-  int32_t n_hot_slots;   /* basis values phi_1..phi_g of the hot dimensions      */
-  int32_t n_vp;          /* stored prefix products (slot 0 = empty prefix = 1)   */
+  int32_t dstride;       /* coefficient stride per leaf (1, or d_out rounded up to 4) */
+  int32_t row;           /* floats per point row (multiple of 4, = 4 mod 32 ideally) */
+  int32_t n_hb;          /* hot basis slots                                       */
+  int32_t n_vp;          /* prefix-product slots                                  */
   int32_t n_hot_dims;
-  int32_t n_tape;        /* hot entries except the root, DFS pre-order           */
-  int32_t n_cold_groups; /* cold dimensions                                      */
-  int32_t n_cold;        /* cold entries                                         */
-  int32_t max_depth;     /* deepest hot entry (<= 8)                             */
-  const int32_t* hot_dim;   /* [n_hot_dims]                                      */
-  const int32_t* hot_deg;   /* [n_hot_dims] max degree                           */
-  const int32_t* hot_soff;  /* [n_hot_dims] first basis slot                     */
-  const int32_t* tape;      /* [n_tape] slot | depth << 16 | vp << 20 (0: none)   */
-  const float* tape_c;      /* [n_tape * d_out] FP32 coefficients                 */
-  const int32_t* cold_dim;  /* [n_cold_groups]                                   */
-  const int32_t* cold_gmax; /* [n_cold_groups] max degree of the group           */
-  const int32_t* cold_off;  /* [n_cold_groups + 1]                               */
-  const int32_t* cold_ent;  /* [n_cold] vp | degree << 24                         */
-  const float* cold_c;      /* [n_cold * d_out]                                   */
-  const float* fam_a;       /* [d_in]                                            */
-  const float* fam_b;       /* [d_in]                                            */
-  const int32_t* fam;       /* [d_in] 0 Legendre, 1 Hermite                      */
-  const float* c0;          /* [d_out] coefficient of the constant               */
+  int32_t n_nodes;       /* hot nodes with children, root first, DFS pre-order    */
+  int32_t n_cold_groups; /* cold dimensions                                       */
+  int32_t max_depth;     /* deepest node (<= 8)                                   */
+  int32_t n_cold_blocks; /* blocks of 4 degree-1 cold dimensions (d_out = 1)    */
+  int32_t node_seg[5];   /* the evaluator's 4 work segments over the nodes,     */
+  int32_t cold_seg[5];   /* the cold groups                                      */
+  int32_t block_seg[5];  /* and the cold blocks (host values)                    */
+  const int32_t* hot_dim;   /* [n_hot_dims]                                       */
+  const int32_t* hot_deg;   /* [n_hot_dims] max degree                            */
+  const int32_t* hot_soff;  /* [n_hot_dims] first basis slot                      */
+  const int32_t* node;      /* [n_nodes][4] slot | depth << 16, prefix slot or -1, run range */
+  const float* node_c;      /* [n_nodes][dstride] own coefficient                  */
+  const int32_t* cold;      /* [n_cold_groups][4] dim, run range, max degree | fam << 8 */
+  const float* cold_ab;     /* [n_cold_groups][2] affine map z = a x + b of the group */
+  const int32_t* blk_dims;  /* [n_cold_blocks][4] the block's dimensions                */
+  const int32_t* blk_run;   /* [n_cold_blocks][4] first slot, slot quads, coefficient offset, 0;
+                               coefficients [quad][slot][dimension] */
+  const float* blk_ab;      /* [n_cold_blocks][2][4] phi_1 = a x + b per dimension      */
+  const int32_t* run;       /* [n_runs][4] start, length, coefficient offset, degree */
+  const float* coef;        /* run coefficients                                    */
+  const float* fam_a;       /* [d_in]                                             */
+  const float* fam_b;       /* [d_in]                                             */
+  const int32_t* fam;       /* [d_in] 0 Legendre, 1 Hermite                       */
+  const float* c0;          /* [d_out] coefficient of the constant                */
 } smx_spectral;
 
 /* FP32 evaluation y[P, d_out] (x FP64 row-major, leading dimension ldx). */

@@ -58,23 +58,30 @@ class SmxSpectral(C.Structure):
     _fields_ = [
         ("d_in", _i32),
         ("d_out", _i32),
-        ("n_hot_slots", _i32),
+        ("dstride", _i32),
+        ("row", _i32),
+        ("n_hb", _i32),
         ("n_vp", _i32),
         ("n_hot_dims", _i32),
-        ("n_tape", _i32),
+        ("n_nodes", _i32),
         ("n_cold_groups", _i32),
-        ("n_cold", _i32),
         ("max_depth", _i32),
+        ("n_cold_blocks", _i32),
+        ("node_seg", _i32 * 5),
+        ("cold_seg", _i32 * 5),
+        ("block_seg", _i32 * 5),
         ("hot_dim", _p),
         ("hot_deg", _p),
         ("hot_soff", _p),
-        ("tape", _p),
-        ("tape_c", _p),
-        ("cold_dim", _p),
-        ("cold_gmax", _p),
-        ("cold_off", _p),
-        ("cold_ent", _p),
-        ("cold_c", _p),
+        ("node", _p),
+        ("node_c", _p),
+        ("cold", _p),
+        ("cold_ab", _p),
+        ("blk_dims", _p),
+        ("blk_run", _p),
+        ("blk_ab", _p),
+        ("run", _p),
+        ("coef", _p),
         ("fam_a", _p),
         ("fam_b", _p),
         ("fam", _p),

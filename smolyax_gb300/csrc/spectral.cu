@@ -181,24 +181,41 @@ __global__ void spectral_scatter_kernel(int64_t R, int dout, const int32_t* __re
 }
 
 // --- FP32 evaluation -----------------------------------------------------------------------
-// One thread per point.  Shared memory: hot basis table HB[slot][TP] and the
-// prefix products VP[slot][TP] of the hot entries that cold entries extend.
-// Hot entries are visited in DFS pre-order; the running products of the
-// current path live in registers st1..st8 (depth is warp-uniform).
-// Cold entries are grouped by their cold (last) dimension, whose x column is
-// streamed once; contribution c * VP[prefix] * phi_g(z).
+// A CTA evaluates 128 points with 512 threads: warp w serves the 32 points of
+// point group w % 4 and work segment w / 4.  Each point owns a row of shared
+// memory (stride `row` floats, row = 4 mod 32 so 128-bit loads of 8
+// consecutive threads hit distinct banks):
+//   [0, n_hb)           phi_g(z_d) of the hot dimensions d, g = 1..maxdeg(d)
+//   [n_hb, n_hb + n_vp) products of the hot nodes that cold entries extend
+//                       (slot n_hb is the empty prefix, = 1)
+// The sum over Lambda is organised as
+//   hot nodes (pre-order, the path products on a register stack):
+//       v_P * (c_P + sum over runs of hot leaf children c * phi)
+//   cold groups (one cold dimension d, its column of x read once):
+//       sum over runs (degree g) of phi_g(z_d) * (sum of c * prefix product)
+// where every run is a 4-aligned range of row slots with its coefficients
+// stored contiguously: one LDS.128 and one warp-uniform LDG.128 feed 4 FMAs.
+constexpr int kSeg = 4;
+constexpr int kTP = 128;
+constexpr int kThreads = kSeg * kTP;
+
 struct SpecArgs {
-  int d_in, dout, n_hot_slots, n_vp, n_hot_dims, n_tape, n_cold_groups, n_cold, max_depth;
+  int d_in, dout, dstride, row, n_hb, n_vp, n_hot_dims, n_nodes, n_cold_groups;
+  int node_seg[kSeg + 1];
+  int cold_seg[kSeg + 1];
+  int block_seg[kSeg + 1];
   const int32_t* hot_dim;
   const int32_t* hot_deg;
   const int32_t* hot_soff;
-  const int32_t* tape;
-  const float* tape_c;
-  const int32_t* cold_dim;
-  const int32_t* cold_gmax;
-  const int32_t* cold_off;
-  const int32_t* cold_ent;
-  const float* cold_c;
+  const int4* node;
+  const float* node_c;
+  const int4* cold;
+  const float2* cold_ab;
+  const int4* blk_dims;
+  const int4* blk_run;
+  const float4* blk_ab;
+  const int4* run;
+  const float* coef;
   const float* fam_a;
   const float* fam_b;
   const int32_t* fam;
@@ -215,20 +232,60 @@ __device__ __forceinline__ void kahan_add(float& sum, float& comp, float v) {
 __constant__ float c_alpha[2][kMaxG];
 __constant__ float c_beta[2][kMaxG];
 
+// s[q] += sum over the run's slots of coef * row value.
 template <int DO>
-__global__ void __launch_bounds__(128) spectral_eval_kernel(SpecArgs a, const double* __restrict__ x, int64_t P,
-                                                            int64_t ldx, float* __restrict__ y, int o0) {
-  extern __shared__ float sm[];
-  const int TP = blockDim.x;
-  float* HB = sm;                              // [n_hot_slots][TP]
-  float* VP = sm + size_t(a.n_hot_slots) * TP; // [n_vp][TP]
-  const int tid = threadIdx.x;
-  const int64_t p = blockIdx.x * int64_t(TP) + tid;
-  const bool live = p < P;
-  const double* xp = x + (live ? p : 0) * ldx;
+__device__ __forceinline__ void dot_run(const float* __restrict__ Rw, const float* __restrict__ coef, int4 r,
+                                        int dstride, int o0, float (&s)[DO]) {
+  const float4* T = reinterpret_cast<const float4*>(Rw + r.x);
+  const int n4 = r.y >> 2;
+  if constexpr (DO == 1) {
+    const float4* Cq = reinterpret_cast<const float4*>(coef + r.z);
+    float s0 = 0.f, s1 = 0.f;
+#pragma unroll 2
+    for (int k = 0; k < n4; ++k) {
+      const float4 t = T[k];
+      const float4 c = __ldg(Cq + k);
+      s0 = fmaf(c.x, t.x, s0);
+      s1 = fmaf(c.y, t.y, s1);
+      s0 = fmaf(c.z, t.z, s0);
+      s1 = fmaf(c.w, t.w, s1);
+    }
+    s[0] += s0 + s1;
+  } else {
+    const float* Cb = coef + r.z + o0;
+    for (int k = 0; k < n4; ++k) {
+      const float4 t = T[k];
+      const float4 c0 = __ldg(reinterpret_cast<const float4*>(Cb + (4 * k + 0) * dstride));
+      const float4 c1 = __ldg(reinterpret_cast<const float4*>(Cb + (4 * k + 1) * dstride));
+      const float4 c2 = __ldg(reinterpret_cast<const float4*>(Cb + (4 * k + 2) * dstride));
+      const float4 c3 = __ldg(reinterpret_cast<const float4*>(Cb + (4 * k + 3) * dstride));
+      const float cs[4][4] = {{c0.x, c0.y, c0.z, c0.w}, {c1.x, c1.y, c1.z, c1.w},
+                              {c2.x, c2.y, c2.z, c2.w}, {c3.x, c3.y, c3.z, c3.w}};
+      const float ts[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+      for (int l = 0; l < 4; ++l)
+#pragma unroll
+        for (int q = 0; q < DO; ++q) s[q] = fmaf(cs[l][q], ts[l], s[q]);
+    }
+  }
+}
 
-  // hot basis table
-  for (int h = 0; h < a.n_hot_dims; ++h) {
+template <int DO>
+__global__ void __launch_bounds__(kThreads, 2) spectral_eval_kernel(SpecArgs a, const double* __restrict__ x,
+                                                                     int64_t P, int64_t ldx, float* __restrict__ y,
+                                                                     int o0) {
+  extern __shared__ __align__(16) float sm[];
+  float* RED = sm + size_t(a.row) * kTP;  // [kSeg][DO][2][kTP]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int seg = warp / (kTP / 32);
+  const int pl = (warp % (kTP / 32)) * 32 + lane;
+  const int64_t p = blockIdx.x * int64_t(kTP) + pl;
+  const bool live = p < P;
+  const double* __restrict__ xp = x + (live ? p : 0) * ldx;
+  float* Rw = sm + size_t(pl) * a.row;
+
+  // phase 0: hot basis values; constant and padding slots
+  for (int h = seg; h < a.n_hot_dims; h += kSeg) {
     const int dim = a.hot_dim[h], g = a.hot_deg[h], so = a.hot_soff[h];
     const int fm = a.fam[dim];
     const float z = fmaf(a.fam_a[dim], float(xp[dim]), a.fam_b[dim]);
@@ -237,93 +294,176 @@ __global__ void __launch_bounds__(128) spectral_eval_kernel(SpecArgs a, const do
       const float pn = c_alpha[fm][n] * z * pc - c_beta[fm][n] * pm1;
       pm1 = pc;
       pc = pn;
-      HB[(so + n) * TP + tid] = pc;
+      Rw[so + n] = pc;
     }
   }
-  VP[tid] = 1.f;  // slot 0: empty prefix
+  if (seg == 0) {
+    Rw[a.n_hb] = 1.f;
+    for (int i = a.n_hb + a.n_vp; i < a.row; ++i) Rw[i] = 0.f;
+  }
   __syncthreads();
 
-  // Accumulation: terms go into `blk` with plain FMAs; every 16 hot entries
-  // and after every cold group `blk` is added to (acc, comp) by compensated
-  // (Kahan) summation, so the rounding of ~1e4 terms stays near 1 ulp.
-  float acc[DO], comp[DO], blk[DO];
+  float acc[DO], comp[DO];
 #pragma unroll
-  for (int q = 0; q < DO; ++q) acc[q] = comp[q] = blk[q] = 0.f;
-  const int nout = min(DO, a.dout - o0);
+  for (int q = 0; q < DO; ++q) acc[q] = comp[q] = 0.f;
 
-  // hot entries, DFS pre-order
-  float st1 = 1.f, st2 = 1.f, st3 = 1.f, st4 = 1.f, st5 = 1.f, st6 = 1.f, st7 = 1.f, st8 = 1.f;
-  for (int e = 0; e < a.n_tape; ++e) {
-    const int w = a.tape[e];
-    const int slot = w & 0xffff;
-    const int depth = (w >> 16) & 0xf;
-    const int vp = w >> 20;
-    const float b = HB[slot * TP + tid];
-    float pr;
-    switch (depth) {
-      case 1: st1 = b; pr = st1; break;
-      case 2: st2 = st1 * b; pr = st2; break;
-      case 3: st3 = st2 * b; pr = st3; break;
-      case 4: st4 = st3 * b; pr = st4; break;
-      case 5: st5 = st4 * b; pr = st5; break;
-      case 6: st6 = st5 * b; pr = st6; break;
-      case 7: st7 = st6 * b; pr = st7; break;
-      default: st8 = st7 * b; pr = st8; break;
+  // phase 1: hot nodes of this segment
+  {
+    float st1 = 1.f, st2 = 1.f, st3 = 1.f, st4 = 1.f, st5 = 1.f, st6 = 1.f, st7 = 1.f, st8 = 1.f;
+    for (int i = a.node_seg[seg]; i < a.node_seg[seg + 1]; ++i) {
+      const int4 nd = __ldg(a.node + i);
+      const int slot = nd.x & 0xffff;
+      const int depth = nd.x >> 16;
+      float v;
+      if (depth == 0) {
+        v = 1.f;
+      } else {
+        const float b = Rw[slot];
+        switch (depth) {
+          case 1: st1 = b; v = st1; break;
+          case 2: st2 = st1 * b; v = st2; break;
+          case 3: st3 = st2 * b; v = st3; break;
+          case 4: st4 = st3 * b; v = st4; break;
+          case 5: st5 = st4 * b; v = st5; break;
+          case 6: st6 = st5 * b; v = st6; break;
+          case 7: st7 = st6 * b; v = st7; break;
+          default: st8 = st7 * b; v = st8; break;
+        }
+      }
+      if (nd.y >= 0) Rw[nd.y] = v;
+      float s[DO];
+#pragma unroll
+      for (int q = 0; q < DO; ++q) s[q] = (q < a.dout - o0) ? __ldg(a.node_c + size_t(i) * a.dstride + o0 + q) : 0.f;
+      for (int r = nd.z; r < nd.w; ++r) dot_run<DO>(Rw, a.coef, __ldg(a.run + r), a.dstride, o0, s);
+#pragma unroll
+      for (int q = 0; q < DO; ++q) kahan_add(acc[q], comp[q], v * s[q]);
     }
-    if (vp) VP[vp * TP + tid] = pr;
-    const float* c = a.tape_c + size_t(e) * a.dout + o0;
-#pragma unroll
-    for (int q = 0; q < DO; ++q)
-      if (q < nout) blk[q] = fmaf(c[q], pr, blk[q]);
-    if ((e & 15) == 15) {
-#pragma unroll
-      for (int q = 0; q < DO; ++q) {
-        kahan_add(acc[q], comp[q], blk[q]);
-        blk[q] = 0.f;
+  }
+  __syncthreads();  // prefix products complete
+
+  // phase 2a: cold blocks of this segment (d_out = 1).  A block is 4 cold
+  // dimensions whose entries all have degree 1, so their contribution is
+  //   sum_j phi_1(z_j) * sum_s c[s][j] * prefix[s]
+  // over one common run of prefix slots: one LDS.128 of prefix products and 4
+  // warp-uniform LDG.128 of coefficients feed 16 FMAs.
+  if constexpr (DO == 1) {
+    const int b0 = a.block_seg[seg], b1 = a.block_seg[seg + 1];
+    float bsum = 0.f;
+    int4 dn = b0 < b1 ? __ldg(a.blk_dims + b0) : make_int4(0, 0, 0, 0);
+    double xn0 = xp[dn.x], xn1 = xp[dn.y], xn2 = xp[dn.z], xn3 = xp[dn.w];
+    for (int bi = b0; bi < b1; ++bi) {
+      const double x0 = xn0, x1 = xn1, x2 = xn2, x3 = xn3;
+      if (bi + 8 < b1) {
+        const int4 pd = __ldg(a.blk_dims + bi + 8);
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(xp + pd.x));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(xp + pd.w));
+      }
+      if (bi + 1 < b1) {
+        dn = __ldg(a.blk_dims + bi + 1);
+        xn0 = xp[dn.x];
+        xn1 = xp[dn.y];
+        xn2 = xp[dn.z];
+        xn3 = xp[dn.w];
+      }
+      const float4 ca = __ldg(a.blk_ab + 2 * bi), cb = __ldg(a.blk_ab + 2 * bi + 1);
+      const int4 rr = __ldg(a.blk_run + bi);
+      const float4* T = reinterpret_cast<const float4*>(Rw + rr.x);
+      const float4* Cq = reinterpret_cast<const float4*>(a.coef + rr.z);
+      float u0 = 0.f, u1 = 0.f, u2 = 0.f, u3 = 0.f;
+      for (int k = 0; k < rr.y; ++k) {
+        const float4 t = T[k];
+        const float4 c0 = __ldg(Cq + 4 * k + 0), c1 = __ldg(Cq + 4 * k + 1);
+        const float4 c2 = __ldg(Cq + 4 * k + 2), c3 = __ldg(Cq + 4 * k + 3);
+        u0 = fmaf(c0.x, t.x, u0); u1 = fmaf(c0.y, t.x, u1); u2 = fmaf(c0.z, t.x, u2); u3 = fmaf(c0.w, t.x, u3);
+        u0 = fmaf(c1.x, t.y, u0); u1 = fmaf(c1.y, t.y, u1); u2 = fmaf(c1.z, t.y, u2); u3 = fmaf(c1.w, t.y, u3);
+        u0 = fmaf(c2.x, t.z, u0); u1 = fmaf(c2.y, t.z, u1); u2 = fmaf(c2.z, t.z, u2); u3 = fmaf(c2.w, t.z, u3);
+        u0 = fmaf(c3.x, t.w, u0); u1 = fmaf(c3.y, t.w, u1); u2 = fmaf(c3.z, t.w, u2); u3 = fmaf(c3.w, t.w, u3);
+      }
+      float v = fmaf(ca.x, float(x0), cb.x) * u0;
+      v = fmaf(fmaf(ca.y, float(x1), cb.y), u1, v);
+      v = fmaf(fmaf(ca.z, float(x2), cb.z), u2, v);
+      v = fmaf(fmaf(ca.w, float(x3), cb.w), u3, v);
+      bsum += v;
+      if (((bi - b0) & 3) == 3) {
+        kahan_add(acc[0], comp[0], bsum);
+        bsum = 0.f;
       }
     }
+    kahan_add(acc[0], comp[0], bsum);
   }
+
+  // phase 2: cold groups of this segment.  Group descriptor: (dim, first
+  // run, end run, max degree | family << 8), affine map (a, b); runs carry
+  // their degree in .w and are sorted by it.  The x column of group gi + 16
+  // is prefetched into L2, the one of group gi + 1 into registers.
+  {
+    const int g0 = a.cold_seg[seg], g1 = a.cold_seg[seg + 1];
+    int4 cg = g0 < g1 ? __ldg(a.cold + g0) : make_int4(0, 0, 0, 0);
+    double xn = g0 < g1 ? xp[cg.x] : 0.0;
+    float blk[DO];
+#pragma unroll
+    for (int q = 0; q < DO; ++q) blk[q] = 0.f;
+    for (int gi = g0; gi < g1; ++gi) {
+      const int4 cur = cg;
+      const double xv = xn;
+      const float2 ab = __ldg(a.cold_ab + gi);
+      if (gi + 16 < g1) {
+        const double* pf = xp + __ldg(&a.cold[gi + 16].x);
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(pf));
+      }
+      if (gi + 1 < g1) {
+        cg = __ldg(a.cold + gi + 1);
+        xn = xp[cg.x];
+      }
+      const int fm = cur.w >> 8;
+      const float z = fmaf(ab.x, float(xv), ab.y);
+      float pm1 = 0.f, pc = 1.f;
+      int gcur = 0;
+      for (int r = cur.y; r < cur.z; ++r) {
+        const int4 rr = __ldg(a.run + r);
+        while (gcur < rr.w) {
+          const float pn = c_alpha[fm][gcur] * z * pc - c_beta[fm][gcur] * pm1;
+          pm1 = pc;
+          pc = pn;
+          ++gcur;
+        }
+        float s[DO];
+#pragma unroll
+        for (int q = 0; q < DO; ++q) s[q] = 0.f;
+        dot_run<DO>(Rw, a.coef, rr, a.dstride, o0, s);
+#pragma unroll
+        for (int q = 0; q < DO; ++q) blk[q] = fmaf(pc, s[q], blk[q]);
+      }
+      if (((gi - g0) & 3) == 3) {
+#pragma unroll
+        for (int q = 0; q < DO; ++q) {
+          kahan_add(acc[q], comp[q], blk[q]);
+          blk[q] = 0.f;
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < DO; ++q) kahan_add(acc[q], comp[q], blk[q]);
+  }
+
+  // phase 3: combine the segments
 #pragma unroll
   for (int q = 0; q < DO; ++q) {
-    kahan_add(acc[q], comp[q], blk[q]);
-    blk[q] = 0.f;
+    RED[((seg * DO + q) * 2 + 0) * kTP + pl] = acc[q];
+    RED[((seg * DO + q) * 2 + 1) * kTP + pl] = comp[q];
   }
-  // VP entries are written and read by the same thread only: no barrier needed.
-
-  // cold entries, grouped by cold dimension
-  for (int gi = 0; gi < a.n_cold_groups; ++gi) {
-    const int dim = a.cold_dim[gi], gmax = a.cold_gmax[gi];
-    const int fm = a.fam[dim];
-    const float z = fmaf(a.fam_a[dim], float(xp[dim]), a.fam_b[dim]);
-    float phi[kMaxG];
-    float pm1 = 0.f, pc = 1.f;
-#pragma unroll 4
-    for (int n = 0; n < gmax; ++n) {
-      const float pn = c_alpha[fm][n] * z * pc - c_beta[fm][n] * pm1;
-      pm1 = pc;
-      pc = pn;
-      phi[n] = pc;
-    }
-    for (int c = a.cold_off[gi]; c < a.cold_off[gi + 1]; ++c) {
-      const int w = a.cold_ent[c];
-      const int vp = w & 0xffffff;
-      const int g = w >> 24;
-      const float t = VP[vp * TP + tid] * phi[g - 1];
-      const float* cc = a.cold_c + size_t(c) * a.dout + o0;
-#pragma unroll
-      for (int q = 0; q < DO; ++q)
-        if (q < nout) blk[q] = fmaf(cc[q], t, blk[q]);
-    }
+  __syncthreads();
+  if (seg == 0 && live) {
 #pragma unroll
     for (int q = 0; q < DO; ++q) {
-      kahan_add(acc[q], comp[q], blk[q]);
-      blk[q] = 0.f;
+      if (q >= a.dout - o0) continue;
+      float s = 0.f, cp = 0.f;
+      for (int r = 0; r < kSeg; ++r) {
+        kahan_add(s, cp, RED[((r * DO + q) * 2 + 0) * kTP + pl]);
+        kahan_add(s, cp, -RED[((r * DO + q) * 2 + 1) * kTP + pl]);
+      }
+      y[p * a.dout + o0 + q] = a.c0[o0 + q] + (s - cp);
     }
-  }
-  if (live) {
-#pragma unroll
-    for (int q = 0; q < DO; ++q)
-      if (q < nout) y[p * a.dout + o0 + q] = a.c0[o0 + q] + (acc[q] - comp[q]);
   }
 }
 
@@ -394,52 +534,74 @@ extern "C" int smx_spectral_eval(const smx_spectral* sp, const double* x, int64_
   SMX_REQUIRE(sp != nullptr, "smx_spectral_eval: null plan");
   SMX_REQUIRE(P >= 0 && ldx >= sp->d_in && sp->d_out >= 1, "smx_spectral_eval: bad sizes");
   if (P == 0) return SMX_OK;
-  SMX_REQUIRE(x && y && sp->c0 && sp->fam && sp->fam_a && sp->fam_b, "smx_spectral_eval: null pointer");
-  SMX_REQUIRE(sp->max_depth <= 8, "smx_spectral_eval: hot entries deeper than 8 are not supported");
+  SMX_REQUIRE(x && y && sp->c0 && sp->fam && sp->fam_a && sp->fam_b && sp->node && sp->node_c,
+              "smx_spectral_eval: null pointer");
+  SMX_REQUIRE(sp->max_depth <= 8, "smx_spectral_eval: hot nodes deeper than 8 are not supported");
+  SMX_REQUIRE(sp->row % 4 == 0 && sp->row >= sp->n_hb + sp->n_vp && sp->n_vp >= 1, "smx_spectral_eval: bad row");
+  SMX_REQUIRE(sp->d_out == 1 || sp->dstride % 4 == 0, "smx_spectral_eval: coefficient stride not 4-aligned");
+  for (int i = 0; i < kSeg; ++i) {
+    SMX_REQUIRE(sp->node_seg[i] <= sp->node_seg[i + 1] && sp->cold_seg[i] <= sp->cold_seg[i + 1],
+                "smx_spectral_eval: segments not ordered");
+  }
+  SMX_REQUIRE(sp->node_seg[0] == 0 && sp->node_seg[kSeg] == sp->n_nodes && sp->cold_seg[0] == 0 &&
+                  sp->cold_seg[kSeg] == sp->n_cold_groups && sp->block_seg[0] == 0 &&
+                  sp->block_seg[kSeg] == sp->n_cold_blocks,
+              "smx_spectral_eval: segments do not cover the plan");
+  SMX_REQUIRE(sp->n_cold_blocks == 0 || (sp->d_out == 1 && sp->blk_dims && sp->blk_run && sp->blk_ab),
+              "smx_spectral_eval: cold blocks need d_out = 1");
+  for (int i = 0; i < kSeg; ++i)
+    SMX_REQUIRE(sp->block_seg[i] <= sp->block_seg[i + 1], "smx_spectral_eval: block segments not ordered");
   int rc = upload_consts();
   if (rc) return rc;
   SpecArgs a;
   a.d_in = sp->d_in;
   a.dout = sp->d_out;
-  a.n_hot_slots = sp->n_hot_slots;
+  a.dstride = sp->dstride;
+  a.row = sp->row;
+  a.n_hb = sp->n_hb;
   a.n_vp = sp->n_vp;
   a.n_hot_dims = sp->n_hot_dims;
-  a.n_tape = sp->n_tape;
+  a.n_nodes = sp->n_nodes;
   a.n_cold_groups = sp->n_cold_groups;
-  a.n_cold = sp->n_cold;
-  a.max_depth = sp->max_depth;
+  for (int i = 0; i <= kSeg; ++i) {
+    a.node_seg[i] = sp->node_seg[i];
+    a.cold_seg[i] = sp->cold_seg[i];
+    a.block_seg[i] = sp->block_seg[i];
+  }
   a.hot_dim = sp->hot_dim;
   a.hot_deg = sp->hot_deg;
   a.hot_soff = sp->hot_soff;
-  a.tape = sp->tape;
-  a.tape_c = sp->tape_c;
-  a.cold_dim = sp->cold_dim;
-  a.cold_gmax = sp->cold_gmax;
-  a.cold_off = sp->cold_off;
-  a.cold_ent = sp->cold_ent;
-  a.cold_c = sp->cold_c;
+  a.node = reinterpret_cast<const int4*>(sp->node);
+  a.node_c = sp->node_c;
+  a.cold = reinterpret_cast<const int4*>(sp->cold);
+  a.cold_ab = reinterpret_cast<const float2*>(sp->cold_ab);
+  a.blk_dims = reinterpret_cast<const int4*>(sp->blk_dims);
+  a.blk_run = reinterpret_cast<const int4*>(sp->blk_run);
+  a.blk_ab = reinterpret_cast<const float4*>(sp->blk_ab);
+  a.run = reinterpret_cast<const int4*>(sp->run);
+  a.coef = sp->coef;
   a.fam_a = sp->fam_a;
   a.fam_b = sp->fam_b;
   a.fam = sp->fam;
   a.c0 = sp->c0;
-  const int TP = 128;
-  const size_t smem = size_t(sp->n_hot_slots + sp->n_vp) * TP * sizeof(float);
-  SMX_REQUIRE(smem <= 220 * 1024, "smx_spectral_eval: hot table too large for shared memory");
+  const int DO = sp->d_out == 1 ? 1 : 4;
+  const size_t smem = (size_t(sp->row) + size_t(kSeg) * DO * 2) * kTP * sizeof(float);
+  SMX_REQUIRE(smem <= 220 * 1024, "smx_spectral_eval: per-point row too large for shared memory");
   cudaStream_t st = smx::as_stream(stream);
   static bool attr_set[2] = {false, false};
-  for (int o0 = 0; o0 < sp->d_out; o0 += 4) {
-    if (sp->d_out == 1) {
+  for (int o0 = 0; o0 < sp->d_out; o0 += DO) {
+    if (DO == 1) {
       if (!attr_set[0]) {
         cudaFuncSetAttribute(spectral_eval_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
         attr_set[0] = true;
       }
-      spectral_eval_kernel<1><<<smx::grid_for(P, TP), TP, smem, st>>>(a, x, P, ldx, y, o0);
+      spectral_eval_kernel<1><<<smx::grid_for(P, kTP), kThreads, smem, st>>>(a, x, P, ldx, y, o0);
     } else {
       if (!attr_set[1]) {
         cudaFuncSetAttribute(spectral_eval_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
         attr_set[1] = true;
       }
-      spectral_eval_kernel<4><<<smx::grid_for(P, TP), TP, smem, st>>>(a, x, P, ldx, y, o0);
+      spectral_eval_kernel<4><<<smx::grid_for(P, kTP), kThreads, smem, st>>>(a, x, P, ldx, y, o0);
     }
     SMX_LAUNCH_CHECK("smx_spectral_eval");
   }

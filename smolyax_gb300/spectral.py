@@ -66,92 +66,41 @@ class SpectralPlan:
         self.C64 = C.view(n_lam, d_out)
         del G, ids, A
 
-        # layout: hot dimensions, hot tape (pre-order), cold groups
-        level = tree.level_of()
-        parent = tree.parent.long()
-        dim = tree.dim.long()
-        deg = tree.deg.long()
-        nonroot = torch.arange(1, n_lam, device=dev)
-        inner = nonroot[parent[nonroot] > 0]  # entries whose parent is not the root
-        hot = torch.zeros(d, dtype=torch.bool, device=dev)
-        if inner.numel():
-            hot[dim[parent[inner]]] = True
-        maxdeg = torch.as_tensor(ip._maxdeg, device=dev)
-        hot_dims = torch.nonzero(hot).flatten()
-        hot_deg = maxdeg[hot_dims]
-        hot_soff = torch.zeros_like(hot_deg)
-        if hot_dims.numel() > 1:
-            hot_soff[1:] = torch.cumsum(hot_deg, 0)[:-1]
-        n_hot_slots = int(hot_deg.sum().item()) if hot_dims.numel() else 0
-        hot_index = torch.full((d,), -1, dtype=torch.long, device=dev)
-        hot_index[hot_dims] = torch.arange(hot_dims.numel(), device=dev)
-
-        is_hot_e = torch.zeros(n_lam, dtype=torch.bool, device=dev)
-        is_hot_e[nonroot] = hot[dim[nonroot]]
-        hot_e = nonroot[is_hot_e[nonroot]]
-        cold_e = nonroot[~is_hot_e[nonroot]]
-        # prefix products needed by cold entries: their parents (excluding the root)
-        vp_index = torch.zeros(n_lam, dtype=torch.long, device=dev)
-        if cold_e.numel():
-            par = torch.unique(parent[cold_e])
-            par = par[par > 0]
-            vp_index[par] = torch.arange(1, par.numel() + 1, device=dev)
-            n_vp = int(par.numel()) + 1
-        else:
-            n_vp = 1
-        if n_vp >= 4096:
-            raise RuntimeError("too many stored prefixes (%d) for the FP32 evaluator" % n_vp)
-        # pre-order of hot entries
-        rank = tree.rank(capi.SMX_MODE_PREORDER)
-        hot_e = hot_e[torch.argsort(rank[hot_e])]
-        depth = level[hot_e]
-        max_depth = int(depth.max().item()) if hot_e.numel() else 0
-        if max_depth > 8:
-            raise RuntimeError("hot multi-indices deeper than 8 are not supported by the FP32 evaluator")
-        slot = hot_soff[hot_index[dim[hot_e]]] + deg[hot_e] - 1
-        tape = (slot | (depth << 16) | (vp_index[hot_e] << 20)).to(torch.int32)
-        # cold entries grouped by (dim, deg)
-        if cold_e.numel():
-            key = dim[cold_e] * 64 + deg[cold_e]
-            cold_e = cold_e[torch.argsort(key, stable=True)]
-            cd = dim[cold_e]
-            groups, counts = torch.unique_consecutive(cd, return_counts=True)
-            cold_off = torch.zeros(groups.numel() + 1, dtype=torch.long, device=dev)
-            cold_off[1:] = torch.cumsum(counts, 0)
-            gmax = maxdeg[groups]
-            cold_ent = (vp_index[parent[cold_e]] | (deg[cold_e] << 24)).to(torch.int32)
-        else:
-            groups = torch.zeros(0, dtype=torch.long, device=dev)
-            cold_off = torch.zeros(1, dtype=torch.long, device=dev)
-            gmax = torch.zeros(0, dtype=torch.long, device=dev)
-            cold_ent = torch.zeros(0, dtype=torch.int32, device=dev)
-        C32 = self.C64.float()
+        # layout for the FP32 evaluator (host construction from the device tree)
+        tree_np = dict(
+            parent=tree.parent.cpu().numpy().astype(np.int64),
+            dim=tree.dim.cpu().numpy().astype(np.int64),
+            deg=tree.deg.cpu().numpy().astype(np.int64),
+            level=tree.level_of().cpu().numpy(),
+            rank=tree.rank(capi.SMX_MODE_PREORDER).cpu().numpy(),
+            rem=tree.rem.cpu().numpy(),
+        )
+        C32 = self.C64.float().cpu().numpy()
+        lay = build_layout(tree_np, C32, np.asarray(ip._maxdeg), d, d_out, fam, fa, fb)
+        self.layout = lay
         k = self.keep
-        k["hot_dim"] = hot_dims.to(torch.int32).contiguous()
-        k["hot_deg"] = hot_deg.to(torch.int32).contiguous()
-        k["hot_soff"] = hot_soff.to(torch.int32).contiguous()
-        k["tape"] = tape.contiguous()
-        k["tape_c"] = C32[hot_e].contiguous()
-        k["cold_dim"] = groups.to(torch.int32).contiguous()
-        k["cold_gmax"] = gmax.to(torch.int32).contiguous()
-        k["cold_off"] = cold_off.to(torch.int32).contiguous()
-        k["cold_ent"] = cold_ent.contiguous()
-        k["cold_c"] = C32[cold_e].contiguous()
+        for name in ("hot_dim", "hot_deg", "hot_soff", "node", "cold", "run", "blk_dims", "blk_run"):
+            k[name] = T(lay[name], torch.int32)
+        for name in ("node_c", "coef", "cold_ab", "blk_ab"):
+            k[name] = T(lay[name], torch.float32)
         k["fam_a"] = self.fa64.float().contiguous()
         k["fam_b"] = self.fb64.float().contiguous()
         k["fam"] = self.fam
-        k["c0"] = C32[0].contiguous()
+        k["c0"] = T(C32[0], torch.float32)
         s = capi.SmxSpectral()
         s.d_in, s.d_out = d, d_out
-        s.n_hot_slots, s.n_vp, s.n_hot_dims = n_hot_slots, n_vp, int(hot_dims.numel())
-        s.n_tape, s.n_cold_groups, s.n_cold = int(hot_e.numel()), int(groups.numel()), int(cold_e.numel())
-        s.max_depth = max_depth
-        for name in ("hot_dim", "hot_deg", "hot_soff", "tape", "tape_c", "cold_dim", "cold_gmax", "cold_off",
-                     "cold_ent", "cold_c", "fam_a", "fam_b", "fam", "c0"):
+        for name in ("dstride", "row", "n_hb", "n_vp", "n_hot_dims", "n_nodes", "n_cold_groups", "max_depth",
+                     "n_cold_blocks"):
+            setattr(s, name, int(lay[name]))
+        for i in range(5):
+            s.node_seg[i] = int(lay["node_seg"][i])
+            s.cold_seg[i] = int(lay["cold_seg"][i])
+            s.block_seg[i] = int(lay["block_seg"][i])
+        for name in ("hot_dim", "hot_deg", "hot_soff", "node", "node_c", "cold", "cold_ab", "run", "coef", "fam_a",
+                     "fam_b", "fam", "c0", "blk_dims", "blk_run", "blk_ab"):
             t = k[name]
             setattr(s, name, t.data_ptr() if t.numel() else None)
         self.c = s
-        self.hot_e, self.cold_e = hot_e, cold_e
 
     def ref(self):
         import ctypes
@@ -163,3 +112,255 @@ class SpectralPlan:
         st = capi.stream_ptr(torch.cuda.current_stream())
         call("smx_spectral_eval", self.ref(), ptr(x), int(x.shape[0]), int(x.shape[1]), ptr(y), st)
         return y
+
+
+def _round4(v):
+    return (int(v) + 3) // 4 * 4
+
+
+class _Runs:
+    """Accumulates runs (4-aligned slot ranges with contiguous coefficients)."""
+
+    def __init__(self, dstride):
+        self.dstride = dstride
+        self.tab = []
+        self.coef = []
+        self.ncoef = 0
+
+    def add(self, slots, coefs, max_gap=4, degree=0):
+        """slots: increasing row slots; coefs: [len(slots), d_out]. Returns (r0, r1)."""
+        r0 = len(self.tab)
+        i = 0
+        n = len(slots)
+        while i < n:
+            j = i + 1
+            while j < n and slots[j] - slots[j - 1] <= max_gap:
+                j += 1
+            a0 = int(slots[i]) & ~3
+            length = _round4(int(slots[j - 1]) + 1 - a0)
+            blk = np.zeros((length, self.dstride), dtype=np.float32)
+            blk[np.asarray(slots[i:j]) - a0, : coefs.shape[1]] = coefs[i:j]
+            self.tab.append((a0, length, self.ncoef, degree))
+            self.coef.append(blk.ravel())
+            self.ncoef += blk.size
+            i = j
+        return r0, len(self.tab)
+
+
+def build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb, nseg=4):
+    """Layout of the FP32 evaluator (see ``csrc/spectral.cu``) from the index-set
+    tree (host arrays: parent, dim, deg, level, pre-order rank, remaining budget)
+    and the FP32 coefficients C[entry, d_out]; fam/fa/fb are the per-dimension
+    polynomial family and affine map to its variable."""
+    parent, dim, deg, level, rank, rem = (tr[key] for key in ("parent", "dim", "deg", "level", "rank", "rem"))
+    n = parent.shape[0]
+    dstride = 1 if d_out == 1 else _round4(d_out)
+    nonroot = np.arange(1, n)
+    hot = np.zeros(d, dtype=bool)
+    inner = nonroot[parent[nonroot] > 0]
+    hot[dim[parent[inner]]] = True
+    hot_dims = np.nonzero(hot)[0]
+    hot_deg = maxdeg[hot_dims].astype(np.int64)
+    hot_soff = np.concatenate([[0], np.cumsum(hot_deg)[:-1]]).astype(np.int64) if hot_dims.size else np.zeros(0, np.int64)
+    n_hb = int(hot_deg.sum())
+    hot_index = np.full(d, -1, dtype=np.int64)
+    hot_index[hot_dims] = np.arange(hot_dims.size)
+    is_hot = np.zeros(n, dtype=bool)
+    is_hot[0] = True
+    is_hot[nonroot] = hot[dim[nonroot]]
+    cold_e = nonroot[~is_hot[nonroot]]
+    hot_e = nonroot[is_hot[nonroot]]
+    slot = np.full(n, -1, dtype=np.int64)
+    slot[hot_e] = hot_soff[hot_index[dim[hot_e]]] + deg[hot_e] - 1
+    has_hot_child = np.zeros(n, dtype=bool)
+    has_hot_child[parent[hot_e]] = True
+    has_cold_child = np.zeros(n, dtype=bool)
+    has_cold_child[parent[cold_e]] = True
+    node_mask = is_hot & (has_hot_child | has_cold_child)
+    node_mask[0] = True
+    nodes = np.nonzero(node_mask)[0]
+    nodes = nodes[np.argsort(rank[nodes], kind="stable")]
+    # prefix-product slots, ordered by remaining budget (descending): the
+    # prefixes admissible for a cold pair are then (mostly) a leading range
+    S = np.nonzero(has_cold_child)[0]
+    S = S[S != 0]
+    S = S[np.argsort(-rem[S], kind="stable")]
+    vp_row = np.full(n, -1, dtype=np.int64)
+    vp_row[0] = n_hb
+    vp_row[S] = n_hb + 1 + np.arange(S.size)
+    n_vp = 1 + S.size
+    row = _round4(n_hb + n_vp)
+    while row % 32 != 4:
+        row += 4
+    runs = _Runs(dstride)
+    # leaf children of each node, sorted by slot
+    leaf_e = hot_e[~node_mask[hot_e]]
+    order = np.lexsort((slot[leaf_e], parent[leaf_e]))
+    leaf_e = leaf_e[order]
+    lp = parent[leaf_e]
+    starts = np.searchsorted(lp, nodes, side="left")
+    ends = np.searchsorted(lp, nodes, side="right")
+    node_tab = np.zeros((nodes.size, 4), dtype=np.int64)
+    node_c = np.zeros((nodes.size, dstride), dtype=np.float32)
+    cost_nodes = np.zeros(nodes.size)
+    max_depth = int(level[nodes].max()) if nodes.size else 0
+    for i, e in enumerate(nodes):
+        le = leaf_e[starts[i] : ends[i]]
+        r0, r1 = runs.add(slot[le], C[le])
+        sl = int(slot[e]) if e != 0 else 0
+        node_tab[i] = (sl | (int(level[e]) << 16), int(vp_row[e]) if e != 0 and vp_row[e] >= 0 else -1, r0, r1)
+        if e != 0:  # the root's coefficient is added once, as c0, by the evaluator
+            node_c[i, :d_out] = C[e]
+        cost_nodes[i] = 12 + sum(t[1] for t in runs.tab[r0:r1]) / 4.0 * (1 + d_out)
+    # cold dimensions: entries sorted by (dim, deg, prefix slot)
+    ce = cold_e[np.lexsort((vp_row[parent[cold_e]], deg[cold_e], dim[cold_e]))] if cold_e.size else cold_e
+    bounds = []
+    i = 0
+    while i < ce.size:
+        j = i
+        while j < ce.size and dim[ce[j]] == dim[ce[i]]:
+            j += 1
+        bounds.append((i, j))
+        i = j
+    simple = [b for b in bounds if d_out == 1 and np.all(deg[ce[b[0] : b[1]]] == 1)]
+    general = [b for b in bounds if not (d_out == 1 and np.all(deg[ce[b[0] : b[1]]] == 1))]
+    alpha0 = np.where(np.asarray(fam) == 0, 1.0, np.sqrt(2.0))
+    # blocks of 4 degree-1 cold dimensions sharing one run of prefix slots
+    blk_dims, blk_run, blk_ab, cost_blk = [], [], [], []
+    for q in range(0, len(simple), 4):
+        part = simple[q : q + 4]
+        dims4 = [int(dim[ce[b0]]) for b0, _ in part]
+        slots = np.unique(np.concatenate([vp_row[parent[ce[b0:b1]]] for b0, b1 in part]))
+        a0 = int(slots[0]) & ~3
+        n4 = (_round4(int(slots[-1]) + 1) - a0) // 4
+        blk = np.zeros((n4 * 4, 4), dtype=np.float32)  # [slot][dim]
+        for jj, (b0, b1) in enumerate(part):
+            e = ce[b0:b1]
+            blk[vp_row[parent[e]] - a0, jj] = C[e, 0]
+        ab = np.zeros((2, 4), dtype=np.float32)
+        for jj, dd in enumerate(dims4):
+            ab[0, jj] = alpha0[dd] * fa[dd]
+            ab[1, jj] = alpha0[dd] * fb[dd]
+        while len(dims4) < 4:
+            dims4.append(dims4[0])
+        blk_dims.append(dims4)
+        blk_run.append((a0, n4, runs.ncoef, 0))
+        runs.coef.append(blk.ravel())
+        runs.ncoef += blk.size
+        blk_ab.append(ab.ravel())
+        cost_blk.append(16.0 + 9.0 * n4)
+    # general cold groups: runs carry the degree
+    cold_tab, cold_ab, cost_cold = [], [], []
+    for i, j in general:
+        dd = dim[ce[i]]
+        r_first = len(runs.tab)
+        c = 8.0
+        q = i
+        while q < j:
+            g = deg[ce[q]]
+            q2 = q
+            while q2 < j and deg[ce[q2]] == g:
+                q2 += 1
+            grp = ce[q:q2]
+            r0, r1 = runs.add(vp_row[parent[grp]], C[grp], degree=int(g))
+            c += sum(3 + t[1] / 4.0 * (1 + d_out) for t in runs.tab[r0:r1])
+            q = q2
+        cold_tab.append((int(dd), r_first, len(runs.tab), int(deg[ce[i:j]].max()) | (int(fam[dd]) << 8)))
+        cold_ab.append((fa[dd], fb[dd]))
+        cost_cold.append(c)
+
+    def cuts(cost, allowed):
+        tot = float(np.sum(cost))
+        cum = np.concatenate([[0.0], np.cumsum(cost)])
+        out = [0]
+        for k in range(1, nseg):
+            want = tot * k / nseg
+            cand = [a for a in allowed if a >= out[-1]]
+            out.append(min(cand, key=lambda a: abs(cum[a] - want)) if cand else out[-1])
+        out.append(len(cost))
+        return out
+
+    allowed_nodes = [i for i in range(nodes.size + 1) if i == nodes.size or level[nodes[i]] <= 1]
+    node_seg = cuts(cost_nodes, allowed_nodes)
+    cold_seg = cuts(np.asarray(cost_cold), list(range(len(cost_cold) + 1)))
+    block_seg = cuts(np.asarray(cost_blk), list(range(len(cost_blk) + 1)))
+    as_i32 = lambda v, w: np.asarray(v, dtype=np.int64).reshape(-1, w).astype(np.int32)
+    return dict(
+        dstride=dstride, row=row, n_hb=n_hb, n_vp=n_vp, n_hot_dims=int(hot_dims.size), n_nodes=int(nodes.size),
+        n_cold_groups=len(cold_tab), max_depth=max_depth, node_seg=node_seg, cold_seg=cold_seg,
+        n_cold_blocks=len(blk_dims), block_seg=block_seg,
+        blk_dims=as_i32(blk_dims, 4) if blk_dims else np.zeros((0, 4), np.int32),
+        blk_run=as_i32(blk_run, 4) if blk_run else np.zeros((0, 4), np.int32),
+        blk_ab=np.asarray(blk_ab, dtype=np.float32).reshape(-1, 8),
+        cold_ab=np.asarray(cold_ab, dtype=np.float32).reshape(-1, 2),
+        hot_dim=hot_dims.astype(np.int32), hot_deg=hot_deg.astype(np.int32), hot_soff=hot_soff.astype(np.int32),
+        node=as_i32(node_tab, 4), node_c=node_c, cold=as_i32(cold_tab, 4) if cold_tab else np.zeros((0, 4), np.int32),
+        run=as_i32(runs.tab, 4) if runs.tab else np.zeros((0, 4), np.int32),
+        coef=np.concatenate(runs.coef) if runs.coef else np.zeros(4, np.float32),
+        cost=dict(nodes=float(cost_nodes.sum()), cold=float(np.sum(cost_cold)), blocks=float(np.sum(cost_blk)),
+                  runs=len(runs.tab), coef_floats=int(runs.ncoef), node_seg=node_seg, cold_seg=cold_seg,
+                  block_seg=block_seg),
+    )
+
+
+def evaluate_layout(lay, x, fam, fa, fb, c0):
+    """Host FP64 evaluation of a layout: the kernel's arithmetic, for testing the builder."""
+    P = x.shape[0]
+    d_out = c0.shape[0]
+    ds = lay["dstride"]
+    out = np.tile(np.asarray(c0, dtype=float), (P, 1))
+
+    def phis(dim, g):
+        z = fa[dim] * x[:, dim] + fb[dim]
+        vals, pm1, pc = [], np.zeros(P), np.ones(P)
+        for m in range(g):
+            if fam[dim] == 0:
+                al, be = (2 * m + 1) / (m + 1), m / (m + 1)
+            else:
+                al, be = np.sqrt(2 / (m + 1)), np.sqrt(m / (m + 1))
+            pm1, pc = pc, al * z * pc - be * pm1
+            vals.append(pc)
+        return vals
+
+    R = np.zeros((P, lay["row"]))
+    for h in range(lay["n_hot_dims"]):
+        vals = phis(int(lay["hot_dim"][h]), int(lay["hot_deg"][h]))
+        for m, v in enumerate(vals):
+            R[:, lay["hot_soff"][h] + m] = v
+    R[:, lay["n_hb"]] = 1.0
+
+    def dot(r0, r1):
+        s = np.zeros((P, d_out))
+        for r in range(r0, r1):
+            st, ln, co, _ = lay["run"][r]
+            blk = lay["coef"][co : co + ln * ds].reshape(ln, ds)[:, :d_out].astype(float)
+            s += R[:, st : st + ln] @ blk
+        return s
+
+    stack = [np.ones(P)] * 9
+    for i in range(lay["n_nodes"]):
+        w, vp, r0, r1 = lay["node"][i]
+        depth, sl = int(w) >> 16, int(w) & 0xFFFF
+        if depth == 0:
+            v = np.ones(P)
+        else:
+            v = stack[depth - 1] * R[:, sl]
+            stack[depth] = v
+        if vp >= 0:
+            R[:, vp] = v
+        out += v[:, None] * (lay["node_c"][i, :d_out][None, :] + dot(r0, r1))
+    for bi in range(lay["n_cold_blocks"]):
+        dims4 = lay["blk_dims"][bi]
+        a0, n4, co, _ = lay["blk_run"][bi]
+        blk = lay["coef"][co : co + 16 * n4].reshape(4 * n4, 4).astype(float)
+        u = R[:, a0 : a0 + 4 * n4] @ blk  # (P, 4)
+        ab = lay["blk_ab"][bi].reshape(2, 4)
+        phi = np.stack([ab[0, j] * x[:, dims4[j]] + ab[1, j] for j in range(4)], axis=1)
+        out[:, 0] += np.sum(phi * u, axis=1)
+    for gi in range(lay["n_cold_groups"]):
+        dd, r0, r1, gmax = lay["cold"][gi]
+        vals = phis(int(dd), int(gmax) & 0xFF)
+        for r in range(r0, r1):
+            out += vals[lay["run"][r][3] - 1][:, None] * dot(r, r + 1)
+    return out
+

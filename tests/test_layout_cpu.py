@@ -1,0 +1,99 @@
+"""Host logic of the FP32 evaluator's layout (no GPU needed).
+
+A small index-set tree is built in Python with the same entry layout as the
+device enumeration (root first, children by dimension then degree, parent
+ids, remaining budget, pre-order rank); random coefficients are laid out by
+``build_layout`` and the run-based evaluation (host FP64 replay of the
+kernel's arithmetic) is compared with the direct sum over the index set.
+"""
+import numpy as np
+import pytest
+
+from smolyax_gb300.spectral import build_layout, evaluate_layout
+
+
+def python_tree(k, t):
+    d = len(k)
+    ent = [dict(rem=t, start=0, parent=-1, dim=-1, deg=0, level=0)]
+    cur = [0]
+    while cur:
+        nxt = []
+        for e in cur:
+            E = ent[e]
+            i = E["start"]
+            if i < d:
+                while True:
+                    j = 1
+                    while j * k[i] < E["rem"]:
+                        nxt.append(dict(rem=E["rem"] - j * k[i], start=i + 1, parent=e, dim=i, deg=j,
+                                        level=E["level"] + 1))
+                        j += 1
+                    if i + 1 < d and k[i + 1] < E["rem"]:
+                        i += 1
+                    else:
+                        break
+        base = len(ent)
+        ent.extend(nxt)
+        cur = list(range(base, len(ent)))
+    n = len(ent)
+    children = [[] for _ in range(n)]
+    for e in range(1, n):
+        children[ent[e]["parent"]].append(e)
+    rank = np.zeros(n, dtype=np.int64)
+    order = []
+
+    def visit(e):
+        order.append(e)
+        for c in children[e]:
+            visit(c)
+
+    visit(0)
+    rank[np.array(order)] = np.arange(n)
+    arr = lambda key: np.array([E[key] for E in ent])
+    return dict(parent=arr("parent"), dim=arr("dim"), deg=arr("deg"), level=arr("level"), rank=rank,
+                rem=arr("rem").astype(float))
+
+
+def direct(tr, C, x, fam, fa, fb):
+    n = tr["parent"].shape[0]
+    P = x.shape[0]
+    vals = np.ones((n, P))
+    for e in range(1, n):
+        dd, g = tr["dim"][e], tr["deg"][e]
+        z = fa[dd] * x[:, dd] + fb[dd]
+        pm1, pc = np.zeros(P), np.ones(P)
+        for m in range(g):
+            al, be = ((2 * m + 1) / (m + 1), m / (m + 1)) if fam[dd] == 0 else (np.sqrt(2 / (m + 1)), np.sqrt(m / (m + 1)))
+            pm1, pc = pc, al * z * pc - be * pm1
+        vals[e] = vals[tr["parent"][e]] * pc
+    return vals.T @ C
+
+
+@pytest.mark.parametrize("d,t,d_out,fam_id", [(3, 4.5, 1, 0), (6, 5.0, 2, 1), (12, 6.0, 1, 0), (40, 5.5, 3, 0),
+                                               (60, 5.8, 1, 1), (200, 6.5, 1, 0)])
+def test_layout_matches_direct_sum(d, t, d_out, fam_id):
+    k = list(np.log((2 + np.arange(d)) / np.log(2)))
+    tr = python_tree(k, t)
+    n = tr["parent"].shape[0]
+    rng = np.random.default_rng(d)
+    C = rng.normal(size=(n, d_out)).astype(np.float32)
+    maxdeg = np.zeros(d, dtype=np.int64)
+    for e in range(1, n):
+        maxdeg[tr["dim"][e]] = max(maxdeg[tr["dim"][e]], tr["deg"][e])
+    fam = np.full(d, fam_id)
+    fa, fb = np.full(d, 0.9), np.full(d, 0.05)
+    lay = build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb)
+    x = rng.uniform(-1, 1, (7, d))
+    ref = direct(tr, C.astype(float), x, fam, fa, fb)
+    got = evaluate_layout(lay, x, fam, fa, fb, C[0].astype(float))
+    # blocks hold their affine maps in FP32 (as the kernel reads them): 1e-6
+    scale = np.max(np.abs(ref))
+    np.testing.assert_allclose(got, ref, rtol=1e-6, atol=1e-6 * scale)
+    # structural invariants the kernel relies on
+    assert lay["row"] % 4 == 0 and lay["row"] >= lay["n_hb"] + lay["n_vp"]
+    assert all(r[0] % 4 == 0 and r[1] % 4 == 0 and r[0] + r[1] <= lay["row"] for r in lay["run"])
+    assert lay["node_seg"][0] == 0 and lay["node_seg"][-1] == lay["n_nodes"]
+    assert lay["cold_seg"][0] == 0 and lay["cold_seg"][-1] == lay["n_cold_groups"]
+    assert np.all(np.diff(lay["node_seg"]) >= 0) and np.all(np.diff(lay["cold_seg"]) >= 0)
+    assert lay["max_depth"] <= 8
+    assert lay["block_seg"][-1] == lay["n_cold_blocks"] and (d_out == 1 or lay["n_cold_blocks"] == 0)
