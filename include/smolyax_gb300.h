@@ -254,6 +254,22 @@ typedef struct smx_spectral {
 int smx_spectral_eval(const smx_spectral* plan_host, const double* x, int64_t P, int64_t ldx, float* y,
                       void* stream);
 
+/* ---- allocation-free FP64 evaluation -------------------------------------------------
+ * No counterpart in the reference: an added entry point for callers that
+ * cannot allocate device memory while evaluating (FFI hosts without a CUDA
+ * allocator, services whose device memory belongs to a pool, code that must
+ * not call cudaMalloc because it synchronises the device).  Same result as
+ * smx_eval(plan, 64, ...), but the basis table lives in a library-owned
+ * device array of SMX_STATIC_SCRATCH_BYTES (held by every GPU that loads the
+ * library until the process exits); nothing is allocated.  Calls whose table
+ * (n_values * P doubles) does not fit return SMX_ERR_WORKSPACE: split the
+ * points.  The first call on a device looks up the array's address with that
+ * device current -- make it before any stream capture.  All calls share the
+ * array, so calls that overlap on the GPU race: serialise them. */
+#define SMX_STATIC_SCRATCH_BYTES (32u << 20)
+int smx_eval_f64_noalloc(const smx_plan* plan_host, const double* x, int64_t P, int64_t ldx, double* y,
+                         void* stream);
+
 /* Human-readable description of the last error on this thread (host string). */
 const char* smx_last_error_string(void);
 

@@ -113,6 +113,7 @@ SIGNATURES = {
     "smx_spectral_pairs": (_int, [_int, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
     "smx_spectral_coefficients": (_int, [_p, _p, _p, _p, _p, _p, _p, _i64, _p, _p, _p, _p, _p]),
     "smx_spectral_eval": (_int, [_p, _p, _i64, _i64, _p, _p]),
+    "smx_eval_f64_noalloc": (_int, [_p, _p, _i64, _i64, _p, _p]),
     "smx_last_error_string": (C.c_char_p, []),
     "smx_version": (C.c_char_p, []),
 }
