@@ -254,6 +254,34 @@ typedef struct smx_spectral {
 int smx_spectral_eval(const smx_spectral* plan_host, const double* x, int64_t P, int64_t ldx, float* y,
                       void* stream);
 
+/* Basis-product panel of the orthogonal form for the tensor-core contraction:
+ * A[p][j] = prod over the pairs of entry j of phi_g(z_d) for the K non-root
+ * entries of Lambda in DFS pre-order (tape word: basis slot | depth << 16,
+ * depth <= 8), written as TF32 hi/lo pairs [P x lda] in REVERSED order (entry j
+ * of the tape goes to column K-1-j: summing from small to large terms limits
+ * the truncation of the tensor cores' FP32 accumulation).  Basis slots: for each
+ * listed dimension dims[h], degrees 1..dmax[h] at dsoff[h]. */
+int smx_spectral_panel_tf32(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff, int n_slots,
+                            const int32_t* tape, int K, const float* fam_a, const float* fam_b, const int32_t* fam,
+                            const double* x, int64_t P, int64_t ldx, float* A_hi, float* A_lo, int64_t lda,
+                            void* stream);
+
+/* ---- tensor-core contraction ---------------------------------------------------------
+ * D[M x N] = A B^T (+ bias[n]) with tcgen05.mma kind::tf32 in 3xTF32 form:
+ * A = A_hi + A_lo, B = B_hi + B_lo (row-major [M x K] and [N x K], leading
+ * dimensions multiples of 4, 16-byte aligned), D = A_hi B_hi^T + A_hi B_lo^T +
+ * A_lo B_hi^T accumulated in FP32 in tensor memory.  *err (device int) is set
+ * non-zero if a pipeline wait timed out.  Used for the orthogonal-form
+ * contraction when d_out is large (the dense [points x Lambda] x [Lambda x
+ * d_out] product of interpolation.py:264-304 in orthogonal form) and for the
+ * backward products. */
+int smx_gemm_tf32x3(const float* A_hi, const float* A_lo, int64_t lda, const float* B_hi, const float* B_lo,
+                    int64_t ldb, int M, int N, int K, float* D, int64_t ldd, const float* bias, int* err, void* stream);
+
+/* hi = TF32(src), lo = TF32(src - hi) for a [rows x cols] block. */
+int smx_split_tf32(const float* src, int64_t rows, int64_t cols, int64_t lds, float* hi, float* lo, int64_t ldo,
+                   void* stream);
+
 /* ---- allocation-free FP64 evaluation -------------------------------------------------
  * No counterpart in the reference: an added entry point for callers that
  * cannot allocate device memory while evaluating (FFI hosts without a CUDA

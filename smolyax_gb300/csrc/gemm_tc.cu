@@ -1,0 +1,380 @@
+// Tensor-core contraction on sm_103a: D = A B^T (+ bias) with tcgen05.mma
+// kind::tf32 in 3xTF32 form.
+//
+//   A [M x K], B [N x K] row-major FP32 (K-major operands), each given as a
+//   pair (hi, lo) of TF32-representable arrays with x ~= hi + lo;
+//   D [M x N] FP32 = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T  (+ bias[n])
+// so every product carries ~22 significant bits, accumulated in FP32 in
+// tensor memory.  K is consumed in slices of 32 (128 bytes, SWIZZLE_128B)
+// through a 3-stage TMA pipeline guarded by mbarriers.
+// Every wait is bounded; on timeout the kernel records an error code, skips
+// the epilogue, drains its own copies (bounded) and frees tensor memory.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr int kBM = 128;
+constexpr int kBK = 32;  // fp32 elements per 128-byte row slice
+constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on every wait
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Bounded parity wait; returns false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort_flag) {
+  const uint32_t a = smem_u32(bar);
+  const uint64_t t0 = global_ns();
+  for (uint32_t it = 0;; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (abort_flag && *abort_flag) return false;
+    if ((it & 255) == 255 && global_ns() - t0 > kWaitNs) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int c0, int c1, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (tcgen05 descriptor format, version field = 1).
+__device__ __forceinline__ uint64_t make_desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= uint64_t((saddr & 0x3FFFF) >> 4);        // start address
+  d |= uint64_t(1) << 16;                        // leading byte offset (unused for swizzled K-major)
+  d |= uint64_t(1024 >> 4) << 32;                // stride byte offset
+  d |= uint64_t(1) << 46;                        // version
+  d |= uint64_t(2) << 61;                        // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor: D = F32, A = B = TF32, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// Tiles: 128 x 128 outputs per CTA; the FP32 accumulator of the tensor cores
+// truncates when it adds, so one accumulator must not run over long
+// stretches of K: the MMA thread alternates between two accumulators in
+// tensor memory (columns [0,128) and [128,256)) every kChunk K-tiles, and the
+// four drain warps add each finished accumulator into FP32 registers (one row
+// of 128 outputs per thread, round-to-nearest adds), then release it.
+constexpr int kBN = 128;
+constexpr int kStages = 3;
+constexpr int kChunk = 2;  // K-tiles (of 32) per accumulator use
+constexpr int kThreadsTC = 192;  // warps 0-3 drain/epilogue, warp 4 TMA, warp 5 MMA
+
+struct Smem {
+  static constexpr int kA = kBM * kBK * 4;
+  static constexpr int kB = kBN * kBK * 4;
+  static constexpr int kStage = 2 * kA + 2 * kB;
+  static constexpr int kTiles = kStages * kStage;
+  static constexpr int kTotal = kTiles + 1024 /*align*/ + 256 /*barriers*/;
+};
+
+struct GemmArgs {
+  int M, N, K;
+  float* D;
+  int64_t ldd;
+  const float* bias;
+  int* err;
+};
+
+__global__ void __launch_bounds__(kThreadsTC, 1)
+    gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
+                       const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl, GemmArgs g) {
+  using L = Smem;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(base + L::kTiles);
+  uint64_t* empty = full + kStages;
+  uint64_t* acc_full = empty + kStages;  // [2] MMA -> drain
+  uint64_t* acc_empty = acc_full + 2;    // [2] drain -> MMA
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  volatile int* armed_slot = abort_flag + 1;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
+  const int KT = (g.K + kBK - 1) / kBK;
+  const int NCH = (KT + kChunk - 1) / kChunk;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 4);  // one arrival per drain warp
+    }
+    *abort_flag = 0;
+    *armed_slot = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {  // tensor memory: two accumulators of 128 fp32 columns
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(2 * kBN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 4) {
+    if (lane == 0) {  // ---- TMA producer
+      int armed_upto = 0;
+      for (int kt = 0; kt < KT; ++kt) {
+        const int s = kt % kStages;
+        const uint32_t ph = (kt / kStages) & 1;
+        if (kt >= kStages && !mbar_wait(&empty[s], ph ^ 1, abort_flag)) {
+          atomicExch(g.err, 1);
+          *abort_flag = 1;
+          break;
+        }
+        uint8_t* st = base + s * L::kStage;
+        mbar_expect_tx(&full[s], L::kStage);
+        const int k = kt * kBK;
+        tma_load_2d(st, &tmAh, k, m0, &full[s]);
+        tma_load_2d(st + L::kA, &tmAl, k, m0, &full[s]);
+        tma_load_2d(st + 2 * L::kA, &tmBh, k, n0, &full[s]);
+        tma_load_2d(st + 2 * L::kA + L::kB, &tmBl, k, n0, &full[s]);
+        armed_upto = kt + 1;
+      }
+      *armed_slot = armed_upto;
+    }
+    __syncwarp();
+  } else if (warp == 5) {
+    if (lane == 0) {  // ---- MMA issuer
+      constexpr uint32_t idesc = idesc_tf32(kBM, kBN);
+      bool ok = true;
+      int kt = 0;
+      for (int c = 0; c < NCH && ok; ++c) {
+        const int b = c & 1;
+        if (c >= 2 && !mbar_wait(&acc_empty[b], ((c >> 1) & 1) ^ 1, abort_flag)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t acc = tmem + uint32_t(b * kBN);
+        const int kt_end = min(KT, kt + kChunk);
+        bool first = true;
+        for (; kt < kt_end; ++kt) {
+          const int s = kt % kStages;
+          const uint32_t ph = (kt / kStages) & 1;
+          if (!mbar_wait(&full[s], ph, abort_flag)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t a_hi = smem_u32(base + s * L::kStage);
+          const uint32_t a_lo = a_hi + L::kA;
+          const uint32_t b_hi = a_hi + 2 * L::kA;
+          const uint32_t b_lo = b_hi + L::kB;
+#pragma unroll
+          for (int k8 = 0; k8 < kBK / 8; ++k8) {  // K = 8 tf32 = 32 bytes per MMA
+            const uint32_t off = k8 * 32;
+            const uint64_t dah = make_desc_sw128(a_hi + off), dal = make_desc_sw128(a_lo + off);
+            const uint64_t dbh = make_desc_sw128(b_hi + off), dbl = make_desc_sw128(b_lo + off);
+            mma_tf32(acc, dah, dbh, idesc, first ? 0u : 1u);
+            first = false;
+            mma_tf32(acc, dah, dbl, idesc, 1u);
+            mma_tf32(acc, dal, dbh, idesc, 1u);
+          }
+          mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
+        }
+        mma_commit(&acc_full[b]);  // accumulator b complete (or abandoned on abort)
+      }
+      if (!ok) {
+        atomicExch(g.err, 2);
+        *abort_flag = 1;
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---- drain warps 0-3: warp w owns TMEM lanes 32w .. 32w+31 (rows m0 + 32w + lane)
+    float acc[kBN];
+#pragma unroll
+    for (int j = 0; j < kBN; ++j) acc[j] = 0.f;
+    bool ok = true;
+    const uint32_t lane_base = tmem + (uint32_t(warp * 32) << 16);
+    for (int c = 0; c < NCH; ++c) {
+      const int b = c & 1;
+      ok = __all_sync(0xffffffffu, ok && mbar_wait(&acc_full[b], (c >> 1) & 1, abort_flag) && !*abort_flag);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+      for (int q = 0; q < kBN; q += 16) {
+        uint32_t r[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+            "%14, %15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(lane_base + uint32_t(b * kBN + q)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 16; ++j) acc[q + j] += __uint_as_float(r[j]);
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[b])) : "memory");
+    }
+    if (ok) {
+      const int row = m0 + warp * 32 + lane;
+      if (row < g.M) {
+        float* dr = g.D + int64_t(row) * g.ldd;
+#pragma unroll
+        for (int j = 0; j < kBN; ++j) {
+          const int col = n0 + j;
+          if (col < g.N) dr[col] = acc[j] + (g.bias ? g.bias[col] : 0.f);
+        }
+      }
+    }
+  }
+  // after an abort, wait (bounded) for the last copy armed on every stage
+  if (warp == 4 && lane == 0 && *abort_flag) {
+    const int armed = *armed_slot;
+    for (int kt = max(0, armed - kStages); kt < armed; ++kt)
+      mbar_wait(&full[kt % kStages], (kt / kStages) & 1, nullptr);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kBN));
+  }
+}
+
+// ---- TF32 split: hi = x rounded to TF32 (10-bit mantissa, round to nearest), lo = TF32(x - hi)
+__device__ __forceinline__ float to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__global__ void split_tf32_kernel(const float* __restrict__ src, int64_t rows, int64_t cols, int64_t lds,
+                                  float* __restrict__ hi, float* __restrict__ lo, int64_t ldo) {
+  const int64_t n = rows * cols;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t r = i / cols, c = i - r * cols;
+    const float v = src[r * lds + c];
+    const float h = to_tf32(v);
+    hi[r * ldo + c] = h;
+    lo[r * ldo + c] = to_tf32(v - h);
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::mutex g_encode_mu;
+
+int get_encode() {
+  std::lock_guard<std::mutex> lock(g_encode_mu);
+  if (g_encode) return SMX_OK;
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn)
+    return smx::set_error(SMX_ERR_CUDA, "cuTensorMapEncodeTiled entry point not available");
+  g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  return SMX_OK;
+}
+
+int make_map(CUtensorMap* tm, const float* ptr, int64_t rows, int64_t cols, int64_t ld, int box_rows) {
+  if ((reinterpret_cast<uintptr_t>(ptr) & 15) || (ld * 4) % 16)
+    return smx::set_error(SMX_ERR_ARG, "tensor map: base must be 16-byte aligned and the row pitch a multiple of 16");
+  cuuint64_t dims[2] = {cuuint64_t(cols), cuuint64_t(rows)};
+  cuuint64_t strides[1] = {cuuint64_t(ld * 4)};
+  cuuint32_t box[2] = {cuuint32_t(kBK), cuuint32_t(box_rows)};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(ptr), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return smx::set_error(SMX_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  return SMX_OK;
+}
+
+int launch(const float* Ah, const float* Al, int64_t lda, const float* Bh, const float* Bl, int64_t ldb, int M, int N,
+           int K, float* D, int64_t ldd, const float* bias, int* err, cudaStream_t st) {
+  CUtensorMap tAh, tAl, tBh, tBl;
+  int rc;
+  if ((rc = make_map(&tAh, Ah, M, K, lda, kBM)) || (rc = make_map(&tAl, Al, M, K, lda, kBM)) ||
+      (rc = make_map(&tBh, Bh, N, K, ldb, kBN)) || (rc = make_map(&tBl, Bl, N, K, ldb, kBN)))
+    return rc;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, Smem::kTotal);
+    attr = true;
+  }
+  GemmArgs g{M, N, K, D, ldd, bias, err};
+  dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM);
+  gemm_tf32x3_kernel<<<grid, kThreadsTC, Smem::kTotal, st>>>(tAh, tAl, tBh, tBl, g);
+  SMX_LAUNCH_CHECK("smx_gemm_tf32x3");
+  return SMX_OK;
+}
+
+}  // namespace
+
+extern "C" int smx_split_tf32(const float* src, int64_t rows, int64_t cols, int64_t lds, float* hi, float* lo,
+                              int64_t ldo, void* stream) {
+  SMX_REQUIRE(rows >= 0 && cols >= 0 && lds >= cols && ldo >= cols, "smx_split_tf32: bad sizes");
+  if (rows * cols == 0) return SMX_OK;
+  SMX_REQUIRE(src && hi && lo, "smx_split_tf32: null pointer");
+  split_tf32_kernel<<<smx::grid_for(rows * cols, 256), 256, 0, smx::as_stream(stream)>>>(src, rows, cols, lds, hi, lo,
+                                                                                        ldo);
+  SMX_LAUNCH_CHECK("smx_split_tf32");
+  return SMX_OK;
+}
+
+extern "C" int smx_gemm_tf32x3(const float* A_hi, const float* A_lo, int64_t lda, const float* B_hi, const float* B_lo,
+                               int64_t ldb, int M, int N, int K, float* D, int64_t ldd, const float* bias, int* err,
+                               void* stream) {
+  SMX_REQUIRE(M >= 0 && N >= 0 && K >= 0 && lda >= K && ldb >= K && ldd >= N, "smx_gemm_tf32x3: bad sizes");
+  if (M == 0 || N == 0) return SMX_OK;
+  SMX_REQUIRE(K >= 1 && A_hi && A_lo && B_hi && B_lo && D && err, "smx_gemm_tf32x3: null pointer");
+  int rc = get_encode();
+  if (rc) return rc;
+  return launch(A_hi, A_lo, lda, B_hi, B_lo, ldb, M, N, K, D, ldd, bias, err, smx::as_stream(stream));
+}

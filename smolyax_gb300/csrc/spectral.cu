@@ -607,3 +607,107 @@ extern "C" int smx_spectral_eval(const smx_spectral* sp, const double* x, int64_
   }
   return SMX_OK;
 }
+
+// --- basis-product panel for the tensor-core contraction ------------------------------------
+// A[p][j] = prod over the pairs of entry j of phi_g(z_d), for the non-root
+// entries of Lambda in DFS pre-order (tape word: basis slot | depth << 16).
+// One thread per point: the per-point basis values of all pairs sit in shared
+// memory ([slot][point]), the path products on a register stack; blocks of 32
+// columns go through a shared tile so that the TF32 hi/lo rows are written
+// with coalesced 128-byte stores.
+namespace {
+
+__global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32_t* __restrict__ dims,
+                                                         const int32_t* __restrict__ dmax,
+                                                         const int32_t* __restrict__ dsoff, int n_slots,
+                                                         const int32_t* __restrict__ tape, int K,
+                                                         const float* __restrict__ fam_a,
+                                                         const float* __restrict__ fam_b,
+                                                         const int32_t* __restrict__ fam, const double* __restrict__ x,
+                                                         int64_t P, int64_t ldx, float* __restrict__ Ahi,
+                                                         float* __restrict__ Alo, int64_t lda) {
+  extern __shared__ __align__(16) float sm[];
+  float* row = sm;                       // [n_slots][128]
+  float* tile = sm + size_t(n_slots) * 128;  // [32][129]
+  const int tid = threadIdx.x;
+  const int64_t p0 = blockIdx.x * int64_t(128);
+  const int64_t p = p0 + tid;
+  const double* xp = x + (p < P ? p : 0) * ldx;
+  for (int h = 0; h < n_dims; ++h) {
+    const int dim = dims[h], g = dmax[h], so = dsoff[h];
+    const int fm = fam[dim];
+    const float z = fmaf(fam_a[dim], float(xp[dim]), fam_b[dim]);
+    float pm1 = 0.f, pc = 1.f;
+    for (int n = 0; n < g; ++n) {
+      const float pn = c_alpha[fm][n] * z * pc - c_beta[fm][n] * pm1;
+      pm1 = pc;
+      pc = pn;
+      row[(so + n) * 128 + tid] = pc;
+    }
+  }
+  float st1 = 1.f, st2 = 1.f, st3 = 1.f, st4 = 1.f, st5 = 1.f, st6 = 1.f, st7 = 1.f, st8 = 1.f;
+  for (int jb = 0; jb < K; jb += 32) {
+    const int jn = min(32, K - jb);
+    for (int j = 0; j < jn; ++j) {
+      const int w = __ldg(tape + jb + j);
+      const float b = row[(w & 0xffff) * 128 + tid];
+      float v;
+      switch (w >> 16) {
+        case 1: st1 = b; v = st1; break;
+        case 2: st2 = st1 * b; v = st2; break;
+        case 3: st3 = st2 * b; v = st3; break;
+        case 4: st4 = st3 * b; v = st4; break;
+        case 5: st5 = st4 * b; v = st5; break;
+        case 6: st6 = st5 * b; v = st6; break;
+        case 7: st7 = st6 * b; v = st7; break;
+        default: st8 = st7 * b; v = st8; break;
+      }
+      tile[j * 129 + tid] = v;
+    }
+    __syncthreads();
+    // coalesced write-out: thread t -> column t % 32 of rows t / 32, t / 32 + 4, ...
+    const int c = tid & 31;
+    if (c < jn) {
+      for (int r = tid >> 5; r < 128; r += 4) {
+        if (p0 + r >= P) break;
+        const float v = tile[c * 129 + r];
+        uint32_t h;
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+        const float hf = __uint_as_float(h);
+        uint32_t l;
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(v - hf));
+        // reversed column order: descendants (small coefficients) precede their
+        // ancestors, so the tensor-memory accumulator grows from small to large
+        const int col = K - 1 - (jb + c);
+        Ahi[(p0 + r) * lda + col] = hf;
+        Alo[(p0 + r) * lda + col] = __uint_as_float(l);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+extern "C" int smx_spectral_panel_tf32(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff,
+                                       int n_slots, const int32_t* tape, int K, const float* fam_a,
+                                       const float* fam_b, const int32_t* fam, const double* x, int64_t P, int64_t ldx,
+                                       float* A_hi, float* A_lo, int64_t lda, void* stream) {
+  SMX_REQUIRE(n_dims >= 0 && n_slots >= 0 && K >= 0 && P >= 0 && lda >= K, "smx_spectral_panel_tf32: bad sizes");
+  if (P == 0 || K == 0) return SMX_OK;
+  SMX_REQUIRE(dims && dmax && dsoff && tape && fam_a && fam_b && fam && x && A_hi && A_lo,
+              "smx_spectral_panel_tf32: null pointer");
+  const size_t smem = (size_t(n_slots) * 128 + 32 * 129) * sizeof(float);
+  SMX_REQUIRE(smem <= 220 * 1024, "smx_spectral_panel_tf32: too many basis slots for shared memory");
+  int rc = upload_consts();
+  if (rc) return rc;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(panel_tf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    attr = true;
+  }
+  panel_tf32_kernel<<<smx::grid_for(P, 128), 128, smem, smx::as_stream(stream)>>>(
+      n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, A_hi, A_lo, lda);
+  SMX_LAUNCH_CHECK("smx_spectral_panel_tf32");
+  return SMX_OK;
+}

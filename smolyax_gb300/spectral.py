@@ -20,6 +20,7 @@ from . import _capi as capi
 from ._capi import call, ptr
 
 FAMILIES = {"legendre": 0, "hermite": 1}
+TC_MIN_DOUT = 16  # from this many outputs on, the tensor-core contraction is used
 
 
 class SpectralPlan:
@@ -101,6 +102,39 @@ class SpectralPlan:
             t = k[name]
             setattr(s, name, t.data_ptr() if t.numel() else None)
         self.c = s
+        self.tc = None
+        if d_out >= TC_MIN_DOUT:
+            self._build_tc(tree_np, C32, np.asarray(ip._maxdeg), fam, fa, fb, T, st)
+        self.memory_limit = ip._memory_limit
+
+    def _build_tc(self, tr, C32, maxdeg, fam, fa, fb, T, st):
+        """Operands of the tensor-core contraction: tape over all non-root entries
+        (pre-order), coefficient matrix B = C^T split into TF32 hi/lo."""
+        dims = np.nonzero(maxdeg > 0)[0]
+        dmax = maxdeg[dims]
+        dsoff = np.concatenate([[0], np.cumsum(dmax)[:-1]]) if dims.size else np.zeros(0, np.int64)
+        n_slots = int(dmax.sum())
+        if (n_slots * 128 + 32 * 129) * 4 > 220 * 1024 or int(tr["level"].max()) > 8:
+            return  # the FP32 stream evaluator serves this plan
+        idx = np.full(maxdeg.shape[0], -1, dtype=np.int64)
+        idx[dims] = np.arange(dims.size)
+        n = tr["parent"].shape[0]
+        ent = np.arange(1, n)
+        ent = ent[np.argsort(tr["rank"][ent], kind="stable")]
+        slot = dsoff[idx[tr["dim"][ent]]] + tr["deg"][ent] - 1
+        tape = (slot | (tr["level"][ent] << 16)).astype(np.int32)
+        K = int(ent.size)
+        ldk = _round4(max(K, 1))
+        d_out = C32.shape[1]
+        B = np.zeros((d_out, ldk), dtype=np.float32)
+        B[:, :K] = C32[ent[::-1]].T  # the panel stores the entries in reversed pre-order
+        dev = self.fam.device
+        Bd = T(B, torch.float32)
+        Bh, Bl = torch.empty_like(Bd), torch.empty_like(Bd)
+        call("smx_split_tf32", ptr(Bd), d_out, ldk, ldk, ptr(Bh), ptr(Bl), ldk, st)
+        self.tc = dict(dims=T(dims, torch.int32), dmax=T(dmax, torch.int32), dsoff=T(dsoff, torch.int32),
+                       n_slots=n_slots, tape=T(tape, torch.int32), K=K, ldk=ldk, Bh=Bh, Bl=Bl,
+                       bias=self.keep["c0"], err=torch.zeros(1, dtype=torch.int32, device=dev))
 
     def ref(self):
         import ctypes
@@ -110,7 +144,33 @@ class SpectralPlan:
     def evaluate(self, x, y):
         """y[P, d_out] (FP32) at x[P, d_in] (FP64, contiguous, on the device)."""
         st = capi.stream_ptr(torch.cuda.current_stream())
+        if self.tc is not None:
+            return self._evaluate_tc(x, y, st)
         call("smx_spectral_eval", self.ref(), ptr(x), int(x.shape[0]), int(x.shape[1]), ptr(y), st)
+        return y
+
+    def _evaluate_tc(self, x, y, st):
+        """Tensor-core path: basis-product panel (TF32 hi/lo) in chunks of points,
+        each contracted with the coefficient matrix by the tcgen05 kernel."""
+        tc = self.tc
+        k = self.keep
+        P, d = int(x.shape[0]), int(x.shape[1])
+        d_out = int(y.shape[1])
+        ldk = tc["ldk"]
+        step = max(128, int(self.memory_limit * 1024**3 // (8 * ldk)) // 128 * 128)
+        step = min(step, P)
+        Ah = torch.empty(step, ldk, dtype=torch.float32, device=x.device)
+        Al = torch.empty_like(Ah)
+        if ldk > tc["K"]:
+            Ah[:, tc["K"]:] = 0
+            Al[:, tc["K"]:] = 0
+        for p0 in range(0, P, step):
+            p1 = min(P, p0 + step)
+            call("smx_spectral_panel_tf32", int(tc["dims"].numel()), ptr(tc["dims"]), ptr(tc["dmax"]),
+                 ptr(tc["dsoff"]), tc["n_slots"], ptr(tc["tape"]), tc["K"], ptr(k["fam_a"]), ptr(k["fam_b"]),
+                 ptr(k["fam"]), ptr(x[p0:p1]), p1 - p0, d, ptr(Ah), ptr(Al), ldk, st)
+            call("smx_gemm_tf32x3", ptr(Ah), ptr(Al), ldk, ptr(tc["Bh"]), ptr(tc["Bl"]), ldk, p1 - p0, d_out,
+                 tc["K"], ptr(y[p0:p1]), d_out, ptr(tc["bias"]), ptr(tc["err"]), st)
         return y
 
 

@@ -1,0 +1,53 @@
+"""tcgen05 3xTF32 contraction (``smx_gemm_tf32x3``) against an FP64 product.
+
+Bound: norm-wise relative error 1e-8 K + 2e-6 (22-bit products; the tensor cores accumulate
+in FP32 with truncation, so the bound grows with K <= 5000).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _gemm(A, B, bias=None):
+    import torch
+
+    from smolyax_gb300 import _capi
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    M, K = A.shape
+    N = B.shape[0]
+    ld = (K + 3) // 4 * 4
+    st = _capi.stream_ptr(torch.cuda.current_stream())
+
+    def split(X):
+        Xd = torch.zeros(X.shape[0], ld, dtype=torch.float32, device=dev)
+        Xd[:, :K] = torch.as_tensor(X, dtype=torch.float32)
+        hi = torch.zeros_like(Xd)
+        lo = torch.zeros_like(Xd)
+        _capi.call("smx_split_tf32", _capi.ptr(Xd), X.shape[0], ld, ld, _capi.ptr(hi), _capi.ptr(lo), ld, st)
+        return hi, lo
+
+    Ah, Al = split(A)
+    Bh, Bl = split(B)
+    D = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    b = None if bias is None else torch.as_tensor(bias, dtype=torch.float32, device=dev)
+    _capi.call("smx_gemm_tf32x3", _capi.ptr(Ah), _capi.ptr(Al), ld, _capi.ptr(Bh), _capi.ptr(Bl), ld, M, N, K,
+               _capi.ptr(D), N, _capi.ptr(b), _capi.ptr(err), st)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    return D.cpu().numpy().astype(np.float64)
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 128, 32), (300, 200, 100), (256, 256, 1000), (1000, 64, 5000), (77, 520, 40)])
+def test_gemm_tf32x3(M, N, K):
+    rng = np.random.default_rng(M + N + K)
+    A = rng.normal(size=(M, K)).astype(np.float32)
+    B = rng.normal(size=(N, K)).astype(np.float32)
+    bias = rng.normal(size=N).astype(np.float32)
+    D = _gemm(A, B, bias)
+    ref = A.astype(np.float64) @ B.astype(np.float64).T + bias
+    err = np.max(np.abs(D - ref)) / np.max(np.abs(ref))
+    print("M=%d N=%d K=%d norm-wise rel err %.2e" % (M, N, K, err))
+    assert err < 1e-8 * K + 2e-6

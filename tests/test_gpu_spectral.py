@@ -76,8 +76,9 @@ CASES = {
     "cfg1": (10, 8.831421, "leja", 1, fns.rational(10, seed=0), np.random.default_rng(1).uniform(-1, 1, (10000, 10)), 1e-6),
     "cfg2": (1000, 8.224520, "leja", 1, fns.rational(1000, seed=0),
              np.random.default_rng(1).uniform(-1, 1, (256, 1000)), 1e-6),
+    # d_out = 64: tensor-core contraction (3xTF32, FP32 accumulation in tensor memory)
     "cfg4": (200, 7.853604, "leja", 64, fns.rational_vec(200, 64, seed=0),
-             np.random.default_rng(1).uniform(-1, 1, (64, 200)), 2e-6),
+             np.random.default_rng(1).uniform(-1, 1, (64, 200)), 5e-5),
     "cfg3alt": (100, 7.723434, "gh", 8, fns.exponential(100, 8, seed=0),
                 np.random.default_rng(1).normal(size=(32, 100)), 1e-5),
     "cfg3": (100, 9.464636, "gh", 8, fns.exponential(100, 8, seed=0), np.random.default_rng(1).normal(size=(32, 100)),
@@ -100,3 +101,23 @@ def test_fp32_error_bound(tag):
     assert err < bound
     if x.shape[0] <= 256:
         np.testing.assert_allclose(host_orthogonal_eval(ip, x[:16]), exact[:16], rtol=1e-9)
+
+
+@pytest.mark.parametrize("t,d_out", [(7.723434, 32), (7.723434, 300)])
+def test_tensor_core_path_gauss_hermite(t, d_out):
+    """Gauss-Hermite, d_in = 100, vector output: the tcgen05 path against our FP64 path."""
+    from smolyax_gb300 import nodes
+
+    d = 100
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    ip = _interp(node_gen=nodes.GaussHermite(dim=d), k=k, t=t, d_out=d_out, f=fns.exponential(d, d_out, seed=0))
+    x = np.random.default_rng(3).normal(size=(300, d))
+    assert ip.spectral_plan().tc is not None
+    y64 = ip(x).cpu().numpy()
+    y32 = ip(x, precision="fp32").cpu().numpy().astype(float)
+    # per point, relative to the largest output of that point (a few outputs are
+    # 20x smaller than the others; FP32 cannot resolve them to 1e-6 pointwise)
+    err = float(np.max(np.max(np.abs(y32 - y64), axis=1) / np.max(np.abs(y64), axis=1)))
+    print("GH d_out=%d: tensor-core FP32 per-point norm-wise error vs FP64 %.3e" % (d_out, err))
+    assert err < 2e-6
+
