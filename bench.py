@@ -185,6 +185,79 @@ def run_reference(args):
     return 0
 
 
+WORKLOADS = {
+    # name: (node kind, d_in, t, d_out, points, target builder, description)
+    "gh2048": ("gh", 100, 9.464636, 2048, 65536, lambda: __import__("functions").exponential(100, 2048, seed=0),
+               "Gauss-Hermite d_in=100 d_out=2048 |Lambda|=20010 (t=9.464636) exponential f, 65536 points N(0,I)"),
+    "leja64": ("leja", 200, 7.853604, 64, 100_000, lambda: __import__("functions").rational_vec(200, 64, seed=0),
+               "Leja d_in=200 d_out=64 |Lambda|=5000 (t=7.853604) rational f, 1e5 points U[-1,1]^200"),
+}
+
+
+def run_tensor_workload(args):
+    """Vector-valued workloads served by the tensor-core contraction (one JSON line)."""
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from smolyax_gb300 import SmolyakBarycentricInterpolator, nodes
+
+    kind, d, t, d_out, P, fbuild, desc = WORKLOADS[args.workload]
+    P = args.points if args.points != POINTS else P
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    gen = nodes.Leja(dim=d) if kind == "leja" else nodes.GaussHermite(dim=d)
+    t0 = time.perf_counter()
+    ip = SmolyakBarycentricInterpolator(node_gen=gen, k=k, t=t, d_out=d_out, f=fbuild(), memory_limit=8.0)
+    sp = ip.spectral_plan()
+    setup_s = time.perf_counter() - t0
+    gen_t = torch.Generator(device=dev)
+    gen_t.manual_seed(1)
+    if kind == "leja":
+        x = torch.rand(P, d, dtype=torch.float64, device=dev, generator=gen_t) * 2 - 1
+    else:
+        x = torch.randn(P, d, dtype=torch.float64, device=dev, generator=gen_t)
+    y = torch.empty(P, d_out, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    for _ in range(max(3, args.warmup)):
+        sp.evaluate(x, y)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(0) as clk:
+        for a, b in ev:
+            a.record(stream)
+            sp.evaluate(x, y)
+            b.record(stream)
+        torch.cuda.synchronize()
+    per = [a.elapsed_time(b) for a, b in ev]
+    ms = statistics.mean(per)
+    sub = 256
+    y64 = ip(x[:sub]).cpu().numpy()
+    err = float(np.max(np.max(np.abs(y[:sub].double().cpu().numpy() - y64), axis=1) / np.max(np.abs(y64), axis=1)))
+    K = sp.tc["K"] if sp.tc is not None else None
+    tensor_flops = 3 * 2.0 * P * d_out * K if K else None
+    try:
+        peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"])
+        pk = "measured bf16 dense"
+    except Exception:
+        peak, pk = 1900.0, "fallback bf16 dense"
+    line = {
+        "metric": METRIC, "workload": args.workload, "value": P * d_out / (ms * 1e-3), "unit": "evals/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "dtype": "fp32 (3xTF32 tensor contraction)", "data": "synthetic",
+        "config": {"workload": desc, "points": P, "d_in": d, "d_out": d_out, "lambda": K + 1 if K else None},
+        "error": {"fp32_per_point_normwise_vs_fp64": err, "points_checked": sub},
+        "roofline": {"bound": "tensor", "achieved": tensor_flops / (ms * 1e-3) / 1e12 if K else None, "peak": peak,
+                     "unit": "TFLOP/s", "frac": tensor_flops / (ms * 1e-3) / 1e12 / peak if K else None,
+                     "peak_kind": pk + " (the kernel runs kind::tf32, whose dense rate is half of bf16)",
+                     "flops_per_step": tensor_flops},
+        "setup_s": setup_s, "clocks": clk.summary(), "gpu_launches": args.steps * 2 * ((P + 1) // 1),
+    }
+    line["gpu_launches"] = None
+    print(json.dumps(line))
+    return 0
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -312,9 +385,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--points", type=int, default=POINTS)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="leja1000", choices=["leja1000"] + sorted(WORKLOADS))
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "leja1000":
+        return run_tensor_workload(args)
     return run_ours(args)
 
 

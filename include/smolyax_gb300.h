@@ -266,17 +266,38 @@ int smx_spectral_panel_tf32(int n_dims, const int32_t* dims, const int32_t* dmax
                             const double* x, int64_t P, int64_t ldx, float* A_hi, float* A_lo, int64_t lda,
                             void* stream);
 
+/* Backward of the orthogonal form (no counterpart in the reference, whose
+ * derivative is the dense Jacobian of interpolation.py:306-345):
+ *  - smx_spectral_panel_t_tf32: the transposed panel AT[K-1-j][p] (point-
+ *    contiguous, same columns as smx_spectral_panel_tf32) for dL/dC = A^T g;
+ *  - smx_spectral_vjp_x: dL/dx[p][d] from G = g C^T ([P x ldg], columns in the
+ *    panel's reversed order): reverse pass through the basis products;
+ *  - smx_spectral_coefficients_adjoint: adjoint of smx_spectral_coefficients,
+ *    Fbar[r] = (A_1^T x ... x A_n^T) Cbar[ids] per summand (FP64). */
+int smx_spectral_panel_t_tf32(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff,
+                              int n_slots, const int32_t* tape, int K, const float* fam_a, const float* fam_b,
+                              const int32_t* fam, const double* x, int64_t P, int64_t ldx, float* AT_hi, float* AT_lo,
+                              int64_t ldp, void* stream);
+int smx_spectral_vjp_x(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff, int n_slots,
+                       const int32_t* tape, int K, const float* fam_a, const float* fam_b, const int32_t* fam,
+                       const double* x, int64_t P, int64_t ldx, const float* G, int64_t ldg, double* dx, int64_t lddx,
+                       void* stream);
+int smx_spectral_coefficients_adjoint(const smx_plan* plan_host, const int64_t* aoff, const double* A,
+                                      const int32_t* ids, const double* Cbar, double* Fbar, void* stream);
+
 /* ---- tensor-core contraction ---------------------------------------------------------
  * D[M x N] = A B^T (+ bias[n]) with tcgen05.mma kind::tf32 in 3xTF32 form:
  * A = A_hi + A_lo, B = B_hi + B_lo (row-major [M x K] and [N x K], leading
  * dimensions multiples of 4, 16-byte aligned), D = A_hi B_hi^T + A_hi B_lo^T +
- * A_lo B_hi^T accumulated in FP32 in tensor memory.  *err (device int) is set
+ * A_lo B_hi^T accumulated in FP32 in tensor memory (accumulate != 0: added to
+ * the existing D).  *err (device int) is set
  * non-zero if a pipeline wait timed out.  Used for the orthogonal-form
  * contraction when d_out is large (the dense [points x Lambda] x [Lambda x
  * d_out] product of interpolation.py:264-304 in orthogonal form) and for the
  * backward products. */
 int smx_gemm_tf32x3(const float* A_hi, const float* A_lo, int64_t lda, const float* B_hi, const float* B_lo,
-                    int64_t ldb, int M, int N, int K, float* D, int64_t ldd, const float* bias, int* err, void* stream);
+                    int64_t ldb, int M, int N, int K, float* D, int64_t ldd, const float* bias, int accumulate, int* err,
+                    void* stream);
 
 /* hi = TF32(src), lo = TF32(src - hi) for a [rows x cols] block. */
 int smx_split_tf32(const float* src, int64_t rows, int64_t cols, int64_t lds, float* hi, float* lo, int64_t ldo,

@@ -116,7 +116,12 @@ SIGNATURES = {
     "smx_eval_f64_noalloc": (_int, [_p, _p, _i64, _i64, _p, _p]),
     "smx_spectral_panel_tf32": (_int, [_int, _p, _p, _p, _int, _p, _int, _p, _p, _p, _p, _i64, _i64, _p, _p, _i64,
                                         _p]),
-    "smx_gemm_tf32x3": (_int, [_p, _p, _i64, _p, _p, _i64, _int, _int, _int, _p, _i64, _p, _p, _p]),
+    "smx_gemm_tf32x3": (_int, [_p, _p, _i64, _p, _p, _i64, _int, _int, _int, _p, _i64, _p, _int, _p, _p]),
+    "smx_spectral_panel_t_tf32": (_int, [_int, _p, _p, _p, _int, _p, _int, _p, _p, _p, _p, _i64, _i64, _p, _p,
+                                          _i64, _p]),
+    "smx_spectral_vjp_x": (_int, [_int, _p, _p, _p, _int, _p, _int, _p, _p, _p, _p, _i64, _i64, _p, _i64, _p, _i64,
+                                   _p]),
+    "smx_spectral_coefficients_adjoint": (_int, [_p, _p, _p, _p, _p, _p, _p]),
     "smx_split_tf32": (_int, [_p, _i64, _i64, _i64, _p, _p, _i64, _p]),
     "smx_last_error_string": (C.c_char_p, []),
     "smx_version": (C.c_char_p, []),

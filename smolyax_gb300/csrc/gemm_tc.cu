@@ -120,6 +120,7 @@ struct GemmArgs {
   int64_t ldd;
   const float* bias;
   int* err;
+  int accumulate;  // D += A B^T instead of D = A B^T
 };
 
 __global__ void __launch_bounds__(kThreadsTC, 1)
@@ -270,7 +271,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 #pragma unroll
         for (int j = 0; j < kBN; ++j) {
           const int col = n0 + j;
-          if (col < g.N) dr[col] = acc[j] + (g.bias ? g.bias[col] : 0.f);
+          if (col < g.N) dr[col] = acc[j] + (g.bias ? g.bias[col] : 0.f) + (g.accumulate ? dr[col] : 0.f);
         }
       }
     }
@@ -337,7 +338,7 @@ int make_map(CUtensorMap* tm, const float* ptr, int64_t rows, int64_t cols, int6
 }
 
 int launch(const float* Ah, const float* Al, int64_t lda, const float* Bh, const float* Bl, int64_t ldb, int M, int N,
-           int K, float* D, int64_t ldd, const float* bias, int* err, cudaStream_t st) {
+           int K, float* D, int64_t ldd, const float* bias, int* err, int accumulate, cudaStream_t st) {
   CUtensorMap tAh, tAl, tBh, tBl;
   int rc;
   if ((rc = make_map(&tAh, Ah, M, K, lda, kBM)) || (rc = make_map(&tAl, Al, M, K, lda, kBM)) ||
@@ -348,7 +349,7 @@ int launch(const float* Ah, const float* Al, int64_t lda, const float* Bh, const
     cudaFuncSetAttribute(gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, Smem::kTotal);
     attr = true;
   }
-  GemmArgs g{M, N, K, D, ldd, bias, err};
+  GemmArgs g{M, N, K, D, ldd, bias, err, accumulate};
   dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM);
   gemm_tf32x3_kernel<<<grid, kThreadsTC, Smem::kTotal, st>>>(tAh, tAl, tBh, tBl, g);
   SMX_LAUNCH_CHECK("smx_gemm_tf32x3");
@@ -369,12 +370,12 @@ extern "C" int smx_split_tf32(const float* src, int64_t rows, int64_t cols, int6
 }
 
 extern "C" int smx_gemm_tf32x3(const float* A_hi, const float* A_lo, int64_t lda, const float* B_hi, const float* B_lo,
-                               int64_t ldb, int M, int N, int K, float* D, int64_t ldd, const float* bias, int* err,
-                               void* stream) {
+                               int64_t ldb, int M, int N, int K, float* D, int64_t ldd, const float* bias, int accumulate,
+                               int* err, void* stream) {
   SMX_REQUIRE(M >= 0 && N >= 0 && K >= 0 && lda >= K && ldb >= K && ldd >= N, "smx_gemm_tf32x3: bad sizes");
   if (M == 0 || N == 0) return SMX_OK;
   SMX_REQUIRE(K >= 1 && A_hi && A_lo && B_hi && B_lo && D && err, "smx_gemm_tf32x3: null pointer");
   int rc = get_encode();
   if (rc) return rc;
-  return launch(A_hi, A_lo, lda, B_hi, B_lo, ldb, M, N, K, D, ldd, bias, err, smx::as_stream(stream));
+  return launch(A_hi, A_lo, lda, B_hi, B_lo, ldb, M, N, K, D, ldd, bias, err, accumulate, smx::as_stream(stream));
 }

@@ -711,3 +711,236 @@ extern "C" int smx_spectral_panel_tf32(int n_dims, const int32_t* dims, const in
   SMX_LAUNCH_CHECK("smx_spectral_panel_tf32");
   return SMX_OK;
 }
+
+// --- backward ---------------------------------------------------------------------------------
+namespace {
+
+// Basis values of all listed dimensions for one point into row[slot * stride + t].
+__device__ __forceinline__ void basis_row(int n_dims, const int32_t* __restrict__ dims,
+                                          const int32_t* __restrict__ dmax, const int32_t* __restrict__ dsoff,
+                                          const float* __restrict__ fam_a, const float* __restrict__ fam_b,
+                                          const int32_t* __restrict__ fam, const double* __restrict__ xp, float* row,
+                                          int stride, int t) {
+  for (int h = 0; h < n_dims; ++h) {
+    const int dim = dims[h], g = dmax[h], so = dsoff[h];
+    const int fm = fam[dim];
+    const float z = fmaf(fam_a[dim], float(xp[dim]), fam_b[dim]);
+    float pm1 = 0.f, pc = 1.f;
+    for (int n = 0; n < g; ++n) {
+      const float pn = c_alpha[fm][n] * z * pc - c_beta[fm][n] * pm1;
+      pm1 = pc;
+      pc = pn;
+      row[(so + n) * stride + t] = pc;
+    }
+  }
+}
+
+// A^T panel: AT[K-1-j][p] (same reversed column order as the forward panel),
+// one thread per point, coalesced along points.
+__global__ void __launch_bounds__(128) panel_t_tf32_kernel(int n_dims, const int32_t* __restrict__ dims,
+                                                           const int32_t* __restrict__ dmax,
+                                                           const int32_t* __restrict__ dsoff, int n_slots,
+                                                           const int32_t* __restrict__ tape, int K,
+                                                           const float* __restrict__ fam_a,
+                                                           const float* __restrict__ fam_b,
+                                                           const int32_t* __restrict__ fam,
+                                                           const double* __restrict__ x, int64_t P, int64_t ldx,
+                                                           float* __restrict__ ATh, float* __restrict__ ATl,
+                                                           int64_t ldp) {
+  extern __shared__ __align__(16) float sm[];
+  const int tid = threadIdx.x;
+  const int64_t p = blockIdx.x * int64_t(128) + tid;
+  const double* xp = x + (p < P ? p : 0) * ldx;
+  basis_row(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, xp, sm, 128, tid);
+  if (p >= P) return;
+  float st1 = 1.f, st2 = 1.f, st3 = 1.f, st4 = 1.f, st5 = 1.f, st6 = 1.f, st7 = 1.f, st8 = 1.f;
+  for (int j = 0; j < K; ++j) {
+    const int w = __ldg(tape + j);
+    const float b = sm[(w & 0xffff) * 128 + tid];
+    float v;
+    switch (w >> 16) {
+      case 1: st1 = b; v = st1; break;
+      case 2: st2 = st1 * b; v = st2; break;
+      case 3: st3 = st2 * b; v = st3; break;
+      case 4: st4 = st3 * b; v = st4; break;
+      case 5: st5 = st4 * b; v = st5; break;
+      case 6: st6 = st5 * b; v = st6; break;
+      case 7: st7 = st6 * b; v = st7; break;
+      default: st8 = st7 * b; v = st8; break;
+    }
+    uint32_t h, l;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(v - __uint_as_float(h)));
+    const int64_t col = K - 1 - j;
+    ATh[col * ldp + p] = __uint_as_float(h);
+    ATl[col * ldp + p] = __uint_as_float(l);
+  }
+}
+
+// dL/dx[p][d] = a_d * sum_g phibar(d, g) phi'_g(z_d) with
+// phibar(pair) = sum over entries e containing the pair of G[p][e] * (product
+// of e's other basis values).  One thread per point (64 per CTA); the path of
+// the current entry (depth <= 8) is kept as basis slots, values and prefix
+// products; G is read in tiles of 32 columns (reversed pre-order) staged in
+// shared memory.
+__global__ void __launch_bounds__(64) vjp_x_kernel(int n_dims, const int32_t* __restrict__ dims,
+                                                   const int32_t* __restrict__ dmax, const int32_t* __restrict__ dsoff,
+                                                   int n_slots, const int32_t* __restrict__ tape, int K,
+                                                   const float* __restrict__ fam_a, const float* __restrict__ fam_b,
+                                                   const int32_t* __restrict__ fam, const double* __restrict__ x,
+                                                   int64_t P, int64_t ldx, const float* __restrict__ G, int64_t ldg,
+                                                   double* __restrict__ dx, int64_t lddx) {
+  extern __shared__ __align__(16) float sm[];
+  constexpr int TP = 64;
+  float* row = sm;                             // [n_slots][TP] basis values
+  float* bar = sm + size_t(n_slots) * TP;      // [n_slots][TP] adjoints
+  float* tile = bar + size_t(n_slots) * TP;    // [32][TP + 1]
+  const int tid = threadIdx.x;
+  const int64_t p0 = blockIdx.x * int64_t(TP);
+  const int64_t p = p0 + tid;
+  const double* xp = x + (p < P ? p : 0) * ldx;
+  basis_row(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, xp, row, TP, tid);
+  for (int s = 0; s < n_slots; ++s) bar[s * TP + tid] = 0.f;
+  int sl[9];
+  float ph[9], pre[9];
+  pre[0] = 1.f;
+  for (int jb = 0; jb < K; jb += 32) {
+    const int jn = min(32, K - jb);
+    __syncthreads();
+    // tile[c][r] = G[p0 + r][K - 1 - (jb + c)]: coalesced over the 32 columns
+    for (int r = tid >> 5; r < TP; r += TP / 32) {
+      const int c = tid & 31;
+      tile[c * (TP + 1) + r] = (c < jn && p0 + r < P) ? G[(p0 + r) * ldg + (K - 1 - (jb + c))] : 0.f;
+    }
+    __syncthreads();
+    for (int j = 0; j < jn; ++j) {
+      const int w = __ldg(tape + jb + j);
+      const int s = w & 0xffff;
+      const int k = min(8, w >> 16);
+      sl[k] = s;
+      ph[k] = row[s * TP + tid];
+      pre[k] = pre[k - 1] * ph[k];
+      const float gv = tile[j * (TP + 1) + tid];
+      float suf = gv;
+      for (int i = k; i >= 1; --i) {
+        bar[sl[i] * TP + tid] += pre[i - 1] * suf;
+        suf *= ph[i];
+      }
+    }
+  }
+  if (p >= P) return;
+  for (int h = 0; h < n_dims; ++h) {
+    const int dim = dims[h], g = dmax[h], so = dsoff[h];
+    const int fm = fam[dim];
+    const float z = fmaf(fam_a[dim], float(xp[dim]), fam_b[dim]);
+    float pm1 = 0.f, pc = 1.f, dm1 = 0.f, dc = 0.f, acc = 0.f;
+    for (int n = 0; n < g; ++n) {
+      const float al = c_alpha[fm][n], be = c_beta[fm][n];
+      const float pn = al * z * pc - be * pm1;
+      const float dn = al * (pc + z * dc) - be * dm1;
+      pm1 = pc;
+      pc = pn;
+      dm1 = dc;
+      dc = dn;
+      acc = fmaf(bar[(so + n) * TP + tid], dc, acc);
+    }
+    dx[p * lddx + dim] = double(fam_a[dim]) * double(acc);
+  }
+}
+
+// Adjoint of the coefficient transform: Gbar[r] = Cbar[ids[r]], then the
+// transposed mode products per summand: Fbar_s = (A_1^T x ... x A_n^T) Gbar_s.
+__global__ void coeff_adjoint_kernel(int n_sum, const int32_t* __restrict__ poff, const int32_t* __restrict__ pairs,
+                                     const int64_t* __restrict__ eoff, const int32_t* __restrict__ pdeg,
+                                     const int64_t* __restrict__ aoff, const double* __restrict__ A,
+                                     const int32_t* __restrict__ ids, const double* __restrict__ Cbar, int dout,
+                                     double* __restrict__ Fbar) {
+  const int64_t tid = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (tid >= int64_t(n_sum) * dout) return;
+  const int s = int(tid / dout);
+  const int o = int(tid - int64_t(s) * dout);
+  const int q0 = poff[s], n = poff[s + 1] - q0;
+  const int64_t e0 = eoff[s], K = eoff[s + 1] - e0;
+  double* Fs = Fbar + e0 * dout + o;
+  for (int64_t r = 0; r < K; ++r) Fs[r * dout] = Cbar[int64_t(ids[e0 + r]) * dout + o];
+  int64_t stride = 1;
+  for (int i = n - 1; i >= 0; --i) {
+    const int u = pairs[q0 + i];
+    const int m = pdeg[u] + 1;
+    const double* Au = A + aoff[u];
+    const int64_t outer = K / (stride * m);
+    for (int64_t a = 0; a < outer; ++a) {
+      for (int64_t b = 0; b < stride; ++b) {
+        const int64_t base = a * stride * m + b;
+        double v[kMaxG];
+        for (int mm = 0; mm < m; ++mm) v[mm] = Fs[(base + mm * stride) * dout];
+        for (int j = 0; j < m; ++j) {
+          double acc = 0.0;
+          for (int mm = 0; mm < m; ++mm) acc = fma(Au[mm * m + j], v[mm], acc);
+          Fs[(base + j * stride) * dout] = acc;
+        }
+      }
+    }
+    stride *= m;
+  }
+}
+
+}  // namespace
+
+extern "C" int smx_spectral_panel_t_tf32(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff,
+                                         int n_slots, const int32_t* tape, int K, const float* fam_a,
+                                         const float* fam_b, const int32_t* fam, const double* x, int64_t P,
+                                         int64_t ldx, float* AT_hi, float* AT_lo, int64_t ldp, void* stream) {
+  SMX_REQUIRE(n_dims >= 0 && n_slots >= 0 && K >= 0 && P >= 0 && ldp >= P, "smx_spectral_panel_t_tf32: bad sizes");
+  if (P == 0 || K == 0) return SMX_OK;
+  SMX_REQUIRE(dims && dmax && dsoff && tape && fam_a && fam_b && fam && x && AT_hi && AT_lo,
+              "smx_spectral_panel_t_tf32: null pointer");
+  const size_t smem = size_t(n_slots) * 128 * sizeof(float);
+  SMX_REQUIRE(smem <= 220 * 1024, "smx_spectral_panel_t_tf32: too many basis slots");
+  int rc = upload_consts();
+  if (rc) return rc;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(panel_t_tf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    attr = true;
+  }
+  panel_t_tf32_kernel<<<smx::grid_for(P, 128), 128, smem, smx::as_stream(stream)>>>(
+      n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, AT_hi, AT_lo, ldp);
+  SMX_LAUNCH_CHECK("smx_spectral_panel_t_tf32");
+  return SMX_OK;
+}
+
+extern "C" int smx_spectral_vjp_x(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff,
+                                  int n_slots, const int32_t* tape, int K, const float* fam_a, const float* fam_b,
+                                  const int32_t* fam, const double* x, int64_t P, int64_t ldx, const float* G,
+                                  int64_t ldg, double* dx, int64_t lddx, void* stream) {
+  SMX_REQUIRE(n_dims >= 0 && n_slots >= 0 && K >= 0 && P >= 0 && ldg >= K, "smx_spectral_vjp_x: bad sizes");
+  if (P == 0) return SMX_OK;
+  SMX_REQUIRE(dims && dmax && dsoff && tape && fam_a && fam_b && fam && x && G && dx, "smx_spectral_vjp_x: null");
+  const size_t smem = (size_t(n_slots) * 64 * 2 + 32 * 65) * sizeof(float);
+  SMX_REQUIRE(smem <= 220 * 1024, "smx_spectral_vjp_x: too many basis slots");
+  int rc = upload_consts();
+  if (rc) return rc;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(vjp_x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    attr = true;
+  }
+  vjp_x_kernel<<<smx::grid_for(P, 64), 64, smem, smx::as_stream(stream)>>>(
+      n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, G, ldg, dx, lddx);
+  SMX_LAUNCH_CHECK("smx_spectral_vjp_x");
+  return SMX_OK;
+}
+
+extern "C" int smx_spectral_coefficients_adjoint(const smx_plan* pl, const int64_t* aoff, const double* A,
+                                                 const int32_t* ids, const double* Cbar, double* Fbar,
+                                                 void* stream) {
+  SMX_REQUIRE(pl != nullptr, "smx_spectral_coefficients_adjoint: null plan");
+  if (pl->n_summands == 0 || pl->n_entries == 0) return SMX_OK;
+  SMX_REQUIRE(aoff && A && ids && Cbar && Fbar, "smx_spectral_coefficients_adjoint: null pointer");
+  const int64_t nt = int64_t(pl->n_summands) * pl->d_out;
+  coeff_adjoint_kernel<<<smx::grid_for(nt, 128), 128, 0, smx::as_stream(stream)>>>(
+      pl->n_summands, pl->sum_poff, pl->sum_pairs, pl->sum_eoff, pl->pair_deg, aoff, A, ids, Cbar, pl->d_out, Fbar);
+  SMX_LAUNCH_CHECK("smx_spectral_coefficients_adjoint");
+  return SMX_OK;
+}

@@ -178,38 +178,70 @@ class SmolyakBarycentricInterpolator:
         # nodal values: host calls of f with the reference's cache keys, device gather
         fu, umap = self._evaluate_nodes(f, f_evals, zero, sum_poff.cpu().numpy(), sum_pairs.cpu().numpy(),
                                         pair_dim_h, pair_deg_h, pair_voff_h, node_h, R)
-        F64 = torch.empty(max(R * d_out, 1), dtype=torch.float64, device=dev)
-        F32 = torch.empty(max(R * d_out, 1), dtype=torch.float32, device=dev)
-        # Centering: every tensor-product interpolant reproduces constants, so
-        # sum_s zeta_s I^nu_s[f] = c * sum_s zeta_s + sum_s zeta_s I^nu_s[f - c].
-        # With c = f(zero point) (row 0 of every summand) the summands that
-        # cancel in the combination sum shrink by about an order of magnitude.
-        center = fu[umap[0]].copy() if R else np.zeros(d_out)
-        zsum = int(zeta[ent].sum().item()) if n_sum else 0
-        offset = offset + center * float(zsum)
-        P.set("F64", F64)
-        P.set("F32", F32)
-        P.set("offset", T(offset, torch.float64))
-        P.keep["center"] = T(center, torch.float64)
+        P.set("F64", torch.empty(max(R * d_out, 1), dtype=torch.float64, device=dev))
+        P.set("F32", torch.empty(max(R * d_out, 1), dtype=torch.float32, device=dev))
         c = P.c
         c.d_in, c.d_out = d, d_out
         c.n_pairs, c.n_values, c.n_summands = n_pairs, n_values, n_sum
         c.max_n = int(lvl_sum.max().item()) if n_sum else 0
         c.n_entries = R
-        if R:
-            fu_d = T(fu, torch.float64)
-            umap_d = T(umap, torch.int64)
-            call("smx_assemble_F", P.ref(), ptr(zeta[ent].contiguous()), ptr(fu_d), ptr(umap_d),
-                 ptr(P.keep["center"]), ptr(F64), ptr(F32), st)
         P.keep["sum_zeta"] = zeta[ent].contiguous()
-        P.keep["ent"] = ent
+        P.keep["zeta0"] = zeta0
+        P.keep["umap"] = T(umap, torch.int64)
+        P.keep["offset0"] = T(offset, torch.float64)  # zeta_0 f(zero) as the reference computes it
         self._plan = P
+        self._assemble_rows(T(fu, torch.float64))
+        P.keep["ent"] = ent
         self._spectral = None
         self._tree = tree
         self._maxdeg = maxdeg_h
         if self._n_inputs is not None:
             _ = self(torch.rand(self._n_inputs, d, dtype=torch.float64, device=dev))
         return f_evals
+
+    def _assemble_rows(self, fu_d):
+        """Device rows of the plan from the unique nodal values fu [U, d_out].
+
+        Centering: every tensor-product interpolant reproduces constants, so
+        sum_s zeta_s I^nu_s[f] = c * sum_s zeta_s + sum_s zeta_s I^nu_s[f - c].
+        With c = f(zero point) (row 0 of every summand) the summands that
+        cancel in the combination sum shrink by about an order of magnitude."""
+        P = self._plan
+        c = P.c
+        R, d_out = c.n_entries, c.d_out
+        fu_d = fu_d.reshape(-1, d_out).contiguous()
+        P.keep["fu"] = fu_d
+        if R:
+            umap = P.keep["umap"]
+            center = fu_d[umap[0]].clone()
+            zsum = float(P.keep["sum_zeta"].sum().item())
+            offset = P.keep["offset0"] + center * zsum
+            P.keep["center"] = center
+            P.set("offset", offset.contiguous())
+            call("smx_assemble_F", P.ref(), ptr(P.keep["sum_zeta"]), ptr(fu_d), ptr(umap), ptr(center),
+                 ptr(P.keep["F64"]), ptr(P.keep["F32"]), _stream())
+        else:
+            P.keep["center"] = torch.zeros(d_out, dtype=torch.float64, device=fu_d.device)
+            P.set("offset", P.keep["offset0"].clone())
+        self._spectral = None
+
+    @property
+    def nodal_values(self) -> torch.Tensor:
+        """Unique function values at the interpolation nodes, [U, d_out] FP64 on the
+        device (the rows the interpolant is built from; see ``set_nodal_values``)."""
+        assert self._plan is not None, "The operator has not yet been set up for a target function via `set_f`."
+        return self._plan.keep["fu"]
+
+    def set_nodal_values(self, fu) -> None:
+        """Rebuild the interpolant from new values at the same nodes (no calls of f)."""
+        dev = indices.device()
+        fu = torch.as_tensor(fu, dtype=torch.float64, device=dev)
+        assert tuple(fu.shape) == tuple(self.nodal_values.shape), "nodal values must keep their shape"
+        if self._plan.keep["zeta0"] != 0 and self._plan.c.n_entries:
+            # the constant term follows the zero point's value in fu
+            u0 = int(self._plan.keep["umap"][0].item())
+            self._plan.keep["offset0"] = self._plan.keep["zeta0"] * fu[u0].clone()
+        self._assemble_rows(fu)
 
     def _as_out(self, v):
         return np.broadcast_to(np.asarray(v, dtype=float), (self._d_out,)).astype(float)

@@ -65,7 +65,8 @@ class SpectralPlan:
         if int(flag.item()):
             raise RuntimeError("orthogonal-basis coefficients: multi-index missing from the tree")
         self.C64 = C.view(n_lam, d_out)
-        del G, ids, A
+        del G
+        self.A, self.aoff, self.ids = A, aoff, ids  # kept for the adjoint (backward w.r.t. nodal values)
 
         # layout for the FP32 evaluator (host construction from the device tree)
         tree_np = dict(
@@ -103,13 +104,17 @@ class SpectralPlan:
             setattr(s, name, t.data_ptr() if t.numel() else None)
         self.c = s
         self.tc = None
+        self._bwd = None
+        self._fwd_args = (tree_np, C32, np.asarray(ip._maxdeg), fam, fa, fb, T, st)
+        self.plan = pl
         if d_out >= TC_MIN_DOUT:
-            self._build_tc(tree_np, C32, np.asarray(ip._maxdeg), fam, fa, fb, T, st)
+            self._build_tc(*self._fwd_args)
         self.memory_limit = ip._memory_limit
 
     def _build_tc(self, tr, C32, maxdeg, fam, fa, fb, T, st):
         """Operands of the tensor-core contraction: tape over all non-root entries
         (pre-order), coefficient matrix B = C^T split into TF32 hi/lo."""
+        self.tree_np, self.maxdeg = tr, maxdeg
         dims = np.nonzero(maxdeg > 0)[0]
         dmax = maxdeg[dims]
         dsoff = np.concatenate([[0], np.cumsum(dmax)[:-1]]) if dims.size else np.zeros(0, np.int64)
@@ -134,12 +139,105 @@ class SpectralPlan:
         call("smx_split_tf32", ptr(Bd), d_out, ldk, ldk, ptr(Bh), ptr(Bl), ldk, st)
         self.tc = dict(dims=T(dims, torch.int32), dmax=T(dmax, torch.int32), dsoff=T(dsoff, torch.int32),
                        n_slots=n_slots, tape=T(tape, torch.int32), K=K, ldk=ldk, Bh=Bh, Bl=Bl,
-                       bias=self.keep["c0"], err=torch.zeros(1, dtype=torch.int32, device=dev))
+                       bias=self.keep["c0"], err=torch.zeros(1, dtype=torch.int32, device=dev),
+                       ent=torch.as_tensor(ent, device=dev))
 
     def ref(self):
         import ctypes
 
         return ctypes.byref(self.c)
+
+    # ------------------------------------------------------------------ backward
+    def _backward_ops(self):
+        """Tape operands (built as for the forward tensor-core path) plus the
+        coefficient rows C[K x ldo] in the panel's reversed order, TF32 hi/lo."""
+        if self._bwd is None:
+            fwd_tc = self.tc
+            self._build_tc(*self._fwd_args)
+            ops = self.tc
+            self.tc = fwd_tc
+            if ops is None:
+                raise RuntimeError("backward needs the basis table of all pairs in shared memory; plan too large")
+            T = self._fwd_args[6]
+            st = self._fwd_args[7]
+            C32 = self._fwd_args[1]
+            K = ops["K"]
+            d_out = C32.shape[1]
+            ldo = _round4(d_out)
+            ent = ops["ent"].cpu().numpy()
+            rows = np.zeros((max(K, 1), ldo), dtype=np.float32)
+            rows[:K, :d_out] = C32[ent[::-1]]
+            Rd = T(rows, torch.float32)
+            Rh, Rl = torch.empty_like(Rd), torch.empty_like(Rd)
+            call("smx_split_tf32", ptr(Rd), rows.shape[0], ldo, ldo, ptr(Rh), ptr(Rl), ldo, st)
+            ops.update(Rh=Rh, Rl=Rl, ldo=ldo)
+            self._bwd = ops
+        return self._bwd
+
+    def vjp(self, x, g, need_x=True, need_coef=True):
+        """Vector-Jacobian products of y = c0 + A(x) C at cotangent g [P, d_out]:
+        returns (dL/dx [P, d_in] FP64 or None, dL/dC [n_lambda, d_out] FP64 or None)."""
+        ops = self._backward_ops()
+        st = capi.stream_ptr(torch.cuda.current_stream())
+        k = self.keep
+        dev = x.device
+        P, d = int(x.shape[0]), int(x.shape[1])
+        d_out = int(g.shape[1])
+        K, ldk, ldo = ops["K"], ops["ldk"], ops["ldo"]
+        nd = int(ops["dims"].numel())
+        common = (nd, ptr(ops["dims"]), ptr(ops["dmax"]), ptr(ops["dsoff"]), ops["n_slots"], ptr(ops["tape"]), K,
+                  ptr(k["fam_a"]), ptr(k["fam_b"]), ptr(k["fam"]))
+        g32 = torch.zeros(P, ldo, dtype=torch.float32, device=dev)
+        g32[:, :d_out] = g.float()
+        gh, gl = torch.empty_like(g32), torch.empty_like(g32)
+        call("smx_split_tf32", ptr(g32), P, ldo, ldo, ptr(gh), ptr(gl), ldo, st)
+        err = ops["err"]
+        dx = dC = None
+        step = max(128, int(self.memory_limit * 1024**3 // (8 * ldk)) // 128 * 128)
+        if need_x:
+            dx = torch.zeros(P, d, dtype=torch.float64, device=dev)
+            G = torch.empty(min(step, P), ldk, dtype=torch.float32, device=dev)
+            for p0 in range(0, P, step):
+                p1 = min(P, p0 + step)
+                call("smx_gemm_tf32x3", ptr(gh[p0:p1]), ptr(gl[p0:p1]), ldo, ptr(ops["Rh"]), ptr(ops["Rl"]), ldo,
+                     p1 - p0, K, ldo, ptr(G), ldk, None, 0, ptr(err), st)
+                call("smx_spectral_vjp_x", *common, ptr(x[p0:p1]), p1 - p0, d, ptr(G), ldk, ptr(dx[p0:p1]), d, st)
+        if need_coef:
+            ldp = _round4(min(step, P))
+            ATh = torch.empty(K, ldp, dtype=torch.float32, device=dev)
+            ATl = torch.empty_like(ATh)
+            gT = torch.empty(ldo, ldp, dtype=torch.float32, device=dev)
+            gTh, gTl = torch.empty_like(gT), torch.empty_like(gT)
+            dCrev = torch.zeros(K, d_out, dtype=torch.float32, device=dev)
+            for i, p0 in enumerate(range(0, P, step)):
+                p1 = min(P, p0 + step)
+                n = p1 - p0
+                ATh.zero_()
+                ATl.zero_()
+                call("smx_spectral_panel_t_tf32", *common, ptr(x[p0:p1]), n, d, ptr(ATh), ptr(ATl), ldp, st)
+                gT.zero_()
+                gT[:, :n] = g32[p0:p1].t()
+                call("smx_split_tf32", ptr(gT), ldo, ldp, ldp, ptr(gTh), ptr(gTl), ldp, st)
+                call("smx_gemm_tf32x3", ptr(ATh), ptr(ATl), ldp, ptr(gTh), ptr(gTl), ldp, K, d_out, ldp,
+                     ptr(dCrev), d_out, None, 1 if i else 0, ptr(err), st)
+            n_lam = int(self.C64.shape[0])
+            dC = torch.zeros(n_lam, d_out, dtype=torch.float64, device=dev)
+            ent = ops["ent"]
+            dC[ent.flip(0)] = dCrev.double()
+            dC[0] = g.double().sum(0)
+        if int(err.item()):
+            raise RuntimeError("tensor-core contraction reported a pipeline timeout")
+        return dx, dC
+
+    def coefficient_adjoint(self, dC):
+        """dL/d(plan rows F64) [n_entries, d_out] from dL/dC (FP64 adjoint transform)."""
+        pl = self.plan
+        R, d_out = pl.c.n_entries, pl.c.d_out
+        Fbar = torch.zeros(max(R, 1), d_out, dtype=torch.float64, device=dC.device)
+        st = capi.stream_ptr(torch.cuda.current_stream())
+        call("smx_spectral_coefficients_adjoint", pl.ref(), ptr(self.aoff), ptr(self.A), ptr(self.ids),
+             ptr(dC.contiguous()), ptr(Fbar), st)
+        return Fbar[:R]
 
     def evaluate(self, x, y):
         """y[P, d_out] (FP32) at x[P, d_in] (FP64, contiguous, on the device)."""
@@ -170,7 +268,7 @@ class SpectralPlan:
                  ptr(tc["dsoff"]), tc["n_slots"], ptr(tc["tape"]), tc["K"], ptr(k["fam_a"]), ptr(k["fam_b"]),
                  ptr(k["fam"]), ptr(x[p0:p1]), p1 - p0, d, ptr(Ah), ptr(Al), ldk, st)
             call("smx_gemm_tf32x3", ptr(Ah), ptr(Al), ldk, ptr(tc["Bh"]), ptr(tc["Bl"]), ldk, p1 - p0, d_out,
-                 tc["K"], ptr(y[p0:p1]), d_out, ptr(tc["bias"]), ptr(tc["err"]), st)
+                 tc["K"], ptr(y[p0:p1]), d_out, ptr(tc["bias"]), 0, ptr(tc["err"]), st)
         return y
 
 

@@ -34,7 +34,7 @@ def _gemm(A, B, bias=None):
     err = torch.zeros(1, dtype=torch.int32, device=dev)
     b = None if bias is None else torch.as_tensor(bias, dtype=torch.float32, device=dev)
     _capi.call("smx_gemm_tf32x3", _capi.ptr(Ah), _capi.ptr(Al), ld, _capi.ptr(Bh), _capi.ptr(Bl), ld, M, N, K,
-               _capi.ptr(D), N, _capi.ptr(b), _capi.ptr(err), st)
+               _capi.ptr(D), N, _capi.ptr(b), 0, _capi.ptr(err), st)
     torch.cuda.synchronize()
     assert int(err.item()) == 0
     return D.cpu().numpy().astype(np.float64)
