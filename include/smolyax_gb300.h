@@ -285,6 +285,22 @@ int smx_spectral_vjp_x(int n_dims, const int32_t* dims, const int32_t* dmax, con
 int smx_spectral_coefficients_adjoint(const smx_plan* plan_host, const int64_t* aoff, const double* A,
                                       const int32_t* ids, const double* Cbar, double* Fbar, void* stream);
 
+/* Serving: one persistent launch evaluating many work items (interpolant,
+ * inputs, outputs) of different plans and batch sizes; CTAs take 128-point
+ * tiles from a shared counter.  `plans` and `items` are HOST arrays (copied
+ * into the workspace); ws >= smx_spectral_eval_batch_workspace(n_plans,
+ * n_items, largest d_out).  Results equal those of smx_spectral_eval. */
+typedef struct smx_work {
+  int32_t plan;     /* index into plans                                          */
+  int32_t reserved;
+  const double* x;  /* [P, ldx] FP64 inputs (device)                             */
+  int64_t P, ldx;
+  float* y;         /* [P, d_out] FP32 outputs (device)                          */
+} smx_work;
+size_t smx_spectral_eval_batch_workspace(int n_plans, int n_items, int max_d_out);
+int smx_spectral_eval_batch(const smx_spectral* plans, int n_plans, const smx_work* items, int n_items, void* ws,
+                            size_t ws_bytes, void* stream);
+
 /* ---- tensor-core contraction ---------------------------------------------------------
  * D[M x N] = A B^T (+ bias[n]) with tcgen05.mma kind::tf32 in 3xTF32 form:
  * A = A_hi + A_lo, B = B_hi + B_lo (row-major [M x K] and [N x K], leading

@@ -89,6 +89,12 @@ class SmxSpectral(C.Structure):
     ]
 
 
+class SmxWork(C.Structure):
+    """Mirror of ``struct smx_work``."""
+
+    _fields_ = [("plan", _i32), ("reserved", _i32), ("x", _p), ("P", _i64), ("ldx", _i64), ("y", _p)]
+
+
 # name -> (restype, argtypes); must list every function declared in the header.
 SIGNATURES = {
     "smx_lambda_count": (_int, [_p, _int, _dbl, _int, _p, _p, _i64, _p, _p, _p]),
@@ -116,6 +122,8 @@ SIGNATURES = {
     "smx_eval_f64_noalloc": (_int, [_p, _p, _i64, _i64, _p, _p]),
     "smx_spectral_panel_tf32": (_int, [_int, _p, _p, _p, _int, _p, _int, _p, _p, _p, _p, _i64, _i64, _p, _p, _i64,
                                         _p]),
+    "smx_spectral_eval_batch_workspace": (_sz, [_int, _int, _int]),
+    "smx_spectral_eval_batch": (_int, [_p, _int, _p, _int, _p, _sz, _p]),
     "smx_gemm_tf32x3": (_int, [_p, _p, _i64, _p, _p, _i64, _int, _int, _int, _p, _i64, _p, _int, _p, _p]),
     "smx_spectral_panel_t_tf32": (_int, [_int, _p, _p, _p, _int, _p, _int, _p, _p, _p, _p, _i64, _i64, _p, _p,
                                           _i64, _p]),

@@ -13,6 +13,9 @@
 // evaluation sums terms of the size of the result and runs in FP32.
 #include <math.h>
 
+#include <algorithm>
+#include <vector>
+
 #include "common.cuh"
 
 namespace {
@@ -270,16 +273,17 @@ __device__ __forceinline__ void dot_run(const float* __restrict__ Rw, const floa
   }
 }
 
+// One tile of 128 points of one plan (body shared by the single-plan kernel
+// and the multi-plan batch kernel of the serving loop).
 template <int DO>
-__global__ void __launch_bounds__(kThreads, 2) spectral_eval_kernel(SpecArgs a, const double* __restrict__ x,
-                                                                     int64_t P, int64_t ldx, float* __restrict__ y,
-                                                                     int o0) {
-  extern __shared__ __align__(16) float sm[];
+__device__ __forceinline__ void spectral_eval_tile(const SpecArgs& a, const double* __restrict__ x, int64_t P,
+                                                   int64_t ldx, float* __restrict__ y, int o0, int64_t tile,
+                                                   float* sm) {
   float* RED = sm + size_t(a.row) * kTP;  // [kSeg][DO][2][kTP]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int seg = warp / (kTP / 32);
   const int pl = (warp % (kTP / 32)) * 32 + lane;
-  const int64_t p = blockIdx.x * int64_t(kTP) + pl;
+  const int64_t p = tile * int64_t(kTP) + pl;
   const bool live = p < P;
   const double* __restrict__ xp = x + (live ? p : 0) * ldx;
   float* Rw = sm + size_t(pl) * a.row;
@@ -467,6 +471,52 @@ __global__ void __launch_bounds__(kThreads, 2) spectral_eval_kernel(SpecArgs a, 
   }
 }
 
+template <int DO>
+__global__ void __launch_bounds__(kThreads, 2) spectral_eval_kernel(SpecArgs a, const double* __restrict__ x,
+                                                                     int64_t P, int64_t ldx, float* __restrict__ y,
+                                                                     int o0) {
+  extern __shared__ __align__(16) float sm[];
+  spectral_eval_tile<DO>(a, x, P, ldx, y, o0, blockIdx.x, sm);
+}
+
+// Serving: one persistent launch over a table of work items (plan, inputs,
+// outputs, output chunk) of different interpolants and batch sizes.  CTAs take
+// 128-point tiles from an atomic counter; the tile's item is found by binary
+// search over the items' first tiles.
+struct WorkItem {
+  int plan, o0;
+  int64_t tile0, P, ldx;
+  const double* x;
+  float* y;
+};
+
+__global__ void __launch_bounds__(kThreads, 1) spectral_eval_batch_kernel(const SpecArgs* __restrict__ plans,
+                                                                           const WorkItem* __restrict__ items,
+                                                                           int n_items, int64_t total_tiles,
+                                                                           unsigned long long* counter) {
+  extern __shared__ __align__(16) float sm[];
+  __shared__ int64_t s_tile;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = int64_t(atomicAdd(counter, 1ull));
+    __syncthreads();
+    const int64_t t = s_tile;
+    __syncthreads();
+    if (t >= total_tiles) break;
+    int lo = 0, hi = n_items - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (items[mid].tile0 <= t) lo = mid; else hi = mid - 1;
+    }
+    const WorkItem it = items[lo];
+    const SpecArgs& a = plans[it.plan];
+    if (a.dout == 1)
+      spectral_eval_tile<1>(a, it.x, it.P, it.ldx, it.y, it.o0, t - it.tile0, sm);
+    else
+      spectral_eval_tile<4>(a, it.x, it.P, it.ldx, it.y, it.o0, t - it.tile0, sm);
+    __syncthreads();
+  }
+}
+
 bool g_consts_ready = false;
 
 int upload_consts() {
@@ -529,30 +579,30 @@ extern "C" int smx_spectral_coefficients(const smx_plan* pl, const int64_t* aoff
   return SMX_OK;
 }
 
-extern "C" int smx_spectral_eval(const smx_spectral* sp, const double* x, int64_t P, int64_t ldx, float* y,
-                                 void* stream) {
-  SMX_REQUIRE(sp != nullptr, "smx_spectral_eval: null plan");
-  SMX_REQUIRE(P >= 0 && ldx >= sp->d_in && sp->d_out >= 1, "smx_spectral_eval: bad sizes");
-  if (P == 0) return SMX_OK;
-  SMX_REQUIRE(x && y && sp->c0 && sp->fam && sp->fam_a && sp->fam_b && sp->node && sp->node_c,
-              "smx_spectral_eval: null pointer");
-  SMX_REQUIRE(sp->max_depth <= 8, "smx_spectral_eval: hot nodes deeper than 8 are not supported");
-  SMX_REQUIRE(sp->row % 4 == 0 && sp->row >= sp->n_hb + sp->n_vp && sp->n_vp >= 1, "smx_spectral_eval: bad row");
-  SMX_REQUIRE(sp->d_out == 1 || sp->dstride % 4 == 0, "smx_spectral_eval: coefficient stride not 4-aligned");
-  for (int i = 0; i < kSeg; ++i) {
-    SMX_REQUIRE(sp->node_seg[i] <= sp->node_seg[i + 1] && sp->cold_seg[i] <= sp->cold_seg[i + 1],
-                "smx_spectral_eval: segments not ordered");
-  }
-  SMX_REQUIRE(sp->node_seg[0] == 0 && sp->node_seg[kSeg] == sp->n_nodes && sp->cold_seg[0] == 0 &&
-                  sp->cold_seg[kSeg] == sp->n_cold_groups && sp->block_seg[0] == 0 &&
-                  sp->block_seg[kSeg] == sp->n_cold_blocks,
-              "smx_spectral_eval: segments do not cover the plan");
-  SMX_REQUIRE(sp->n_cold_blocks == 0 || (sp->d_out == 1 && sp->blk_dims && sp->blk_run && sp->blk_ab),
-              "smx_spectral_eval: cold blocks need d_out = 1");
+namespace {
+
+int check_spec(const smx_spectral* sp, const char* who) {
+  if (!sp) return smx::set_error(SMX_ERR_ARG, std::string(who) + ": null plan");
+  if (sp->d_out < 1 || !sp->c0 || !sp->fam || !sp->fam_a || !sp->fam_b || !sp->node || !sp->node_c)
+    return smx::set_error(SMX_ERR_ARG, std::string(who) + ": incomplete plan");
+  if (sp->max_depth > 8) return smx::set_error(SMX_ERR_UNSUPPORTED, std::string(who) + ": hot nodes deeper than 8");
+  if (sp->row % 4 != 0 || sp->row < sp->n_hb + sp->n_vp || sp->n_vp < 1)
+    return smx::set_error(SMX_ERR_ARG, std::string(who) + ": bad row");
+  if (sp->d_out != 1 && sp->dstride % 4 != 0)
+    return smx::set_error(SMX_ERR_ARG, std::string(who) + ": coefficient stride not 4-aligned");
   for (int i = 0; i < kSeg; ++i)
-    SMX_REQUIRE(sp->block_seg[i] <= sp->block_seg[i + 1], "smx_spectral_eval: block segments not ordered");
-  int rc = upload_consts();
-  if (rc) return rc;
+    if (sp->node_seg[i] > sp->node_seg[i + 1] || sp->cold_seg[i] > sp->cold_seg[i + 1] ||
+        sp->block_seg[i] > sp->block_seg[i + 1])
+      return smx::set_error(SMX_ERR_ARG, std::string(who) + ": segments not ordered");
+  if (sp->node_seg[0] != 0 || sp->node_seg[kSeg] != sp->n_nodes || sp->cold_seg[0] != 0 ||
+      sp->cold_seg[kSeg] != sp->n_cold_groups || sp->block_seg[0] != 0 || sp->block_seg[kSeg] != sp->n_cold_blocks)
+    return smx::set_error(SMX_ERR_ARG, std::string(who) + ": segments do not cover the plan");
+  if (sp->n_cold_blocks && (sp->d_out != 1 || !sp->blk_dims || !sp->blk_run || !sp->blk_ab))
+    return smx::set_error(SMX_ERR_ARG, std::string(who) + ": cold blocks need d_out = 1");
+  return SMX_OK;
+}
+
+SpecArgs to_args(const smx_spectral* sp) {
   SpecArgs a;
   a.d_in = sp->d_in;
   a.dout = sp->d_out;
@@ -584,8 +634,28 @@ extern "C" int smx_spectral_eval(const smx_spectral* sp, const double* x, int64_
   a.fam_b = sp->fam_b;
   a.fam = sp->fam;
   a.c0 = sp->c0;
+  return a;
+}
+
+size_t spec_smem(const smx_spectral* sp) {
   const int DO = sp->d_out == 1 ? 1 : 4;
-  const size_t smem = (size_t(sp->row) + size_t(kSeg) * DO * 2) * kTP * sizeof(float);
+  return (size_t(sp->row) + size_t(kSeg) * DO * 2) * kTP * sizeof(float);
+}
+
+}  // namespace
+
+extern "C" int smx_spectral_eval(const smx_spectral* sp, const double* x, int64_t P, int64_t ldx, float* y,
+                                 void* stream) {
+  int rc = check_spec(sp, "smx_spectral_eval");
+  if (rc) return rc;
+  SMX_REQUIRE(P >= 0 && ldx >= sp->d_in, "smx_spectral_eval: bad sizes");
+  if (P == 0) return SMX_OK;
+  SMX_REQUIRE(x && y, "smx_spectral_eval: null pointer");
+  rc = upload_consts();
+  if (rc) return rc;
+  const SpecArgs a = to_args(sp);
+  const int DO = sp->d_out == 1 ? 1 : 4;
+  const size_t smem = spec_smem(sp);
   SMX_REQUIRE(smem <= 220 * 1024, "smx_spectral_eval: per-point row too large for shared memory");
   cudaStream_t st = smx::as_stream(stream);
   static bool attr_set[2] = {false, false};
@@ -605,6 +675,79 @@ extern "C" int smx_spectral_eval(const smx_spectral* sp, const double* x, int64_
     }
     SMX_LAUNCH_CHECK("smx_spectral_eval");
   }
+  return SMX_OK;
+}
+
+extern "C" size_t smx_spectral_eval_batch_workspace(int n_plans, int n_items, int max_d_out) {
+  const int chunks = max_d_out <= 1 ? 1 : (max_d_out + 3) / 4;
+  return size_t(n_plans) * sizeof(SpecArgs) + size_t(n_items) * chunks * sizeof(WorkItem) + 1024;
+}
+
+extern "C" int smx_spectral_eval_batch(const smx_spectral* plans, int n_plans, const smx_work* items, int n_items,
+                                       void* ws, size_t ws_bytes, void* stream) {
+  SMX_REQUIRE(n_plans >= 1 && n_items >= 0 && plans && (n_items == 0 || items) && ws,
+              "smx_spectral_eval_batch: bad arguments");
+  if (n_items == 0) return SMX_OK;
+  int max_dout = 1;
+  size_t smem = 0;
+  std::vector<SpecArgs> args(n_plans);
+  for (int i = 0; i < n_plans; ++i) {
+    int rc = check_spec(&plans[i], "smx_spectral_eval_batch");
+    if (rc) return rc;
+    args[i] = to_args(&plans[i]);
+    max_dout = std::max(max_dout, plans[i].d_out);
+    smem = std::max(smem, spec_smem(&plans[i]));
+  }
+  SMX_REQUIRE(smem <= 220 * 1024, "smx_spectral_eval_batch: per-point row too large for shared memory");
+  std::vector<WorkItem> work;
+  int64_t tiles = 0;
+  for (int j = 0; j < n_items; ++j) {
+    const smx_work& w = items[j];
+    SMX_REQUIRE(w.plan >= 0 && w.plan < n_plans && w.P >= 0 && w.ldx >= plans[w.plan].d_in,
+                "smx_spectral_eval_batch: bad work item");
+    if (w.P == 0) continue;
+    SMX_REQUIRE(w.x && w.y, "smx_spectral_eval_batch: null work pointers");
+    const int dout = plans[w.plan].d_out;
+    const int DO = dout == 1 ? 1 : 4;
+    for (int o0 = 0; o0 < dout; o0 += DO) {
+      WorkItem it;
+      it.plan = w.plan;
+      it.o0 = o0;
+      it.tile0 = tiles;
+      it.P = w.P;
+      it.ldx = w.ldx;
+      it.x = w.x;
+      it.y = w.y;
+      work.push_back(it);
+      tiles += (w.P + kTP - 1) / kTP;
+    }
+  }
+  if (work.empty()) return SMX_OK;
+  SMX_REQUIRE(ws_bytes >= smx_spectral_eval_batch_workspace(n_plans, n_items, max_dout),
+              "smx_spectral_eval_batch: workspace too small");
+  int rc = upload_consts();
+  if (rc) return rc;
+  uint8_t* wsb = static_cast<uint8_t*>(ws);
+  unsigned long long* counter = reinterpret_cast<unsigned long long*>(wsb);
+  SpecArgs* d_args = reinterpret_cast<SpecArgs*>(wsb + 256);
+  WorkItem* d_items = reinterpret_cast<WorkItem*>(wsb + 256 + ((n_plans * sizeof(SpecArgs) + 255) / 256) * 256);
+  cudaStream_t st = smx::as_stream(stream);
+  cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
+  cudaMemcpyAsync(d_args, args.data(), n_plans * sizeof(SpecArgs), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d_items, work.data(), work.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, st);
+  SMX_LAUNCH_CHECK("smx_spectral_eval_batch copies");
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(spectral_eval_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    attr = true;
+  }
+  int dev = 0, sms = 0, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, spectral_eval_batch_kernel, kThreads, smem);
+  const int64_t grid = std::min<int64_t>(tiles, int64_t(std::max(1, sms) * std::max(1, per_sm)));
+  spectral_eval_batch_kernel<<<unsigned(grid), kThreads, smem, st>>>(d_args, d_items, int(work.size()), tiles, counter);
+  SMX_LAUNCH_CHECK("smx_spectral_eval_batch");
   return SMX_OK;
 }
 
@@ -791,7 +934,7 @@ __global__ void __launch_bounds__(64) vjp_x_kernel(int n_dims, const int32_t* __
                                                    int64_t P, int64_t ldx, const float* __restrict__ G, int64_t ldg,
                                                    double* __restrict__ dx, int64_t lddx) {
   extern __shared__ __align__(16) float sm[];
-  constexpr int TP = 64;
+  const int TP = blockDim.x;                   // 64, 32 or 16 points per CTA (shared memory permitting)
   float* row = sm;                             // [n_slots][TP] basis values
   float* bar = sm + size_t(n_slots) * TP;      // [n_slots][TP] adjoints
   float* tile = bar + size_t(n_slots) * TP;    // [32][TP + 1]
@@ -808,8 +951,8 @@ __global__ void __launch_bounds__(64) vjp_x_kernel(int n_dims, const int32_t* __
     const int jn = min(32, K - jb);
     __syncthreads();
     // tile[c][r] = G[p0 + r][K - 1 - (jb + c)]: coalesced over the 32 columns
-    for (int r = tid >> 5; r < TP; r += TP / 32) {
-      const int c = tid & 31;
+    for (int idx = tid; idx < 32 * TP; idx += TP) {
+      const int c = idx & 31, r = idx >> 5;
       tile[c * (TP + 1) + r] = (c < jn && p0 + r < P) ? G[(p0 + r) * ldg + (K - 1 - (jb + c))] : 0.f;
     }
     __syncthreads();
@@ -917,7 +1060,9 @@ extern "C" int smx_spectral_vjp_x(int n_dims, const int32_t* dims, const int32_t
   SMX_REQUIRE(n_dims >= 0 && n_slots >= 0 && K >= 0 && P >= 0 && ldg >= K, "smx_spectral_vjp_x: bad sizes");
   if (P == 0) return SMX_OK;
   SMX_REQUIRE(dims && dmax && dsoff && tape && fam_a && fam_b && fam && x && G && dx, "smx_spectral_vjp_x: null");
-  const size_t smem = (size_t(n_slots) * 64 * 2 + 32 * 65) * sizeof(float);
+  int TP = 64;
+  while (TP > 16 && (size_t(n_slots) * TP * 2 + 32 * (TP + 1)) * sizeof(float) > 220 * 1024) TP /= 2;
+  const size_t smem = (size_t(n_slots) * TP * 2 + 32 * (TP + 1)) * sizeof(float);
   SMX_REQUIRE(smem <= 220 * 1024, "smx_spectral_vjp_x: too many basis slots");
   int rc = upload_consts();
   if (rc) return rc;
@@ -926,7 +1071,7 @@ extern "C" int smx_spectral_vjp_x(int n_dims, const int32_t* dims, const int32_t
     cudaFuncSetAttribute(vjp_x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     attr = true;
   }
-  vjp_x_kernel<<<smx::grid_for(P, 64), 64, smem, smx::as_stream(stream)>>>(
+  vjp_x_kernel<<<smx::grid_for(P, TP), TP, smem, smx::as_stream(stream)>>>(
       n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, G, ldg, dx, lddx);
   SMX_LAUNCH_CHECK("smx_spectral_vjp_x");
   return SMX_OK;

@@ -247,11 +247,21 @@ class SmolyakBarycentricInterpolator:
         return np.broadcast_to(np.asarray(v, dtype=float), (self._d_out,)).astype(float)
 
     def _evaluate_nodes(self, f, f_evals, zero, sum_poff, sum_pairs, pdim, pdeg, pvoff, node, R):
-        """Unique function values and the row -> value map (``interpolation.py:201-228``)."""
+        """Unique function values and the row -> value map (``interpolation.py:201-228``).
+
+        Keys follow the reference's cache: nested rules key by the sparse node
+        multi-index ((dim, mu), ...), non-nested rules by that key inside a
+        dictionary per multi-index nu.  Missing values are computed by calling f
+        once per node (the reference's convention) or, if f has a true attribute
+        ``vectorized``, once on the stacked [n, d_in] array of missing nodes."""
         nested = self._is_nested
+        vectorized = bool(getattr(f, "vectorized", False))
         keys = {}
         vals = []
         umap = np.empty(R, dtype=np.int64)
+        pending = []  # (cache, key, point) of values still to compute
+        pending_keys = set()
+        rows = []  # (cache, key) per row
         r = 0
         n_sum = len(sum_poff) - 1
         for s in range(n_sum):
@@ -265,33 +275,43 @@ class SmolyakBarycentricInterpolator:
             else:
                 nu = tuple(zip(dims, degs))
                 cache = f_evals.get(nu, {})
+                f_evals[nu] = cache
                 ukey = nu
             n = len(dims)
             mu = [0] * n
             K = int(np.prod([g + 1 for g in degs]))
             for _ in range(K):
                 key = tuple((dims[i], mu[i]) for i in range(n) if mu[i] > 0)
-                if key not in cache:
+                if key not in cache and (ukey, key) not in pending_keys:
                     x = zero.copy()
                     for i in range(n):
                         x[dims[i]] = node[offs[i] + mu[i]]
-                    cache[key] = f(x)
-                    self._n_f_evals_new += 1
-                gk = (ukey, key)
-                idx = keys.get(gk)
-                if idx is None:
-                    idx = len(vals)
-                    keys[gk] = idx
-                    vals.append(self._as_out(cache[key]))
-                umap[r] = idx
+                    pending.append((cache, key, x))
+                    pending_keys.add((ukey, key))
+                rows.append((cache, ukey, key))
                 r += 1
                 for i in range(n - 1, -1, -1):
                     mu[i] += 1
                     if mu[i] <= degs[i]:
                         break
                     mu[i] = 0
-            if not nested:
-                f_evals[ukey] = cache
+        if pending:
+            if vectorized:
+                out = np.asarray(f(np.stack([p[2] for p in pending])), dtype=float).reshape(len(pending), -1)
+                for (cache, key, _), v in zip(pending, out):
+                    cache[key] = v
+            else:
+                for cache, key, x in pending:
+                    cache[key] = f(x)
+            self._n_f_evals_new += len(pending)
+        for r, (cache, ukey, key) in enumerate(rows):
+            gk = (ukey, key)
+            idx = keys.get(gk)
+            if idx is None:
+                idx = len(vals)
+                keys[gk] = idx
+                vals.append(self._as_out(cache[key]))
+            umap[r] = idx
         fu = np.array(vals, dtype=float).reshape(-1, self._d_out) if vals else np.zeros((1, self._d_out))
         return fu, umap
 

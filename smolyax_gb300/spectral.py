@@ -119,7 +119,8 @@ class SpectralPlan:
         dmax = maxdeg[dims]
         dsoff = np.concatenate([[0], np.cumsum(dmax)[:-1]]) if dims.size else np.zeros(0, np.int64)
         n_slots = int(dmax.sum())
-        if (n_slots * 128 + 32 * 129) * 4 > 220 * 1024 or int(tr["level"].max()) > 8:
+        limit = (n_slots * 128 + 32 * 129) * 4 > 220 * 1024
+        if int(tr["level"].max()) > 8 or (limit and not getattr(self, "_for_backward", False)):
             return  # the FP32 stream evaluator serves this plan
         idx = np.full(maxdeg.shape[0], -1, dtype=np.int64)
         idx[dims] = np.arange(dims.size)
@@ -153,7 +154,9 @@ class SpectralPlan:
         coefficient rows C[K x ldo] in the panel's reversed order, TF32 hi/lo."""
         if self._bwd is None:
             fwd_tc = self.tc
+            self._for_backward = True
             self._build_tc(*self._fwd_args)
+            self._for_backward = False
             ops = self.tc
             self.tc = fwd_tc
             if ops is None:
@@ -174,7 +177,7 @@ class SpectralPlan:
             self._bwd = ops
         return self._bwd
 
-    def vjp(self, x, g, need_x=True, need_coef=True):
+    def vjp(self, x, g, need_x=True, need_coef=True, check=True):
         """Vector-Jacobian products of y = c0 + A(x) C at cotangent g [P, d_out]:
         returns (dL/dx [P, d_in] FP64 or None, dL/dC [n_lambda, d_out] FP64 or None)."""
         ops = self._backward_ops()
@@ -225,7 +228,7 @@ class SpectralPlan:
             ent = ops["ent"]
             dC[ent.flip(0)] = dCrev.double()
             dC[0] = g.double().sum(0)
-        if int(err.item()):
+        if check and int(err.item()):
             raise RuntimeError("tensor-core contraction reported a pipeline timeout")
         return dx, dC
 
