@@ -258,6 +258,90 @@ def run_tensor_workload(args):
     return 0
 
 
+def serving_fleet(seed=0):
+    """16 interpolants: d_in log-uniform [4, 1000], d_out in {1, 16, 256, 1024},
+    |Lambda| log-uniform [1e2, 1e5], Leja or Gauss-Hermite at random (seed 0)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(16):
+        d_in = int(round(np.exp(rng.uniform(np.log(4), np.log(1000)))))
+        d_out = int(rng.choice([1, 16, 256, 1024]))
+        lam = int(round(np.exp(rng.uniform(np.log(1e2), np.log(1e5)))))
+        kind = "leja" if rng.random() < 0.5 else "gh"
+        out.append((i, d_in, d_out, lam, kind))
+    return out
+
+
+def _vec_target(kind, d, d_out, seed):
+    rng = np.random.default_rng(seed)
+    if kind == "leja":
+        W = rng.uniform(0, 1, (d_out, d)) / (np.arange(d) + 1) ** 2
+        W *= 0.5 / W.sum(axis=1, keepdims=True)
+        f = lambda x: 1.0 / (1.0 + np.asarray(x) @ W.T)
+    else:
+        A = rng.normal(0.0, 0.3, (d_out, d)) / (np.arange(d) + 1) ** 1.5
+        f = lambda x: np.exp(-(np.asarray(x) @ A.T))
+    f.vectorized = True
+    return f
+
+
+def run_serving(args):
+    """Poisson stream of eval/gradient requests over the 16-interpolant fleet."""
+    import torch
+
+    from smolyax_gb300 import SmolyakBarycentricInterpolator, indices, nodes
+    from smolyax_gb300.serving import Request, Server, replay
+
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    ips, fleet = {}, serving_fleet(0)
+    for i, d, d_out, lam, kind in fleet:
+        k = np.log((2 + np.arange(d)) / np.log(2))
+        t = indices.find_approximate_threshold(k, lam, nested=True, accuracy=0.01)
+        gen = nodes.Leja(dim=d) if kind == "leja" else nodes.GaussHermite(dim=d)
+        ips["ip%02d" % i] = SmolyakBarycentricInterpolator(node_gen=gen, k=k, t=t, d_out=d_out,
+                                                            f=_vec_target(kind, d, d_out, i), memory_limit=2.0)
+    server = Server(ips, memory_budget=48.0, n_streams=8)
+    setup_s = time.perf_counter() - t0
+    rng = np.random.default_rng(1)
+    pools = {}
+    for name, ip in ips.items():
+        kind = "leja" if isinstance(ip._node_gen, nodes.Leja) else "gh"
+        xs = rng.uniform(-1, 1, (65536, ip.d_in)) if kind == "leja" else rng.normal(size=(65536, ip.d_in)) / np.sqrt(2)
+        pools[name] = xs
+    n_req = args.requests
+    reqs, arrivals = [], np.cumsum(rng.exponential(1.0 / args.rate, n_req))
+    names = sorted(ips)
+    for j in range(n_req):
+        name = names[rng.integers(len(names))]
+        P = int(np.exp(rng.uniform(0, np.log(65536))))
+        op = "grad" if rng.random() < 0.2 else "eval"
+        reqs.append(Request(name, pools[name][:P], op=op, precision="fp32"))
+    with ClockSampler(0) as clk:
+        wall = replay(server, arrivals, reqs)
+    st = server.stats()
+    ev = [r for r in reqs if r.op == "eval" and r.error is None]
+    evals = sum(r.points * ips[r.name].d_out for r in ev)
+    lat_e = np.array([r.latency for r in ev]) * 1e3
+    lat_g = np.array([r.latency for r in reqs if r.op == "grad" and r.error is None]) * 1e3
+    line = {
+        "metric": METRIC, "workload": "serving", "value": evals / wall, "unit": "evals/s", "n_gpus": 1,
+        "higher_is_better": True, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": "16 resident interpolants (d_in 4-1000, d_out 1-1024, |Lambda| 1e2-1e5, Leja/GH, seed 0);"
+                               " Poisson stream, 80% eval / 20% gradient, batch log-uniform [1, 65536]",
+                   "requests": n_req, "rate_per_s": args.rate},
+        "latency_ms": {"p50": float(np.percentile(lat_e, 50)), "p99": float(np.percentile(lat_e, 99)),
+                       "grad_p50": float(np.percentile(lat_g, 50)) if lat_g.size else None,
+                       "grad_p99": float(np.percentile(lat_g, 99)) if lat_g.size else None},
+        "wall_s": wall, "setup_s": setup_s, "launches": st["launches"], "merged_launches": st["batch_launches"],
+        "completed": st["completed"], "rejected": st["rejected"], "clocks": clk.summary(),
+        "fleet": [dict(d_in=d, d_out=o, lam=l, kind=kd, K=int(ips["ip%02d" % i]._tree.size),
+                       tensor=ips["ip%02d" % i].spectral_plan().tc is not None) for i, d, o, l, kd in fleet],
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -385,10 +469,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--points", type=int, default=POINTS)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="leja1000", choices=["leja1000"] + sorted(WORKLOADS))
+    ap.add_argument("--workload", default="leja1000", choices=["leja1000", "serving"] + sorted(WORKLOADS))
+    ap.add_argument("--requests", type=int, default=300)
+    ap.add_argument("--rate", type=float, default=200.0)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "serving":
+        return run_serving(args)
     if args.workload != "leja1000":
         return run_tensor_workload(args)
     return run_ours(args)

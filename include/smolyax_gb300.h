@@ -261,10 +261,11 @@ int smx_spectral_eval(const smx_spectral* plan_host, const double* x, int64_t P,
  * of the tape goes to column K-1-j: summing from small to large terms limits
  * the truncation of the tensor cores' FP32 accumulation).  Basis slots: for each
  * listed dimension dims[h], degrees 1..dmax[h] at dsoff[h]. */
+size_t smx_spectral_panel_workspace(int n_slots, int64_t P);
 int smx_spectral_panel_tf32(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff, int n_slots,
                             const int32_t* tape, int K, const float* fam_a, const float* fam_b, const int32_t* fam,
-                            const double* x, int64_t P, int64_t ldx, float* A_hi, float* A_lo, int64_t lda,
-                            void* stream);
+                            const double* x, int64_t P, int64_t ldx, float* A_hi, float* A_lo, int64_t lda, void* ws,
+                            size_t ws_bytes, void* stream);
 
 /* Backward of the orthogonal form (no counterpart in the reference, whose
  * derivative is the dense Jacobian of interpolation.py:306-345):

@@ -20,7 +20,8 @@
 
 namespace {
 
-constexpr int kMaxG = 24;  // max degree of a pair handled by the set-up kernels
+constexpr int kMaxG = 24;     // max degree + 1 handled by the on-device basis-change inversion
+constexpr int kMaxRec = 512;  // max degree of the three-term recurrence tables and mode products
 
 // phi_{n+1} = alpha_n z phi_n - beta_n phi_{n-1}, phi_0 = 1, phi_{-1} = 0.
 __host__ __device__ inline void rec_coeffs(int fam, int n, double* a, double* b) {
@@ -113,7 +114,7 @@ __global__ void spectral_transform_kernel(int n_sum, const int32_t* __restrict__
     for (int64_t a = 0; a < outer; ++a) {
       for (int64_t b = 0; b < stride; ++b) {
         const int64_t base = a * stride * m + b;
-        double v[kMaxG];
+        double v[kMaxRec];
         for (int j = 0; j < m; ++j) v[j] = Gs[(base + j * stride) * dout];
         for (int mm = 0; mm < m; ++mm) {
           double acc = 0.0;
@@ -232,8 +233,8 @@ __device__ __forceinline__ void kahan_add(float& sum, float& comp, float v) {
   sum = t;
 }
 
-__constant__ float c_alpha[2][kMaxG];
-__constant__ float c_beta[2][kMaxG];
+__constant__ float c_alpha[2][kMaxRec];
+__constant__ float c_beta[2][kMaxRec];
 
 // s[q] += sum over the run's slots of coef * row value.
 template <int DO>
@@ -521,9 +522,9 @@ bool g_consts_ready = false;
 
 int upload_consts() {
   if (g_consts_ready) return SMX_OK;
-  float al[2][kMaxG], be[2][kMaxG];
+  static float al[2][kMaxRec], be[2][kMaxRec];
   for (int f = 0; f < 2; ++f)
-    for (int n = 0; n < kMaxG; ++n) {
+    for (int n = 0; n < kMaxRec; ++n) {
       double a, b;
       rec_coeffs(f, n, &a, &b);
       al[f][n] = float(a);
@@ -768,12 +769,16 @@ __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32
                                                          const float* __restrict__ fam_b,
                                                          const int32_t* __restrict__ fam, const double* __restrict__ x,
                                                          int64_t P, int64_t ldx, float* __restrict__ Ahi,
-                                                         float* __restrict__ Alo, int64_t lda) {
+                                                         float* __restrict__ Alo, int64_t lda,
+                                                         float* __restrict__ grow) {
   extern __shared__ __align__(16) float sm[];
-  float* row = sm;                       // [n_slots][128]
-  float* tile = sm + size_t(n_slots) * 128;  // [32][129]
+  // basis row: shared memory [n_slots][128], or (large plans) global scratch
+  // [n_slots][gridDim.x * 128] read through L1
+  const int64_t rstride = grow ? int64_t(gridDim.x) * 128 : 128;
+  float* tile = grow ? sm : sm + size_t(n_slots) * 128;  // [32][129]
   const int tid = threadIdx.x;
   const int64_t p0 = blockIdx.x * int64_t(128);
+  float* row = grow ? grow + p0 : sm;
   const int64_t p = p0 + tid;
   const double* xp = x + (p < P ? p : 0) * ldx;
   for (int h = 0; h < n_dims; ++h) {
@@ -785,7 +790,7 @@ __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32
       const float pn = c_alpha[fm][n] * z * pc - c_beta[fm][n] * pm1;
       pm1 = pc;
       pc = pn;
-      row[(so + n) * 128 + tid] = pc;
+      row[(so + n) * rstride + tid] = pc;
     }
   }
   float st1 = 1.f, st2 = 1.f, st3 = 1.f, st4 = 1.f, st5 = 1.f, st6 = 1.f, st7 = 1.f, st8 = 1.f;
@@ -793,7 +798,7 @@ __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32
     const int jn = min(32, K - jb);
     for (int j = 0; j < jn; ++j) {
       const int w = __ldg(tape + jb + j);
-      const float b = row[(w & 0xffff) * 128 + tid];
+      const float b = row[(w & 0xffff) * rstride + tid];
       float v;
       switch (w >> 16) {
         case 1: st1 = b; v = st1; break;
@@ -832,16 +837,25 @@ __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32
 
 }  // namespace
 
+extern "C" size_t smx_spectral_panel_workspace(int n_slots, int64_t P) {
+  const size_t smem = (size_t(n_slots) * 128 + 32 * 129) * sizeof(float);
+  if (smem <= 220 * 1024) return 0;
+  return size_t(n_slots) * size_t((P + 127) / 128 * 128) * sizeof(float);
+}
+
 extern "C" int smx_spectral_panel_tf32(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff,
                                        int n_slots, const int32_t* tape, int K, const float* fam_a,
                                        const float* fam_b, const int32_t* fam, const double* x, int64_t P, int64_t ldx,
-                                       float* A_hi, float* A_lo, int64_t lda, void* stream) {
+                                       float* A_hi, float* A_lo, int64_t lda, void* ws, size_t ws_bytes,
+                                       void* stream) {
   SMX_REQUIRE(n_dims >= 0 && n_slots >= 0 && K >= 0 && P >= 0 && lda >= K, "smx_spectral_panel_tf32: bad sizes");
   if (P == 0 || K == 0) return SMX_OK;
   SMX_REQUIRE(dims && dmax && dsoff && tape && fam_a && fam_b && fam && x && A_hi && A_lo,
               "smx_spectral_panel_tf32: null pointer");
-  const size_t smem = (size_t(n_slots) * 128 + 32 * 129) * sizeof(float);
-  SMX_REQUIRE(smem <= 220 * 1024, "smx_spectral_panel_tf32: too many basis slots for shared memory");
+  const size_t need = smx_spectral_panel_workspace(n_slots, P);
+  SMX_REQUIRE(ws_bytes >= need && (need == 0 || ws), "smx_spectral_panel_tf32: workspace too small");
+  float* grow = need ? static_cast<float*>(ws) : nullptr;
+  const size_t smem = grow ? size_t(32 * 129) * sizeof(float) : (size_t(n_slots) * 128 + 32 * 129) * sizeof(float);
   int rc = upload_consts();
   if (rc) return rc;
   static bool attr = false;
@@ -850,7 +864,7 @@ extern "C" int smx_spectral_panel_tf32(int n_dims, const int32_t* dims, const in
     attr = true;
   }
   panel_tf32_kernel<<<smx::grid_for(P, 128), 128, smem, smx::as_stream(stream)>>>(
-      n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, A_hi, A_lo, lda);
+      n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, A_hi, A_lo, lda, grow);
   SMX_LAUNCH_CHECK("smx_spectral_panel_tf32");
   return SMX_OK;
 }
@@ -1015,7 +1029,7 @@ __global__ void coeff_adjoint_kernel(int n_sum, const int32_t* __restrict__ poff
     for (int64_t a = 0; a < outer; ++a) {
       for (int64_t b = 0; b < stride; ++b) {
         const int64_t base = a * stride * m + b;
-        double v[kMaxG];
+        double v[kMaxRec];
         for (int mm = 0; mm < m; ++mm) v[mm] = Fs[(base + mm * stride) * dout];
         for (int j = 0; j < m; ++j) {
           double acc = 0.0;

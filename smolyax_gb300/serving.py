@@ -184,7 +184,16 @@ class Server:
         if batch:
             self._launch_batch(batch, batch_stream, now)
         for req, nb, stream in singles:
-            self._launch_single(req, nb, stream, now)
+            try:
+                self._launch_single(req, nb, stream, now)
+            except (RuntimeError, ValueError) as e:  # the plan cannot serve this request
+                req.error = str(e)
+                req.t_done = time.perf_counter()
+                req.done.set()
+                with self.lock:
+                    self.rejected.append(req)
+                    self.in_use -= nb
+                    self.free_streams.append(stream)
 
     def _h2d(self, req, stream):
         xh = torch.from_numpy(req.x).pin_memory()

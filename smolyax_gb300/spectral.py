@@ -21,6 +21,52 @@ from ._capi import call, ptr
 
 FAMILIES = {"legendre": 0, "hermite": 1}
 TC_MIN_DOUT = 16  # from this many outputs on, the tensor-core contraction is used
+MAX_DEGREE = 512  # recurrence tables of the kernels
+
+
+def _phi_table(fam, z, n):
+    """phi_0..phi_n at z (rows), the kernels' three-term recurrence in FP64."""
+    out = np.empty((n + 1,) + np.shape(z))
+    out[0] = 1.0
+    pm1, p = np.zeros_like(z), np.ones_like(z)
+    for m in range(n):
+        if fam == 0:
+            a, b = (2 * m + 1) / (m + 1), m / (m + 1)
+        else:
+            a, b = np.sqrt(2.0 / (m + 1)), np.sqrt(m / (m + 1))
+        pm1, p = p, a * z * p - b * pm1
+        out[m + 1] = p
+    return out
+
+
+def basis_change_quadrature(pdim, pdeg, pvoff, node, fam, fa, fb):
+    """Per pair, A[m][j] = coefficient of phi_m in the Lagrange polynomial l_j of
+    the pair's nodes, by Gauss quadrature (exact for these degrees, no matrix
+    inversion): A[m][j] = sum_q w_q l_j(s_q) phi_m(s_q) / h_m."""
+    out = []
+    for u in range(len(pdeg)):
+        g = int(pdeg[u])
+        d = int(pdim[u])
+        z = fa[d] * node[pvoff[u] : pvoff[u] + g + 1] + fb[d]
+        if fam[d] == 0:
+            sq, wq = np.polynomial.legendre.leggauss(g + 1)
+            h = 2.0 / (2 * np.arange(g + 1) + 1)
+        else:
+            sq, wq = np.polynomial.hermite.hermgauss(g + 1)
+            h = np.full(g + 1, np.sqrt(np.pi))
+        bw = 1.0 / np.prod(np.where(np.eye(g + 1, dtype=bool), 1.0, z[:, None] - z[None, :]), axis=1)
+        diff = sq[:, None] - z[None, :]
+        hit = diff == 0
+        with np.errstate(divide="ignore", invalid="ignore"):
+            L = bw[None, :] / diff
+        with np.errstate(divide="ignore", invalid="ignore"):
+            L = L / L.sum(axis=1, keepdims=True)
+        rows = np.nonzero(hit.any(axis=1))[0]
+        L[rows] = hit[rows].astype(float)
+        Phi = _phi_table(int(fam[d]), sq, g)  # [m][q]
+        A = (Phi * wq[None, :]) @ L / h[:, None]
+        out.append(A.ravel())
+    return np.concatenate(out) if out else np.zeros(1)
 
 
 class SpectralPlan:
@@ -48,13 +94,22 @@ class SpectralPlan:
         pdeg_h = pl.keep["pair_deg"].cpu().numpy().astype(np.int64)
         aoff_h = np.concatenate([[0], np.cumsum((pdeg_h + 1) ** 2)[:-1]]) if c.n_pairs else np.zeros(1, np.int64)
         aoff = T(aoff_h, torch.int64)
-        A = torch.empty(max(int(((pdeg_h + 1) ** 2).sum()), 1), dtype=torch.float64, device=dev)
         flag = torch.zeros(1, dtype=torch.int32, device=dev)
-        call("smx_spectral_pairs", c.n_pairs, ptr(pl.keep["pair_dim"]), ptr(pl.keep["pair_deg"]),
-             ptr(pl.keep["pair_voff"]), ptr(aoff), ptr(pl.keep["node"]), ptr(self.fam), ptr(self.fa64),
-             ptr(self.fb64), ptr(A), ptr(flag), st)
-        if int(flag.item()):
-            raise RuntimeError("orthogonal-basis set-up failed (code %d)" % int(flag.item()))
+        if c.n_pairs and int(pdeg_h.max()) >= MAX_DEGREE:
+            raise RuntimeError("pair degree %d exceeds the orthogonal form's limit %d" % (int(pdeg_h.max()),
+                                                                                       MAX_DEGREE - 1))
+        if c.n_pairs and int(pdeg_h.max()) + 1 > 24:
+            # high degrees: inversion-free basis change by Gauss quadrature (host, FP64)
+            A = T(basis_change_quadrature(pl.keep["pair_dim"].cpu().numpy(), pdeg_h,
+                                          pl.keep["pair_voff"].cpu().numpy(), pl.keep["node"].cpu().numpy(),
+                                          fam, fa, fb), torch.float64)
+        else:
+            A = torch.empty(max(int(((pdeg_h + 1) ** 2).sum()), 1), dtype=torch.float64, device=dev)
+            call("smx_spectral_pairs", c.n_pairs, ptr(pl.keep["pair_dim"]), ptr(pl.keep["pair_deg"]),
+                 ptr(pl.keep["pair_voff"]), ptr(aoff), ptr(pl.keep["node"]), ptr(self.fam), ptr(self.fa64),
+                 ptr(self.fb64), ptr(A), ptr(flag), st)
+            if int(flag.item()):
+                raise RuntimeError("orthogonal-basis set-up failed (code %d)" % int(flag.item()))
         n_lam = tree.size
         R = c.n_entries
         G = torch.empty(max(R * d_out, 1), dtype=torch.float64, device=dev)
@@ -107,7 +162,8 @@ class SpectralPlan:
         self._bwd = None
         self._fwd_args = (tree_np, C32, np.asarray(ip._maxdeg), fam, fa, fb, T, st)
         self.plan = pl
-        if d_out >= TC_MIN_DOUT:
+        stream_fits = (lay["row"] + 4 * (1 if d_out == 1 else 4) * 2) * 128 * 4 <= 220 * 1024
+        if d_out >= TC_MIN_DOUT or not stream_fits:
             self._build_tc(*self._fwd_args)
         self.memory_limit = ip._memory_limit
 
@@ -119,8 +175,7 @@ class SpectralPlan:
         dmax = maxdeg[dims]
         dsoff = np.concatenate([[0], np.cumsum(dmax)[:-1]]) if dims.size else np.zeros(0, np.int64)
         n_slots = int(dmax.sum())
-        limit = (n_slots * 128 + 32 * 129) * 4 > 220 * 1024
-        if int(tr["level"].max()) > 8 or (limit and not getattr(self, "_for_backward", False)):
+        if int(tr["level"].max()) > 8:
             return  # the FP32 stream evaluator serves this plan
         idx = np.full(maxdeg.shape[0], -1, dtype=np.int64)
         idx[dims] = np.arange(dims.size)
@@ -154,13 +209,11 @@ class SpectralPlan:
         coefficient rows C[K x ldo] in the panel's reversed order, TF32 hi/lo."""
         if self._bwd is None:
             fwd_tc = self.tc
-            self._for_backward = True
             self._build_tc(*self._fwd_args)
-            self._for_backward = False
             ops = self.tc
             self.tc = fwd_tc
             if ops is None:
-                raise RuntimeError("backward needs the basis table of all pairs in shared memory; plan too large")
+                raise RuntimeError("backward needs Smolyak index depth <= 8 (register product stack)")
             T = self._fwd_args[6]
             st = self._fwd_args[7]
             C32 = self._fwd_args[1]
@@ -267,9 +320,11 @@ class SpectralPlan:
             Al[:, tc["K"]:] = 0
         for p0 in range(0, P, step):
             p1 = min(P, p0 + step)
+            nws = capi.size("smx_spectral_panel_workspace", tc["n_slots"], p1 - p0)
+            ws = torch.empty(max(nws, 1), dtype=torch.uint8, device=x.device)
             call("smx_spectral_panel_tf32", int(tc["dims"].numel()), ptr(tc["dims"]), ptr(tc["dmax"]),
                  ptr(tc["dsoff"]), tc["n_slots"], ptr(tc["tape"]), tc["K"], ptr(k["fam_a"]), ptr(k["fam_b"]),
-                 ptr(k["fam"]), ptr(x[p0:p1]), p1 - p0, d, ptr(Ah), ptr(Al), ldk, st)
+                 ptr(k["fam"]), ptr(x[p0:p1]), p1 - p0, d, ptr(Ah), ptr(Al), ldk, ptr(ws), nws, st)
             call("smx_gemm_tf32x3", ptr(Ah), ptr(Al), ldk, ptr(tc["Bh"]), ptr(tc["Bl"]), ldk, p1 - p0, d_out,
                  tc["K"], ptr(y[p0:p1]), d_out, ptr(tc["bias"]), 0, ptr(tc["err"]), st)
         return y
