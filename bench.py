@@ -58,7 +58,7 @@ def peaks():
 
 def ncu_traffic():
     """DRAM bytes per launch of the FP32 evaluator from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "spectral_eval_cfg2.txt")
+    path = os.path.join(ROOT, "profiles", "spectral_eval_leja1000.txt")
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_launch_full_size:"):
@@ -142,10 +142,9 @@ def cpu_reference_rate(points, threads, seconds=12.0, seed=1):
 
 
 def dist_setup():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from smolyax_gb300.replicas import rank_info
+
+    return rank_info()
 
 
 def run_reference(args):
@@ -185,11 +184,24 @@ def run_reference(args):
     return 0
 
 
+def _vec_target(kind, d, d_out, seed):
+    rng = np.random.default_rng(seed)
+    if kind == "leja":
+        W = rng.uniform(0, 1, (d_out, d)) / (np.arange(d) + 1) ** 2
+        W *= 0.5 / W.sum(axis=1, keepdims=True)
+        f = lambda x: 1.0 / (1.0 + np.asarray(x) @ W.T)
+    else:
+        A = rng.normal(0.0, 0.3, (d_out, d)) / (np.arange(d) + 1) ** 1.5
+        f = lambda x: np.exp(-(np.asarray(x) @ A.T))
+    f.vectorized = True
+    return f
+
+
 WORKLOADS = {
     # name: (node kind, d_in, t, d_out, points, target builder, description)
-    "gh2048": ("gh", 100, 9.464636, 2048, 65536, lambda: __import__("functions").exponential(100, 2048, seed=0),
+    "gh2048": ("gh", 100, 9.464636, 2048, 65536, lambda: _vec_target("gh", 100, 2048, 0),
                "Gauss-Hermite d_in=100 d_out=2048 |Lambda|=20010 (t=9.464636) exponential f, 65536 points N(0,I)"),
-    "leja64": ("leja", 200, 7.853604, 64, 100_000, lambda: __import__("functions").rational_vec(200, 64, seed=0),
+    "leja64": ("leja", 200, 7.853604, 64, 100_000, lambda: _vec_target("leja", 200, 64, 0),
                "Leja d_in=200 d_out=64 |Lambda|=5000 (t=7.853604) rational f, 1e5 points U[-1,1]^200"),
 }
 
@@ -198,7 +210,6 @@ def run_tensor_workload(args):
     """Vector-valued workloads served by the tensor-core contraction (one JSON line)."""
     import torch
 
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
     from smolyax_gb300 import SmolyakBarycentricInterpolator, nodes
 
     kind, d, t, d_out, P, fbuild, desc = WORKLOADS[args.workload]
@@ -251,9 +262,10 @@ def run_tensor_workload(args):
                      "unit": "TFLOP/s", "frac": tensor_flops / (ms * 1e-3) / 1e12 / peak if K else None,
                      "peak_kind": pk + " (the kernel runs kind::tf32, whose dense rate is half of bf16)",
                      "flops_per_step": tensor_flops},
-        "setup_s": setup_s, "clocks": clk.summary(), "gpu_launches": args.steps * 2 * ((P + 1) // 1),
+        "setup_s": setup_s, "clocks": clk.summary(),
+        # per step: one panel and one tensor-core GEMM per chunk of points, or one evaluator launch per 4 outputs
+        "gpu_launches": args.steps * (2 * sp.tc_chunks(P) if sp.tc is not None else (d_out + 3) // 4),
     }
-    line["gpu_launches"] = None
     print(json.dumps(line))
     return 0
 
@@ -270,19 +282,6 @@ def serving_fleet(seed=0):
         kind = "leja" if rng.random() < 0.5 else "gh"
         out.append((i, d_in, d_out, lam, kind))
     return out
-
-
-def _vec_target(kind, d, d_out, seed):
-    rng = np.random.default_rng(seed)
-    if kind == "leja":
-        W = rng.uniform(0, 1, (d_out, d)) / (np.arange(d) + 1) ** 2
-        W *= 0.5 / W.sum(axis=1, keepdims=True)
-        f = lambda x: 1.0 / (1.0 + np.asarray(x) @ W.T)
-    else:
-        A = rng.normal(0.0, 0.3, (d_out, d)) / (np.arange(d) + 1) ** 1.5
-        f = lambda x: np.exp(-(np.asarray(x) @ A.T))
-    f.vectorized = True
-    return f
 
 
 def run_serving(args):
@@ -346,18 +345,14 @@ def run_ours(args):
     import torch
     import torch.distributed as dist
 
-    from smolyax_gb300 import SmolyakBarycentricInterpolator, nodes
+    from smolyax_gb300 import SmolyakBarycentricInterpolator, nodes, replicas
 
-    world, rank, local = dist_setup()
-    if world > 1:
-        dist.init_process_group("nccl")
+    world, rank, local = replicas.init("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
     def barrier():
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
+        replicas.barrier(dev)
 
     k = np.log((2 + np.arange(D_IN)) / np.log(2))
     ip = SmolyakBarycentricInterpolator(node_gen=nodes.Leja(dim=D_IN), k=k, t=T_THR, d_out=D_OUT, f=target(D_IN))
@@ -408,10 +403,7 @@ def run_ours(args):
     ms32 = statistics.mean(per32)
     ms64 = statistics.mean(per64)
     ms_e2e = statistics.mean(e2e_per)
-    if world > 1:
-        tmax = torch.tensor([ms32, ms_e2e, ms64], device=dev)
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        ms32, ms_e2e, ms64 = (float(v) for v in tmax.tolist())
+    ms32, ms_e2e, ms64 = replicas.max_over_ranks([ms32, ms_e2e, ms64], device=dev)
     if rank != 0:
         dist.destroy_process_group() if world > 1 else None
         return 0

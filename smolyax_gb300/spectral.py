@@ -303,6 +303,15 @@ class SpectralPlan:
         call("smx_spectral_eval", self.ref(), ptr(x), int(x.shape[0]), int(x.shape[1]), ptr(y), st)
         return y
 
+    def _tc_step(self, P):
+        """Points per panel chunk (the hi/lo panel of one chunk fits the memory limit)."""
+        step = max(128, int(self.memory_limit * 1024**3 // (8 * self.tc["ldk"])) // 128 * 128)
+        return max(1, min(step, P))
+
+    def tc_chunks(self, P):
+        """Number of panel chunks (each one panel and one GEMM launch) for P points."""
+        return -(-int(P) // self._tc_step(P)) if P else 0
+
     def _evaluate_tc(self, x, y, st):
         """Tensor-core path: basis-product panel (TF32 hi/lo) in chunks of points,
         each contracted with the coefficient matrix by the tcgen05 kernel."""
@@ -311,8 +320,7 @@ class SpectralPlan:
         P, d = int(x.shape[0]), int(x.shape[1])
         d_out = int(y.shape[1])
         ldk = tc["ldk"]
-        step = max(128, int(self.memory_limit * 1024**3 // (8 * ldk)) // 128 * 128)
-        step = min(step, P)
+        step = self._tc_step(P)
         Ah = torch.empty(step, ldk, dtype=torch.float32, device=x.device)
         Al = torch.empty_like(Ah)
         if ldk > tc["K"]:
