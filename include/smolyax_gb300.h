@@ -254,6 +254,56 @@ typedef struct smx_spectral {
 int smx_spectral_eval(const smx_spectral* plan_host, const double* x, int64_t P, int64_t ldx, float* y,
                       void* stream);
 
+/* Blocked FP32 evaluator of the orthogonal form for one output (d_out = 1):
+ * the same polynomial as smx_spectral_eval, summed as
+ *   y = c0 + sum over hot nodes a of V_a(x) * sum_{(a,s)} c * Phi_s(x)
+ *          + sum over cold groups of sum_s (sum_{k<K} Vc_k(x) W[k][s]) * phi_s(x)
+ * where hot slots/nodes are those of dimensions with children in the index
+ * set, Vc_k the values of the prefixes of cold entries ordered by remaining
+ * budget (the admissible prefixes of a cold slot are then a leading range, so
+ * W is a staircase), and every group holds 4 cold slots.  Tables (host
+ * struct of device pointers; int32 / float32):
+ *   node[n_nodes][12]  entry offset, entry count (even), path depth, 0, path slots * 128 (8)
+ *   vc[k_c][12]        same format, prefixes of cold entries
+ *   hot_ent[2 * n]     (slot * 128, coefficient bits) pairs
+ *   grp[G][12]         K, W offset, fast flag, slots, dims[4], degrees[4] (0 = unused)
+ *   grp_ab[G][8]       a[4], b[4]: phi = a x + b (fast groups, degree 1) or z = a x + b
+ *   W[sum 4 K]         staircase coefficients, [K][4] per group
+ *   warp_off[17], items[n_items]: work list of each of the 16 warps of a block
+ *                      (hot node index, or 2^30 | group index)
+ * This re-expresses the reference's evaluation (interpolation.py:264-304) the
+ * same way smx_spectral_eval does. */
+typedef struct smx_blocked {
+  int32_t d_in;
+  int32_t n_hs;       /* hot basis slots                          */
+  int32_t k_c;        /* prefix rows of cold entries              */
+  int32_t n_hot_dims;
+  int32_t n_nodes;
+  int32_t n_groups;
+  int32_t n_items;
+  float c0;           /* coefficient of the constant              */
+  const int32_t* hot_dim;
+  const int32_t* hot_deg;
+  const int32_t* hot_soff;
+  const int32_t* node;
+  const int32_t* vc;
+  const int32_t* hot_ent;
+  const int32_t* grp;
+  const float* grp_ab;
+  const float* W;
+  const int32_t* warp_off;
+  const int32_t* items;
+  const float* fa;    /* [d_in] affine map z = fa x + fb of every dimension */
+  const float* fb;
+  const int32_t* fam; /* [d_in] 0 Legendre, 1 Hermite                       */
+} smx_blocked;
+
+/* Shared memory of one block: (n_hs + k_c) * 512 + 16384 bytes (<= 220 KiB). */
+size_t smx_blocked_smem(const smx_blocked* plan_host);
+/* y[P] (FP32) at x[P, ldx] (FP64); one persistent block per SM. */
+int smx_blocked_eval(const smx_blocked* plan_host, const double* x, int64_t P, int64_t ldx, float* y,
+                     void* stream);
+
 /* Basis-product panel of the orthogonal form for the tensor-core contraction:
  * A[p][j] = prod over the pairs of entry j of phi_g(z_d) for the K non-root
  * entries of Lambda in DFS pre-order (tape word: basis slot | depth << 16,
@@ -301,6 +351,15 @@ typedef struct smx_work {
 size_t smx_spectral_eval_batch_workspace(int n_plans, int n_items, int max_d_out);
 int smx_spectral_eval_batch(const smx_spectral* plans, int n_plans, const smx_work* items, int n_items, void* ws,
                             size_t ws_bytes, void* stream);
+
+/* Serving: one persistent launch over the 128-point tiles of many work items
+ * (struct smx_work, `plan` indexing `plans`), each of a blocked plan; every
+ * tile is evaluated exactly as by smx_blocked_eval.  Workspace:
+ * smx_blocked_eval_batch_workspace bytes (device). */
+size_t smx_blocked_eval_batch_workspace(int n_plans, int n_items);
+int smx_blocked_eval_batch(const smx_blocked* plans_host, int n_plans, const smx_work* items_host, int n_items,
+                           void* ws, size_t ws_bytes, void* stream);
+
 
 /* ---- tensor-core contraction ---------------------------------------------------------
  * D[M x N] = A B^T (+ bias[n]) with tcgen05.mma kind::tf32 in 3xTF32 form:

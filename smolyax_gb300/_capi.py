@@ -89,6 +89,35 @@ class SmxSpectral(C.Structure):
     ]
 
 
+class SmxBlocked(C.Structure):
+    """Mirror of ``struct smx_blocked``."""
+
+    _fields_ = [
+        ("d_in", _i32),
+        ("n_hs", _i32),
+        ("k_c", _i32),
+        ("n_hot_dims", _i32),
+        ("n_nodes", _i32),
+        ("n_groups", _i32),
+        ("n_items", _i32),
+        ("c0", C.c_float),
+        ("hot_dim", _p),
+        ("hot_deg", _p),
+        ("hot_soff", _p),
+        ("node", _p),
+        ("vc", _p),
+        ("hot_ent", _p),
+        ("grp", _p),
+        ("grp_ab", _p),
+        ("W", _p),
+        ("warp_off", _p),
+        ("items", _p),
+        ("fa", _p),
+        ("fb", _p),
+        ("fam", _p),
+    ]
+
+
 class SmxWork(C.Structure):
     """Mirror of ``struct smx_work``."""
 
@@ -119,6 +148,10 @@ SIGNATURES = {
     "smx_spectral_pairs": (_int, [_int, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
     "smx_spectral_coefficients": (_int, [_p, _p, _p, _p, _p, _p, _p, _i64, _p, _p, _p, _p, _p]),
     "smx_spectral_eval": (_int, [_p, _p, _i64, _i64, _p, _p]),
+    "smx_blocked_smem": (_sz, [_p]),
+    "smx_blocked_eval": (_int, [_p, _p, _i64, _i64, _p, _p]),
+    "smx_blocked_eval_batch_workspace": (_sz, [_int, _int]),
+    "smx_blocked_eval_batch": (_int, [_p, _int, _p, _int, _p, _sz, _p]),
     "smx_eval_f64_noalloc": (_int, [_p, _p, _i64, _i64, _p, _p]),
     "smx_spectral_panel_workspace": (_sz, [_int, _i64]),
     "smx_spectral_panel_tf32": (_int, [_int, _p, _p, _p, _int, _p, _int, _p, _p, _p, _p, _i64, _i64, _p, _p, _i64,

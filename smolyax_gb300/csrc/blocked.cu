@@ -1,0 +1,473 @@
+// Blocked FP32 evaluator of the orthogonal-polynomial form, one output.
+//
+// One persistent block of 16 warps per SM walks 128-point tiles.  Per tile:
+//   phase 0  Phi[s][.]  basis values of the hot slots            (shared memory)
+//   phase 1  Vc[k][.]   values of the prefixes of cold entries   (shared memory)
+//   phase 2  every warp runs its own list of work items over all 128 points
+//            (lane l holds points l, l+32, l+64, l+96):
+//            hot node a:  y += V_a * sum_{(a,s)} c * Phi[s]        (gather form)
+//            cold group:  T[4 pts][4 slots] = sum_{k<K} Vc[k] W[k] (staircase
+//                         block, 16 FFMA per shared load), then
+//                         y += sum_s T[.][s] * phi_s(x)            (x read once)
+//   phase 3  per-point sum over the warps in a fixed order, y = c_0 + sum.
+// Coefficients and descriptors are read with warp-uniform loads (L1-resident);
+// x is streamed with L1-bypassing loads, prefetched into L2 four items ahead.
+// The cancellation-free orthogonal form is summed with Kahan compensation per
+// warp and in the final reduction.
+#include <math.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr int kW = 16;           // warps per block
+constexpr int kT = 128;          // points per tile
+constexpr int kThr = kW * 32;
+constexpr int kRec = 512;        // recurrence table length
+constexpr int kPrefetch = 4;     // items of look-ahead for the L2 prefetch of x
+constexpr int kColdBit = 1 << 30;
+
+__constant__ float b_alpha[2][kRec];
+__constant__ float b_beta[2][kRec];
+
+struct BArgs {
+  int n_hs, k_c, n_hot_dims;
+  float c0;
+  const int32_t* hot_dim;
+  const int32_t* hot_deg;
+  const int32_t* hot_soff;
+  const int4* node;      // [n_nodes][3]: {entry offset, entry count, depth, 0}, path[0..3], path[4..7]
+  const int4* vc;        // [k_c][3] same format (path only)
+  const int4* hot_ent;   // pairs {smem offset, coefficient bits} x 2
+  const int4* grp;       // [G][3]: {K, W offset, fast, slots}, dims, degrees
+  const float4* grp_ab;  // [G][2]: affine maps (a, b) of the 4 slots
+  const float4* W;       // staircase coefficients, one float4 per prefix row
+  const int32_t* warp_off;
+  const int32_t* items;
+  const float* fa;
+  const float* fb;
+  const int32_t* fam;
+};
+
+// FP64 -> FP32 with integer operations (truncation of the mantissa; |v| below
+// 2^-126 gives a signed zero; |v| must be below 2^128).  Keeps the conversions
+// off the FP64 pipe.  Layout facts used: IEEE-754 binary64 = sign, 11-bit
+// exponent (bias 1023), 52-bit fraction; binary32 = sign, 8-bit exponent (bias
+// 127), 23-bit fraction.  The top 9 exponent bits and 23 fraction bits are
+// shifted into place together; adding 2^30 re-biases the exponent modulo 2^32.
+__device__ __forceinline__ float f64_to_f32(double v) {
+  const unsigned hi = static_cast<unsigned>(__double2hiint(v));
+  const unsigned lo = static_cast<unsigned>(__double2loint(v));
+  const unsigned t = __funnelshift_l(lo, hi, 3) + 0x40000000u;
+  const unsigned r = (t & 0x7fffffffu) | (hi & 0x80000000u);
+  return __uint_as_float((hi & 0x7fffffffu) >= 0x38100000u ? r : (hi & 0x80000000u));
+}
+
+__device__ __forceinline__ void ld2_stream(const double* p, double& a, double& b) {
+  asm volatile("ld.global.nc.L1::no_allocate.v2.f64 {%0, %1}, [%2];" : "=d"(a), "=d"(b) : "l"(p));
+}
+
+__device__ __forceinline__ double ld1_stream(const double* p) {
+  double a;
+  asm volatile("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(a) : "l"(p));
+  return a;
+}
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+  const float yv = v - c;
+  const float t = s + yv;
+  c = (t - s) - yv;
+  s = t;
+}
+
+__device__ __forceinline__ float phi_rec(int fm, float z, int g) {
+  float pm1 = 0.f, pc = 1.f;
+  for (int n = 0; n < g; ++n) {
+    const float pn = b_alpha[fm][n] * z * pc - b_beta[fm][n] * pm1;
+    pm1 = pc;
+    pc = pn;
+  }
+  return pc;
+}
+
+// Tile point of shared-memory position q: rows are stored as lane-major quads,
+// point l + 32 i (lane l) at position 4 l + i.
+__device__ __forceinline__ int quad_point(int q) { return 32 * (q & 3) + (q >> 2); }
+
+__device__ __forceinline__ float4 path_value(const float* __restrict__ PH, int4 h0, int4 pa, int4 pb, int q0) {
+  float4 v = make_float4(1.f, 1.f, 1.f, 1.f);
+  const int path[8] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w};
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    if (q < h0.z) {
+      const float4 f = *reinterpret_cast<const float4*>(PH + path[q] + q0);
+      v.x *= f.x;
+      v.y *= f.y;
+      v.z *= f.z;
+      v.w *= f.w;
+    }
+  }
+  return v;
+}
+
+// One 128-point tile of one plan (shared by the single-plan kernel and the
+// multi-plan batch kernel of the serving loop).
+__device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __restrict__ x, int64_t P, int64_t ldx,
+                                             float* __restrict__ y, int fastx, int64_t tile, float* sm) {
+  float* PH = sm;
+  float* VC = sm + size_t(a.n_hs) * kT;
+  float* RS = VC + size_t(a.k_c) * kT;
+  float* RC = RS + kW * kT;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q0 = lane * 4;
+  const int it0 = a.warp_off[warp], it1 = a.warp_off[warp + 1];
+  {
+    const int64_t p0 = tile * kT;
+    int64_t prow[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) prow[i] = min(p0 + lane + 32 * i, P - 1) * ldx;
+
+    // phase 0: basis values of the hot slots
+    for (int i = threadIdx.x; i < a.n_hot_dims * kT; i += kThr) {
+      const int h = i >> 7, q = i & (kT - 1);
+      const int64_t p = min(p0 + quad_point(q), P - 1);
+      const int dim = __ldg(a.hot_dim + h), g = __ldg(a.hot_deg + h), so = __ldg(a.hot_soff + h);
+      const int fm = __ldg(a.fam + dim);
+      const float z = fmaf(__ldg(a.fa + dim), f64_to_f32(ld1_stream(x + p * ldx + dim)), __ldg(a.fb + dim));
+      float pm1 = 0.f, pc = 1.f;
+      for (int n = 0; n < g; ++n) {
+        const float pn = b_alpha[fm][n] * z * pc - b_beta[fm][n] * pm1;
+        pm1 = pc;
+        pc = pn;
+        PH[(so + n) * kT + q] = pc;
+      }
+    }
+    __syncthreads();
+
+    // phase 1: prefix rows of the cold entries
+    for (int i = threadIdx.x; i < a.k_c * kT; i += kThr) {
+      const int k = i >> 7, q = i & (kT - 1);
+      const int4 h0 = __ldg(a.vc + 3 * k), pa = __ldg(a.vc + 3 * k + 1), pb = __ldg(a.vc + 3 * k + 2);
+      const int path[8] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w};
+      float v = 1.f;
+#pragma unroll
+      for (int s = 0; s < 8; ++s)
+        if (s < h0.z) v *= PH[path[s] + q];
+      VC[k * kT + q] = v;
+    }
+    __syncthreads();
+
+    // phase 2: this warp's items
+    float ys[4] = {0.f, 0.f, 0.f, 0.f}, yc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int it = it0; it < it1; ++it) {
+      if (it + kPrefetch < it1) {
+        const int nc = __ldg(a.items + it + kPrefetch);
+        if (nc & kColdBit) {
+          const int d0 = __ldg(&a.grp[3 * (nc & (kColdBit - 1)) + 1].x);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) asm volatile("prefetch.global.L2 [%0];" ::"l"(x + prow[i] + d0));
+        }
+      }
+      const int code = __ldg(a.items + it);
+      if (!(code & kColdBit)) {
+        // hot node: gather over its hot entries, times the path product
+        const int4 h0 = __ldg(a.node + 3 * code), pa = __ldg(a.node + 3 * code + 1),
+                   pb = __ldg(a.node + 3 * code + 2);
+        const int4* E = a.hot_ent + (h0.x >> 1);
+        const int ne = h0.y >> 1;
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 2
+        for (int e = 0; e < ne; ++e) {
+          const int4 ee = __ldg(E + e);
+          const float4 f0 = *reinterpret_cast<const float4*>(PH + ee.x + q0);
+          const float4 f1 = *reinterpret_cast<const float4*>(PH + ee.z + q0);
+          const float c0 = __int_as_float(ee.y), c1 = __int_as_float(ee.w);
+          acc.x = fmaf(c0, f0.x, acc.x);
+          acc.y = fmaf(c0, f0.y, acc.y);
+          acc.z = fmaf(c0, f0.z, acc.z);
+          acc.w = fmaf(c0, f0.w, acc.w);
+          acc.x = fmaf(c1, f1.x, acc.x);
+          acc.y = fmaf(c1, f1.y, acc.y);
+          acc.z = fmaf(c1, f1.z, acc.z);
+          acc.w = fmaf(c1, f1.w, acc.w);
+        }
+        const float4 v = path_value(PH, h0, pa, pb, q0);
+        kahan_add(ys[0], yc[0], v.x * acc.x);
+        kahan_add(ys[1], yc[1], v.y * acc.y);
+        kahan_add(ys[2], yc[2], v.z * acc.z);
+        kahan_add(ys[3], yc[3], v.w * acc.w);
+        continue;
+      }
+      // cold group: staircase block, then the x-dot epilogue
+      const int g = code & (kColdBit - 1);
+      const int4 gd = __ldg(a.grp + 3 * g), gdim = __ldg(a.grp + 3 * g + 1), gdeg = __ldg(a.grp + 3 * g + 2);
+      double xv[4][4];
+      if (gd.z && fastx) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          ld2_stream(x + prow[i] + gdim.x, xv[i][0], xv[i][1]);
+          ld2_stream(x + prow[i] + gdim.x + 2, xv[i][2], xv[i][3]);
+        }
+      } else {
+        const int dd[4] = {gdim.x, gdim.y, gdim.z, gdim.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) xv[i][j] = ld1_stream(x + prow[i] + dd[j]);
+      }
+      float T[4][4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) T[i][j] = 0.f;
+      const float4* Wg = a.W + (gd.y >> 2);
+      const float* Vk = VC + q0;
+#pragma unroll 4
+      for (int k = 0; k < gd.x; ++k) {
+        const float4 v = *reinterpret_cast<const float4*>(Vk + k * kT);
+        const float4 w = __ldg(Wg + k);
+        const float vv[4] = {v.x, v.y, v.z, v.w};
+        const float ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) T[i][j] = fmaf(vv[i], ww[j], T[i][j]);
+      }
+      const float4 A = __ldg(a.grp_ab + 2 * g), B = __ldg(a.grp_ab + 2 * g + 1);
+      const float Aa[4] = {A.x, A.y, A.z, A.w}, Bb[4] = {B.x, B.y, B.z, B.w};
+      if (gd.z) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          float s = 0.f;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) s = fmaf(T[i][j], fmaf(Aa[j], f64_to_f32(xv[i][j]), Bb[j]), s);
+          kahan_add(ys[i], yc[i], s);
+        }
+      } else {
+        const int dd[4] = {gdim.x, gdim.y, gdim.z, gdim.w};
+        const int gg[4] = {gdeg.x, gdeg.y, gdeg.z, gdeg.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          float s = 0.f;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            if (gg[j] == 0) continue;
+            const float z = fmaf(Aa[j], f64_to_f32(xv[i][j]), Bb[j]);
+            s = fmaf(T[i][j], phi_rec(__ldg(a.fam + dd[j]), z, gg[j]), s);
+          }
+          kahan_add(ys[i], yc[i], s);
+        }
+      }
+    }
+
+    // phase 3: per-point sum over the warps, fixed order
+    *reinterpret_cast<float4*>(RS + warp * kT + q0) = make_float4(ys[0], ys[1], ys[2], ys[3]);
+    *reinterpret_cast<float4*>(RC + warp * kT + q0) = make_float4(yc[0], yc[1], yc[2], yc[3]);
+    __syncthreads();
+    if (threadIdx.x < kT) {
+      const int q = threadIdx.x;
+      float s = 0.f, c = 0.f;
+      for (int w = 0; w < kW; ++w) {
+        kahan_add(s, c, RS[w * kT + q]);
+        kahan_add(s, c, -RC[w * kT + q]);
+      }
+      const int64_t p = p0 + quad_point(q);
+      if (p < P) y[p] = a.c0 + (s - c);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kThr, 1)
+    blocked_eval_kernel(BArgs a, const double* __restrict__ x, int64_t P, int64_t ldx, float* __restrict__ y,
+                        int fastx) {
+  extern __shared__ __align__(16) float sm[];
+  const int64_t n_tiles = (P + kT - 1) / kT;
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) blocked_tile(a, x, P, ldx, y, fastx, tile, sm);
+}
+
+struct BWork {
+  int plan, fastx;
+  int64_t tile0, P, ldx;
+  const double* x;
+  float* y;
+};
+
+// Persistent multi-plan launch: blocks take tiles of any work item from a
+// shared counter.
+__global__ void __launch_bounds__(kThr, 1)
+    blocked_eval_batch_kernel(const BArgs* __restrict__ plans, const BWork* __restrict__ items, int n_items,
+                              int64_t total_tiles, unsigned long long* counter) {
+  extern __shared__ __align__(16) float sm[];
+  __shared__ int64_t s_tile;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = int64_t(atomicAdd(counter, 1ull));
+    __syncthreads();
+    const int64_t t = s_tile;
+    __syncthreads();
+    if (t >= total_tiles) break;
+    int lo = 0, hi = n_items - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (items[mid].tile0 <= t) lo = mid; else hi = mid - 1;
+    }
+    const BWork it = items[lo];
+    blocked_tile(plans[it.plan], it.x, it.P, it.ldx, it.y, it.fastx, t - it.tile0, sm);
+  }
+}
+
+std::mutex g_mu;
+bool g_ready[64] = {};
+int g_sms[64] = {};
+
+int prepare(int* sms) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    return smx::set_error(SMX_ERR_CUDA, "smx_blocked_eval: no current device");
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_ready[dev]) {
+    static float al[2][kRec], be[2][kRec];
+    for (int f = 0; f < 2; ++f)
+      for (int n = 0; n < kRec; ++n) {
+        // phi_{n+1} = alpha_n z phi_n - beta_n phi_{n-1}: Legendre, normalised Hermite
+        al[f][n] = f == 0 ? float(double(2 * n + 1) / double(n + 1)) : float(sqrt(2.0 / double(n + 1)));
+        be[f][n] = f == 0 ? float(double(n) / double(n + 1)) : float(sqrt(double(n) / double(n + 1)));
+      }
+    if (cudaMemcpyToSymbol(b_alpha, al, sizeof(al)) != cudaSuccess ||
+        cudaMemcpyToSymbol(b_beta, be, sizeof(be)) != cudaSuccess ||
+        cudaFuncSetAttribute(blocked_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(blocked_eval_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) !=
+            cudaSuccess ||
+        cudaDeviceGetAttribute(&g_sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return smx::set_error(SMX_ERR_CUDA, "smx_blocked_eval: device set-up failed");
+    g_ready[dev] = true;
+  }
+  *sms = g_sms[dev];
+  return SMX_OK;
+}
+
+size_t smem_of(const smx_blocked* b) {
+  return (size_t(b->n_hs) + size_t(b->k_c)) * kT * sizeof(float) + 2 * size_t(kW) * kT * sizeof(float);
+}
+
+int check_plan(const smx_blocked* b, const char* what) {
+  if (!b || b->d_in <= 0 || b->n_hs < 0 || b->k_c < 0 || b->n_hot_dims < 0 || b->n_items < 0 || !b->warp_off ||
+      !b->items || !b->fa || !b->fb || !b->fam ||
+      (b->n_hot_dims > 0 && !(b->hot_dim && b->hot_deg && b->hot_soff)) || (b->k_c > 0 && !b->vc) ||
+      (b->n_groups > 0 && !(b->grp && b->grp_ab && b->W)))
+    return smx::set_error(SMX_ERR_ARG, std::string(what) + ": bad plan");
+  if (smem_of(b) > 220 * 1024)
+    return smx::set_error(SMX_ERR_UNSUPPORTED, std::string(what) + ": tables exceed shared memory");
+  return SMX_OK;
+}
+
+BArgs to_args(const smx_blocked* b) {
+  BArgs a;
+  a.n_hs = b->n_hs;
+  a.k_c = b->k_c;
+  a.n_hot_dims = b->n_hot_dims;
+  a.c0 = b->c0;
+  a.hot_dim = b->hot_dim;
+  a.hot_deg = b->hot_deg;
+  a.hot_soff = b->hot_soff;
+  a.node = reinterpret_cast<const int4*>(b->node);
+  a.vc = reinterpret_cast<const int4*>(b->vc);
+  a.hot_ent = reinterpret_cast<const int4*>(b->hot_ent);
+  a.grp = reinterpret_cast<const int4*>(b->grp);
+  a.grp_ab = reinterpret_cast<const float4*>(b->grp_ab);
+  a.W = reinterpret_cast<const float4*>(b->W);
+  a.warp_off = b->warp_off;
+  a.items = b->items;
+  a.fa = b->fa;
+  a.fb = b->fb;
+  a.fam = b->fam;
+  return a;
+}
+
+int fast_x(const double* x, int64_t ldx) { return (ldx % 2 == 0) && (reinterpret_cast<uintptr_t>(x) % 16 == 0); }
+
+}  // namespace
+
+extern "C" size_t smx_blocked_smem(const smx_blocked* b) { return b ? smem_of(b) : 0; }
+
+extern "C" int smx_blocked_eval(const smx_blocked* b, const double* x, int64_t P, int64_t ldx, float* y,
+                                void* stream) {
+  int rc = check_plan(b, "smx_blocked_eval");
+  if (rc) return rc;
+  SMX_REQUIRE(P >= 0 && ldx >= b->d_in, "smx_blocked_eval: bad sizes");
+  if (P == 0) return SMX_OK;
+  SMX_REQUIRE(x && y, "smx_blocked_eval: null pointer");
+  int sms = 0;
+  rc = prepare(&sms);
+  if (rc) return rc;
+  const int64_t tiles = (P + kT - 1) / kT;
+  const unsigned grid = static_cast<unsigned>(tiles < sms ? tiles : sms);
+  blocked_eval_kernel<<<grid, kThr, smem_of(b), smx::as_stream(stream)>>>(to_args(b), x, P, ldx, y,
+                                                                                   fast_x(x, ldx));
+  SMX_LAUNCH_CHECK("smx_blocked_eval");
+  return SMX_OK;
+}
+
+extern "C" size_t smx_blocked_eval_batch_workspace(int n_plans, int n_items) {
+  if (n_plans < 0 || n_items < 0) return 0;
+  return 256 + (size_t(n_plans) * sizeof(BArgs) + 255) / 256 * 256 + size_t(n_items) * sizeof(BWork);
+}
+
+extern "C" int smx_blocked_eval_batch(const smx_blocked* plans, int n_plans, const smx_work* items, int n_items,
+                                      void* ws, size_t ws_bytes, void* stream) {
+  SMX_REQUIRE(n_plans >= 1 && n_items >= 0 && plans && (n_items == 0 || items) && ws,
+              "smx_blocked_eval_batch: bad arguments");
+  if (n_items == 0) return SMX_OK;
+  SMX_REQUIRE(ws_bytes >= smx_blocked_eval_batch_workspace(n_plans, n_items),
+              "smx_blocked_eval_batch: workspace too small");
+  std::vector<BArgs> args(n_plans);
+  size_t smem = 0;
+  for (int i = 0; i < n_plans; ++i) {
+    int rc = check_plan(&plans[i], "smx_blocked_eval_batch");
+    if (rc) return rc;
+    args[i] = to_args(&plans[i]);
+    smem = std::max(smem, smem_of(&plans[i]));
+  }
+  std::vector<BWork> work;
+  int64_t tiles = 0;
+  for (int j = 0; j < n_items; ++j) {
+    const smx_work& w = items[j];
+    SMX_REQUIRE(w.plan >= 0 && w.plan < n_plans && w.P >= 0 && w.ldx >= plans[w.plan].d_in,
+                "smx_blocked_eval_batch: bad work item");
+    if (w.P == 0) continue;
+    SMX_REQUIRE(w.x && w.y, "smx_blocked_eval_batch: null work pointers");
+    BWork it;
+    it.plan = w.plan;
+    it.fastx = fast_x(w.x, w.ldx);
+    it.tile0 = tiles;
+    it.P = w.P;
+    it.ldx = w.ldx;
+    it.x = w.x;
+    it.y = w.y;
+    work.push_back(it);
+    tiles += (w.P + kT - 1) / kT;
+  }
+  if (work.empty()) return SMX_OK;
+  int sms = 0;
+  int rc = prepare(&sms);
+  if (rc) return rc;
+  uint8_t* wsb = static_cast<uint8_t*>(ws);
+  unsigned long long* counter = reinterpret_cast<unsigned long long*>(wsb);
+  BArgs* d_args = reinterpret_cast<BArgs*>(wsb + 256);
+  BWork* d_items = reinterpret_cast<BWork*>(wsb + 256 + (size_t(n_plans) * sizeof(BArgs) + 255) / 256 * 256);
+  cudaStream_t st = smx::as_stream(stream);
+  cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
+  cudaMemcpyAsync(d_args, args.data(), args.size() * sizeof(BArgs), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d_items, work.data(), work.size() * sizeof(BWork), cudaMemcpyHostToDevice, st);
+  SMX_LAUNCH_CHECK("smx_blocked_eval_batch copies");
+  const int64_t grid = std::min<int64_t>(tiles, int64_t(std::max(1, sms)));
+  blocked_eval_batch_kernel<<<unsigned(grid), kThr, smem, st>>>(d_args, d_items, int(work.size()), tiles, counter);
+  SMX_LAUNCH_CHECK("smx_blocked_eval_batch");
+  return SMX_OK;
+}

@@ -7,11 +7,13 @@ interpolants and batch sizes:
 * admission -- requests wait in FIFO order and are admitted while a stream
   slot is free and their device memory (inputs, outputs, scratch) fits the
   budget; a request that can never fit is rejected;
-* batching  -- at every scheduling step, all admitted FP32 evaluations whose
-  plans use the CUDA-core evaluator are merged into ONE persistent launch
-  (``smx_spectral_eval_batch``: CTAs take 128-point tiles of any request from
-  a shared counter); tensor-core evaluations, FP64 evaluations and gradients
-  run on their own streams, so their work overlaps on the device;
+* batching  -- at every scheduling step, the admitted FP32 evaluations whose
+  plans use a CUDA-core evaluator are merged into one persistent launch per
+  evaluator kind (``smx_blocked_eval_batch`` for one-output plans with blocked
+  tables, ``smx_spectral_eval_batch`` for the others: blocks take 128-point
+  tiles of any request from a shared counter); tensor-core evaluations, FP64
+  evaluations and gradients run on their own streams, so their work overlaps
+  on the device;
 * completion -- each admission group records a CUDA event; the loop polls the
   events, copies results to the host, frees memory and slots, and admits
   requests that arrived meanwhile.
@@ -147,8 +149,15 @@ class Server:
             b += min(P, 1 << 20) * sp.tc["ldk"] * 8
         return b
 
+    def _kind(self, req):
+        """'blocked' / 'stream': merged into a persistent multi-plan launch; None: own launch."""
+        sp = self.spec[req.name]
+        if req.op != "eval" or req.precision != "fp32" or sp.tc is not None:
+            return None
+        return "blocked" if sp.blocked is not None else "stream"
+
     def _admit(self):
-        batch, singles = [], []
+        batches, singles = {}, []
         with self.lock:
             avail = len(self.free_streams)  # streams not yet promised in this step
             while self.waiting:
@@ -163,26 +172,22 @@ class Server:
                     continue
                 if self.in_use + nb > self.budget:
                     break
-                batched = req.op == "eval" and req.precision == "fp32" and self.spec[req.name].tc is None
-                if batched and not batch:
+                kind = self._kind(req)
+                if kind is None or kind not in batches:
                     if avail < 1:
                         break
-                    avail -= 1  # the merged launch's stream
-                elif not batched:
-                    if avail < 1:
-                        break
-                    avail -= 1
+                    avail -= 1  # an own launch, or the first request of a merged launch
                 self.waiting.popleft()
-                if batched:
-                    batch.append((req, nb))
-                else:
+                if kind is None:
                     singles.append((req, nb, self.free_streams.popleft()))
+                else:
+                    batches.setdefault(kind, []).append((req, nb))
                 self.in_use += nb
                 self.admitted += 1
-            batch_stream = self.free_streams.popleft() if batch else None
+            streams = {kind: self.free_streams.popleft() for kind in batches}
         now = time.perf_counter()
-        if batch:
-            self._launch_batch(batch, batch_stream, now)
+        for kind, batch in batches.items():
+            self._launch_batch(kind, batch, streams[kind], now)
         for req, nb, stream in singles:
             try:
                 self._launch_single(req, nb, stream, now)
@@ -202,15 +207,17 @@ class Server:
             xd.copy_(xh, non_blocking=True)
         return xh, xd
 
-    def _launch_batch(self, batch, stream, now):
+    def _launch_batch(self, kind, batch, stream, now):
         g = _Group(stream, [r for r, _ in batch], sum(nb for _, nb in batch))
         plan_idx = {}
         plans = []
         for req, _ in batch:
             if req.name not in plan_idx:
                 plan_idx[req.name] = len(plans)
-                plans.append(self.spec[req.name].c)
-        arr = (capi.SmxSpectral * len(plans))(*plans)
+                sp = self.spec[req.name]
+                plans.append(sp.blocked if kind == "blocked" else sp.c)
+        struct = capi.SmxBlocked if kind == "blocked" else capi.SmxSpectral
+        arr = (struct * len(plans))(*plans)
         items = (capi.SmxWork * len(batch))()
         with torch.cuda.stream(stream):
             for i, (req, _) in enumerate(batch):
@@ -224,12 +231,15 @@ class Server:
                 items[i].P = req.points
                 items[i].ldx = req.x.shape[1]
                 items[i].y = y.data_ptr()
-            max_dout = max(p.d_out for p in plans)
-            ws = torch.empty(capi.size("smx_spectral_eval_batch_workspace", len(plans), len(batch), max_dout),
-                             dtype=torch.uint8, device=self.dev)
+            if kind == "blocked":
+                nws = capi.size("smx_blocked_eval_batch_workspace", len(plans), len(batch))
+            else:
+                max_dout = max(p.d_out for p in plans)
+                nws = capi.size("smx_spectral_eval_batch_workspace", len(plans), len(batch), max_dout)
+            ws = torch.empty(nws, dtype=torch.uint8, device=self.dev)
             g.keep.append(ws)
-            call("smx_spectral_eval_batch", arr, len(plans), items, len(batch), ptr(ws), ws.numel(),
-                 capi.stream_ptr(stream))
+            fn = "smx_blocked_eval_batch" if kind == "blocked" else "smx_spectral_eval_batch"
+            call(fn, arr, len(plans), items, len(batch), ptr(ws), ws.numel(), capi.stream_ptr(stream))
             g.host = [torch.empty(y.shape, dtype=y.dtype, pin_memory=True) for y in g.outputs]
             for h, y in zip(g.host, g.outputs):
                 h.copy_(y, non_blocking=True)

@@ -166,6 +166,9 @@ class SpectralPlan:
         if d_out >= TC_MIN_DOUT or not stream_fits:
             self._build_tc(*self._fwd_args)
         self.memory_limit = ip._memory_limit
+        self.blocked = None
+        if d_out == 1 and self.tc is None:
+            self._build_blocked(tree_np, C32[:, 0], np.asarray(ip._maxdeg), d, fam, fa, fb, T)
 
     def _build_tc(self, tr, C32, maxdeg, fam, fa, fb, T, st):
         """Operands of the tensor-core contraction: tape over all non-root entries
@@ -197,6 +200,29 @@ class SpectralPlan:
                        n_slots=n_slots, tape=T(tape, torch.int32), K=K, ldk=ldk, Bh=Bh, Bl=Bl,
                        bias=self.keep["c0"], err=torch.zeros(1, dtype=torch.int32, device=dev),
                        ent=torch.as_tensor(ent, device=dev))
+
+    def _build_blocked(self, tr, c, maxdeg, d, fam, fa, fb, T):
+        """Tables of the blocked evaluator (one output), if the plan fits it."""
+        from .blocked import build_blocked
+
+        lay = build_blocked(tr, c, maxdeg, d, fam, fa, fb)
+        if lay is None:
+            return
+        kb = {}
+        for name in ("hot_dim", "hot_deg", "hot_soff", "node", "vc", "hot_ent", "grp", "warp_off", "items"):
+            kb[name] = T(lay[name], torch.int32)
+        for name in ("grp_ab", "W"):
+            kb[name] = T(lay[name], torch.float32)
+        b = capi.SmxBlocked()
+        for name in ("d_in", "n_hs", "k_c", "n_hot_dims", "n_nodes", "n_groups", "n_items"):
+            setattr(b, name, int(lay[name]))
+        b.c0 = float(lay["c0"])
+        for name, t in kb.items():
+            setattr(b, name, t.data_ptr() if t.numel() else None)
+        b.fa, b.fb, b.fam = (self.keep[k].data_ptr() for k in ("fam_a", "fam_b", "fam"))
+        self.blocked = b
+        self.blocked_keep = kb
+        self.blocked_layout = lay
 
     def ref(self):
         import ctypes
@@ -300,6 +326,12 @@ class SpectralPlan:
         st = capi.stream_ptr(torch.cuda.current_stream())
         if self.tc is not None:
             return self._evaluate_tc(x, y, st)
+        if self.blocked is not None:
+            import ctypes
+
+            call("smx_blocked_eval", ctypes.byref(self.blocked), ptr(x), int(x.shape[0]), int(x.shape[1]), ptr(y),
+                 st)
+            return y
         call("smx_spectral_eval", self.ref(), ptr(x), int(x.shape[0]), int(x.shape[1]), ptr(y), st)
         return y
 

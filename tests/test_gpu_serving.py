@@ -59,7 +59,8 @@ def test_mix_equals_alone(fleet):
 
     reqs = _requests(fleet, 11)
     server = Server(fleet, memory_budget=0.25, n_streams=4)
-    arrivals = np.sort(np.random.default_rng(3).exponential(0.002, len(reqs)).cumsum())
+    # a burst of 12 requests at t = 0 (merged launches), then staggered arrivals
+    arrivals = np.concatenate([np.zeros(12), np.random.default_rng(3).exponential(0.002, len(reqs) - 12).cumsum()])
     wall = replay(server, arrivals, reqs)
     st = server.stats()
     print("served %d requests in %.3fs, %d launches (%d merged), p50 %.2f ms p99 %.2f ms" % (
