@@ -11,7 +11,8 @@
 //                         y += sum_s T[.][s] * phi_s(x)            (x read once)
 //   phase 3  per-point sum over the warps in a fixed order, y = c_0 + sum.
 // Coefficients and descriptors are read with warp-uniform loads (L1-resident);
-// x is streamed with L1-bypassing loads, prefetched into L2 four items ahead.
+// x is streamed with L1-bypassing loads (a software L2 prefetch measured slower:
+// its per-row requests load the L1 pipeline more than the latency it hides).
 // The cancellation-free orthogonal form is summed with Kahan compensation per
 // warp and in the final reduction.
 #include <math.h>
@@ -29,7 +30,6 @@ constexpr int kW = 16;           // warps per block
 constexpr int kT = 128;          // points per tile
 constexpr int kThr = kW * 32;
 constexpr int kRec = 512;        // recurrence table length
-constexpr int kPrefetch = 4;     // items of look-ahead for the L2 prefetch of x
 constexpr int kColdBit = 1 << 30;
 
 __constant__ float b_alpha[2][kRec];
@@ -70,6 +70,12 @@ __device__ __forceinline__ float f64_to_f32(double v) {
 
 __device__ __forceinline__ void ld2_stream(const double* p, double& a, double& b) {
   asm volatile("ld.global.nc.L1::no_allocate.v2.f64 {%0, %1}, [%2];" : "=d"(a), "=d"(b) : "l"(p));
+}
+
+__device__ __forceinline__ void ld4_stream(const double* p, double& a, double& b, double& c, double& d) {
+  asm volatile("ld.global.nc.L1::no_allocate.v4.f64 {%0, %1, %2, %3}, [%4];"
+               : "=d"(a), "=d"(b), "=d"(c), "=d"(d)
+               : "l"(p));
 }
 
 __device__ __forceinline__ double ld1_stream(const double* p) {
@@ -115,8 +121,9 @@ __device__ __forceinline__ float4 path_value(const float* __restrict__ PH, int4 
   return v;
 }
 
-// One 128-point tile of one plan (shared by the single-plan kernel and the
-// multi-plan batch kernel of the serving loop).
+// One tile of 32 * NP points of one plan (lane l: points l + 32 i, i < NP),
+// shared by the single-plan kernel and the multi-plan batch kernel.
+template <int NP>
 __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __restrict__ x, int64_t P, int64_t ldx,
                                              float* __restrict__ y, int fastx, int64_t tile, float* sm) {
   float* PH = sm;
@@ -127,10 +134,10 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
   const int q0 = lane * 4;
   const int it0 = a.warp_off[warp], it1 = a.warp_off[warp + 1];
   {
-    const int64_t p0 = tile * kT;
-    int64_t prow[4];
+    const int64_t p0 = tile * (32 * NP);
+    int64_t prow[NP];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) prow[i] = min(p0 + lane + 32 * i, P - 1) * ldx;
+    for (int i = 0; i < NP; ++i) prow[i] = min(p0 + lane + 32 * i, P - 1) * ldx;
 
     // phase 0: basis values of the hot slots
     for (int i = threadIdx.x; i < a.n_hot_dims * kT; i += kThr) {
@@ -163,16 +170,10 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
     __syncthreads();
 
     // phase 2: this warp's items
-    float ys[4] = {0.f, 0.f, 0.f, 0.f}, yc[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int it = it0; it < it1; ++it) {
-      if (it + kPrefetch < it1) {
-        const int nc = __ldg(a.items + it + kPrefetch);
-        if (nc & kColdBit) {
-          const int d0 = __ldg(&a.grp[3 * (nc & (kColdBit - 1)) + 1].x);
+    float ys[NP], yc[NP];
 #pragma unroll
-          for (int i = 0; i < 4; ++i) asm volatile("prefetch.global.L2 [%0];" ::"l"(x + prow[i] + d0));
-        }
-      }
+    for (int i = 0; i < NP; ++i) ys[i] = yc[i] = 0.f;
+    for (int it = it0; it < it1; ++it) {
       const int code = __ldg(a.items + it);
       if (!(code & kColdBit)) {
         // hot node: gather over its hot entries, times the path product
@@ -197,32 +198,34 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
           acc.w = fmaf(c1, f1.w, acc.w);
         }
         const float4 v = path_value(PH, h0, pa, pb, q0);
-        kahan_add(ys[0], yc[0], v.x * acc.x);
-        kahan_add(ys[1], yc[1], v.y * acc.y);
-        kahan_add(ys[2], yc[2], v.z * acc.z);
-        kahan_add(ys[3], yc[3], v.w * acc.w);
+        const float va[4] = {v.x * acc.x, v.y * acc.y, v.z * acc.z, v.w * acc.w};
+#pragma unroll
+        for (int i = 0; i < NP; ++i) kahan_add(ys[i], yc[i], va[i]);
         continue;
       }
       // cold group: staircase block, then the x-dot epilogue
       const int g = code & (kColdBit - 1);
       const int4 gd = __ldg(a.grp + 3 * g), gdim = __ldg(a.grp + 3 * g + 1), gdeg = __ldg(a.grp + 3 * g + 2);
-      double xv[4][4];
-      if (gd.z && fastx) {
+      double xv[NP][4];
+      if (gd.z && fastx == 2) {  // rows 32-byte aligned: one 32-byte load per point
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < NP; ++i) ld4_stream(x + prow[i] + gdim.x, xv[i][0], xv[i][1], xv[i][2], xv[i][3]);
+      } else if (gd.z && fastx) {
+#pragma unroll
+        for (int i = 0; i < NP; ++i) {
           ld2_stream(x + prow[i] + gdim.x, xv[i][0], xv[i][1]);
           ld2_stream(x + prow[i] + gdim.x + 2, xv[i][2], xv[i][3]);
         }
       } else {
         const int dd[4] = {gdim.x, gdim.y, gdim.z, gdim.w};
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < NP; ++i)
 #pragma unroll
           for (int j = 0; j < 4; ++j) xv[i][j] = ld1_stream(x + prow[i] + dd[j]);
       }
-      float T[4][4];
+      float T[NP][4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < NP; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) T[i][j] = 0.f;
       const float4* Wg = a.W + (gd.y >> 2);
@@ -234,7 +237,7 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
         const float vv[4] = {v.x, v.y, v.z, v.w};
         const float ww[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < NP; ++i)
 #pragma unroll
           for (int j = 0; j < 4; ++j) T[i][j] = fmaf(vv[i], ww[j], T[i][j]);
       }
@@ -242,7 +245,7 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
       const float Aa[4] = {A.x, A.y, A.z, A.w}, Bb[4] = {B.x, B.y, B.z, B.w};
       if (gd.z) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < NP; ++i) {
           float s = 0.f;
 #pragma unroll
           for (int j = 0; j < 4; ++j) s = fmaf(T[i][j], fmaf(Aa[j], f64_to_f32(xv[i][j]), Bb[j]), s);
@@ -252,7 +255,7 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
         const int dd[4] = {gdim.x, gdim.y, gdim.z, gdim.w};
         const int gg[4] = {gdeg.x, gdeg.y, gdeg.z, gdeg.w};
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < NP; ++i) {
           float s = 0.f;
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
@@ -266,10 +269,12 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
     }
 
     // phase 3: per-point sum over the warps, fixed order
-    *reinterpret_cast<float4*>(RS + warp * kT + q0) = make_float4(ys[0], ys[1], ys[2], ys[3]);
-    *reinterpret_cast<float4*>(RC + warp * kT + q0) = make_float4(yc[0], yc[1], yc[2], yc[3]);
+    *reinterpret_cast<float4*>(RS + warp * kT + q0) =
+        make_float4(ys[0], NP > 1 ? ys[1 % NP] : 0.f, NP > 2 ? ys[2 % NP] : 0.f, NP > 3 ? ys[3 % NP] : 0.f);
+    *reinterpret_cast<float4*>(RC + warp * kT + q0) =
+        make_float4(yc[0], NP > 1 ? yc[1 % NP] : 0.f, NP > 2 ? yc[2 % NP] : 0.f, NP > 3 ? yc[3 % NP] : 0.f);
     __syncthreads();
-    if (threadIdx.x < kT) {
+    if (threadIdx.x < kT && (threadIdx.x & 3) < NP) {
       const int q = threadIdx.x;
       float s = 0.f, c = 0.f;
       for (int w = 0; w < kW; ++w) {
@@ -283,12 +288,14 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
   }
 }
 
+template <int NP>
 __global__ void __launch_bounds__(kThr, 1)
     blocked_eval_kernel(BArgs a, const double* __restrict__ x, int64_t P, int64_t ldx, float* __restrict__ y,
                         int fastx) {
   extern __shared__ __align__(16) float sm[];
-  const int64_t n_tiles = (P + kT - 1) / kT;
-  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) blocked_tile(a, x, P, ldx, y, fastx, tile, sm);
+  const int64_t n_tiles = (P + 32 * NP - 1) / (32 * NP);
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x)
+    blocked_tile<NP>(a, x, P, ldx, y, fastx, tile, sm);
 }
 
 struct BWork {
@@ -317,7 +324,7 @@ __global__ void __launch_bounds__(kThr, 1)
       if (items[mid].tile0 <= t) lo = mid; else hi = mid - 1;
     }
     const BWork it = items[lo];
-    blocked_tile(plans[it.plan], it.x, it.P, it.ldx, it.y, it.fastx, t - it.tile0, sm);
+    blocked_tile<4>(plans[it.plan], it.x, it.P, it.ldx, it.y, it.fastx, t - it.tile0, sm);
   }
 }
 
@@ -340,7 +347,7 @@ int prepare(int* sms) {
       }
     if (cudaMemcpyToSymbol(b_alpha, al, sizeof(al)) != cudaSuccess ||
         cudaMemcpyToSymbol(b_beta, be, sizeof(be)) != cudaSuccess ||
-        cudaFuncSetAttribute(blocked_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) !=
+        cudaFuncSetAttribute(blocked_eval_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) !=
             cudaSuccess ||
         cudaFuncSetAttribute(blocked_eval_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) !=
             cudaSuccess ||
@@ -390,7 +397,12 @@ BArgs to_args(const smx_blocked* b) {
   return a;
 }
 
-int fast_x(const double* x, int64_t ldx) { return (ldx % 2 == 0) && (reinterpret_cast<uintptr_t>(x) % 16 == 0); }
+// 2: rows 32-byte aligned (4 dimensions per load), 1: 16-byte aligned, 0: scalar loads
+int fast_x(const double* x, int64_t ldx) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(x);
+  if (ldx % 4 == 0 && a % 32 == 0) return 2;
+  return (ldx % 2 == 0) && (a % 16 == 0) ? 1 : 0;
+}
 
 }  // namespace
 
@@ -406,10 +418,12 @@ extern "C" int smx_blocked_eval(const smx_blocked* b, const double* x, int64_t P
   int sms = 0;
   rc = prepare(&sms);
   if (rc) return rc;
-  const int64_t tiles = (P + kT - 1) / kT;
+  // 128-point tiles (96-point tiles measured slower even where they cut the
+  // last round of blocks: most per-item work does not scale with the points)
+  const int64_t tiles = (P + 127) / 128;
   const unsigned grid = static_cast<unsigned>(tiles < sms ? tiles : sms);
-  blocked_eval_kernel<<<grid, kThr, smem_of(b), smx::as_stream(stream)>>>(to_args(b), x, P, ldx, y,
-                                                                                   fast_x(x, ldx));
+  blocked_eval_kernel<4><<<grid, kThr, smem_of(b), smx::as_stream(stream)>>>(to_args(b), x, P, ldx, y,
+                                                                           fast_x(x, ldx));
   SMX_LAUNCH_CHECK("smx_blocked_eval");
   return SMX_OK;
 }
