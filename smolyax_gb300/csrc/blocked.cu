@@ -31,6 +31,7 @@ constexpr int kT = 128;          // points per tile
 constexpr int kThr = kW * 32;
 constexpr int kRec = 512;        // recurrence table length
 constexpr int kColdBit = 1 << 30;
+constexpr int kHotPass = 16;     // hot dimensions per thread and pass of phase 0
 
 __constant__ float b_alpha[2][kRec];
 __constant__ float b_beta[2][kRec];
@@ -121,6 +122,28 @@ __device__ __forceinline__ float4 path_value(const float* __restrict__ PH, int4 
   return v;
 }
 
+// x values of a cold group's 4 dimensions for the lane's NP points.
+template <int NP>
+__device__ __forceinline__ void load_x(const double* __restrict__ x, const int64_t (&prow)[NP], int fastx, int4 gd,
+                                       int4 gdim, double (&xv)[NP][4]) {
+  if (gd.z && fastx == 2) {  // rows 32-byte aligned: one 32-byte load per point
+#pragma unroll
+    for (int i = 0; i < NP; ++i) ld4_stream(x + prow[i] + gdim.x, xv[i][0], xv[i][1], xv[i][2], xv[i][3]);
+  } else if (gd.z && fastx) {
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+      ld2_stream(x + prow[i] + gdim.x, xv[i][0], xv[i][1]);
+      ld2_stream(x + prow[i] + gdim.x + 2, xv[i][2], xv[i][3]);
+    }
+  } else {
+    const int dd[4] = {gdim.x, gdim.y, gdim.z, gdim.w};
+#pragma unroll
+    for (int i = 0; i < NP; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) xv[i][j] = ld1_stream(x + prow[i] + dd[j]);
+  }
+}
+
 // One tile of 32 * NP points of one plan (lane l: points l + 32 i, i < NP),
 // shared by the single-plan kernel and the multi-plan batch kernel.
 template <int NP>
@@ -139,19 +162,34 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
 #pragma unroll
     for (int i = 0; i < NP; ++i) prow[i] = min(p0 + lane + 32 * i, P - 1) * ldx;
 
-    // phase 0: basis values of the hot slots
-    for (int i = threadIdx.x; i < a.n_hot_dims * kT; i += kThr) {
-      const int h = i >> 7, q = i & (kT - 1);
-      const int64_t p = min(p0 + quad_point(q), P - 1);
-      const int dim = __ldg(a.hot_dim + h), g = __ldg(a.hot_deg + h), so = __ldg(a.hot_soff + h);
-      const int fm = __ldg(a.fam + dim);
-      const float z = fmaf(__ldg(a.fa + dim), f64_to_f32(ld1_stream(x + p * ldx + dim)), __ldg(a.fb + dim));
-      float pm1 = 0.f, pc = 1.f;
-      for (int n = 0; n < g; ++n) {
-        const float pn = b_alpha[fm][n] * z * pc - b_beta[fm][n] * pm1;
-        pm1 = pc;
-        pc = pn;
-        PH[(so + n) * kT + q] = pc;
+    // phase 0: basis values of the hot slots.  Thread (q, hb) handles the hot
+    // dimensions hb, hb + 4, ... of tile point q; its x loads (up to 16 per
+    // pass) are all issued before the first is used.
+    {
+      const int q = threadIdx.x & (kT - 1), hb = threadIdx.x >> 7;
+      const double* xp = x + min(p0 + quad_point(q), P - 1) * ldx;
+      for (int h0 = 0; h0 < a.n_hot_dims; h0 += 4 * kHotPass) {
+        double xh[kHotPass];
+#pragma unroll
+        for (int r = 0; r < kHotPass; ++r) {
+          const int h = h0 + hb + 4 * r;
+          xh[r] = h < a.n_hot_dims ? __ldg(xp + __ldg(a.hot_dim + h)) : 0.0;
+        }
+#pragma unroll
+        for (int r = 0; r < kHotPass; ++r) {
+          const int h = h0 + hb + 4 * r;
+          if (h >= a.n_hot_dims) break;
+          const int dim = __ldg(a.hot_dim + h), g = __ldg(a.hot_deg + h), so = __ldg(a.hot_soff + h);
+          const int fm = __ldg(a.fam + dim);
+          const float z = fmaf(__ldg(a.fa + dim), f64_to_f32(xh[r]), __ldg(a.fb + dim));
+          float pm1 = 0.f, pc = 1.f;
+          for (int n = 0; n < g; ++n) {
+            const float pn = b_alpha[fm][n] * z * pc - b_beta[fm][n] * pm1;
+            pm1 = pc;
+            pc = pn;
+            PH[(so + n) * kT + q] = pc;
+          }
+        }
       }
     }
     __syncthreads();
@@ -173,16 +211,18 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
     float ys[NP], yc[NP];
 #pragma unroll
     for (int i = 0; i < NP; ++i) ys[i] = yc[i] = 0.f;
-    for (int it = it0; it < it1; ++it) {
+    // hot items come first in every warp's list, cold groups after them
+    int it = it0;
+    for (; it < it1; ++it) {
       const int code = __ldg(a.items + it);
-      if (!(code & kColdBit)) {
+      if (code & kColdBit) break;
         // hot node: gather over its hot entries, times the path product
         const int4 h0 = __ldg(a.node + 3 * code), pa = __ldg(a.node + 3 * code + 1),
                    pb = __ldg(a.node + 3 * code + 2);
         const int4* E = a.hot_ent + (h0.x >> 1);
         const int ne = h0.y >> 1;
         float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll 2
+#pragma unroll 4
         for (int e = 0; e < ne; ++e) {
           const int4 ee = __ldg(E + e);
           const float4 f0 = *reinterpret_cast<const float4*>(PH + ee.x + q0);
@@ -201,69 +241,73 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
         const float va[4] = {v.x * acc.x, v.y * acc.y, v.z * acc.z, v.w * acc.w};
 #pragma unroll
         for (int i = 0; i < NP; ++i) kahan_add(ys[i], yc[i], va[i]);
-        continue;
-      }
-      // cold group: staircase block, then the x-dot epilogue
-      const int g = code & (kColdBit - 1);
-      const int4 gd = __ldg(a.grp + 3 * g), gdim = __ldg(a.grp + 3 * g + 1), gdeg = __ldg(a.grp + 3 * g + 2);
+    }
+
+    // cold groups, software-pipelined: the x values of group n + 1 are loaded
+    // while group n is contracted; they are turned into basis values at the
+    // start of the next iteration.
+    if (it < it1) {
+      int g = __ldg(a.items + it) & (kColdBit - 1);
+      int4 gd = __ldg(a.grp + 3 * g), gdim = __ldg(a.grp + 3 * g + 1);
       double xv[NP][4];
-      if (gd.z && fastx == 2) {  // rows 32-byte aligned: one 32-byte load per point
+      load_x<NP>(x, prow, fastx, gd, gdim, xv);
+      for (; it < it1; ++it) {
+        // basis values of this group from the x values that have arrived
+        float ph[NP][4];
+        {
+          const float4 A = __ldg(a.grp_ab + 2 * g), B = __ldg(a.grp_ab + 2 * g + 1);
+          const float Aa[4] = {A.x, A.y, A.z, A.w}, Bb[4] = {B.x, B.y, B.z, B.w};
+          if (gd.z) {
 #pragma unroll
-        for (int i = 0; i < NP; ++i) ld4_stream(x + prow[i] + gdim.x, xv[i][0], xv[i][1], xv[i][2], xv[i][3]);
-      } else if (gd.z && fastx) {
+            for (int i = 0; i < NP; ++i)
 #pragma unroll
-        for (int i = 0; i < NP; ++i) {
-          ld2_stream(x + prow[i] + gdim.x, xv[i][0], xv[i][1]);
-          ld2_stream(x + prow[i] + gdim.x + 2, xv[i][2], xv[i][3]);
-        }
-      } else {
-        const int dd[4] = {gdim.x, gdim.y, gdim.z, gdim.w};
+              for (int j = 0; j < 4; ++j) ph[i][j] = fmaf(Aa[j], f64_to_f32(xv[i][j]), Bb[j]);
+          } else {
+            const int4 gdeg = __ldg(a.grp + 3 * g + 2);
+            const int dd[4] = {gdim.x, gdim.y, gdim.z, gdim.w};
+            const int gg[4] = {gdeg.x, gdeg.y, gdeg.z, gdeg.w};
 #pragma unroll
-        for (int i = 0; i < NP; ++i)
+            for (int j = 0; j < 4; ++j) {
+              const int fm = gg[j] ? __ldg(a.fam + dd[j]) : 0;
 #pragma unroll
-          for (int j = 0; j < 4; ++j) xv[i][j] = ld1_stream(x + prow[i] + dd[j]);
-      }
-      float T[NP][4];
-#pragma unroll
-      for (int i = 0; i < NP; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) T[i][j] = 0.f;
-      const float4* Wg = a.W + (gd.y >> 2);
-      const float* Vk = VC + q0;
-#pragma unroll 4
-      for (int k = 0; k < gd.x; ++k) {
-        const float4 v = *reinterpret_cast<const float4*>(Vk + k * kT);
-        const float4 w = __ldg(Wg + k);
-        const float vv[4] = {v.x, v.y, v.z, v.w};
-        const float ww[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-        for (int i = 0; i < NP; ++i)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) T[i][j] = fmaf(vv[i], ww[j], T[i][j]);
-      }
-      const float4 A = __ldg(a.grp_ab + 2 * g), B = __ldg(a.grp_ab + 2 * g + 1);
-      const float Aa[4] = {A.x, A.y, A.z, A.w}, Bb[4] = {B.x, B.y, B.z, B.w};
-      if (gd.z) {
-#pragma unroll
-        for (int i = 0; i < NP; ++i) {
-          float s = 0.f;
-#pragma unroll
-          for (int j = 0; j < 4; ++j) s = fmaf(T[i][j], fmaf(Aa[j], f64_to_f32(xv[i][j]), Bb[j]), s);
-          kahan_add(ys[i], yc[i], s);
-        }
-      } else {
-        const int dd[4] = {gdim.x, gdim.y, gdim.z, gdim.w};
-        const int gg[4] = {gdeg.x, gdeg.y, gdeg.z, gdeg.w};
-#pragma unroll
-        for (int i = 0; i < NP; ++i) {
-          float s = 0.f;
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            if (gg[j] == 0) continue;
-            const float z = fmaf(Aa[j], f64_to_f32(xv[i][j]), Bb[j]);
-            s = fmaf(T[i][j], phi_rec(__ldg(a.fam + dd[j]), z, gg[j]), s);
+              for (int i = 0; i < NP; ++i)
+                ph[i][j] = gg[j] ? phi_rec(fm, fmaf(Aa[j], f64_to_f32(xv[i][j]), Bb[j]), gg[j]) : 0.f;
+            }
           }
-          kahan_add(ys[i], yc[i], s);
+        }
+        // next group: descriptors and x loads in flight during this contraction
+        const int4 gdc = gd;
+        if (it + 1 < it1) {
+          g = __ldg(a.items + it + 1) & (kColdBit - 1);
+          gd = __ldg(a.grp + 3 * g);
+          gdim = __ldg(a.grp + 3 * g + 1);
+          load_x<NP>(x, prow, fastx, gd, gdim, xv);
+        }
+        // staircase block T[i][j] = sum_k Vc[k][i] W[k][j]
+        float T[NP][4];
+#pragma unroll
+        for (int i = 0; i < NP; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) T[i][j] = 0.f;
+        const float4* Wg = a.W + (gdc.y >> 2);
+        const float* Vk = VC + q0;
+#pragma unroll 4
+        for (int k = 0; k < gdc.x; ++k) {
+          const float4 v = *reinterpret_cast<const float4*>(Vk + k * kT);
+          const float4 w = __ldg(Wg + k);
+          const float vv[4] = {v.x, v.y, v.z, v.w};
+          const float ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+          for (int i = 0; i < NP; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) T[i][j] = fmaf(vv[i], ww[j], T[i][j]);
+        }
+#pragma unroll
+        for (int i = 0; i < NP; ++i) {
+          float sacc = 0.f;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) sacc = fmaf(T[i][j], ph[i][j], sacc);
+          kahan_add(ys[i], yc[i], sacc);
         }
       }
     }
