@@ -205,6 +205,7 @@ class SpectralPlan:
         """Tables of the blocked evaluator (one output), if the plan fits it."""
         from .blocked import build_blocked
 
+        self._blocked_args = (tr, c, maxdeg, d, fam, fa, fb, T)
         lay = build_blocked(tr, c, maxdeg, d, fam, fa, fb)
         if lay is None:
             return
