@@ -58,7 +58,7 @@ def peaks():
 
 def ncu_traffic():
     """DRAM bytes per launch of the FP32 evaluator from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "spectral_eval_leja1000.txt")
+    path = os.path.join(ROOT, "profiles", "blocked_eval_leja1000.txt")
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_launch_full_size:"):

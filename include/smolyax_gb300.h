@@ -396,6 +396,13 @@ int smx_eval_f64_noalloc(const smx_plan* plan_host, const double* x, int64_t P, 
                          void* stream);
 
 /* Human-readable description of the last error on this thread (host string). */
+/* Device address of page-locked (pinned) host memory, for kernels that read
+ * host inputs directly over the host link instead of copying them first;
+ * SMX_ERR_ARG if `host` is not page-locked host memory, SMX_ERR_UNSUPPORTED
+ * if it is not mapped for the current device.  (No counterpart in the
+ * reference: its inputs are copied to the device by JAX, interpolation.py:257.) */
+int smx_host_device_pointer(const void* host, void** dev);
+
 const char* smx_last_error_string(void);
 
 /* Library version string (host). */

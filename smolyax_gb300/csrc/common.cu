@@ -134,3 +134,19 @@ extern "C" int smx_scan_i64(const int64_t* in, int64_t* out, int64_t n, void* ws
 extern "C" const char* smx_last_error_string(void) { return smx::g_last_error.c_str(); }
 
 extern "C" const char* smx_version(void) { return "smolyax_gb300 0.1 (sm_103a)"; }
+
+extern "C" int smx_host_device_pointer(const void* host, void** dev) {
+  SMX_REQUIRE(host != nullptr && dev != nullptr, "smx_host_device_pointer: null pointer");
+  *dev = nullptr;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+    cudaGetLastError();
+    return smx::set_error(SMX_ERR_ARG, "smx_host_device_pointer: not page-locked host memory");
+  }
+  if (cudaHostGetDevicePointer(dev, const_cast<void*>(host), 0) != cudaSuccess || *dev == nullptr) {
+    cudaGetLastError();
+    *dev = nullptr;
+    return smx::set_error(SMX_ERR_UNSUPPORTED, "smx_host_device_pointer: host memory not mapped for the device");
+  }
+  return SMX_OK;
+}

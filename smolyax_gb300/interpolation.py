@@ -22,6 +22,9 @@ from ._capi import call, ptr
 
 ArrayLike = Union[np.ndarray, torch.Tensor]
 
+# host inputs of at least this many rows are copied and evaluated in overlapped chunks (FP32)
+_OVERLAP_MIN_ROWS = 16384
+
 
 def _stream():
     return capi.stream_ptr(torch.cuda.current_stream())
@@ -330,6 +333,44 @@ class SmolyakBarycentricInterpolator:
         self._n_inputs = int(x.shape[0])
         return x.contiguous()
 
+    def _host_rows(self, x):
+        """Rows of a 2-D host input of width d_in (0 for device inputs and other shapes)."""
+        if isinstance(x, torch.Tensor):
+            return int(x.shape[0]) if x.device.type == "cpu" and x.dim() == 2 and x.shape[1] == self._d_in else 0
+        if isinstance(x, np.ndarray) and x.ndim == 2 and x.shape[1] == self._d_in:
+            return int(x.shape[0])
+        return 0
+
+    def _call_fp32_host(self, x):
+        """FP32 evaluation of a large host input: the rows are copied in chunks on
+        two side streams, each chunk evaluated as soon as it has arrived, so the
+        host->device transfer (the bound of this call) overlaps the evaluation."""
+        assert self._plan is not None, "The operator has not yet been set up for a target function via `set_f`."
+        xh = x if isinstance(x, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64))
+        xh = xh.to(torch.float64).contiguous()
+        Pn = int(xh.shape[0])
+        self._n_inputs = Pn
+        sp = self.spectral_plan()
+        dev = indices.device()
+        xd = torch.empty(Pn, self._d_in, dtype=torch.float64, device=dev)
+        y = torch.empty(Pn, self._d_out, dtype=torch.float32, device=dev)
+        cur = torch.cuda.current_stream(dev)
+        streams = [torch.cuda.Stream(device=dev) for _ in range(2)]
+        n_chunks = max(2, min(8, Pn // (_OVERLAP_MIN_ROWS // 2)))
+        step = -(-Pn // n_chunks)
+        for i, p0 in enumerate(range(0, Pn, step)):
+            p1 = min(Pn, p0 + step)
+            s = streams[i % 2]
+            s.wait_stream(cur)
+            with torch.cuda.stream(s):
+                xd[p0:p1].copy_(xh[p0:p1], non_blocking=True)
+                sp.evaluate(xd[p0:p1], y[p0:p1])
+        for s in streams:
+            cur.wait_stream(s)
+            xd.record_stream(s)
+            y.record_stream(s)
+        return y
+
     def _chunk(self, bytes_per_point):
         lim = max(1, int(self._memory_limit * 1024**3 // max(1, bytes_per_point)))
         return lim
@@ -347,6 +388,8 @@ class SmolyakBarycentricInterpolator:
         """Evaluate the interpolant at points x, shape (n_points, d_in) or (d_in,) -> (n_points, d_out).
 
         ``precision`` overrides the constructor's choice for this call."""
+        if (precision or self._precision) == "fp32" and self._host_rows(x) >= _OVERLAP_MIN_ROWS:
+            return self._call_fp32_host(x)
         x = self._validate_input(x)
         Pn = int(x.shape[0])
         if (precision or self._precision) == "fp32":

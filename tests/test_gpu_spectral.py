@@ -121,3 +121,23 @@ def test_tensor_core_path_gauss_hermite(t, d_out):
     print("GH d_out=%d: tensor-core FP32 per-point norm-wise error vs FP64 %.3e" % (d_out, err))
     assert err < 2e-6
 
+
+
+@pytest.mark.parametrize("d_out", [1, 3])
+def test_host_input_overlap_equals_device_input(d_out):
+    """Large host inputs are copied and evaluated in overlapped chunks: same
+    values as evaluating the device copy in one call (pinned, pageable, numpy)."""
+    import torch
+
+    from smolyax_gb300 import nodes
+    from smolyax_gb300.interpolation import _OVERLAP_MIN_ROWS
+
+    d, t = 30, 6.0
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    ip = _interp(node_gen=nodes.Leja(dim=d), k=k, t=t, d_out=d_out, f=fns.rational_vec(d, d_out, seed=4))
+    x = np.random.default_rng(5).uniform(-1, 1, (2 * _OVERLAP_MIN_ROWS + 77, d))
+    ref = ip(torch.as_tensor(x, device="cuda"), precision="fp32").cpu().numpy()
+    for xin in (torch.from_numpy(x).pin_memory(), torch.from_numpy(x), x):
+        got = ip(xin, precision="fp32")
+        assert got.device.type == "cuda" and got.shape == (x.shape[0], d_out)
+        np.testing.assert_array_equal(got.cpu().numpy(), ref)
