@@ -8,12 +8,15 @@
 //   integral: Q[o]       offset[o] + sum_r qw(r) F[r][o]
 #include <math.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace {
 
 constexpr int kMaxN = 4;   // summands with more active dimensions use the generic path
 constexpr int kOC = 4;     // outputs accumulated per pass
+constexpr int kMaxGridY = 65535;
 
 // --- barycentric weights (barycentric.py:13-31) ---------------------------------------
 __global__ void bary_weights_kernel(int n_pairs, const int32_t* __restrict__ deg, const int32_t* __restrict__ voff,
@@ -164,10 +167,12 @@ struct PlanArgs {
   const double* offset;
 };
 
+// Grid: points along x, chunks of kOC outputs along y (from output o_base).
 __global__ void contract64_kernel(PlanArgs a, const double* __restrict__ Lt, int64_t P, double* __restrict__ y,
-                                  int o0) {
+                                  int o_base) {
   const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (p >= P) return;
+  const int o0 = o_base + int(blockIdx.y) * kOC;
+  if (p >= P || o0 >= a.dout) return;
   const int nout = min(kOC, a.dout - o0);
   // Two-level sum: summands accumulate into `blk`, which is folded into `acc`
   // every 32 summands, so rounding grows with 32 + n_sum/32 instead of n_sum.
@@ -198,9 +203,10 @@ __global__ void contract64_kernel(PlanArgs a, const double* __restrict__ Lt, int
 // active slot.  Each thread owns one point, so the read-modify-writes of its
 // row of J never race.
 __global__ void jacobian64_kernel(PlanArgs a, const double* __restrict__ Lt, const double* __restrict__ dLt, int64_t P,
-                                  double* __restrict__ J, int o0) {
+                                  double* __restrict__ J, int o_base) {
   const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (p >= P) return;
+  const int o0 = o_base + int(blockIdx.y) * kOC;
+  if (p >= P || o0 >= a.dout) return;
   const int nout = min(kOC, a.dout - o0);
   double* Jp = J + p * int64_t(a.dout) * a.d_in;
   for (int s = 0; s < a.n_sum; ++s) {
@@ -340,8 +346,11 @@ extern "C" int smx_contract_f64(const smx_plan* pl, const double* Lt, int64_t P,
   if (P == 0) return SMX_OK;
   SMX_REQUIRE(y && (pl->n_summands == 0 || Lt), "smx_contract_f64: null pointer");
   PlanArgs a = args_of(pl, pl->F64);
-  for (int o0 = 0; o0 < pl->d_out; o0 += kOC) {
-    contract64_kernel<<<smx::grid_for(P, 128), 128, 0, smx::as_stream(stream)>>>(a, Lt, P, y, o0);
+  // all output chunks in one launch (blockIdx.y), so few points still fill the GPU
+  const int chunks = (pl->d_out + kOC - 1) / kOC;
+  for (int c0 = 0; c0 < chunks; c0 += kMaxGridY) {
+    const dim3 grid(smx::grid_for(P, 128), unsigned(std::min(kMaxGridY, chunks - c0)));
+    contract64_kernel<<<grid, 128, 0, smx::as_stream(stream)>>>(a, Lt, P, y, c0 * kOC);
     SMX_LAUNCH_CHECK("smx_contract_f64");
   }
   return SMX_OK;
@@ -386,8 +395,10 @@ extern "C" int smx_jacobian(const smx_plan* pl, const double* x, int64_t P, int6
   rc = smx_basis_f64(pl, x, P, ldx, Lt, dLt, stream);
   if (rc) return rc;
   PlanArgs a = args_of(pl, pl->F64);
-  for (int o0 = 0; o0 < pl->d_out; o0 += kOC) {
-    jacobian64_kernel<<<smx::grid_for(P, 128), 128, 0, st>>>(a, Lt, dLt, P, J, o0);
+  const int chunks = (pl->d_out + kOC - 1) / kOC;
+  for (int c0 = 0; c0 < chunks; c0 += kMaxGridY) {
+    const dim3 grid(smx::grid_for(P, 128), unsigned(std::min(kMaxGridY, chunks - c0)));
+    jacobian64_kernel<<<grid, 128, 0, st>>>(a, Lt, dLt, P, J, c0 * kOC);
     SMX_LAUNCH_CHECK("smx_jacobian");
   }
   return SMX_OK;

@@ -796,21 +796,30 @@ __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32
   float st1 = 1.f, st2 = 1.f, st3 = 1.f, st4 = 1.f, st5 = 1.f, st6 = 1.f, st7 = 1.f, st8 = 1.f;
   for (int jb = 0; jb < K; jb += 32) {
     const int jn = min(32, K - jb);
-    for (int j = 0; j < jn; ++j) {
-      const int w = __ldg(tape + jb + j);
-      const float b = row[(w & 0xffff) * rstride + tid];
-      float v;
-      switch (w >> 16) {
-        case 1: st1 = b; v = st1; break;
-        case 2: st2 = st1 * b; v = st2; break;
-        case 3: st3 = st2 * b; v = st3; break;
-        case 4: st4 = st3 * b; v = st4; break;
-        case 5: st5 = st4 * b; v = st5; break;
-        case 6: st6 = st5 * b; v = st6; break;
-        case 7: st7 = st6 * b; v = st7; break;
-        default: st8 = st7 * b; v = st8; break;
+    // 8 tape entries at a time: their basis values are loaded together (the
+    // loads are independent; only the stack updates are sequential)
+    for (int j = 0; j < jn; j += 8) {
+      int w[8];
+      float b[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) w[u] = j + u < jn ? __ldg(tape + jb + j + u) : (1 << 16);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) b[u] = row[(w[u] & 0xffff) * rstride + tid];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        float v;
+        switch (w[u] >> 16) {
+          case 1: st1 = b[u]; v = st1; break;
+          case 2: st2 = st1 * b[u]; v = st2; break;
+          case 3: st3 = st2 * b[u]; v = st3; break;
+          case 4: st4 = st3 * b[u]; v = st4; break;
+          case 5: st5 = st4 * b[u]; v = st5; break;
+          case 6: st6 = st5 * b[u]; v = st6; break;
+          case 7: st7 = st6 * b[u]; v = st7; break;
+          default: st8 = st7 * b[u]; v = st8; break;
+        }
+        if (j + u < jn) tile[(j + u) * 129 + tid] = v;
       }
-      tile[j * 129 + tid] = v;
     }
     __syncthreads();
     // coalesced write-out: thread t -> column t % 32 of rows t / 32, t / 32 + 4, ...
@@ -837,9 +846,14 @@ __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32
 
 }  // namespace
 
+// Basis rows stay in shared memory only while that leaves room for several
+// blocks per SM (the tape walk is latency-bound); otherwise they go to a
+// point-contiguous global scratch that is read coalesced through L1/L2.
+constexpr size_t kPanelSmemRows = 24 * 1024;
+
 extern "C" size_t smx_spectral_panel_workspace(int n_slots, int64_t P) {
   const size_t smem = (size_t(n_slots) * 128 + 32 * 129) * sizeof(float);
-  if (smem <= 220 * 1024) return 0;
+  if (smem <= kPanelSmemRows) return 0;
   return size_t(n_slots) * size_t((P + 127) / 128 * 128) * sizeof(float);
 }
 
