@@ -29,6 +29,7 @@ namespace {
 constexpr int kW = 16;           // warps per block
 constexpr int kT = 128;          // points per tile
 constexpr int kThr = kW * 32;
+constexpr int kHB = kThr / kT;   // thread groups of 128 in phase 0 (one hot dimension each)
 constexpr int kRec = 512;        // recurrence table length
 constexpr int kColdBit = 1 << 30;
 constexpr int kHotPass = 16;     // hot dimensions per thread and pass of phase 0
@@ -163,21 +164,21 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
     for (int i = 0; i < NP; ++i) prow[i] = min(p0 + lane + 32 * i, P - 1) * ldx;
 
     // phase 0: basis values of the hot slots.  Thread (q, hb) handles the hot
-    // dimensions hb, hb + 4, ... of tile point q; its x loads (up to 16 per
+    // dimensions hb, hb + kHB, ... of tile point q; its x loads (up to 16 per
     // pass) are all issued before the first is used.
     {
       const int q = threadIdx.x & (kT - 1), hb = threadIdx.x >> 7;
       const double* xp = x + min(p0 + quad_point(q), P - 1) * ldx;
-      for (int h0 = 0; h0 < a.n_hot_dims; h0 += 4 * kHotPass) {
+      for (int h0 = 0; h0 < a.n_hot_dims; h0 += kHB * kHotPass) {
         double xh[kHotPass];
 #pragma unroll
         for (int r = 0; r < kHotPass; ++r) {
-          const int h = h0 + hb + 4 * r;
+          const int h = h0 + hb + kHB * r;
           xh[r] = h < a.n_hot_dims ? __ldg(xp + __ldg(a.hot_dim + h)) : 0.0;
         }
 #pragma unroll
         for (int r = 0; r < kHotPass; ++r) {
-          const int h = h0 + hb + 4 * r;
+          const int h = h0 + hb + kHB * r;
           if (h >= a.n_hot_dims) break;
           const int dim = __ldg(a.hot_dim + h), g = __ldg(a.hot_deg + h), so = __ldg(a.hot_soff + h);
           const int fm = __ldg(a.fam + dim);

@@ -40,7 +40,7 @@ def test_blocked_tables_match_direct_sum(d, t, fam_id):
     hot = np.sort(items[items < (1 << 30)])
     node = lay["node"].reshape(-1, 12)
     assert np.array_equal(hot, np.nonzero(node[:, 1] > 0)[0])
-    assert lay["smem"] == (lay["n_hs"] + lay["k_c"]) * 512 + 16384
+    assert lay["smem"] == (lay["n_hs"] + lay["k_c"]) * 512 + 2 * N_WARPS * 512
 
 
 def test_blocked_balance_at_high_dimension():
