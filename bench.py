@@ -273,6 +273,68 @@ def run_tensor_workload(args):
     return 0
 
 
+def run_backward_workload(args):
+    """Forward + hand-written backward through torch.autograd (dL/dx and dL/d
+    nodal values) at d_in=200, d_out=64, |Lambda|=5000, 1e5 points, with a
+    random FP32 cotangent (one JSON line)."""
+    import torch
+
+    from smolyax_gb300 import SmolyakBarycentricInterpolator, nodes
+    from smolyax_gb300.autograd import interpolate
+
+    d, t, d_out, P = 200, 7.853604, 64, 100_000
+    P = args.points if args.points != POINTS else P
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    t0 = time.perf_counter()
+    ip = SmolyakBarycentricInterpolator(node_gen=nodes.Leja(dim=d), k=k, t=t, d_out=d_out,
+                                        f=_vec_target("leja", d, d_out, 0), memory_limit=8.0)
+    ip.spectral_plan()._backward_ops()
+    setup_s = time.perf_counter() - t0
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1)
+    x0 = torch.rand(P, d, dtype=torch.float64, device=dev, generator=gen) * 2 - 1
+    g = torch.randn(P, d_out, dtype=torch.float32, device=dev, generator=gen)
+    fu = ip.nodal_values.clone().requires_grad_(True)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        x = x0.detach().requires_grad_(True)
+        fu.grad = None
+        y = interpolate(ip, x, fu)
+        y.backward(g)
+        return x.grad, fu.grad
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    evf = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(0) as clk:
+        for (a, b), (fa, fb) in zip(ev, evf):
+            a.record(stream)
+            fa.record(stream)
+            ip(x0, precision="fp32")
+            fb.record(stream)
+            step()
+            b.record(stream)
+        torch.cuda.synchronize()
+    ms_fwd = statistics.mean(fa.elapsed_time(fb) for fa, fb in evf)
+    ms = statistics.mean(a.elapsed_time(b) for a, b in ev) - ms_fwd
+    line = {
+        "metric": METRIC, "workload": "leja64bwd", "value": P * d_out / (ms * 1e-3), "unit": "evals/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "dtype": "fp32 (3xTF32 tensor contractions, FP64 coefficient adjoint)", "data": "synthetic",
+        "config": {"workload": "Leja d_in=200 d_out=64 |Lambda|=5000 (t=7.853604) rational f, 1e5 points U[-1,1]^200,"
+                               " forward + backward (dL/dx and dL/d nodal values), FP32 cotangent N(0,1)",
+                   "points": P, "d_in": d, "d_out": d_out},
+        "forward_ms": ms_fwd, "backward_ms": ms - ms_fwd, "setup_s": setup_s, "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def serving_fleet(seed=0):
     """16 interpolants: d_in log-uniform [4, 1000], d_out in {1, 16, 256, 1024},
     |Lambda| log-uniform [1e2, 1e5], Leja or Gauss-Hermite at random (seed 0)."""
@@ -464,7 +526,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--points", type=int, default=POINTS)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="leja1000", choices=["leja1000", "serving"] + sorted(WORKLOADS))
+    ap.add_argument("--workload", default="leja1000",
+                    choices=["leja1000", "serving", "leja64bwd"] + sorted(WORKLOADS))
     ap.add_argument("--requests", type=int, default=300)
     ap.add_argument("--rate", type=float, default=200.0)
     args = ap.parse_args()
@@ -472,6 +535,8 @@ def main():
         return run_reference(args)
     if args.workload == "serving":
         return run_serving(args)
+    if args.workload == "leja64bwd":
+        return run_backward_workload(args)
     if args.workload != "leja1000":
         return run_tensor_workload(args)
     return run_ours(args)
