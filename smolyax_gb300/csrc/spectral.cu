@@ -891,7 +891,7 @@ __device__ __forceinline__ void basis_row(int n_dims, const int32_t* __restrict_
                                           const int32_t* __restrict__ dmax, const int32_t* __restrict__ dsoff,
                                           const float* __restrict__ fam_a, const float* __restrict__ fam_b,
                                           const int32_t* __restrict__ fam, const double* __restrict__ xp, float* row,
-                                          int stride, int t) {
+                                          int64_t stride, int t) {
   for (int h = 0; h < n_dims; ++h) {
     const int dim = dims[h], g = dmax[h], so = dsoff[h];
     const int fm = fam[dim];
@@ -907,7 +907,9 @@ __device__ __forceinline__ void basis_row(int n_dims, const int32_t* __restrict_
 }
 
 // A^T panel: AT[K-1-j][p] (same reversed column order as the forward panel),
-// one thread per point, coalesced along points.
+// one thread per point, coalesced along points.  Basis values in the
+// point-contiguous global scratch rowg[slot][p]; the tape is read 8 entries
+// at a time so that their basis values load together.
 __global__ void __launch_bounds__(128) panel_t_tf32_kernel(int n_dims, const int32_t* __restrict__ dims,
                                                            const int32_t* __restrict__ dmax,
                                                            const int32_t* __restrict__ dsoff, int n_slots,
@@ -917,64 +919,82 @@ __global__ void __launch_bounds__(128) panel_t_tf32_kernel(int n_dims, const int
                                                            const int32_t* __restrict__ fam,
                                                            const double* __restrict__ x, int64_t P, int64_t ldx,
                                                            float* __restrict__ ATh, float* __restrict__ ATl,
-                                                           int64_t ldp) {
-  extern __shared__ __align__(16) float sm[];
+                                                           int64_t ldp, float* __restrict__ rowg, int64_t rstride) {
   const int tid = threadIdx.x;
   const int64_t p = blockIdx.x * int64_t(128) + tid;
   const double* xp = x + (p < P ? p : 0) * ldx;
-  basis_row(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, xp, sm, 128, tid);
+  float* row = rowg + blockIdx.x * int64_t(128) + tid;
+  basis_row(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, xp, row, rstride, 0);
   if (p >= P) return;
   float st1 = 1.f, st2 = 1.f, st3 = 1.f, st4 = 1.f, st5 = 1.f, st6 = 1.f, st7 = 1.f, st8 = 1.f;
-  for (int j = 0; j < K; ++j) {
-    const int w = __ldg(tape + j);
-    const float b = sm[(w & 0xffff) * 128 + tid];
-    float v;
-    switch (w >> 16) {
-      case 1: st1 = b; v = st1; break;
-      case 2: st2 = st1 * b; v = st2; break;
-      case 3: st3 = st2 * b; v = st3; break;
-      case 4: st4 = st3 * b; v = st4; break;
-      case 5: st5 = st4 * b; v = st5; break;
-      case 6: st6 = st5 * b; v = st6; break;
-      case 7: st7 = st6 * b; v = st7; break;
-      default: st8 = st7 * b; v = st8; break;
+  for (int j = 0; j < K; j += 8) {
+    int w[8];
+    float bb[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) w[u] = j + u < K ? __ldg(tape + j + u) : (1 << 16);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) bb[u] = row[int64_t(w[u] & 0xffff) * rstride];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const float b = bb[u];
+      float v;
+      switch (w[u] >> 16) {
+        case 1: st1 = b; v = st1; break;
+        case 2: st2 = st1 * b; v = st2; break;
+        case 3: st3 = st2 * b; v = st3; break;
+        case 4: st4 = st3 * b; v = st4; break;
+        case 5: st5 = st4 * b; v = st5; break;
+        case 6: st6 = st5 * b; v = st6; break;
+        case 7: st7 = st6 * b; v = st7; break;
+        default: st8 = st7 * b; v = st8; break;
+      }
+      if (j + u < K) {
+        uint32_t h, l;
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(v - __uint_as_float(h)));
+        const int64_t col = K - 1 - (j + u);
+        ATh[col * ldp + p] = __uint_as_float(h);
+        ATl[col * ldp + p] = __uint_as_float(l);
+      }
     }
-    uint32_t h, l;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(v - __uint_as_float(h)));
-    const int64_t col = K - 1 - j;
-    ATh[col * ldp + p] = __uint_as_float(h);
-    ATl[col * ldp + p] = __uint_as_float(l);
   }
 }
 
 // dL/dx[p][d] = a_d * sum_g phibar(d, g) phi'_g(z_d) with
 // phibar(pair) = sum over entries e containing the pair of G[p][e] * (product
-// of e's other basis values).  One thread per point (64 per CTA); the path of
-// the current entry (depth <= 8) is kept as basis slots, values and prefix
-// products; G is read in tiles of 32 columns (reversed pre-order) staged in
-// shared memory.
-__global__ void __launch_bounds__(64) vjp_x_kernel(int n_dims, const int32_t* __restrict__ dims,
-                                                   const int32_t* __restrict__ dmax, const int32_t* __restrict__ dsoff,
-                                                   int n_slots, const int32_t* __restrict__ tape, int K,
-                                                   const float* __restrict__ fam_a, const float* __restrict__ fam_b,
-                                                   const int32_t* __restrict__ fam, const double* __restrict__ x,
-                                                   int64_t P, int64_t ldx, const float* __restrict__ G, int64_t ldg,
-                                                   double* __restrict__ dx, int64_t lddx) {
+// of e's other basis values).  One thread per point, 32 per block: the basis
+// values sit in a point-contiguous global scratch (rowg[slot][p], written by
+// this kernel and read back coalesced), the adjoints of the block's points in
+// shared memory ([n_slots][32]), G in tiles of 32 columns (reversed
+// pre-order).  The path of the current entry (depth <= 8) is kept in
+// registers: slots s_i, basis values f_i and prefix products q_i; the tape is
+// read 8 entries at a time so their basis values load together.
+constexpr int kVjpTP = 32;
+
+__global__ void __launch_bounds__(kVjpTP) vjp_x_kernel(int n_dims, const int32_t* __restrict__ dims,
+                                                       const int32_t* __restrict__ dmax,
+                                                       const int32_t* __restrict__ dsoff, int n_slots,
+                                                       const int32_t* __restrict__ tape, int K,
+                                                       const float* __restrict__ fam_a,
+                                                       const float* __restrict__ fam_b,
+                                                       const int32_t* __restrict__ fam, const double* __restrict__ x,
+                                                       int64_t P, int64_t ldx, const float* __restrict__ G,
+                                                       int64_t ldg, double* __restrict__ dx, int64_t lddx,
+                                                       float* __restrict__ rowg, int64_t rstride) {
   extern __shared__ __align__(16) float sm[];
-  const int TP = blockDim.x;                   // 64, 32 or 16 points per CTA (shared memory permitting)
-  float* row = sm;                             // [n_slots][TP] basis values
-  float* bar = sm + size_t(n_slots) * TP;      // [n_slots][TP] adjoints
+  constexpr int TP = kVjpTP;
+  float* bar = sm;                             // [n_slots][TP] adjoints
   float* tile = bar + size_t(n_slots) * TP;    // [32][TP + 1]
   const int tid = threadIdx.x;
   const int64_t p0 = blockIdx.x * int64_t(TP);
   const int64_t p = p0 + tid;
   const double* xp = x + (p < P ? p : 0) * ldx;
-  basis_row(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, xp, row, TP, tid);
+  float* row = rowg + p;
+  basis_row(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, xp, row, rstride, 0);
   for (int s = 0; s < n_slots; ++s) bar[s * TP + tid] = 0.f;
-  int sl[9];
-  float ph[9], pre[9];
-  pre[0] = 1.f;
+  int s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0, s6 = 0, s7 = 0, s8 = 0;
+  float f1 = 1.f, f2 = 1.f, f3 = 1.f, f4 = 1.f, f5 = 1.f, f6 = 1.f, f7 = 1.f, f8 = 1.f;
+  float q1 = 1.f, q2 = 1.f, q3 = 1.f, q4 = 1.f, q5 = 1.f, q6 = 1.f, q7 = 1.f;
   for (int jb = 0; jb < K; jb += 32) {
     const int jn = min(32, K - jb);
     __syncthreads();
@@ -984,18 +1004,41 @@ __global__ void __launch_bounds__(64) vjp_x_kernel(int n_dims, const int32_t* __
       tile[c * (TP + 1) + r] = (c < jn && p0 + r < P) ? G[(p0 + r) * ldg + (K - 1 - (jb + c))] : 0.f;
     }
     __syncthreads();
-    for (int j = 0; j < jn; ++j) {
-      const int w = __ldg(tape + jb + j);
-      const int s = w & 0xffff;
-      const int k = min(8, w >> 16);
-      sl[k] = s;
-      ph[k] = row[s * TP + tid];
-      pre[k] = pre[k - 1] * ph[k];
-      const float gv = tile[j * (TP + 1) + tid];
-      float suf = gv;
-      for (int i = k; i >= 1; --i) {
-        bar[sl[i] * TP + tid] += pre[i - 1] * suf;
-        suf *= ph[i];
+    for (int j = 0; j < jn; j += 8) {
+      int w[8];
+      float b[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) w[u] = j + u < jn ? __ldg(tape + jb + j + u) : 0;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) b[u] = row[int64_t(w[u] & 0xffff) * rstride];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = min(8, w[u] >> 16);  // 0: padding past the end of the tape
+        const int sl = (w[u] & 0xffff) * TP + tid;
+        switch (k) {
+          case 1: s1 = sl; f1 = b[u]; q1 = b[u]; break;
+          case 2: s2 = sl; f2 = b[u]; q2 = q1 * b[u]; break;
+          case 3: s3 = sl; f3 = b[u]; q3 = q2 * b[u]; break;
+          case 4: s4 = sl; f4 = b[u]; q4 = q3 * b[u]; break;
+          case 5: s5 = sl; f5 = b[u]; q5 = q4 * b[u]; break;
+          case 6: s6 = sl; f6 = b[u]; q6 = q5 * b[u]; break;
+          case 7: s7 = sl; f7 = b[u]; q7 = q6 * b[u]; break;
+          case 8: s8 = sl; f8 = b[u]; break;
+          default: break;
+        }
+        // adjoints of the path's factors: bar(s_i) += G * prod_{i' != i} f_i'
+        float suf = k ? tile[(j + u) * (TP + 1) + tid] : 0.f;
+        switch (k) {
+          case 8: bar[s8] += q7 * suf; suf *= f8; [[fallthrough]];
+          case 7: bar[s7] += q6 * suf; suf *= f7; [[fallthrough]];
+          case 6: bar[s6] += q5 * suf; suf *= f6; [[fallthrough]];
+          case 5: bar[s5] += q4 * suf; suf *= f5; [[fallthrough]];
+          case 4: bar[s4] += q3 * suf; suf *= f4; [[fallthrough]];
+          case 3: bar[s3] += q2 * suf; suf *= f3; [[fallthrough]];
+          case 2: bar[s2] += q1 * suf; suf *= f2; [[fallthrough]];
+          case 1: bar[s1] += suf; break;
+          default: break;
+        }
       }
     }
   }
@@ -1058,39 +1101,46 @@ __global__ void coeff_adjoint_kernel(int n_sum, const int32_t* __restrict__ poff
 
 }  // namespace
 
+extern "C" size_t smx_spectral_panel_t_workspace(int n_slots, int64_t P) {
+  if (n_slots < 0 || P < 0) return 0;
+  return size_t(n_slots) * size_t((P + 127) / 128 * 128) * sizeof(float);
+}
+
 extern "C" int smx_spectral_panel_t_tf32(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff,
                                          int n_slots, const int32_t* tape, int K, const float* fam_a,
                                          const float* fam_b, const int32_t* fam, const double* x, int64_t P,
-                                         int64_t ldx, float* AT_hi, float* AT_lo, int64_t ldp, void* stream) {
+                                         int64_t ldx, float* AT_hi, float* AT_lo, int64_t ldp, void* ws,
+                                         size_t ws_bytes, void* stream) {
   SMX_REQUIRE(n_dims >= 0 && n_slots >= 0 && K >= 0 && P >= 0 && ldp >= P, "smx_spectral_panel_t_tf32: bad sizes");
   if (P == 0 || K == 0) return SMX_OK;
   SMX_REQUIRE(dims && dmax && dsoff && tape && fam_a && fam_b && fam && x && AT_hi && AT_lo,
               "smx_spectral_panel_t_tf32: null pointer");
-  const size_t smem = size_t(n_slots) * 128 * sizeof(float);
-  SMX_REQUIRE(smem <= 220 * 1024, "smx_spectral_panel_t_tf32: too many basis slots");
+  SMX_REQUIRE(ws && ws_bytes >= smx_spectral_panel_t_workspace(n_slots, P),
+              "smx_spectral_panel_t_tf32: workspace too small");
   int rc = upload_consts();
   if (rc) return rc;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(panel_t_tf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    attr = true;
-  }
-  panel_t_tf32_kernel<<<smx::grid_for(P, 128), 128, smem, smx::as_stream(stream)>>>(
-      n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, AT_hi, AT_lo, ldp);
+  const int64_t rstride = (P + 127) / 128 * 128;
+  panel_t_tf32_kernel<<<smx::grid_for(P, 128), 128, 0, smx::as_stream(stream)>>>(
+      n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, AT_hi, AT_lo, ldp,
+      static_cast<float*>(ws), rstride);
   SMX_LAUNCH_CHECK("smx_spectral_panel_t_tf32");
   return SMX_OK;
+}
+
+extern "C" size_t smx_spectral_vjp_x_workspace(int n_slots, int64_t P) {
+  if (n_slots < 0 || P < 0) return 0;
+  return size_t(n_slots) * size_t((P + kVjpTP - 1) / kVjpTP * kVjpTP) * sizeof(float);
 }
 
 extern "C" int smx_spectral_vjp_x(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff,
                                   int n_slots, const int32_t* tape, int K, const float* fam_a, const float* fam_b,
                                   const int32_t* fam, const double* x, int64_t P, int64_t ldx, const float* G,
-                                  int64_t ldg, double* dx, int64_t lddx, void* stream) {
+                                  int64_t ldg, double* dx, int64_t lddx, void* ws, size_t ws_bytes, void* stream) {
   SMX_REQUIRE(n_dims >= 0 && n_slots >= 0 && K >= 0 && P >= 0 && ldg >= K, "smx_spectral_vjp_x: bad sizes");
   if (P == 0) return SMX_OK;
   SMX_REQUIRE(dims && dmax && dsoff && tape && fam_a && fam_b && fam && x && G && dx, "smx_spectral_vjp_x: null");
-  int TP = 64;
-  while (TP > 16 && (size_t(n_slots) * TP * 2 + 32 * (TP + 1)) * sizeof(float) > 220 * 1024) TP /= 2;
-  const size_t smem = (size_t(n_slots) * TP * 2 + 32 * (TP + 1)) * sizeof(float);
+  SMX_REQUIRE(ws && ws_bytes >= smx_spectral_vjp_x_workspace(n_slots, P), "smx_spectral_vjp_x: workspace too small");
+  const size_t smem = (size_t(n_slots) * kVjpTP + 32 * (kVjpTP + 1)) * sizeof(float);
   SMX_REQUIRE(smem <= 220 * 1024, "smx_spectral_vjp_x: too many basis slots");
   int rc = upload_consts();
   if (rc) return rc;
@@ -1099,8 +1149,10 @@ extern "C" int smx_spectral_vjp_x(int n_dims, const int32_t* dims, const int32_t
     cudaFuncSetAttribute(vjp_x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     attr = true;
   }
-  vjp_x_kernel<<<smx::grid_for(P, TP), TP, smem, smx::as_stream(stream)>>>(
-      n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, G, ldg, dx, lddx);
+  const int64_t rstride = (P + kVjpTP - 1) / kVjpTP * kVjpTP;
+  vjp_x_kernel<<<smx::grid_for(P, kVjpTP), kVjpTP, smem, smx::as_stream(stream)>>>(
+      n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, G, ldg, dx, lddx,
+      static_cast<float*>(ws), rstride);
   SMX_LAUNCH_CHECK("smx_spectral_vjp_x");
   return SMX_OK;
 }

@@ -141,8 +141,9 @@ class Server:
         b = P * d_in * 8 + P * d_out * (4 if req.precision == "fp32" else 8)
         sp = self.spec[req.name]
         if req.op == "grad":
-            K = (sp._bwd or {}).get("ldk", ip._tree.size)
-            b += P * d_in * 8 + P * K * 4 + P * 4 * ((d_out + 3) // 4 * 4) * 3
+            bwd = sp._bwd or {}
+            K = bwd.get("ldk", ip._tree.size)
+            b += P * d_in * 8 + P * K * 4 + P * 4 * ((d_out + 3) // 4 * 4) * 3 + P * 4 * bwd.get("n_slots", d_in)
         elif req.precision == "fp64":
             b += P * ip._plan.c.n_values * 8
         elif sp.tc is not None:

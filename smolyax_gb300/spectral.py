@@ -280,11 +280,14 @@ class SpectralPlan:
         if need_x:
             dx = torch.zeros(P, d, dtype=torch.float64, device=dev)
             G = torch.empty(min(step, P), ldk, dtype=torch.float32, device=dev)
+            nws = capi.size("smx_spectral_vjp_x_workspace", ops["n_slots"], min(step, P))
+            ws = torch.empty(max(nws, 1), dtype=torch.uint8, device=dev)
             for p0 in range(0, P, step):
                 p1 = min(P, p0 + step)
                 call("smx_gemm_tf32x3", ptr(gh[p0:p1]), ptr(gl[p0:p1]), ldo, ptr(ops["Rh"]), ptr(ops["Rl"]), ldo,
                      p1 - p0, K, ldo, ptr(G), ldk, None, 0, ptr(err), st)
-                call("smx_spectral_vjp_x", *common, ptr(x[p0:p1]), p1 - p0, d, ptr(G), ldk, ptr(dx[p0:p1]), d, st)
+                call("smx_spectral_vjp_x", *common, ptr(x[p0:p1]), p1 - p0, d, ptr(G), ldk, ptr(dx[p0:p1]), d,
+                     ptr(ws), nws, st)
         if need_coef:
             ldp = _round4(min(step, P))
             ATh = torch.empty(K, ldp, dtype=torch.float32, device=dev)
@@ -292,12 +295,15 @@ class SpectralPlan:
             gT = torch.empty(ldo, ldp, dtype=torch.float32, device=dev)
             gTh, gTl = torch.empty_like(gT), torch.empty_like(gT)
             dCrev = torch.zeros(K, d_out, dtype=torch.float32, device=dev)
+            nws = capi.size("smx_spectral_panel_t_workspace", ops["n_slots"], min(step, P))
+            ws = torch.empty(max(nws, 1), dtype=torch.uint8, device=dev)
             for i, p0 in enumerate(range(0, P, step)):
                 p1 = min(P, p0 + step)
                 n = p1 - p0
                 ATh.zero_()
                 ATl.zero_()
-                call("smx_spectral_panel_t_tf32", *common, ptr(x[p0:p1]), n, d, ptr(ATh), ptr(ATl), ldp, st)
+                call("smx_spectral_panel_t_tf32", *common, ptr(x[p0:p1]), n, d, ptr(ATh), ptr(ATl), ldp, ptr(ws), nws,
+                     st)
                 gT.zero_()
                 gT[:, :n] = g32[p0:p1].t()
                 call("smx_split_tf32", ptr(gT), ldo, ldp, ldp, ptr(gTh), ptr(gTl), ldp, st)
