@@ -300,9 +300,14 @@ typedef struct smx_blocked {
 
 /* Shared memory of one block: (n_hs + k_c) * 512 + 16384 bytes (<= 220 KiB). */
 size_t smx_blocked_smem(const smx_blocked* plan_host);
-/* y[P] (FP32) at x[P, ldx] (FP64); one persistent block per SM. */
-int smx_blocked_eval(const smx_blocked* plan_host, const double* x, int64_t P, int64_t ldx, float* y,
-                     void* stream);
+/* y[P] (FP32) at x[P, ldx] (FP64); one persistent block per SM.  When the
+ * tiles leave a partial last round, its tiles are shared by several blocks
+ * (fixed-order sum of their partial results). */
+int smx_blocked_eval(const smx_blocked* plan_host, const double* x, int64_t P, int64_t ldx, float* y, void* ws,
+                     size_t ws_bytes, void* stream);
+/* Scratch for the split of the last round of tiles across blocks (partial
+ * sums and counters); without it (ws = NULL) every tile is one block's work. */
+size_t smx_blocked_eval_workspace(const smx_blocked* plan_host, int64_t P);
 
 /* Basis-product panel of the orthogonal form for the tensor-core contraction:
  * A[p][j] = prod over the pairs of entry j of phi_g(z_d) for the K non-root

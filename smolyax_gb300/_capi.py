@@ -150,7 +150,8 @@ SIGNATURES = {
     "smx_spectral_eval": (_int, [_p, _p, _i64, _i64, _p, _p]),
     "smx_blocked_smem": (_sz, [_p]),
     "smx_host_device_pointer": (_int, [_p, _p]),
-    "smx_blocked_eval": (_int, [_p, _p, _i64, _i64, _p, _p]),
+    "smx_blocked_eval": (_int, [_p, _p, _i64, _i64, _p, _p, _sz, _p]),
+    "smx_blocked_eval_workspace": (_sz, [_p, _i64]),
     "smx_blocked_eval_batch_workspace": (_sz, [_int, _int]),
     "smx_blocked_eval_batch": (_int, [_p, _int, _p, _int, _p, _sz, _p]),
     "smx_eval_f64_noalloc": (_int, [_p, _p, _i64, _i64, _p, _p]),

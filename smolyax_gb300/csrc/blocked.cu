@@ -33,6 +33,7 @@ constexpr int kHB = kThr / kT;   // thread groups of 128 in phase 0 (one hot dim
 constexpr int kRec = 512;        // recurrence table length
 constexpr int kColdBit = 1 << 30;
 constexpr int kHotPass = 16;     // hot dimensions per thread and pass of phase 0
+constexpr int kMaxSplit = 16;    // blocks sharing one tile of the last round
 
 __constant__ float b_alpha[2][kRec];
 __constant__ float b_beta[2][kRec];
@@ -147,9 +148,14 @@ __device__ __forceinline__ void load_x(const double* __restrict__ x, const int64
 
 // One tile of 32 * NP points of one plan (lane l: points l + 32 i, i < NP),
 // shared by the single-plan kernel and the multi-plan batch kernel.
+// With split_S > 1 the block runs every split_S-th item (from split_c) of each
+// warp's list and leaves its per-point partial sums in part[split_c]; the last
+// of the split_S blocks of the tile (counted in *ctr) adds them in order.
 template <int NP>
 __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __restrict__ x, int64_t P, int64_t ldx,
-                                             float* __restrict__ y, int fastx, int64_t tile, float* sm) {
+                                             float* __restrict__ y, int fastx, int64_t tile, float* sm,
+                                             int split_c = 0, int split_S = 1, float* part = nullptr,
+                                             unsigned int* ctr = nullptr) {
   float* PH = sm;
   float* VC = sm + size_t(a.n_hs) * kT;
   float* RS = VC + size_t(a.k_c) * kT;
@@ -213,8 +219,8 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
 #pragma unroll
     for (int i = 0; i < NP; ++i) ys[i] = yc[i] = 0.f;
     // hot items come first in every warp's list, cold groups after them
-    int it = it0;
-    for (; it < it1; ++it) {
+    int it = it0 + split_c;
+    for (; it < it1; it += split_S) {
       const int code = __ldg(a.items + it);
       if (code & kColdBit) break;
         // hot node: gather over its hot entries, times the path product
@@ -252,7 +258,7 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
       int4 gd = __ldg(a.grp + 3 * g), gdim = __ldg(a.grp + 3 * g + 1);
       double xv[NP][4];
       load_x<NP>(x, prow, fastx, gd, gdim, xv);
-      for (; it < it1; ++it) {
+      for (; it < it1; it += split_S) {
         // basis values of this group from the x values that have arrived
         float ph[NP][4];
         {
@@ -278,8 +284,8 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
         }
         // next group: descriptors and x loads in flight during this contraction
         const int4 gdc = gd;
-        if (it + 1 < it1) {
-          g = __ldg(a.items + it + 1) & (kColdBit - 1);
+        if (it + split_S < it1) {
+          g = __ldg(a.items + it + split_S) & (kColdBit - 1);
           gd = __ldg(a.grp + 3 * g);
           gdim = __ldg(a.grp + 3 * g + 1);
           load_x<NP>(x, prow, fastx, gd, gdim, xv);
@@ -327,7 +333,30 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
         kahan_add(s, c, -RC[w * kT + q]);
       }
       const int64_t p = p0 + quad_point(q);
-      if (p < P) y[p] = a.c0 + (s - c);
+      if (split_S == 1) {
+        if (p < P) y[p] = a.c0 + (s - c);
+      } else {
+        part[(2 * split_c) * kT + q] = s;
+        part[(2 * split_c + 1) * kT + q] = c;
+        __threadfence();
+      }
+    }
+    if (split_S > 1) {
+      __shared__ unsigned int s_last;
+      __syncthreads();
+      if (threadIdx.x == 0) s_last = atomicAdd(ctr, 1u) == unsigned(split_S - 1);
+      __syncthreads();
+      if (s_last && threadIdx.x < kT && (threadIdx.x & 3) < NP) {
+        __threadfence();
+        const int q = threadIdx.x;
+        float s = 0.f, c = 0.f;
+        for (int cc = 0; cc < split_S; ++cc) {
+          kahan_add(s, c, __ldcg(part + (2 * cc) * kT + q));
+          kahan_add(s, c, -__ldcg(part + (2 * cc + 1) * kT + q));
+        }
+        const int64_t p = p0 + quad_point(q);
+        if (p < P) y[p] = a.c0 + (s - c);
+      }
     }
     __syncthreads();
   }
@@ -336,11 +365,18 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
 template <int NP>
 __global__ void __launch_bounds__(kThr, 1)
     blocked_eval_kernel(BArgs a, const double* __restrict__ x, int64_t P, int64_t ldx, float* __restrict__ y,
-                        int fastx) {
+                        int fastx, float* __restrict__ part, unsigned int* __restrict__ ctr) {
   extern __shared__ __align__(16) float sm[];
   const int64_t n_tiles = (P + 32 * NP - 1) / (32 * NP);
-  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x)
-    blocked_tile<NP>(a, x, P, ldx, y, fastx, tile, sm);
+  const int64_t G = gridDim.x, rounds = n_tiles / G, rem = n_tiles - rounds * G;
+  for (int64_t r = 0; r < rounds; ++r) blocked_tile<NP>(a, x, P, ldx, y, fastx, blockIdx.x + r * G, sm);
+  if (rem == 0) return;
+  // last round: each remaining tile is shared by S blocks (S = 1 without a full round before it)
+  const int S = rounds > 0 && part != nullptr ? int(G / rem < kMaxSplit ? G / rem : kMaxSplit) : 1;
+  const int64_t t = blockIdx.x / S;
+  if (t >= rem) return;
+  const int c = int(blockIdx.x - t * S);
+  blocked_tile<NP>(a, x, P, ldx, y, fastx, rounds * G + t, sm, c, S, part + t * (2 * kMaxSplit * kT), ctr + t);
 }
 
 struct BWork {
@@ -453,8 +489,16 @@ int fast_x(const double* x, int64_t ldx) {
 
 extern "C" size_t smx_blocked_smem(const smx_blocked* b) { return b ? smem_of(b) : 0; }
 
-extern "C" int smx_blocked_eval(const smx_blocked* b, const double* x, int64_t P, int64_t ldx, float* y,
-                                void* stream) {
+extern "C" size_t smx_blocked_eval_workspace(const smx_blocked* b, int64_t P) {
+  (void)b;
+  (void)P;
+  int sms = 0;
+  if (prepare(&sms) != SMX_OK) return 0;
+  return size_t(sms) * (2 * kMaxSplit * kT * sizeof(float) + sizeof(unsigned int));
+}
+
+extern "C" int smx_blocked_eval(const smx_blocked* b, const double* x, int64_t P, int64_t ldx, float* y, void* ws,
+                                size_t ws_bytes, void* stream) {
   int rc = check_plan(b, "smx_blocked_eval");
   if (rc) return rc;
   SMX_REQUIRE(P >= 0 && ldx >= b->d_in, "smx_blocked_eval: bad sizes");
@@ -467,8 +511,17 @@ extern "C" int smx_blocked_eval(const smx_blocked* b, const double* x, int64_t P
   // last round of blocks: most per-item work does not scale with the points)
   const int64_t tiles = (P + 127) / 128;
   const unsigned grid = static_cast<unsigned>(tiles < sms ? tiles : sms);
+  // scratch of the last-round tile split: partial sums and counters
+  float* part = nullptr;
+  unsigned int* ctr = nullptr;
+  if (ws && ws_bytes >= smx_blocked_eval_workspace(b, P) && tiles > sms) {
+    part = static_cast<float*>(ws);
+    ctr = reinterpret_cast<unsigned int*>(static_cast<char*>(ws) + size_t(sms) * 2 * kMaxSplit * kT * sizeof(float));
+    if (cudaMemsetAsync(ctr, 0, size_t(sms) * sizeof(unsigned int), smx::as_stream(stream)) != cudaSuccess)
+      return smx::set_error(SMX_ERR_CUDA, "smx_blocked_eval: counter reset failed");
+  }
   blocked_eval_kernel<4><<<grid, kThr, smem_of(b), smx::as_stream(stream)>>>(to_args(b), x, P, ldx, y,
-                                                                           fast_x(x, ldx));
+                                                                           fast_x(x, ldx), part, ctr);
   SMX_LAUNCH_CHECK("smx_blocked_eval");
   return SMX_OK;
 }

@@ -87,6 +87,7 @@ class Server:
 
     def __init__(self, interpolants: dict, memory_budget: float = 8.0, n_streams: int = 8):
         self.dev = torch.device("cuda", torch.cuda.current_device())
+        self.sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
         self.ips = dict(interpolants)
         self.names = list(self.ips)
         self.spec = {}
@@ -155,7 +156,11 @@ class Server:
         sp = self.spec[req.name]
         if req.op != "eval" or req.precision != "fp32" or sp.tc is not None:
             return None
-        return "blocked" if sp.blocked is not None else "stream"
+        if sp.blocked is not None:
+            # a request of a full round of tiles or more fills the GPU alone (and
+            # is then evaluated exactly as alone, with the last-round split)
+            return None if req.points > 128 * self.sms else "blocked"
+        return "stream"
 
     def _admit(self):
         batches, singles = {}, []

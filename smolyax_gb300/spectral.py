@@ -336,8 +336,10 @@ class SpectralPlan:
         if self.blocked is not None:
             import ctypes
 
-            call("smx_blocked_eval", ctypes.byref(self.blocked), ptr(x), int(x.shape[0]), int(x.shape[1]), ptr(y),
-                 st)
+            P = int(x.shape[0])
+            nws = capi.size("smx_blocked_eval_workspace", ctypes.byref(self.blocked), P)
+            ws = torch.empty(max(nws, 1), dtype=torch.uint8, device=x.device)
+            call("smx_blocked_eval", ctypes.byref(self.blocked), ptr(x), P, int(x.shape[1]), ptr(y), ptr(ws), nws, st)
             return y
         call("smx_spectral_eval", self.ref(), ptr(x), int(x.shape[0]), int(x.shape[1]), ptr(y), st)
         return y
