@@ -173,3 +173,29 @@ def test_blocked_last_round_split():
     scale = y64.abs().max().item()
     assert (y.double() - y_unsplit).abs().max().item() <= 2e-6 * scale
     assert (y.double() - y64).abs().max().item() <= 1e-6 * scale
+
+
+@pytest.mark.parametrize("kind,d,t", [("gh", 30, 6.5), ("leja", 30, 7.5), ("gh", 30, 7.5), ("leja", 60, 7.0)])
+def test_blocked_evaluator_generic_groups(kind, d, t):
+    """One-output plans on the blocked evaluator: Gauss-Hermite families, cold
+    groups with non-contiguous dimensions and degree-2 cold slots (the generic
+    group path) -- FP32 values within 1e-6 of the FP64 path (relative to the
+    largest value)."""
+    import torch
+
+    from smolyax_gb300 import nodes
+
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    gen = nodes.Leja(dim=d) if kind == "leja" else nodes.GaussHermite(dim=d)
+    f = fns.rational_vec(d, 1, seed=d) if kind == "leja" else fns.exponential(d, 1, seed=d)
+    ip = _interp(node_gen=gen, k=k, t=t, d_out=1, f=f)
+    sp = ip.spectral_plan()
+    assert sp.blocked is not None
+    rng = np.random.default_rng(d)
+    x = rng.uniform(-1, 1, (3000, d)) if kind == "leja" else rng.normal(size=(3000, d)) / np.sqrt(2)
+    x = torch.as_tensor(x, device="cuda")
+    y32 = ip(x, precision="fp32").double()
+    y64 = ip(x, precision="fp64")
+    err = ((y32 - y64).abs().max() / y64.abs().max()).item()
+    print("%s d=%d t=%.1f: FP32 error %.2e" % (kind, d, t, err))
+    assert err < 1e-6
