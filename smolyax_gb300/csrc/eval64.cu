@@ -35,6 +35,31 @@ __global__ void bary_weights_kernel(int n_pairs, const int32_t* __restrict__ deg
   }
 }
 
+// Normalised barycentric basis of one pair of degree G (no node hit): one
+// reciprocal per node difference and one per row sum, kept in registers (FP64
+// division is the expensive operation of this kernel on the FP64 pipe).
+template <int G>
+__device__ __forceinline__ void basis_pair(double xv, const double* __restrict__ nd, const double* __restrict__ bw,
+                                           double* __restrict__ Lt, double* __restrict__ dLt, int o, int64_t P,
+                                           int64_t p) {
+  double r[G + 1], b[G + 1];
+  double S = 0.0, Sd = 0.0;
+#pragma unroll
+  for (int j = 0; j <= G; ++j) {
+    r[j] = 1.0 / __dsub_rn(xv, nd[j]);
+    b[j] = bw[j] * r[j];
+    S += b[j];
+    Sd -= b[j] * r[j];
+  }
+  const double iS = 1.0 / S;
+#pragma unroll
+  for (int j = 0; j <= G; ++j) {
+    const double l = b[j] * iS;
+    Lt[int64_t(o + j) * P + p] = l;
+    if (dLt) dLt[int64_t(o + j) * P + p] = (-b[j] * r[j]) * iS - l * Sd * iS;
+  }
+}
+
 // --- basis table (barycentric.py:34-66, normalisation :117; derivative :126-155, :213-219)
 __global__ void basis64_kernel(int n_pairs, const int32_t* __restrict__ pdim, const int32_t* __restrict__ pdeg,
                                const int32_t* __restrict__ pvoff, const double* __restrict__ node,
@@ -60,20 +85,32 @@ __global__ void basis64_kernel(int n_pairs, const int32_t* __restrict__ pdim, co
       }
       continue;
     }
-    double S = 0.0, Sd = 0.0;
-    for (int j = 0; j <= g; ++j) {
-      const double df = __dsub_rn(xv, node[o + j]);
-      S += bw[o + j] / df;
-      if (dLt) Sd += -bw[o + j] / (df * df);
-    }
-    for (int j = 0; j <= g; ++j) {
-      const double df = __dsub_rn(xv, node[o + j]);
-      const double b = bw[o + j] / df;
-      const double l = b / S;
-      Lt[int64_t(o + j) * P + p] = l;
-      if (dLt) {
-        const double db = -bw[o + j] / (df * df);
-        dLt[int64_t(o + j) * P + p] = db / S - l * Sd / S;
+    switch (g) {
+      case 0: basis_pair<0>(xv, node + o, bw + o, Lt, dLt, o, P, p); break;
+      case 1: basis_pair<1>(xv, node + o, bw + o, Lt, dLt, o, P, p); break;
+      case 2: basis_pair<2>(xv, node + o, bw + o, Lt, dLt, o, P, p); break;
+      case 3: basis_pair<3>(xv, node + o, bw + o, Lt, dLt, o, P, p); break;
+      case 4: basis_pair<4>(xv, node + o, bw + o, Lt, dLt, o, P, p); break;
+      case 5: basis_pair<5>(xv, node + o, bw + o, Lt, dLt, o, P, p); break;
+      case 6: basis_pair<6>(xv, node + o, bw + o, Lt, dLt, o, P, p); break;
+      case 7: basis_pair<7>(xv, node + o, bw + o, Lt, dLt, o, P, p); break;
+      case 8: basis_pair<8>(xv, node + o, bw + o, Lt, dLt, o, P, p); break;
+      default: {
+        double S = 0.0, Sd = 0.0;
+        for (int j = 0; j <= g; ++j) {
+          const double r = 1.0 / __dsub_rn(xv, node[o + j]);
+          const double b = bw[o + j] * r;
+          S += b;
+          Sd -= b * r;
+        }
+        const double iS = 1.0 / S;
+        for (int j = 0; j <= g; ++j) {
+          const double r = 1.0 / __dsub_rn(xv, node[o + j]);
+          const double b = bw[o + j] * r;
+          const double l = b * iS;
+          Lt[int64_t(o + j) * P + p] = l;
+          if (dLt) dLt[int64_t(o + j) * P + p] = (-b * r) * iS - l * Sd * iS;
+        }
       }
     }
   }
@@ -83,36 +120,37 @@ __global__ void basis64_kernel(int n_pairs, const int32_t* __restrict__ pdim, co
 // Level L of a summand with N active pairs: sum over mu_L of l_L[mu_L] * (inner).
 // The innermost level reads rows of F.  `dslot` selects a pair whose basis is
 // replaced by its derivative table (jacobian); -1 for evaluation.
-template <int L, int N>
+template <int OC, int L, int N>
 __device__ inline void clevel(const double* __restrict__ Lt, const double* __restrict__ dLt, int dslot, int64_t P,
                               int64_t p, const int (&voff)[kMaxN], const int (&deg)[kMaxN],
                               const double* __restrict__ Fs, int dout, int o0, int nout, int64_t row,
-                              double (&acc)[kOC]) {
+                              double (&acc)[OC]) {
   const int g = deg[L];
   const double* lt = (dslot == L ? dLt : Lt) + int64_t(voff[L]) * P + p;
   for (int j = 0; j <= g; ++j) {
     const double l = lt[int64_t(j) * P];
-    double sub[kOC];
+    double sub[OC];
     if constexpr (L == N - 1) {
       const double* fr = Fs + (row * (g + 1) + j) * dout + o0;
 #pragma unroll
-      for (int q = 0; q < kOC; ++q) sub[q] = q < nout ? fr[q] : 0.0;
+      for (int q = 0; q < OC; ++q) sub[q] = q < nout ? fr[q] : 0.0;
     } else {
 #pragma unroll
-      for (int q = 0; q < kOC; ++q) sub[q] = 0.0;
-      clevel<L + 1, N>(Lt, dLt, dslot, P, p, voff, deg, Fs, dout, o0, nout, row * (g + 1) + j, sub);
+      for (int q = 0; q < OC; ++q) sub[q] = 0.0;
+      clevel<OC, L + 1, N>(Lt, dLt, dslot, P, p, voff, deg, Fs, dout, o0, nout, row * (g + 1) + j, sub);
     }
 #pragma unroll
-    for (int q = 0; q < kOC; ++q) acc[q] = fma(l, sub[q], acc[q]);
+    for (int q = 0; q < OC; ++q) acc[q] = fma(l, sub[q], acc[q]);
   }
 }
 
 // Generic path (any number of pairs): full product per entry.
+template <int OC>
 __device__ inline void cgeneric(const double* __restrict__ Lt, const double* __restrict__ dLt, int dslot, int64_t P,
                                 int64_t p, const int32_t* __restrict__ pairs, int n,
                                 const int32_t* __restrict__ pvoff, const int32_t* __restrict__ pdeg,
                                 const double* __restrict__ Fs, int64_t K, int dout, int o0, int nout,
-                                double (&acc)[kOC]) {
+                                double (&acc)[OC]) {
   int mu[SMX_MAX_DEPTH];
   for (int i = 0; i < n; ++i) mu[i] = 0;
   for (int64_t r = 0; r < K; ++r) {
@@ -123,7 +161,7 @@ __device__ inline void cgeneric(const double* __restrict__ Lt, const double* __r
     }
     const double* fr = Fs + r * dout + o0;
 #pragma unroll
-    for (int q = 0; q < kOC; ++q)
+    for (int q = 0; q < OC; ++q)
       if (q < nout) acc[q] = fma(w, fr[q], acc[q]);
     for (int i = n - 1; i >= 0; --i) {  // row-major increment, last pair fastest
       if (++mu[i] <= pdeg[pairs[i]]) break;
@@ -132,13 +170,14 @@ __device__ inline void cgeneric(const double* __restrict__ Lt, const double* __r
   }
 }
 
+template <int OC>
 __device__ inline void contract_summand(const double* __restrict__ Lt, const double* __restrict__ dLt, int dslot,
                                         int64_t P, int64_t p, const int32_t* __restrict__ pairs, int n,
                                         const int32_t* __restrict__ pvoff, const int32_t* __restrict__ pdeg,
                                         const double* __restrict__ Fs, int64_t K, int dout, int o0, int nout,
-                                        double (&acc)[kOC]) {
+                                        double (&acc)[OC]) {
   if (n > kMaxN) {
-    cgeneric(Lt, dLt, dslot, P, p, pairs, n, pvoff, pdeg, Fs, K, dout, o0, nout, acc);
+    cgeneric<OC>(Lt, dLt, dslot, P, p, pairs, n, pvoff, pdeg, Fs, K, dout, o0, nout, acc);
     return;
   }
   int voff[kMaxN], deg[kMaxN];
@@ -148,10 +187,10 @@ __device__ inline void contract_summand(const double* __restrict__ Lt, const dou
     deg[i] = i < n ? pdeg[pairs[i]] : 0;
   }
   switch (n) {
-    case 1: clevel<0, 1>(Lt, dLt, dslot, P, p, voff, deg, Fs, dout, o0, nout, 0, acc); break;
-    case 2: clevel<0, 2>(Lt, dLt, dslot, P, p, voff, deg, Fs, dout, o0, nout, 0, acc); break;
-    case 3: clevel<0, 3>(Lt, dLt, dslot, P, p, voff, deg, Fs, dout, o0, nout, 0, acc); break;
-    default: clevel<0, 4>(Lt, dLt, dslot, P, p, voff, deg, Fs, dout, o0, nout, 0, acc); break;
+    case 1: clevel<OC, 0, 1>(Lt, dLt, dslot, P, p, voff, deg, Fs, dout, o0, nout, 0, acc); break;
+    case 2: clevel<OC, 0, 2>(Lt, dLt, dslot, P, p, voff, deg, Fs, dout, o0, nout, 0, acc); break;
+    case 3: clevel<OC, 0, 3>(Lt, dLt, dslot, P, p, voff, deg, Fs, dout, o0, nout, 0, acc); break;
+    default: clevel<OC, 0, 4>(Lt, dLt, dslot, P, p, voff, deg, Fs, dout, o0, nout, 0, acc); break;
   }
 }
 
@@ -167,58 +206,65 @@ struct PlanArgs {
   const double* offset;
 };
 
-// Grid: points along x, chunks of kOC outputs along y (from output o_base).
+// Grid: points along x, chunks of OC outputs along y (from output o_base).
+template <int OC>
 __global__ void contract64_kernel(PlanArgs a, const double* __restrict__ Lt, int64_t P, double* __restrict__ y,
                                   int o_base) {
   const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  const int o0 = o_base + int(blockIdx.y) * kOC;
+  const int o0 = o_base + int(blockIdx.y) * OC;
   if (p >= P || o0 >= a.dout) return;
-  const int nout = min(kOC, a.dout - o0);
+  const int nout = min(OC, a.dout - o0);
   // Two-level sum: summands accumulate into `blk`, which is folded into `acc`
   // every 32 summands, so rounding grows with 32 + n_sum/32 instead of n_sum.
-  double acc[kOC] = {0.0, 0.0, 0.0, 0.0};
-  double blk[kOC] = {0.0, 0.0, 0.0, 0.0};
+  double acc[OC], blk[OC];
+#pragma unroll
+  for (int q = 0; q < OC; ++q) acc[q] = blk[q] = 0.0;
   for (int s = 0; s < a.n_sum; ++s) {
     const int q0 = a.poff[s], n = a.poff[s + 1] - q0;
     const int64_t e0 = a.eoff[s], K = a.eoff[s + 1] - e0;
-    double one[kOC] = {0.0, 0.0, 0.0, 0.0};
-    contract_summand(Lt, nullptr, -1, P, p, a.pairs + q0, n, a.pvoff, a.pdeg, a.F + e0 * a.dout, K, a.dout, o0, nout,
+    double one[OC];
+#pragma unroll
+    for (int q = 0; q < OC; ++q) one[q] = 0.0;
+    contract_summand<OC>(Lt, nullptr, -1, P, p, a.pairs + q0, n, a.pvoff, a.pdeg, a.F + e0 * a.dout, K, a.dout, o0, nout,
                      one);
 #pragma unroll
-    for (int q = 0; q < kOC; ++q) blk[q] += one[q];
+    for (int q = 0; q < OC; ++q) blk[q] += one[q];
     if ((s & 31) == 31) {
 #pragma unroll
-      for (int q = 0; q < kOC; ++q) {
+      for (int q = 0; q < OC; ++q) {
         acc[q] += blk[q];
         blk[q] = 0.0;
       }
     }
   }
 #pragma unroll
-  for (int q = 0; q < kOC; ++q)
+  for (int q = 0; q < OC; ++q)
     if (q < nout) y[p * a.dout + o0 + q] = a.offset[o0 + q] + (acc[q] + blk[q]);
 }
 
 // Jacobian: J[p][o][dim] += derivative contraction of every summand and every
 // active slot.  Each thread owns one point, so the read-modify-writes of its
 // row of J never race.
+template <int OC>
 __global__ void jacobian64_kernel(PlanArgs a, const double* __restrict__ Lt, const double* __restrict__ dLt, int64_t P,
                                   double* __restrict__ J, int o_base) {
   const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  const int o0 = o_base + int(blockIdx.y) * kOC;
+  const int o0 = o_base + int(blockIdx.y) * OC;
   if (p >= P || o0 >= a.dout) return;
-  const int nout = min(kOC, a.dout - o0);
+  const int nout = min(OC, a.dout - o0);
   double* Jp = J + p * int64_t(a.dout) * a.d_in;
   for (int s = 0; s < a.n_sum; ++s) {
     const int q0 = a.poff[s], n = a.poff[s + 1] - q0;
     const int64_t e0 = a.eoff[s], K = a.eoff[s + 1] - e0;
     for (int i = 0; i < n; ++i) {
-      double acc[kOC] = {0.0, 0.0, 0.0, 0.0};
-      contract_summand(Lt, dLt, i, P, p, a.pairs + q0, n, a.pvoff, a.pdeg, a.F + e0 * a.dout, K, a.dout, o0, nout,
+      double acc[OC];
+#pragma unroll
+      for (int q = 0; q < OC; ++q) acc[q] = 0.0;
+      contract_summand<OC>(Lt, dLt, i, P, p, a.pairs + q0, n, a.pvoff, a.pdeg, a.F + e0 * a.dout, K, a.dout, o0, nout,
                        acc);
       const int dim = a.pdim[a.pairs[q0 + i]];
 #pragma unroll
-      for (int q = 0; q < kOC; ++q)
+      for (int q = 0; q < OC; ++q)
         if (q < nout) Jp[int64_t(o0 + q) * a.d_in + dim] += acc[q];
     }
   }
@@ -347,10 +393,15 @@ extern "C" int smx_contract_f64(const smx_plan* pl, const double* Lt, int64_t P,
   SMX_REQUIRE(y && (pl->n_summands == 0 || Lt), "smx_contract_f64: null pointer");
   PlanArgs a = args_of(pl, pl->F64);
   // all output chunks in one launch (blockIdx.y), so few points still fill the GPU
-  const int chunks = (pl->d_out + kOC - 1) / kOC;
+  // one output: one accumulator per entry (the FP64 pipe is the bound)
+  const int oc = pl->d_out == 1 ? 1 : kOC;
+  const int chunks = (pl->d_out + oc - 1) / oc;
   for (int c0 = 0; c0 < chunks; c0 += kMaxGridY) {
     const dim3 grid(smx::grid_for(P, 128), unsigned(std::min(kMaxGridY, chunks - c0)));
-    contract64_kernel<<<grid, 128, 0, smx::as_stream(stream)>>>(a, Lt, P, y, c0 * kOC);
+    if (oc == 1)
+      contract64_kernel<1><<<grid, 128, 0, smx::as_stream(stream)>>>(a, Lt, P, y, c0);
+    else
+      contract64_kernel<kOC><<<grid, 128, 0, smx::as_stream(stream)>>>(a, Lt, P, y, c0 * kOC);
     SMX_LAUNCH_CHECK("smx_contract_f64");
   }
   return SMX_OK;
@@ -395,10 +446,14 @@ extern "C" int smx_jacobian(const smx_plan* pl, const double* x, int64_t P, int6
   rc = smx_basis_f64(pl, x, P, ldx, Lt, dLt, stream);
   if (rc) return rc;
   PlanArgs a = args_of(pl, pl->F64);
-  const int chunks = (pl->d_out + kOC - 1) / kOC;
+  const int oc = pl->d_out == 1 ? 1 : kOC;
+  const int chunks = (pl->d_out + oc - 1) / oc;
   for (int c0 = 0; c0 < chunks; c0 += kMaxGridY) {
     const dim3 grid(smx::grid_for(P, 128), unsigned(std::min(kMaxGridY, chunks - c0)));
-    jacobian64_kernel<<<grid, 128, 0, st>>>(a, Lt, dLt, P, J, c0 * kOC);
+    if (oc == 1)
+      jacobian64_kernel<1><<<grid, 128, 0, st>>>(a, Lt, dLt, P, J, c0);
+    else
+      jacobian64_kernel<kOC><<<grid, 128, 0, st>>>(a, Lt, dLt, P, J, c0 * kOC);
     SMX_LAUNCH_CHECK("smx_jacobian");
   }
   return SMX_OK;
