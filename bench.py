@@ -68,7 +68,77 @@ def ncu_traffic():
     return None
 
 
-class ClockSampler:
+class NvmlClockSampler:
+    """SM clock and clock-event reasons read through NVML (the driver's
+    libnvidia-ml, read-only queries) every ~1 ms while the timed region runs."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index):
+        import ctypes
+        import threading
+
+        self.index = index
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.handle = ctypes.c_void_p()
+        ok = False
+        try:
+            import torch
+
+            uuid = getattr(torch.cuda.get_device_properties(index), "uuid", None)
+            if uuid is not None:
+                ok = self.lib.nvmlDeviceGetHandleByUUID(("GPU-" + str(uuid)).encode(), ctypes.byref(self.handle)) == 0
+        except Exception:
+            ok = False
+        if not ok and self.lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(self.handle)) != 0:
+            raise OSError("no NVML handle")
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        self.lib.nvmlDeviceGetMaxClockInfo(self.handle, ctypes.c_int(1), ctypes.byref(mx))
+        self.max_mhz = float(mx.value)
+        self.samples, self.reasons = [], set()
+        self.stop = threading.Event()
+        self.thread = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        import ctypes
+
+        mhz, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop.is_set():
+            if self.lib.nvmlDeviceGetClockInfo(self.handle, ctypes.c_int(1), ctypes.byref(mhz)) == 0:
+                self.samples.append(float(mhz.value))
+            if self.reasons_fn(self.handle, ctypes.byref(rs)) == 0:
+                for bit, name in self.REASONS.items():
+                    if rs.value & bit:
+                        self.reasons.add(name)
+            time.sleep(0.001)
+
+    def __enter__(self):
+        self.thread.start()
+        return self
+
+    def __exit__(self, *exc):
+        self.stop.set()
+        self.thread.join(timeout=5)
+
+    def summary(self):
+        return {"sm_mhz": statistics.median(self.samples) if self.samples else None, "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(self.reasons), "samples": len(self.samples), "source": "nvml"}
+
+
+def ClockSampler(index):
+    """NVML sampler when the driver library loads, else nvidia-smi."""
+    try:
+        return NvmlClockSampler(index)
+    except Exception:
+        return SmiClockSampler(index)
+
+
+class SmiClockSampler:
     """nvidia-smi clock/throttle samples while the timed region runs."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
@@ -113,7 +183,7 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi"}
 
 
 def cpu_reference_rate(points, threads, seconds=12.0, seed=1):
