@@ -321,6 +321,12 @@ int smx_spectral_panel_tf32(int n_dims, const int32_t* dims, const int32_t* dmax
                             const int32_t* tape, int K, const float* fam_a, const float* fam_b, const int32_t* fam,
                             const double* x, int64_t P, int64_t ldx, float* A_hi, float* A_lo, int64_t lda, void* ws,
                             size_t ws_bytes, void* stream);
+/* Same panel as TF32 hi/lo pairs rounded to BF16 (bit patterns, 2 bytes each)
+ * for smx_gemm_bf16x3. */
+int smx_spectral_panel_bf16(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff, int n_slots,
+                            const int32_t* tape, int K, const float* fam_a, const float* fam_b, const int32_t* fam,
+                            const double* x, int64_t P, int64_t ldx, uint16_t* A_hi, uint16_t* A_lo, int64_t lda,
+                            void* ws, size_t ws_bytes, void* stream);
 
 /* Backward of the orthogonal form (no counterpart in the reference, whose
  * derivative is the dense Jacobian of interpolation.py:306-345):
@@ -383,6 +389,18 @@ int smx_blocked_eval_batch(const smx_blocked* plans_host, int n_plans, const smx
 int smx_gemm_tf32x3(const float* A_hi, const float* A_lo, int64_t lda, const float* B_hi, const float* B_lo,
                     int64_t ldb, int M, int N, int K, float* D, int64_t ldd, const float* bias, int accumulate, int* err,
                     void* stream);
+
+/* Split-BF16 form of the same contraction (kind::f16, both operands BF16,
+ * FP32 accumulation): D = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T with
+ * A = A_hi + A_lo, B = B_hi + B_lo in BF16 (2-byte bit patterns; leading
+ * dimensions multiples of 8).  About 16 significant bits per product: an
+ * option for d_out >= 16 when ~1e-5 relative error is acceptable. */
+int smx_gemm_bf16x3(const uint16_t* A_hi, const uint16_t* A_lo, int64_t lda, const uint16_t* B_hi,
+                    const uint16_t* B_lo, int64_t ldb, int M, int N, int K, float* D, int64_t ldd, const float* bias,
+                    int accumulate, int* err, void* stream);
+/* hi = BF16(src), lo = BF16(src - hi) for a [rows x cols] block (2-byte outputs). */
+int smx_split_bf16(const float* src, int64_t rows, int64_t cols, int64_t lds, uint16_t* hi, uint16_t* lo,
+                   int64_t ldo, void* stream);
 
 /* hi = TF32(src), lo = TF32(src - hi) for a [rows x cols] block. */
 int smx_split_tf32(const float* src, int64_t rows, int64_t cols, int64_t lds, float* hi, float* lo, int64_t ldo,

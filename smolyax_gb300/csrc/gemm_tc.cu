@@ -11,6 +11,7 @@
 // the epilogue, drains its own copies (bounded) and frees tensor memory.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <cuda_bf16.h>
 
 #include <mutex>
 
@@ -19,7 +20,7 @@
 namespace {
 
 constexpr int kBM = 128;
-constexpr int kBK = 32;  // fp32 elements per 128-byte row slice
+constexpr int kBK = 32;  // fp32 elements per 128-byte row slice (64 for bf16)
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on every wait
 
 __device__ __forceinline__ uint64_t global_ns() {
@@ -77,17 +78,27 @@ __device__ __forceinline__ uint64_t make_desc_sw128(uint32_t saddr) {
   return d;
 }
 
-// Instruction descriptor: D = F32, A = B = TF32, both K-major, M x N.
-__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+// Instruction descriptor: D = F32, A = B = TF32 (kind::tf32, format 2) or
+// BF16 (kind::f16, format 1), both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_mma(int M, int N, bool bf16) {
+  return (1u << 4) | ((bf16 ? 1u : 2u) << 7) | ((bf16 ? 1u : 2u) << 10) | (uint32_t(N >> 3) << 17) |
+         (uint32_t(M >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+template <bool BF16>
+__device__ __forceinline__ void mma_op(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+  if constexpr (BF16) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+  } else {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+  }
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -123,9 +134,13 @@ struct GemmArgs {
   int accumulate;  // D += A B^T instead of D = A B^T
 };
 
+// BF16 = false: kind::tf32 on FP32 operands (32 per 128-byte slice); true:
+// kind::f16 on BF16 operands (64 per slice).  Same slices, stages and MMAs.
+template <bool BF16>
 __global__ void __launch_bounds__(kThreadsTC, 1)
     gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                        const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl, GemmArgs g) {
+  constexpr int EK = BF16 ? 2 * kBK : kBK;  // elements per K-tile
   using L = Smem;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -139,7 +154,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
-  const int KT = (g.K + kBK - 1) / kBK;
+  const int KT = (g.K + EK - 1) / EK;
   const int NCH = (KT + kChunk - 1) / kChunk;
 
   if (threadIdx.x == 0) {
@@ -178,7 +193,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         }
         uint8_t* st = base + s * L::kStage;
         mbar_expect_tx(&full[s], L::kStage);
-        const int k = kt * kBK;
+        const int k = kt * EK;
         tma_load_2d(st, &tmAh, k, m0, &full[s]);
         tma_load_2d(st + L::kA, &tmAl, k, m0, &full[s]);
         tma_load_2d(st + 2 * L::kA, &tmBh, k, n0, &full[s]);
@@ -190,7 +205,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     __syncwarp();
   } else if (warp == 5) {
     if (lane == 0) {  // ---- MMA issuer
-      constexpr uint32_t idesc = idesc_tf32(kBM, kBN);
+      constexpr uint32_t idesc = idesc_mma(kBM, kBN, BF16);
       bool ok = true;
       int kt = 0;
       for (int c = 0; c < NCH && ok; ++c) {
@@ -216,14 +231,14 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
           const uint32_t b_hi = a_hi + 2 * L::kA;
           const uint32_t b_lo = b_hi + L::kB;
 #pragma unroll
-          for (int k8 = 0; k8 < kBK / 8; ++k8) {  // K = 8 tf32 = 32 bytes per MMA
+          for (int k8 = 0; k8 < 4; ++k8) {  // 32 bytes (8 tf32 or 16 bf16) of K per MMA
             const uint32_t off = k8 * 32;
             const uint64_t dah = make_desc_sw128(a_hi + off), dal = make_desc_sw128(a_lo + off);
             const uint64_t dbh = make_desc_sw128(b_hi + off), dbl = make_desc_sw128(b_lo + off);
-            mma_tf32(acc, dah, dbh, idesc, first ? 0u : 1u);
+            mma_op<BF16>(acc, dah, dbh, idesc, first ? 0u : 1u);
             first = false;
-            mma_tf32(acc, dah, dbl, idesc, 1u);
-            mma_tf32(acc, dal, dbh, idesc, 1u);
+            mma_op<BF16>(acc, dah, dbl, idesc, 1u);
+            mma_op<BF16>(acc, dal, dbh, idesc, 1u);
           }
           mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
         }
@@ -323,37 +338,53 @@ int get_encode() {
   return SMX_OK;
 }
 
-int make_map(CUtensorMap* tm, const float* ptr, int64_t rows, int64_t cols, int64_t ld, int box_rows) {
-  if ((reinterpret_cast<uintptr_t>(ptr) & 15) || (ld * 4) % 16)
+int make_map(CUtensorMap* tm, const void* ptr, int64_t rows, int64_t cols, int64_t ld, int box_rows, bool bf16 = false) {
+  const int es = bf16 ? 2 : 4;
+  if ((reinterpret_cast<uintptr_t>(ptr) & 15) || (ld * es) % 16)
     return smx::set_error(SMX_ERR_ARG, "tensor map: base must be 16-byte aligned and the row pitch a multiple of 16");
   cuuint64_t dims[2] = {cuuint64_t(cols), cuuint64_t(rows)};
-  cuuint64_t strides[1] = {cuuint64_t(ld * 4)};
-  cuuint32_t box[2] = {cuuint32_t(kBK), cuuint32_t(box_rows)};
+  cuuint64_t strides[1] = {cuuint64_t(ld * es)};
+  cuuint32_t box[2] = {cuuint32_t(bf16 ? 2 * kBK : kBK), cuuint32_t(box_rows)};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = g_encode(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(ptr), dims, strides, box, estr,
+  CUresult r = g_encode(tm, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                        const_cast<void*>(ptr), dims, strides, box, estr,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return smx::set_error(SMX_ERR_CUDA, "cuTensorMapEncodeTiled failed");
   return SMX_OK;
 }
 
-int launch(const float* Ah, const float* Al, int64_t lda, const float* Bh, const float* Bl, int64_t ldb, int M, int N,
+template <bool BF16>
+int launch(const void* Ah, const void* Al, int64_t lda, const void* Bh, const void* Bl, int64_t ldb, int M, int N,
            int K, float* D, int64_t ldd, const float* bias, int* err, int accumulate, cudaStream_t st) {
   CUtensorMap tAh, tAl, tBh, tBl;
   int rc;
-  if ((rc = make_map(&tAh, Ah, M, K, lda, kBM)) || (rc = make_map(&tAl, Al, M, K, lda, kBM)) ||
-      (rc = make_map(&tBh, Bh, N, K, ldb, kBN)) || (rc = make_map(&tBl, Bl, N, K, ldb, kBN)))
+  if ((rc = make_map(&tAh, Ah, M, K, lda, kBM, BF16)) || (rc = make_map(&tAl, Al, M, K, lda, kBM, BF16)) ||
+      (rc = make_map(&tBh, Bh, N, K, ldb, kBN, BF16)) || (rc = make_map(&tBl, Bl, N, K, ldb, kBN, BF16)))
     return rc;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, Smem::kTotal);
+    cudaFuncSetAttribute(gemm_tf32x3_kernel<BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, Smem::kTotal);
     attr = true;
   }
   GemmArgs g{M, N, K, D, ldd, bias, err, accumulate};
   dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM);
-  gemm_tf32x3_kernel<<<grid, kThreadsTC, Smem::kTotal, st>>>(tAh, tAl, tBh, tBl, g);
-  SMX_LAUNCH_CHECK("smx_gemm_tf32x3");
+  gemm_tf32x3_kernel<BF16><<<grid, kThreadsTC, Smem::kTotal, st>>>(tAh, tAl, tBh, tBl, g);
+  SMX_LAUNCH_CHECK(BF16 ? "smx_gemm_bf16x3" : "smx_gemm_tf32x3");
   return SMX_OK;
+}
+
+// ---- BF16 split: hi = x rounded to BF16 (round to nearest even), lo = BF16(x - hi)
+__global__ void split_bf16_kernel(const float* __restrict__ src, int64_t rows, int64_t cols, int64_t lds,
+                                  __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, int64_t ldo) {
+  const int64_t n = rows * cols;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t r = i / cols, c = i - r * cols;
+    const float v = src[r * lds + c];
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    hi[r * ldo + c] = h;
+    lo[r * ldo + c] = __float2bfloat16_rn(v - __bfloat162float(h));
+  }
 }
 
 }  // namespace
@@ -377,5 +408,29 @@ extern "C" int smx_gemm_tf32x3(const float* A_hi, const float* A_lo, int64_t lda
   SMX_REQUIRE(K >= 1 && A_hi && A_lo && B_hi && B_lo && D && err, "smx_gemm_tf32x3: null pointer");
   int rc = get_encode();
   if (rc) return rc;
-  return launch(A_hi, A_lo, lda, B_hi, B_lo, ldb, M, N, K, D, ldd, bias, err, accumulate, smx::as_stream(stream));
+  return launch<false>(A_hi, A_lo, lda, B_hi, B_lo, ldb, M, N, K, D, ldd, bias, err, accumulate,
+                       smx::as_stream(stream));
+}
+
+extern "C" int smx_gemm_bf16x3(const uint16_t* A_hi, const uint16_t* A_lo, int64_t lda, const uint16_t* B_hi,
+                               const uint16_t* B_lo, int64_t ldb, int M, int N, int K, float* D, int64_t ldd,
+                               const float* bias, int accumulate, int* err, void* stream) {
+  SMX_REQUIRE(M >= 0 && N >= 0 && K >= 0 && lda >= K && ldb >= K && ldd >= N, "smx_gemm_bf16x3: bad sizes");
+  if (M == 0 || N == 0) return SMX_OK;
+  SMX_REQUIRE(K >= 1 && A_hi && A_lo && B_hi && B_lo && D && err, "smx_gemm_bf16x3: null pointer");
+  int rc = get_encode();
+  if (rc) return rc;
+  return launch<true>(A_hi, A_lo, lda, B_hi, B_lo, ldb, M, N, K, D, ldd, bias, err, accumulate,
+                      smx::as_stream(stream));
+}
+
+extern "C" int smx_split_bf16(const float* src, int64_t rows, int64_t cols, int64_t lds, uint16_t* hi, uint16_t* lo,
+                              int64_t ldo, void* stream) {
+  SMX_REQUIRE(rows >= 0 && cols >= 0 && lds >= cols && ldo >= cols, "smx_split_bf16: bad sizes");
+  if (rows * cols == 0) return SMX_OK;
+  SMX_REQUIRE(src && hi && lo, "smx_split_bf16: null pointer");
+  split_bf16_kernel<<<smx::grid_for(rows * cols, 256), 256, 0, smx::as_stream(stream)>>>(
+      src, rows, cols, lds, reinterpret_cast<__nv_bfloat16*>(hi), reinterpret_cast<__nv_bfloat16*>(lo), ldo);
+  SMX_LAUNCH_CHECK("smx_split_bf16");
+  return SMX_OK;
 }

@@ -16,6 +16,8 @@
 #include <algorithm>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 
 namespace {
@@ -761,6 +763,9 @@ extern "C" int smx_spectral_eval_batch(const smx_spectral* plans, int n_plans, c
 // with coalesced 128-byte stores.
 namespace {
 
+// BF16 = true: the hi/lo pair is written as BF16 (round to nearest even) for
+// the kind::f16 contraction.
+template <bool BF16>
 __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32_t* __restrict__ dims,
                                                          const int32_t* __restrict__ dmax,
                                                          const int32_t* __restrict__ dsoff, int n_slots,
@@ -768,8 +773,8 @@ __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32
                                                          const float* __restrict__ fam_a,
                                                          const float* __restrict__ fam_b,
                                                          const int32_t* __restrict__ fam, const double* __restrict__ x,
-                                                         int64_t P, int64_t ldx, float* __restrict__ Ahi,
-                                                         float* __restrict__ Alo, int64_t lda,
+                                                         int64_t P, int64_t ldx, void* __restrict__ Ahi,
+                                                         void* __restrict__ Alo, int64_t lda,
                                                          float* __restrict__ grow) {
   extern __shared__ __align__(16) float sm[];
   // basis row: shared memory [n_slots][128], or (large plans) global scratch
@@ -828,16 +833,22 @@ __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32
       for (int r = tid >> 5; r < 128; r += 4) {
         if (p0 + r >= P) break;
         const float v = tile[c * 129 + r];
-        uint32_t h;
-        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
-        const float hf = __uint_as_float(h);
-        uint32_t l;
-        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(v - hf));
         // reversed column order: descendants (small coefficients) precede their
         // ancestors, so the tensor-memory accumulator grows from small to large
         const int col = K - 1 - (jb + c);
-        Ahi[(p0 + r) * lda + col] = hf;
-        Alo[(p0 + r) * lda + col] = __uint_as_float(l);
+        if constexpr (BF16) {
+          const __nv_bfloat16 h = __float2bfloat16_rn(v);
+          static_cast<__nv_bfloat16*>(Ahi)[(p0 + r) * lda + col] = h;
+          static_cast<__nv_bfloat16*>(Alo)[(p0 + r) * lda + col] = __float2bfloat16_rn(v - __bfloat162float(h));
+        } else {
+          uint32_t h;
+          asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+          const float hf = __uint_as_float(h);
+          uint32_t l;
+          asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(v - hf));
+          static_cast<float*>(Ahi)[(p0 + r) * lda + col] = hf;
+          static_cast<float*>(Alo)[(p0 + r) * lda + col] = __uint_as_float(l);
+        }
       }
     }
     __syncthreads();
@@ -857,30 +868,49 @@ extern "C" size_t smx_spectral_panel_workspace(int n_slots, int64_t P) {
   return size_t(n_slots) * size_t((P + 127) / 128 * 128) * sizeof(float);
 }
 
-extern "C" int smx_spectral_panel_tf32(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff,
-                                       int n_slots, const int32_t* tape, int K, const float* fam_a,
-                                       const float* fam_b, const int32_t* fam, const double* x, int64_t P, int64_t ldx,
-                                       float* A_hi, float* A_lo, int64_t lda, void* ws, size_t ws_bytes,
-                                       void* stream) {
-  SMX_REQUIRE(n_dims >= 0 && n_slots >= 0 && K >= 0 && P >= 0 && lda >= K, "smx_spectral_panel_tf32: bad sizes");
+namespace {
+template <bool BF16>
+int panel_launch(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff, int n_slots,
+                 const int32_t* tape, int K, const float* fam_a, const float* fam_b, const int32_t* fam,
+                 const double* x, int64_t P, int64_t ldx, void* A_hi, void* A_lo, int64_t lda, void* ws,
+                 size_t ws_bytes, void* stream, const char* what) {
+  SMX_REQUIRE(n_dims >= 0 && n_slots >= 0 && K >= 0 && P >= 0 && lda >= K, what);
   if (P == 0 || K == 0) return SMX_OK;
-  SMX_REQUIRE(dims && dmax && dsoff && tape && fam_a && fam_b && fam && x && A_hi && A_lo,
-              "smx_spectral_panel_tf32: null pointer");
+  SMX_REQUIRE(dims && dmax && dsoff && tape && fam_a && fam_b && fam && x && A_hi && A_lo, what);
   const size_t need = smx_spectral_panel_workspace(n_slots, P);
-  SMX_REQUIRE(ws_bytes >= need && (need == 0 || ws), "smx_spectral_panel_tf32: workspace too small");
+  SMX_REQUIRE(ws_bytes >= need && (need == 0 || ws), what);
   float* grow = need ? static_cast<float*>(ws) : nullptr;
   const size_t smem = grow ? size_t(32 * 129) * sizeof(float) : (size_t(n_slots) * 128 + 32 * 129) * sizeof(float);
   int rc = upload_consts();
   if (rc) return rc;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(panel_tf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    cudaFuncSetAttribute(panel_tf32_kernel<BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     attr = true;
   }
-  panel_tf32_kernel<<<smx::grid_for(P, 128), 128, smem, smx::as_stream(stream)>>>(
+  panel_tf32_kernel<BF16><<<smx::grid_for(P, 128), 128, smem, smx::as_stream(stream)>>>(
       n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, A_hi, A_lo, lda, grow);
-  SMX_LAUNCH_CHECK("smx_spectral_panel_tf32");
+  SMX_LAUNCH_CHECK(what);
   return SMX_OK;
+}
+}  // namespace
+
+extern "C" int smx_spectral_panel_tf32(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff,
+                                       int n_slots, const int32_t* tape, int K, const float* fam_a,
+                                       const float* fam_b, const int32_t* fam, const double* x, int64_t P, int64_t ldx,
+                                       float* A_hi, float* A_lo, int64_t lda, void* ws, size_t ws_bytes,
+                                       void* stream) {
+  return panel_launch<false>(n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, A_hi, A_lo,
+                             lda, ws, ws_bytes, stream, "smx_spectral_panel_tf32");
+}
+
+extern "C" int smx_spectral_panel_bf16(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff,
+                                       int n_slots, const int32_t* tape, int K, const float* fam_a,
+                                       const float* fam_b, const int32_t* fam, const double* x, int64_t P, int64_t ldx,
+                                       uint16_t* A_hi, uint16_t* A_lo, int64_t lda, void* ws, size_t ws_bytes,
+                                       void* stream) {
+  return panel_launch<true>(n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, A_hi, A_lo,
+                            lda, ws, ws_bytes, stream, "smx_spectral_panel_bf16");
 }
 
 // --- backward ---------------------------------------------------------------------------------

@@ -387,11 +387,21 @@ class SmolyakBarycentricInterpolator:
     def __call__(self, x: ArrayLike, precision: str = None) -> torch.Tensor:
         """Evaluate the interpolant at points x, shape (n_points, d_in) or (d_in,) -> (n_points, d_out).
 
-        ``precision`` overrides the constructor's choice for this call."""
+        ``precision`` overrides the constructor's choice for this call; "bf16x3"
+        (plans with 16 or more outputs) runs the contraction with split-BF16
+        operands (error bound 1e-4 relative, FP32 results)."""
+        if precision not in (None, "fp64", "fp32", "bf16x3"):
+            raise ValueError("precision must be 'fp64', 'fp32' or 'bf16x3'")
         if (precision or self._precision) == "fp32" and self._host_rows(x) >= _OVERLAP_MIN_ROWS:
             return self._call_fp32_host(x)
         x = self._validate_input(x)
         Pn = int(x.shape[0])
+        if precision == "bf16x3":
+            sp = self.spectral_plan()
+            if sp.tc is None:
+                raise ValueError("precision='bf16x3' needs the tensor-core form (16 or more outputs)")
+            y16 = torch.empty(Pn, self._d_out, dtype=torch.float32, device=x.device)
+            return sp.evaluate(x, y16, mode="bf16x3") if Pn else y16
         if (precision or self._precision) == "fp32":
             sp = self.spectral_plan()
             y32 = torch.empty(Pn, self._d_out, dtype=torch.float32, device=x.device)

@@ -197,7 +197,7 @@ class SpectralPlan:
         Bh, Bl = torch.empty_like(Bd), torch.empty_like(Bd)
         call("smx_split_tf32", ptr(Bd), d_out, ldk, ldk, ptr(Bh), ptr(Bl), ldk, st)
         self.tc = dict(dims=T(dims, torch.int32), dmax=T(dmax, torch.int32), dsoff=T(dsoff, torch.int32),
-                       n_slots=n_slots, tape=T(tape, torch.int32), K=K, ldk=ldk, Bh=Bh, Bl=Bl,
+                       n_slots=n_slots, tape=T(tape, torch.int32), K=K, ldk=ldk, Bh=Bh, Bl=Bl, Bd=Bd,
                        bias=self.keep["c0"], err=torch.zeros(1, dtype=torch.int32, device=dev),
                        ent=torch.as_tensor(ent, device=dev))
 
@@ -328,9 +328,15 @@ class SpectralPlan:
              ptr(dC.contiguous()), ptr(Fbar), st)
         return Fbar[:R]
 
-    def evaluate(self, x, y):
-        """y[P, d_out] (FP32) at x[P, d_in] (FP64, contiguous, on the device)."""
+    def evaluate(self, x, y, mode="tf32x3"):
+        """y[P, d_out] (FP32) at x[P, d_in] (FP64, contiguous, on the device).
+        ``mode="bf16x3"`` runs the tensor-core contraction with split-BF16
+        operands (plans with the tensor-core form only)."""
         st = capi.stream_ptr(torch.cuda.current_stream())
+        if mode == "bf16x3":
+            if self.tc is None:
+                raise ValueError("bf16x3 needs the tensor-core form of the plan (16 or more outputs)")
+            return self._evaluate_tc(x, y, st, bf16=True)
         if self.tc is not None:
             return self._evaluate_tc(x, y, st)
         if self.blocked is not None:
@@ -353,13 +359,47 @@ class SpectralPlan:
         """Number of panel chunks (each one panel and one GEMM launch) for P points."""
         return -(-int(P) // self._tc_step(P)) if P else 0
 
-    def _evaluate_tc(self, x, y, st):
-        """Tensor-core path: basis-product panel (TF32 hi/lo) in chunks of points,
-        each contracted with the coefficient matrix by the tcgen05 kernel."""
+    def _bf16_operands(self):
+        """Coefficient matrix B split to BF16 hi/lo, rows padded to 8 entries."""
+        tc = self.tc
+        if "Bh16" not in tc:
+            d_out = int(tc["Bd"].shape[0])
+            ld16 = (tc["K"] + 7) // 8 * 8
+            Bd = torch.zeros(d_out, ld16, dtype=torch.float32, device=tc["Bd"].device)
+            Bd[:, : tc["ldk"]] = tc["Bd"]
+            Bh, Bl = torch.empty(d_out, ld16, dtype=torch.bfloat16, device=Bd.device), torch.empty(
+                d_out, ld16, dtype=torch.bfloat16, device=Bd.device)
+            call("smx_split_bf16", ptr(Bd), d_out, ld16, ld16, ptr(Bh), ptr(Bl), ld16,
+                 capi.stream_ptr(torch.cuda.current_stream()))
+            tc.update(Bh16=Bh, Bl16=Bl, ld16=ld16)
+        return tc["Bh16"], tc["Bl16"], tc["ld16"]
+
+    def _evaluate_tc(self, x, y, st, bf16=False):
+        """Tensor-core path: basis-product panel (TF32 or BF16 hi/lo) in chunks
+        of points, each contracted with the coefficient matrix by the tcgen05
+        kernel."""
         tc = self.tc
         k = self.keep
         P, d = int(x.shape[0]), int(x.shape[1])
         d_out = int(y.shape[1])
+        if bf16:
+            Bh, Bl, ld16 = self._bf16_operands()
+            step = self._tc_step(P)
+            Ah = torch.empty(step, ld16, dtype=torch.bfloat16, device=x.device)
+            Al = torch.empty_like(Ah)
+            if ld16 > tc["K"]:
+                Ah[:, tc["K"]:] = 0
+                Al[:, tc["K"]:] = 0
+            for p0 in range(0, P, step):
+                p1 = min(P, p0 + step)
+                nws = capi.size("smx_spectral_panel_workspace", tc["n_slots"], p1 - p0)
+                ws = torch.empty(max(nws, 1), dtype=torch.uint8, device=x.device)
+                call("smx_spectral_panel_bf16", int(tc["dims"].numel()), ptr(tc["dims"]), ptr(tc["dmax"]),
+                     ptr(tc["dsoff"]), tc["n_slots"], ptr(tc["tape"]), tc["K"], ptr(k["fam_a"]), ptr(k["fam_b"]),
+                     ptr(k["fam"]), ptr(x[p0:p1]), p1 - p0, d, ptr(Ah), ptr(Al), ld16, ptr(ws), nws, st)
+                call("smx_gemm_bf16x3", ptr(Ah), ptr(Al), ld16, ptr(Bh), ptr(Bl), ld16, p1 - p0, d_out, tc["K"],
+                     ptr(y[p0:p1]), d_out, ptr(tc["bias"]), 0, ptr(tc["err"]), st)
+            return y
         ldk = tc["ldk"]
         step = self._tc_step(P)
         Ah = torch.empty(step, ldk, dtype=torch.float32, device=x.device)

@@ -51,3 +51,62 @@ def test_gemm_tf32x3(M, N, K):
     err = np.max(np.abs(D - ref)) / np.max(np.abs(ref))
     print("M=%d N=%d K=%d norm-wise rel err %.2e" % (M, N, K, err))
     assert err < 1e-8 * K + 2e-6
+
+
+def _gemm_bf16(A, B, bias=None):
+    import torch
+
+    from smolyax_gb300 import _capi
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    M, K = A.shape
+    N = B.shape[0]
+    ld = (K + 7) // 8 * 8  # BF16 rows: 16-byte pitch for the tensor maps
+    st = _capi.stream_ptr(torch.cuda.current_stream())
+
+    def split(X):
+        Xd = torch.zeros(X.shape[0], ld, dtype=torch.float32, device=dev)
+        Xd[:, :K] = torch.as_tensor(X, dtype=torch.float32)
+        hi = torch.zeros(X.shape[0], ld, dtype=torch.bfloat16, device=dev)
+        lo = torch.zeros_like(hi)
+        _capi.call("smx_split_bf16", _capi.ptr(Xd), X.shape[0], ld, ld, _capi.ptr(hi), _capi.ptr(lo), ld, st)
+        return Xd, hi, lo
+
+    Ad, Ah, Al = split(A)
+    Bd, Bh, Bl = split(B)
+    # the split is hi = round-to-nearest BF16 of x, lo = BF16 of the remainder
+    assert torch.equal(Ah, Ad.to(torch.bfloat16))
+    assert torch.equal(Al, (Ad - Ah.float()).to(torch.bfloat16))
+    D = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    b = None if bias is None else torch.as_tensor(bias, dtype=torch.float32, device=dev)
+    _capi.call("smx_gemm_bf16x3", _capi.ptr(Ah), _capi.ptr(Al), ld, _capi.ptr(Bh), _capi.ptr(Bl), ld, M, N, K,
+               _capi.ptr(D), N, _capi.ptr(b), 0, _capi.ptr(err), st)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    # the three products the kernel forms, in FP64: hi.hi + hi.lo + lo.hi
+    h = lambda t: t.double().cpu().numpy()  # noqa: E731
+    ref3 = (h(Ah) @ h(Bh).T + h(Ah) @ h(Bl).T + h(Al) @ h(Bh).T)[:, :N]
+    if bias is not None:
+        ref3 = ref3 + bias
+    return D.cpu().numpy().astype(np.float64), ref3
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (300, 200, 100), (256, 256, 1000), (1000, 64, 5000), (77, 520, 41)])
+def test_gemm_bf16x3(M, N, K):
+    """Split-BF16 contraction: three BF16 products accumulated in FP32 in tensor
+    memory.  Against the FP64 product of the FP32 operands the error is that of
+    the 16-bit split (lo.lo dropped, lo rounded): norm-wise bound 1e-4; against
+    the FP64 value of the same three products it is FP32 accumulation only."""
+    rng = np.random.default_rng(M + N + K)
+    A = rng.normal(size=(M, K)).astype(np.float32)
+    B = rng.normal(size=(N, K)).astype(np.float32)
+    bias = rng.normal(size=N).astype(np.float32)
+    D, ref3 = _gemm_bf16(A, B, bias)
+    ref = A.astype(np.float64) @ B.astype(np.float64).T + bias
+    scale = np.max(np.abs(ref))
+    err = np.max(np.abs(D - ref)) / scale
+    err3 = np.max(np.abs(D - ref3)) / scale
+    print("M=%d N=%d K=%d bf16x3 norm-wise rel err %.2e (vs its own three products %.2e)" % (M, N, K, err, err3))
+    assert err3 < 1e-8 * K + 2e-6
+    assert err < 1e-4

@@ -123,6 +123,36 @@ def test_tensor_core_path_gauss_hermite(t, d_out):
 
 
 
+def test_bf16x3_contraction_gauss_hermite():
+    """precision="bf16x3": panel and coefficients split to BF16 hi/lo, three
+    BF16 products per entry accumulated in FP32.  Stated accuracy: 1e-4 per-point
+    norm-wise (the split keeps ~16 bits); the TF32 split (22 bits) is the
+    default FP32 form."""
+    from smolyax_gb300 import nodes
+
+    d, d_out = 100, 32
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    ip = _interp(node_gen=nodes.GaussHermite(dim=d), k=k, t=7.723434, d_out=d_out,
+                 f=fns.exponential(d, d_out, seed=0))
+    x = np.random.default_rng(3).normal(size=(1000, d))
+    assert ip.spectral_plan().tc is not None
+    y64 = ip(x).cpu().numpy()
+    y16 = ip(x, precision="bf16x3").cpu().numpy().astype(float)
+    err = float(np.max(np.max(np.abs(y16 - y64), axis=1) / np.max(np.abs(y64), axis=1)))
+    print("GH d_out=%d: bf16x3 per-point norm-wise error vs FP64 %.3e" % (d_out, err))
+    assert err < 1e-4
+
+
+def test_bf16x3_needs_tensor_core_form():
+    from smolyax_gb300 import nodes
+
+    d = 10
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    ip = _interp(node_gen=nodes.Leja(dim=d), k=k, t=5.0, d_out=1, f=fns.rational(d, seed=0))
+    with pytest.raises(ValueError):
+        ip(np.zeros((4, d)), precision="bf16x3")
+
+
 @pytest.mark.parametrize("d_out", [1, 3])
 def test_host_input_overlap_equals_device_input(d_out):
     """Large host inputs are copied and evaluated in overlapped chunks: same
