@@ -296,9 +296,14 @@ typedef struct smx_blocked {
   const float* fa;    /* [d_in] affine map z = fa x + fb of every dimension */
   const float* fb;
   const int32_t* fam; /* [d_in] 0 Legendre, 1 Hermite                       */
+  int32_t n_ent;      /* int32 words of hot_ent (a multiple of 4)          */
+  int32_t n_w;        /* float4 rows of W                                  */
 } smx_blocked;
 
-/* Shared memory of one block: (n_hs + k_c) * 512 + 16384 bytes (<= 220 KiB). */
+/* Shared memory of one block's tile arrays: (n_hs + k_c) * 512 + 16384 bytes
+ * (<= 220 KiB).  When n_ent and n_w are given and the tables fit beside the
+ * tile arrays, smx_blocked_eval also keeps a copy of the tables (node, vc,
+ * hot_ent, grp, grp_ab, W, items, warp_off) in each block's shared memory. */
 size_t smx_blocked_smem(const smx_blocked* plan_host);
 /* y[P] (FP32) at x[P, ldx] (FP64); one persistent block per SM.  When the
  * tiles leave a partial last round, its tiles are shared by several blocks
@@ -321,8 +326,8 @@ int smx_spectral_panel_tf32(int n_dims, const int32_t* dims, const int32_t* dmax
                             const int32_t* tape, int K, const float* fam_a, const float* fam_b, const int32_t* fam,
                             const double* x, int64_t P, int64_t ldx, float* A_hi, float* A_lo, int64_t lda, void* ws,
                             size_t ws_bytes, void* stream);
-/* Same panel as TF32 hi/lo pairs rounded to BF16 (bit patterns, 2 bytes each)
- * for smx_gemm_bf16x3. */
+/* Same panel as BF16 hi/lo pairs (hi = BF16 rounded to nearest, lo = BF16 of
+ * the remainder; bit patterns, 2 bytes each) for smx_gemm_bf16x3. */
 int smx_spectral_panel_bf16(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff, int n_slots,
                             const int32_t* tape, int K, const float* fam_a, const float* fam_b, const int32_t* fam,
                             const double* x, int64_t P, int64_t ldx, uint16_t* A_hi, uint16_t* A_lo, int64_t lda,

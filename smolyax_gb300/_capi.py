@@ -115,6 +115,8 @@ class SmxBlocked(C.Structure):
         ("fa", _p),
         ("fb", _p),
         ("fam", _p),
+        ("n_ent", _i32),
+        ("n_w", _i32),
     ]
 
 

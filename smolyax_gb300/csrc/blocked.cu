@@ -87,6 +87,16 @@ __device__ __forceinline__ double ld1_stream(const double* p) {
   return a;
 }
 
+// Table load: shared memory when the block holds its own copy of the tables
+// (TS), else a read-only global load.
+template <bool TS, typename T>
+__device__ __forceinline__ T tl(const T* p) {
+  if constexpr (TS)
+    return *p;
+  else
+    return __ldg(p);
+}
+
 __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   const float yv = v - c;
   const float t = s + yv;
@@ -151,7 +161,7 @@ __device__ __forceinline__ void load_x(const double* __restrict__ x, const int64
 // With split_S > 1 the block runs every split_S-th item (from split_c) of each
 // warp's list and leaves its per-point partial sums in part[split_c]; the last
 // of the split_S blocks of the tile (counted in *ctr) adds them in order.
-template <int NP>
+template <int NP, bool TS>
 __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __restrict__ x, int64_t P, int64_t ldx,
                                              float* __restrict__ y, int fastx, int64_t tile, float* sm,
                                              int split_c = 0, int split_S = 1, float* part = nullptr,
@@ -162,7 +172,7 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
   float* RC = RS + kW * kT;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int q0 = lane * 4;
-  const int it0 = a.warp_off[warp], it1 = a.warp_off[warp + 1];
+  const int it0 = tl<TS>(a.warp_off + warp), it1 = tl<TS>(a.warp_off + warp + 1);
   {
     const int64_t p0 = tile * (32 * NP);
     int64_t prow[NP];
@@ -204,7 +214,7 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
     // phase 1: prefix rows of the cold entries
     for (int i = threadIdx.x; i < a.k_c * kT; i += kThr) {
       const int k = i >> 7, q = i & (kT - 1);
-      const int4 h0 = __ldg(a.vc + 3 * k), pa = __ldg(a.vc + 3 * k + 1), pb = __ldg(a.vc + 3 * k + 2);
+      const int4 h0 = tl<TS>(a.vc + 3 * k), pa = tl<TS>(a.vc + 3 * k + 1), pb = tl<TS>(a.vc + 3 * k + 2);
       const int path[8] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w};
       float v = 1.f;
 #pragma unroll
@@ -221,17 +231,17 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
     // hot items come first in every warp's list, cold groups after them
     int it = it0 + split_c;
     for (; it < it1; it += split_S) {
-      const int code = __ldg(a.items + it);
+      const int code = tl<TS>(a.items + it);
       if (code & kColdBit) break;
         // hot node: gather over its hot entries, times the path product
-        const int4 h0 = __ldg(a.node + 3 * code), pa = __ldg(a.node + 3 * code + 1),
-                   pb = __ldg(a.node + 3 * code + 2);
+        const int4 h0 = tl<TS>(a.node + 3 * code), pa = tl<TS>(a.node + 3 * code + 1),
+                   pb = tl<TS>(a.node + 3 * code + 2);
         const int4* E = a.hot_ent + (h0.x >> 1);
         const int ne = h0.y >> 1;
         float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 4
         for (int e = 0; e < ne; ++e) {
-          const int4 ee = __ldg(E + e);
+          const int4 ee = tl<TS>(E + e);
           const float4 f0 = *reinterpret_cast<const float4*>(PH + ee.x + q0);
           const float4 f1 = *reinterpret_cast<const float4*>(PH + ee.z + q0);
           const float c0 = __int_as_float(ee.y), c1 = __int_as_float(ee.w);
@@ -254,15 +264,15 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
     // while group n is contracted; they are turned into basis values at the
     // start of the next iteration.
     if (it < it1) {
-      int g = __ldg(a.items + it) & (kColdBit - 1);
-      int4 gd = __ldg(a.grp + 3 * g), gdim = __ldg(a.grp + 3 * g + 1);
+      int g = tl<TS>(a.items + it) & (kColdBit - 1);
+      int4 gd = tl<TS>(a.grp + 3 * g), gdim = tl<TS>(a.grp + 3 * g + 1);
       double xv[NP][4];
       load_x<NP>(x, prow, fastx, gd, gdim, xv);
       for (; it < it1; it += split_S) {
         // basis values of this group from the x values that have arrived
         float ph[NP][4];
         {
-          const float4 A = __ldg(a.grp_ab + 2 * g), B = __ldg(a.grp_ab + 2 * g + 1);
+          const float4 A = tl<TS>(a.grp_ab + 2 * g), B = tl<TS>(a.grp_ab + 2 * g + 1);
           const float Aa[4] = {A.x, A.y, A.z, A.w}, Bb[4] = {B.x, B.y, B.z, B.w};
           if (gd.z) {
 #pragma unroll
@@ -270,7 +280,7 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
 #pragma unroll
               for (int j = 0; j < 4; ++j) ph[i][j] = fmaf(Aa[j], f64_to_f32(xv[i][j]), Bb[j]);
           } else {
-            const int4 gdeg = __ldg(a.grp + 3 * g + 2);
+            const int4 gdeg = tl<TS>(a.grp + 3 * g + 2);
             const int dd[4] = {gdim.x, gdim.y, gdim.z, gdim.w};
             const int gg[4] = {gdeg.x, gdeg.y, gdeg.z, gdeg.w};
 #pragma unroll
@@ -285,9 +295,9 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
         // next group: descriptors and x loads in flight during this contraction
         const int4 gdc = gd;
         if (it + split_S < it1) {
-          g = __ldg(a.items + it + split_S) & (kColdBit - 1);
-          gd = __ldg(a.grp + 3 * g);
-          gdim = __ldg(a.grp + 3 * g + 1);
+          g = tl<TS>(a.items + it + split_S) & (kColdBit - 1);
+          gd = tl<TS>(a.grp + 3 * g);
+          gdim = tl<TS>(a.grp + 3 * g + 1);
           load_x<NP>(x, prow, fastx, gd, gdim, xv);
         }
         // staircase block T[i][j] = sum_k Vc[k][i] W[k][j]
@@ -301,7 +311,7 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
 #pragma unroll 4
         for (int k = 0; k < gdc.x; ++k) {
           const float4 v = *reinterpret_cast<const float4*>(Vk + k * kT);
-          const float4 w = __ldg(Wg + k);
+          const float4 w = tl<TS>(Wg + k);
           const float vv[4] = {v.x, v.y, v.z, v.w};
           const float ww[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
@@ -362,21 +372,56 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
   }
 }
 
-template <int NP>
+// Byte offsets of the tables copied into shared memory (TS), after the tile
+// arrays; every table starts on a 16-byte boundary.
+struct TabOff {
+  int node, vc, hot_ent, grp, grp_ab, W, items, warp_off, end;
+  int n_ent16, n_w, n_items;  // 16-byte words of hot_ent, rows of W, work items
+};
+
+template <typename T>
+__device__ __forceinline__ const T* tab_copy(uint8_t* base, int off, const T* src, int n16) {
+  int4* d = reinterpret_cast<int4*>(base + off);
+  const int4* s = reinterpret_cast<const int4*>(src);
+  for (int i = threadIdx.x; i < n16; i += kThr) d[i] = __ldg(s + i);
+  return reinterpret_cast<const T*>(base + off);
+}
+
+template <int NP, bool TS>
 __global__ void __launch_bounds__(kThr, 1)
-    blocked_eval_kernel(BArgs a, const double* __restrict__ x, int64_t P, int64_t ldx, float* __restrict__ y,
-                        int fastx, float* __restrict__ part, unsigned int* __restrict__ ctr) {
+    blocked_eval_kernel(BArgs a, TabOff to, const double* __restrict__ x, int64_t P, int64_t ldx,
+                        float* __restrict__ y, int fastx, float* __restrict__ part, unsigned int* __restrict__ ctr) {
   extern __shared__ __align__(16) float sm[];
+  if constexpr (TS) {
+    // the block's own copy of the warp-uniform tables, read once
+    uint8_t* tb = reinterpret_cast<uint8_t*>(sm + (size_t(a.n_hs) + a.k_c + 2 * kW) * kT);
+    // node, vc and grp rows are 48 bytes, grp_ab rows 32: their spans are exact
+    a.node = tab_copy(tb, to.node, a.node, (to.vc - to.node) / 16);
+    a.vc = tab_copy(tb, to.vc, a.vc, (to.hot_ent - to.vc) / 16);
+    a.hot_ent = tab_copy(tb, to.hot_ent, a.hot_ent, to.n_ent16);
+    a.grp = tab_copy(tb, to.grp, a.grp, (to.grp_ab - to.grp) / 16);
+    a.grp_ab = tab_copy(tb, to.grp_ab, a.grp_ab, (to.W - to.grp_ab) / 16);
+    a.W = tab_copy(tb, to.W, a.W, to.n_w);
+    {
+      int32_t* d = reinterpret_cast<int32_t*>(tb + to.items);
+      for (int i = threadIdx.x; i < to.n_items; i += kThr) d[i] = __ldg(a.items + i);
+      a.items = d;
+      int32_t* w = reinterpret_cast<int32_t*>(tb + to.warp_off);
+      if (threadIdx.x <= kW) w[threadIdx.x] = __ldg(a.warp_off + threadIdx.x);
+      a.warp_off = w;
+    }
+    __syncthreads();
+  }
   const int64_t n_tiles = (P + 32 * NP - 1) / (32 * NP);
   const int64_t G = gridDim.x, rounds = n_tiles / G, rem = n_tiles - rounds * G;
-  for (int64_t r = 0; r < rounds; ++r) blocked_tile<NP>(a, x, P, ldx, y, fastx, blockIdx.x + r * G, sm);
+  for (int64_t r = 0; r < rounds; ++r) blocked_tile<NP, TS>(a, x, P, ldx, y, fastx, blockIdx.x + r * G, sm);
   if (rem == 0) return;
   // last round: each remaining tile is shared by S blocks (S = 1 without a full round before it)
   const int S = rounds > 0 && part != nullptr ? int(G / rem < kMaxSplit ? G / rem : kMaxSplit) : 1;
   const int64_t t = blockIdx.x / S;
   if (t >= rem) return;
   const int c = int(blockIdx.x - t * S);
-  blocked_tile<NP>(a, x, P, ldx, y, fastx, rounds * G + t, sm, c, S, part + t * (2 * kMaxSplit * kT), ctr + t);
+  blocked_tile<NP, TS>(a, x, P, ldx, y, fastx, rounds * G + t, sm, c, S, part + t * (2 * kMaxSplit * kT), ctr + t);
 }
 
 struct BWork {
@@ -405,7 +450,7 @@ __global__ void __launch_bounds__(kThr, 1)
       if (items[mid].tile0 <= t) lo = mid; else hi = mid - 1;
     }
     const BWork it = items[lo];
-    blocked_tile<4>(plans[it.plan], it.x, it.P, it.ldx, it.y, it.fastx, t - it.tile0, sm);
+    blocked_tile<4, false>(plans[it.plan], it.x, it.P, it.ldx, it.y, it.fastx, t - it.tile0, sm);
   }
 }
 
@@ -428,8 +473,10 @@ int prepare(int* sms) {
       }
     if (cudaMemcpyToSymbol(b_alpha, al, sizeof(al)) != cudaSuccess ||
         cudaMemcpyToSymbol(b_beta, be, sizeof(be)) != cudaSuccess ||
-        cudaFuncSetAttribute(blocked_eval_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) !=
-            cudaSuccess ||
+        cudaFuncSetAttribute(blocked_eval_kernel<4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             220 * 1024) != cudaSuccess ||
+        cudaFuncSetAttribute(blocked_eval_kernel<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             220 * 1024) != cudaSuccess ||
         cudaFuncSetAttribute(blocked_eval_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) !=
             cudaSuccess ||
         cudaDeviceGetAttribute(&g_sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
@@ -442,6 +489,33 @@ int prepare(int* sms) {
 
 size_t smem_of(const smx_blocked* b) {
   return (size_t(b->n_hs) + size_t(b->k_c)) * kT * sizeof(float) + 2 * size_t(kW) * kT * sizeof(float);
+}
+
+// Layout of the tables in shared memory (after the tile arrays); end = bytes.
+TabOff tab_offsets(const smx_blocked* b) {
+  auto up = [](int64_t v) { return int((v + 15) / 16 * 16); };
+  TabOff t;
+  t.node = 0;
+  t.vc = t.node + up(int64_t(b->n_nodes) * 48);
+  t.hot_ent = t.vc + up(int64_t(b->k_c) * 48);
+  t.grp = t.hot_ent + up(int64_t(b->n_ent) * 4);
+  t.grp_ab = t.grp + up(int64_t(b->n_groups) * 48);
+  t.W = t.grp_ab + up(int64_t(b->n_groups) * 32);
+  t.items = t.W + up(int64_t(b->n_w) * 16);
+  t.warp_off = t.items + up(int64_t(b->n_items) * 4);
+  t.end = t.warp_off + up(int64_t(kW + 1) * 4);
+  t.n_ent16 = b->n_ent / 4;
+  t.n_w = b->n_w;
+  t.n_items = b->n_items;
+  return t;
+}
+
+// The tables' sizes are given and they fit beside the tile arrays.
+bool tables_in_smem(const smx_blocked* b) {
+  if (b->n_ent <= 0 || b->n_w <= 0 || b->n_ent % 4 || !b->node || !b->hot_ent || !b->grp || !b->grp_ab || !b->W ||
+      (b->k_c > 0 && !b->vc))
+    return false;
+  return smem_of(b) + size_t(tab_offsets(b).end) <= 220 * 1024;
 }
 
 int check_plan(const smx_blocked* b, const char* what) {
@@ -520,8 +594,14 @@ extern "C" int smx_blocked_eval(const smx_blocked* b, const double* x, int64_t P
     if (cudaMemsetAsync(ctr, 0, size_t(sms) * sizeof(unsigned int), smx::as_stream(stream)) != cudaSuccess)
       return smx::set_error(SMX_ERR_CUDA, "smx_blocked_eval: counter reset failed");
   }
-  blocked_eval_kernel<4><<<grid, kThr, smem_of(b), smx::as_stream(stream)>>>(to_args(b), x, P, ldx, y,
-                                                                           fast_x(x, ldx), part, ctr);
+  if (tables_in_smem(b)) {
+    const TabOff to = tab_offsets(b);
+    blocked_eval_kernel<4, true><<<grid, kThr, smem_of(b) + to.end, smx::as_stream(stream)>>>(
+        to_args(b), to, x, P, ldx, y, fast_x(x, ldx), part, ctr);
+  } else {
+    blocked_eval_kernel<4, false><<<grid, kThr, smem_of(b), smx::as_stream(stream)>>>(
+        to_args(b), TabOff{}, x, P, ldx, y, fast_x(x, ldx), part, ctr);
+  }
   SMX_LAUNCH_CHECK("smx_blocked_eval");
   return SMX_OK;
 }

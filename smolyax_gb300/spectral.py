@@ -221,6 +221,8 @@ class SpectralPlan:
         for name, t in kb.items():
             setattr(b, name, t.data_ptr() if t.numel() else None)
         b.fa, b.fb, b.fam = (self.keep[k].data_ptr() for k in ("fam_a", "fam_b", "fam"))
+        b.n_ent = int(np.asarray(lay["hot_ent"]).size)
+        b.n_w = int(np.asarray(lay["W"]).size) // 4
         self.blocked = b
         self.blocked_keep = kb
         self.blocked_layout = lay
