@@ -55,6 +55,8 @@ struct BArgs {
   const float* fa;
   const float* fb;
   const int32_t* fam;
+  const int4* hd;     // per hot dimension {dim, degree, slot offset, family} (shared-memory tables only)
+  const float2* hab;  // per hot dimension affine map {a, b}                  (shared-memory tables only)
 };
 
 // FP64 -> FP32 with integer operations (truncation of the mantissa; |v| below
@@ -118,20 +120,25 @@ __device__ __forceinline__ float phi_rec(int fm, float z, int g) {
 // point l + 32 i (lane l) at position 4 l + i.
 __device__ __forceinline__ int quad_point(int q) { return 32 * (q & 3) + (q >> 2); }
 
-__device__ __forceinline__ float4 path_value(const float* __restrict__ PH, int4 h0, int4 pa, int4 pb, int q0) {
-  float4 v = make_float4(1.f, 1.f, 1.f, 1.f);
+// Packed FP32 pairs (two lanes of one FFMA2/FMUL2 instruction); each element
+// is rounded as the scalar operation would be.
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+
+// Product of the path's basis values for the lane's 4 points, as pairs (0,1), (2,3).
+__device__ __forceinline__ void path_value(const float* __restrict__ PH, int4 h0, int4 pa, int4 pb, int q0,
+                                           float2& v01, float2& v23) {
+  v01 = v23 = make_float2(1.f, 1.f);
   const int path[8] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w};
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     if (q < h0.z) {
       const float4 f = *reinterpret_cast<const float4*>(PH + path[q] + q0);
-      v.x *= f.x;
-      v.y *= f.y;
-      v.z *= f.z;
-      v.w *= f.w;
+      v01 = __fmul2_rn(v01, lo2(f));
+      v23 = __fmul2_rn(v23, hi2(f));
     }
   }
-  return v;
 }
 
 // x values of a cold group's 4 dimensions for the lane's NP points.
@@ -166,6 +173,7 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
                                              float* __restrict__ y, int fastx, int64_t tile, float* sm,
                                              int split_c = 0, int split_S = 1, float* part = nullptr,
                                              unsigned int* ctr = nullptr) {
+  static_assert(NP == 4, "points are processed as two pairs per lane");
   float* PH = sm;
   float* VC = sm + size_t(a.n_hs) * kT;
   float* RS = VC + size_t(a.k_c) * kT;
@@ -190,15 +198,24 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
 #pragma unroll
         for (int r = 0; r < kHotPass; ++r) {
           const int h = h0 + hb + kHB * r;
-          xh[r] = h < a.n_hot_dims ? __ldg(xp + __ldg(a.hot_dim + h)) : 0.0;
+          xh[r] = h < a.n_hot_dims ? __ldg(xp + (TS ? a.hd[h].x : __ldg(a.hot_dim + h))) : 0.0;
         }
 #pragma unroll
         for (int r = 0; r < kHotPass; ++r) {
           const int h = h0 + hb + kHB * r;
           if (h >= a.n_hot_dims) break;
-          const int dim = __ldg(a.hot_dim + h), g = __ldg(a.hot_deg + h), so = __ldg(a.hot_soff + h);
-          const int fm = __ldg(a.fam + dim);
-          const float z = fmaf(__ldg(a.fa + dim), f64_to_f32(xh[r]), __ldg(a.fb + dim));
+          int g, so, fm;
+          float fa, fb;
+          if constexpr (TS) {
+            const int4 d4 = a.hd[h];
+            const float2 ab = a.hab[h];
+            g = d4.y, so = d4.z, fm = d4.w, fa = ab.x, fb = ab.y;
+          } else {
+            const int dim = __ldg(a.hot_dim + h);
+            g = __ldg(a.hot_deg + h), so = __ldg(a.hot_soff + h), fm = __ldg(a.fam + dim);
+            fa = __ldg(a.fa + dim), fb = __ldg(a.fb + dim);
+          }
+          const float z = fmaf(fa, f64_to_f32(xh[r]), fb);
           float pm1 = 0.f, pc = 1.f;
           for (int n = 0; n < g; ++n) {
             const float pn = b_alpha[fm][n] * z * pc - b_beta[fm][n] * pm1;
@@ -238,24 +255,22 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
                    pb = tl<TS>(a.node + 3 * code + 2);
         const int4* E = a.hot_ent + (h0.x >> 1);
         const int ne = h0.y >> 1;
-        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 a01 = make_float2(0.f, 0.f), a23 = a01;
 #pragma unroll 4
         for (int e = 0; e < ne; ++e) {
           const int4 ee = tl<TS>(E + e);
           const float4 f0 = *reinterpret_cast<const float4*>(PH + ee.x + q0);
           const float4 f1 = *reinterpret_cast<const float4*>(PH + ee.z + q0);
-          const float c0 = __int_as_float(ee.y), c1 = __int_as_float(ee.w);
-          acc.x = fmaf(c0, f0.x, acc.x);
-          acc.y = fmaf(c0, f0.y, acc.y);
-          acc.z = fmaf(c0, f0.z, acc.z);
-          acc.w = fmaf(c0, f0.w, acc.w);
-          acc.x = fmaf(c1, f1.x, acc.x);
-          acc.y = fmaf(c1, f1.y, acc.y);
-          acc.z = fmaf(c1, f1.z, acc.z);
-          acc.w = fmaf(c1, f1.w, acc.w);
+          const float2 c0 = dup2(__int_as_float(ee.y)), c1 = dup2(__int_as_float(ee.w));
+          a01 = __ffma2_rn(c0, lo2(f0), a01);
+          a23 = __ffma2_rn(c0, hi2(f0), a23);
+          a01 = __ffma2_rn(c1, lo2(f1), a01);
+          a23 = __ffma2_rn(c1, hi2(f1), a23);
         }
-        const float4 v = path_value(PH, h0, pa, pb, q0);
-        const float va[4] = {v.x * acc.x, v.y * acc.y, v.z * acc.z, v.w * acc.w};
+        float2 v01, v23;
+        path_value(PH, h0, pa, pb, q0, v01, v23);
+        const float2 p01 = __fmul2_rn(v01, a01), p23 = __fmul2_rn(v23, a23);
+        const float va[4] = {p01.x, p01.y, p23.x, p23.y};
 #pragma unroll
         for (int i = 0; i < NP; ++i) kahan_add(ys[i], yc[i], va[i]);
     }
@@ -270,16 +285,20 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
       load_x<NP>(x, prow, fastx, gd, gdim, xv);
       for (; it < it1; it += split_S) {
         // basis values of this group from the x values that have arrived
-        float ph[NP][4];
+        // (ph2[h][j]: slot j of points 2h, 2h + 1)
+        float2 ph2[2][4];
         {
           const float4 A = tl<TS>(a.grp_ab + 2 * g), B = tl<TS>(a.grp_ab + 2 * g + 1);
           const float Aa[4] = {A.x, A.y, A.z, A.w}, Bb[4] = {B.x, B.y, B.z, B.w};
           if (gd.z) {
 #pragma unroll
-            for (int i = 0; i < NP; ++i)
+            for (int h = 0; h < 2; ++h)
 #pragma unroll
-              for (int j = 0; j < 4; ++j) ph[i][j] = fmaf(Aa[j], f64_to_f32(xv[i][j]), Bb[j]);
+              for (int j = 0; j < 4; ++j)
+                ph2[h][j] = __ffma2_rn(dup2(Aa[j]), make_float2(f64_to_f32(xv[2 * h][j]), f64_to_f32(xv[2 * h + 1][j])),
+                                       dup2(Bb[j]));
           } else {
+            float ph[NP][4];
             const int4 gdeg = tl<TS>(a.grp + 3 * g + 2);
             const int dd[4] = {gdim.x, gdim.y, gdim.z, gdim.w};
             const int gg[4] = {gdeg.x, gdeg.y, gdeg.z, gdeg.w};
@@ -290,6 +309,10 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
               for (int i = 0; i < NP; ++i)
                 ph[i][j] = gg[j] ? phi_rec(fm, fmaf(Aa[j], f64_to_f32(xv[i][j]), Bb[j]), gg[j]) : 0.f;
             }
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+#pragma unroll
+              for (int j = 0; j < 4; ++j) ph2[h][j] = make_float2(ph[2 * h][j], ph[2 * h + 1][j]);
           }
         }
         // next group: descriptors and x loads in flight during this contraction
@@ -300,31 +323,33 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
           gdim = tl<TS>(a.grp + 3 * g + 1);
           load_x<NP>(x, prow, fastx, gd, gdim, xv);
         }
-        // staircase block T[i][j] = sum_k Vc[k][i] W[k][j]
-        float T[NP][4];
+        // staircase block T[i][j] = sum_k Vc[k][i] W[k][j], as pairs of points
+        // (T2[h][j] = T[2h][j], T[2h + 1][j])
+        float2 T2[2][4];
 #pragma unroll
-        for (int i = 0; i < NP; ++i)
+        for (int h = 0; h < 2; ++h)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) T[i][j] = 0.f;
+          for (int j = 0; j < 4; ++j) T2[h][j] = make_float2(0.f, 0.f);
         const float4* Wg = a.W + (gdc.y >> 2);
         const float* Vk = VC + q0;
 #pragma unroll 4
         for (int k = 0; k < gdc.x; ++k) {
           const float4 v = *reinterpret_cast<const float4*>(Vk + k * kT);
           const float4 w = tl<TS>(Wg + k);
-          const float vv[4] = {v.x, v.y, v.z, v.w};
           const float ww[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
-          for (int i = 0; i < NP; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) T[i][j] = fmaf(vv[i], ww[j], T[i][j]);
+          for (int j = 0; j < 4; ++j) {
+            T2[0][j] = __ffma2_rn(lo2(v), dup2(ww[j]), T2[0][j]);
+            T2[1][j] = __ffma2_rn(hi2(v), dup2(ww[j]), T2[1][j]);
+          }
         }
 #pragma unroll
-        for (int i = 0; i < NP; ++i) {
-          float sacc = 0.f;
+        for (int h = 0; h < 2; ++h) {
+          float2 sacc = make_float2(0.f, 0.f);
 #pragma unroll
-          for (int j = 0; j < 4; ++j) sacc = fmaf(T[i][j], ph[i][j], sacc);
-          kahan_add(ys[i], yc[i], sacc);
+          for (int j = 0; j < 4; ++j) sacc = __ffma2_rn(T2[h][j], ph2[h][j], sacc);
+          kahan_add(ys[2 * h], yc[2 * h], sacc.x);
+          kahan_add(ys[2 * h + 1], yc[2 * h + 1], sacc.y);
         }
       }
     }
@@ -375,7 +400,7 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
 // Byte offsets of the tables copied into shared memory (TS), after the tile
 // arrays; every table starts on a 16-byte boundary.
 struct TabOff {
-  int node, vc, hot_ent, grp, grp_ab, W, items, warp_off, end;
+  int node, vc, hot_ent, grp, grp_ab, W, items, warp_off, hd, hab, end;
   int n_ent16, n_w, n_items;  // 16-byte words of hot_ent, rows of W, work items
 };
 
@@ -409,6 +434,15 @@ __global__ void __launch_bounds__(kThr, 1)
       int32_t* w = reinterpret_cast<int32_t*>(tb + to.warp_off);
       if (threadIdx.x <= kW) w[threadIdx.x] = __ldg(a.warp_off + threadIdx.x);
       a.warp_off = w;
+      int4* hd = reinterpret_cast<int4*>(tb + to.hd);
+      float2* hab = reinterpret_cast<float2*>(tb + to.hab);
+      for (int h = threadIdx.x; h < a.n_hot_dims; h += kThr) {
+        const int dim = __ldg(a.hot_dim + h);
+        hd[h] = make_int4(dim, __ldg(a.hot_deg + h), __ldg(a.hot_soff + h), __ldg(a.fam + dim));
+        hab[h] = make_float2(__ldg(a.fa + dim), __ldg(a.fb + dim));
+      }
+      a.hd = hd;
+      a.hab = hab;
     }
     __syncthreads();
   }
@@ -503,7 +537,9 @@ TabOff tab_offsets(const smx_blocked* b) {
   t.W = t.grp_ab + up(int64_t(b->n_groups) * 32);
   t.items = t.W + up(int64_t(b->n_w) * 16);
   t.warp_off = t.items + up(int64_t(b->n_items) * 4);
-  t.end = t.warp_off + up(int64_t(kW + 1) * 4);
+  t.hd = t.warp_off + up(int64_t(kW + 1) * 4);
+  t.hab = t.hd + up(int64_t(b->n_hot_dims) * 16);
+  t.end = t.hab + up(int64_t(b->n_hot_dims) * 8);
   t.n_ent16 = b->n_ent / 4;
   t.n_w = b->n_w;
   t.n_items = b->n_items;
@@ -549,6 +585,8 @@ BArgs to_args(const smx_blocked* b) {
   a.fa = b->fa;
   a.fb = b->fb;
   a.fam = b->fam;
+  a.hd = nullptr;
+  a.hab = nullptr;
   return a;
 }
 
