@@ -168,9 +168,15 @@ __device__ __forceinline__ void load_x(const double* __restrict__ x, const int64
 // With split_S > 1 the block runs every split_S-th item (from split_c) of each
 // warp's list and leaves its per-point partial sums in part[split_c]; the last
 // of the split_S blocks of the tile (counted in *ctr) adds them in order.
+//
+// Hot-dimension x values of the first phase-0 pass travel between tiles: once
+// a warp has finished phase 2 of one tile it issues the loads of the block's
+// next tile (xpre, have = true), which then arrive during the other warps'
+// phase 2 and the reduction.
 template <int NP, bool TS>
 __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __restrict__ x, int64_t P, int64_t ldx,
                                              float* __restrict__ y, int fastx, int64_t tile, float* sm,
+                                             double (&xpre)[kHotPass], bool& have, int64_t next,
                                              int split_c = 0, int split_S = 1, float* part = nullptr,
                                              unsigned int* ctr = nullptr) {
   static_assert(NP == 4, "points are processed as two pairs per lane");
@@ -195,10 +201,15 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
       const double* xp = x + min(p0 + quad_point(q), P - 1) * ldx;
       for (int h0 = 0; h0 < a.n_hot_dims; h0 += kHB * kHotPass) {
         double xh[kHotPass];
+        if (h0 == 0 && have) {
 #pragma unroll
-        for (int r = 0; r < kHotPass; ++r) {
-          const int h = h0 + hb + kHB * r;
-          xh[r] = h < a.n_hot_dims ? __ldg(xp + (TS ? a.hd[h].x : __ldg(a.hot_dim + h))) : 0.0;
+          for (int r = 0; r < kHotPass; ++r) xh[r] = xpre[r];
+        } else {
+#pragma unroll
+          for (int r = 0; r < kHotPass; ++r) {
+            const int h = h0 + hb + kHB * r;
+            xh[r] = h < a.n_hot_dims ? __ldg(xp + (TS ? a.hd[h].x : __ldg(a.hot_dim + h))) : 0.0;
+          }
         }
 #pragma unroll
         for (int r = 0; r < kHotPass; ++r) {
@@ -354,6 +365,19 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
       }
     }
 
+    // first phase-0 pass of the next tile: its x loads fly during the reduction
+    // (written on every path, so that xpre is dead between phase 0 and here)
+    have = next >= 0;
+    {
+      const int q = threadIdx.x & (kT - 1), hb = threadIdx.x >> 7;
+      const double* xp = x + min((have ? next : tile) * kT + quad_point(q), P - 1) * ldx;
+#pragma unroll
+      for (int r = 0; r < kHotPass; ++r) {
+        const int h = hb + kHB * r;
+        xpre[r] = have && h < a.n_hot_dims ? __ldg(xp + (TS ? a.hd[h].x : __ldg(a.hot_dim + h))) : 0.0;
+      }
+    }
+
     // phase 3: per-point sum over the warps, fixed order
     *reinterpret_cast<float4*>(RS + warp * kT + q0) =
         make_float4(ys[0], NP > 1 ? ys[1 % NP] : 0.f, NP > 2 ? ys[2 % NP] : 0.f, NP > 3 ? ys[3 % NP] : 0.f);
@@ -448,14 +472,19 @@ __global__ void __launch_bounds__(kThr, 1)
   }
   const int64_t n_tiles = (P + 32 * NP - 1) / (32 * NP);
   const int64_t G = gridDim.x, rounds = n_tiles / G, rem = n_tiles - rounds * G;
-  for (int64_t r = 0; r < rounds; ++r) blocked_tile<NP, TS>(a, x, P, ldx, y, fastx, blockIdx.x + r * G, sm);
-  if (rem == 0) return;
   // last round: each remaining tile is shared by S blocks (S = 1 without a full round before it)
   const int S = rounds > 0 && part != nullptr ? int(G / rem < kMaxSplit ? G / rem : kMaxSplit) : 1;
-  const int64_t t = blockIdx.x / S;
-  if (t >= rem) return;
+  const int64_t t = rem > 0 ? blockIdx.x / S : rem;
+  const int64_t last = t < rem ? rounds * G + t : -1;  // this block's share of the last round
+  double xpre[kHotPass];
+  bool have = false;
+  for (int64_t r = 0; r < rounds; ++r)
+    blocked_tile<NP, TS>(a, x, P, ldx, y, fastx, blockIdx.x + r * G, sm, xpre, have,
+                         r + 1 < rounds ? blockIdx.x + (r + 1) * G : last);
+  if (last < 0) return;
   const int c = int(blockIdx.x - t * S);
-  blocked_tile<NP, TS>(a, x, P, ldx, y, fastx, rounds * G + t, sm, c, S, part + t * (2 * kMaxSplit * kT), ctr + t);
+  blocked_tile<NP, TS>(a, x, P, ldx, y, fastx, last, sm, xpre, have, -1, c, S, part + t * (2 * kMaxSplit * kT),
+                       ctr + t);
 }
 
 struct BWork {
@@ -484,7 +513,9 @@ __global__ void __launch_bounds__(kThr, 1)
       if (items[mid].tile0 <= t) lo = mid; else hi = mid - 1;
     }
     const BWork it = items[lo];
-    blocked_tile<4, false>(plans[it.plan], it.x, it.P, it.ldx, it.y, it.fastx, t - it.tile0, sm);
+    double xpre[kHotPass];
+    bool have = false;
+    blocked_tile<4, false>(plans[it.plan], it.x, it.P, it.ldx, it.y, it.fastx, t - it.tile0, sm, xpre, have, -1);
   }
 }
 
