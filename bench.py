@@ -357,8 +357,9 @@ def run_tensor_workload(args):
                      "note": "3 kind::tf32 passes per product; kind::tf32 runs at half the bf16 dense rate"},
         "bf16x3": bf16,
         "setup_s": setup_s, "clocks": clk.summary(),
-        # per step: one panel and one tensor-core GEMM per chunk of points, or one evaluator launch per 4 outputs
-        "gpu_launches": args.steps * (2 * sp.tc_chunks(P) if sp.tc is not None else (d_out + 3) // 4),
+        # per step: per chunk of points a panel (+ its basis rows) and a tensor-core GEMM, or one
+        # evaluator launch per 4 outputs
+        "gpu_launches": args.steps * (sp.tc_launches(P) if sp.tc is not None else (d_out + 3) // 4),
     }
     print(json.dumps(line))
     return 0

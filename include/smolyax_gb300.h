@@ -320,18 +320,21 @@ size_t smx_blocked_eval_workspace(const smx_blocked* plan_host, int64_t P);
  * depth <= 8), written as TF32 hi/lo pairs [P x lda] in REVERSED order (entry j
  * of the tape goes to column K-1-j: summing from small to large terms limits
  * the truncation of the tensor cores' FP32 accumulation).  Basis slots: for each
- * listed dimension dims[h], degrees 1..dmax[h] at dsoff[h]. */
+ * listed dimension dims[h], degrees 1..dmax[h] at dsoff[h].  The tape is walked
+ * in n_seg independent segments [seg[s], seg[s+1]) (seg[0] = 0, seg[n_seg] = K,
+ * every seg[s] the position of a depth-1 entry; seg may be NULL for n_seg = 1),
+ * one block of points per segment. */
 size_t smx_spectral_panel_workspace(int n_slots, int64_t P);
 int smx_spectral_panel_tf32(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff, int n_slots,
-                            const int32_t* tape, int K, const float* fam_a, const float* fam_b, const int32_t* fam,
-                            const double* x, int64_t P, int64_t ldx, float* A_hi, float* A_lo, int64_t lda, void* ws,
-                            size_t ws_bytes, void* stream);
+                            const int32_t* tape, int K, const int32_t* seg, int n_seg, const float* fam_a,
+                            const float* fam_b, const int32_t* fam, const double* x, int64_t P, int64_t ldx,
+                            float* A_hi, float* A_lo, int64_t lda, void* ws, size_t ws_bytes, void* stream);
 /* Same panel as BF16 hi/lo pairs (hi = BF16 rounded to nearest, lo = BF16 of
  * the remainder; bit patterns, 2 bytes each) for smx_gemm_bf16x3. */
 int smx_spectral_panel_bf16(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff, int n_slots,
-                            const int32_t* tape, int K, const float* fam_a, const float* fam_b, const int32_t* fam,
-                            const double* x, int64_t P, int64_t ldx, uint16_t* A_hi, uint16_t* A_lo, int64_t lda,
-                            void* ws, size_t ws_bytes, void* stream);
+                            const int32_t* tape, int K, const int32_t* seg, int n_seg, const float* fam_a,
+                            const float* fam_b, const int32_t* fam, const double* x, int64_t P, int64_t ldx,
+                            uint16_t* A_hi, uint16_t* A_lo, int64_t lda, void* ws, size_t ws_bytes, void* stream);
 
 /* Backward of the orthogonal form (no counterpart in the reference, whose
  * derivative is the dense Jacobian of interpolation.py:306-345):

@@ -757,34 +757,26 @@ extern "C" int smx_spectral_eval_batch(const smx_spectral* plans, int n_plans, c
 // --- basis-product panel for the tensor-core contraction ------------------------------------
 // A[p][j] = prod over the pairs of entry j of phi_g(z_d), for the non-root
 // entries of Lambda in DFS pre-order (tape word: basis slot | depth << 16).
-// One thread per point: the per-point basis values of all pairs sit in shared
-// memory ([slot][point]), the path products on a register stack; blocks of 32
-// columns go through a shared tile so that the TF32 hi/lo rows are written
-// with coalesced 128-byte stores.
+// One thread per point and tape segment (blockIdx.y): the per-point basis
+// values of all pairs sit in shared memory ([slot][point]) or, for large plans,
+// in a global scratch written by panel_basis_kernel; the path products sit on a
+// register stack; blocks of 32 columns go through a shared tile so that the
+// hi/lo rows are written with coalesced 128-byte stores.  Every segment starts
+// at a depth-1 entry: in DFS pre-order it then holds whole subtrees, so its
+// stack starts fresh and the segments of one point are independent.
 namespace {
 
-// BF16 = true: the hi/lo pair is written as BF16 (round to nearest even) for
-// the kind::f16 contraction.
-template <bool BF16>
-__global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32_t* __restrict__ dims,
-                                                         const int32_t* __restrict__ dmax,
-                                                         const int32_t* __restrict__ dsoff, int n_slots,
-                                                         const int32_t* __restrict__ tape, int K,
-                                                         const float* __restrict__ fam_a,
-                                                         const float* __restrict__ fam_b,
-                                                         const int32_t* __restrict__ fam, const double* __restrict__ x,
-                                                         int64_t P, int64_t ldx, void* __restrict__ Ahi,
-                                                         void* __restrict__ Alo, int64_t lda,
-                                                         float* __restrict__ grow) {
-  extern __shared__ __align__(16) float sm[];
-  // basis row: shared memory [n_slots][128], or (large plans) global scratch
-  // [n_slots][gridDim.x * 128] read through L1
-  const int64_t rstride = grow ? int64_t(gridDim.x) * 128 : 128;
-  float* tile = grow ? sm : sm + size_t(n_slots) * 128;  // [32][129]
-  const int tid = threadIdx.x;
-  const int64_t p0 = blockIdx.x * int64_t(128);
-  float* row = grow ? grow + p0 : sm;
-  const int64_t p = p0 + tid;
+// Basis rows grow[slot][p] (stride rstride) of the listed dimensions, one
+// thread per point.
+__global__ void __launch_bounds__(128) panel_basis_kernel(int n_dims, const int32_t* __restrict__ dims,
+                                                          const int32_t* __restrict__ dmax,
+                                                          const int32_t* __restrict__ dsoff,
+                                                          const float* __restrict__ fam_a,
+                                                          const float* __restrict__ fam_b,
+                                                          const int32_t* __restrict__ fam,
+                                                          const double* __restrict__ x, int64_t P, int64_t ldx,
+                                                          float* __restrict__ grow, int64_t rstride) {
+  const int64_t p = blockIdx.x * int64_t(128) + threadIdx.x;
   const double* xp = x + (p < P ? p : 0) * ldx;
   for (int h = 0; h < n_dims; ++h) {
     const int dim = dims[h], g = dmax[h], so = dsoff[h];
@@ -795,19 +787,67 @@ __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32
       const float pn = c_alpha[fm][n] * z * pc - c_beta[fm][n] * pm1;
       pm1 = pc;
       pc = pn;
-      row[(so + n) * rstride + tid] = pc;
+      grow[(so + n) * rstride + p] = pc;
     }
   }
+}
+
+// BF16 = true: the hi/lo pair is written as BF16 (round to nearest even) for
+// the kind::f16 contraction.
+template <bool BF16>
+__global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32_t* __restrict__ dims,
+                                                         const int32_t* __restrict__ dmax,
+                                                         const int32_t* __restrict__ dsoff, int n_slots,
+                                                         const int32_t* __restrict__ tape, int K,
+                                                         const int32_t* __restrict__ seg,
+                                                         const float* __restrict__ fam_a,
+                                                         const float* __restrict__ fam_b,
+                                                         const int32_t* __restrict__ fam, const double* __restrict__ x,
+                                                         int64_t P, int64_t ldx, void* __restrict__ Ahi,
+                                                         void* __restrict__ Alo, int64_t lda,
+                                                         const float* __restrict__ grow, int64_t gstride) {
+  extern __shared__ __align__(16) float sm[];
+  // basis row: shared memory [n_slots][128], or (large plans) the global
+  // scratch [n_slots][gstride] read through L1
+  const int64_t rstride = grow ? gstride : 128;
+  float* tile = grow ? sm : sm + size_t(n_slots) * 128;  // [32][129]
+  const int tid = threadIdx.x;
+  // blockIdx.x = segment (the segments of one block of points run side by side
+  // and share its basis rows in cache), blockIdx.y strides over point blocks
+  const int64_t n_pb = (P + 127) / 128;
+  for (int64_t pb = blockIdx.y; pb < n_pb; pb += gridDim.y) {
+  const int64_t p0 = pb * 128;
+  const float* row = grow ? grow + p0 : sm;
+  if (!grow) {
+    const int64_t p = p0 + tid;
+    const double* xp = x + (p < P ? p : 0) * ldx;
+    for (int h = 0; h < n_dims; ++h) {
+      const int dim = dims[h], g = dmax[h], so = dsoff[h];
+      const int fm = fam[dim];
+      const float z = fmaf(fam_a[dim], float(xp[dim]), fam_b[dim]);
+      float pm1 = 0.f, pc = 1.f;
+      for (int n = 0; n < g; ++n) {
+        const float pn = c_alpha[fm][n] * z * pc - c_beta[fm][n] * pm1;
+        pm1 = pc;
+        pc = pn;
+        sm[(so + n) * 128 + tid] = pc;
+      }
+    }
+  }
+  const int jbeg = seg ? seg[blockIdx.x] : 0, jend = seg ? seg[blockIdx.x + 1] : K;
   float st1 = 1.f, st2 = 1.f, st3 = 1.f, st4 = 1.f, st5 = 1.f, st6 = 1.f, st7 = 1.f, st8 = 1.f;
-  for (int jb = 0; jb < K; jb += 32) {
-    const int jn = min(32, K - jb);
+  // tiles of up to 32 entries, cut so that each covers one aligned group of 32
+  // output columns (column K-1-j): full 128-byte lines of the FP32 rows
+  for (int jb = jbeg, jn = 0; jb < jend; jb += jn) {
+    jn = min(jend - jb, ((K - jb - 1) & 31) + 1);
     // 8 tape entries at a time: their basis values are loaded together (the
     // loads are independent; only the stack updates are sequential)
     for (int j = 0; j < jn; j += 8) {
       int w[8];
       float b[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) w[u] = j + u < jn ? __ldg(tape + jb + j + u) : (1 << 16);
+      // past the tile: depth 8, whose stack slot no other depth reads
+      for (int u = 0; u < 8; ++u) w[u] = j + u < jn ? __ldg(tape + jb + j + u) : (8 << 16);
 #pragma unroll
       for (int u = 0; u < 8; ++u) b[u] = row[(w[u] & 0xffff) * rstride + tid];
 #pragma unroll
@@ -853,6 +893,7 @@ __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32
     }
     __syncthreads();
   }
+  }
 }
 
 }  // namespace
@@ -871,15 +912,18 @@ extern "C" size_t smx_spectral_panel_workspace(int n_slots, int64_t P) {
 namespace {
 template <bool BF16>
 int panel_launch(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff, int n_slots,
-                 const int32_t* tape, int K, const float* fam_a, const float* fam_b, const int32_t* fam,
-                 const double* x, int64_t P, int64_t ldx, void* A_hi, void* A_lo, int64_t lda, void* ws,
-                 size_t ws_bytes, void* stream, const char* what) {
-  SMX_REQUIRE(n_dims >= 0 && n_slots >= 0 && K >= 0 && P >= 0 && lda >= K, what);
+                 const int32_t* tape, int K, const int32_t* seg, int n_seg, const float* fam_a, const float* fam_b,
+                 const int32_t* fam, const double* x, int64_t P, int64_t ldx, void* A_hi, void* A_lo, int64_t lda,
+                 void* ws, size_t ws_bytes, void* stream, const char* what) {
+  SMX_REQUIRE(n_dims >= 0 && n_slots >= 0 && K >= 0 && P >= 0 && lda >= K && n_seg >= 1 && n_seg <= 65535 &&
+                  (n_seg == 1 || seg),
+              what);
   if (P == 0 || K == 0) return SMX_OK;
   SMX_REQUIRE(dims && dmax && dsoff && tape && fam_a && fam_b && fam && x && A_hi && A_lo, what);
   const size_t need = smx_spectral_panel_workspace(n_slots, P);
   SMX_REQUIRE(ws_bytes >= need && (need == 0 || ws), what);
   float* grow = need ? static_cast<float*>(ws) : nullptr;
+  const int64_t gstride = (P + 127) / 128 * 128;
   const size_t smem = grow ? size_t(32 * 129) * sizeof(float) : (size_t(n_slots) * 128 + 32 * 129) * sizeof(float);
   int rc = upload_consts();
   if (rc) return rc;
@@ -888,29 +932,36 @@ int panel_launch(int n_dims, const int32_t* dims, const int32_t* dmax, const int
     cudaFuncSetAttribute(panel_tf32_kernel<BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     attr = true;
   }
-  panel_tf32_kernel<BF16><<<smx::grid_for(P, 128), 128, smem, smx::as_stream(stream)>>>(
-      n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, A_hi, A_lo, lda, grow);
+  cudaStream_t st = smx::as_stream(stream);
+  if (grow)
+    panel_basis_kernel<<<smx::grid_for(P, 128), 128, 0, st>>>(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, x, P,
+                                                              ldx, grow, gstride);
+  const int64_t n_pb = (P + 127) / 128;
+  const dim3 grid(n_seg, unsigned(n_pb < 65535 ? n_pb : 65535));
+  panel_tf32_kernel<BF16><<<grid, 128, smem, st>>>(n_dims, dims, dmax, dsoff, n_slots, tape, K,
+                                                   n_seg > 1 ? seg : nullptr, fam_a, fam_b, fam, x, P, ldx, A_hi,
+                                                   A_lo, lda, grow, gstride);
   SMX_LAUNCH_CHECK(what);
   return SMX_OK;
 }
 }  // namespace
 
 extern "C" int smx_spectral_panel_tf32(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff,
-                                       int n_slots, const int32_t* tape, int K, const float* fam_a,
-                                       const float* fam_b, const int32_t* fam, const double* x, int64_t P, int64_t ldx,
-                                       float* A_hi, float* A_lo, int64_t lda, void* ws, size_t ws_bytes,
-                                       void* stream) {
-  return panel_launch<false>(n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, A_hi, A_lo,
-                             lda, ws, ws_bytes, stream, "smx_spectral_panel_tf32");
+                                       int n_slots, const int32_t* tape, int K, const int32_t* seg, int n_seg,
+                                       const float* fam_a, const float* fam_b, const int32_t* fam, const double* x,
+                                       int64_t P, int64_t ldx, float* A_hi, float* A_lo, int64_t lda, void* ws,
+                                       size_t ws_bytes, void* stream) {
+  return panel_launch<false>(n_dims, dims, dmax, dsoff, n_slots, tape, K, seg, n_seg, fam_a, fam_b, fam, x, P, ldx,
+                             A_hi, A_lo, lda, ws, ws_bytes, stream, "smx_spectral_panel_tf32");
 }
 
 extern "C" int smx_spectral_panel_bf16(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff,
-                                       int n_slots, const int32_t* tape, int K, const float* fam_a,
-                                       const float* fam_b, const int32_t* fam, const double* x, int64_t P, int64_t ldx,
-                                       uint16_t* A_hi, uint16_t* A_lo, int64_t lda, void* ws, size_t ws_bytes,
-                                       void* stream) {
-  return panel_launch<true>(n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, A_hi, A_lo,
-                            lda, ws, ws_bytes, stream, "smx_spectral_panel_bf16");
+                                       int n_slots, const int32_t* tape, int K, const int32_t* seg, int n_seg,
+                                       const float* fam_a, const float* fam_b, const int32_t* fam, const double* x,
+                                       int64_t P, int64_t ldx, uint16_t* A_hi, uint16_t* A_lo, int64_t lda, void* ws,
+                                       size_t ws_bytes, void* stream) {
+  return panel_launch<true>(n_dims, dims, dmax, dsoff, n_slots, tape, K, seg, n_seg, fam_a, fam_b, fam, x, P, ldx,
+                            A_hi, A_lo, lda, ws, ws_bytes, stream, "smx_spectral_panel_bf16");
 }
 
 // --- backward ---------------------------------------------------------------------------------

@@ -199,7 +199,10 @@ class SpectralPlan:
         self.tc = dict(dims=T(dims, torch.int32), dmax=T(dmax, torch.int32), dsoff=T(dsoff, torch.int32),
                        n_slots=n_slots, tape=T(tape, torch.int32), K=K, ldk=ldk, Bh=Bh, Bl=Bl, Bd=Bd,
                        bias=self.keep["c0"], err=torch.zeros(1, dtype=torch.int32, device=dev),
-                       ent=torch.as_tensor(ent, device=dev))
+                       ent=torch.as_tensor(ent, device=dev),
+                       # tape positions of the depth-1 entries: where independent segments may start
+                       lvl1=np.nonzero(tr["level"][ent] == 1)[0],
+                       sms=torch.cuda.get_device_properties(dev).multi_processor_count)
 
     def _build_blocked(self, tr, c, maxdeg, d, fam, fa, fb, T):
         """Tables of the blocked evaluator (one output), if the plan fits it."""
@@ -354,12 +357,38 @@ class SpectralPlan:
 
     def _tc_step(self, P):
         """Points per panel chunk (the hi/lo panel of one chunk fits the memory limit)."""
-        step = max(128, int(self.memory_limit * 1024**3 // (8 * self.tc["ldk"])) // 128 * 128)
+        step = max(128, int(self.memory_limit * 1024**3 // (8 * ((self.tc["K"] + 31) // 32 * 32))) // 128 * 128)
         return max(1, min(step, P))
 
     def tc_chunks(self, P):
         """Number of panel chunks (each one panel and one GEMM launch) for P points."""
         return -(-int(P) // self._tc_step(P)) if P else 0
+
+    def tc_launches(self, P):
+        """Kernel launches of one tensor-core evaluation of P points: per chunk the
+        panel (plus its basis-row kernel when the rows go to global scratch) and
+        the GEMM."""
+        scratch = capi.size("smx_spectral_panel_workspace", self.tc["n_slots"], 1) > 0
+        return self.tc_chunks(P) * (3 if scratch else 2)
+
+    def _segments(self, n):
+        """Tape segments of one panel launch over n points: enough (point block,
+        segment) blocks for ~12 per SM, segments of >= 256 entries, each
+        starting at a depth-1 entry.  Returns (bounds on the device or None, count)."""
+        tc = self.tc
+        K, pos = tc["K"], tc["lvl1"]
+        n_pb = -(-int(n) // 128)
+        want = max(1, min(32, -(-12 * tc["sms"] // max(n_pb, 1)), K // 256, int(pos.size)))
+        if want <= 1:
+            return None, 1
+        cache = tc.setdefault("segs", {})
+        if want not in cache:
+            targets = (np.arange(1, want) * K) // want
+            b = pos[np.minimum(np.searchsorted(pos, targets), pos.size - 1)]
+            bounds = np.unique(np.concatenate([[0], b, [K]])).astype(np.int32)
+            cache[want] = torch.as_tensor(bounds, device=tc["tape"].device)
+        t = cache[want]
+        return t, int(t.numel()) - 1
 
     def _bf16_operands(self):
         """Coefficient matrix B split to BF16 hi/lo, rows padded to 8 entries."""
@@ -387,36 +416,35 @@ class SpectralPlan:
         if bf16:
             Bh, Bl, ld16 = self._bf16_operands()
             step = self._tc_step(P)
-            Ah = torch.empty(step, ld16, dtype=torch.bfloat16, device=x.device)
+            lda = (tc["K"] + 63) // 64 * 64  # 128-byte panel rows
+            Ah = torch.empty(step, lda, dtype=torch.bfloat16, device=x.device)
             Al = torch.empty_like(Ah)
-            if ld16 > tc["K"]:
-                Ah[:, tc["K"]:] = 0
-                Al[:, tc["K"]:] = 0
             for p0 in range(0, P, step):
                 p1 = min(P, p0 + step)
                 nws = capi.size("smx_spectral_panel_workspace", tc["n_slots"], p1 - p0)
                 ws = torch.empty(max(nws, 1), dtype=torch.uint8, device=x.device)
+                seg, n_seg = self._segments(p1 - p0)
                 call("smx_spectral_panel_bf16", int(tc["dims"].numel()), ptr(tc["dims"]), ptr(tc["dmax"]),
-                     ptr(tc["dsoff"]), tc["n_slots"], ptr(tc["tape"]), tc["K"], ptr(k["fam_a"]), ptr(k["fam_b"]),
-                     ptr(k["fam"]), ptr(x[p0:p1]), p1 - p0, d, ptr(Ah), ptr(Al), ld16, ptr(ws), nws, st)
-                call("smx_gemm_bf16x3", ptr(Ah), ptr(Al), ld16, ptr(Bh), ptr(Bl), ld16, p1 - p0, d_out, tc["K"],
+                     ptr(tc["dsoff"]), tc["n_slots"], ptr(tc["tape"]), tc["K"], ptr(seg), n_seg, ptr(k["fam_a"]),
+                     ptr(k["fam_b"]), ptr(k["fam"]), ptr(x[p0:p1]), p1 - p0, d, ptr(Ah), ptr(Al), lda, ptr(ws), nws,
+                     st)
+                call("smx_gemm_bf16x3", ptr(Ah), ptr(Al), lda, ptr(Bh), ptr(Bl), ld16, p1 - p0, d_out, tc["K"],
                      ptr(y[p0:p1]), d_out, ptr(tc["bias"]), 0, ptr(tc["err"]), st)
             return y
         ldk = tc["ldk"]
         step = self._tc_step(P)
-        Ah = torch.empty(step, ldk, dtype=torch.float32, device=x.device)
+        lda = (tc["K"] + 31) // 32 * 32  # 128-byte panel rows
+        Ah = torch.empty(step, lda, dtype=torch.float32, device=x.device)
         Al = torch.empty_like(Ah)
-        if ldk > tc["K"]:
-            Ah[:, tc["K"]:] = 0
-            Al[:, tc["K"]:] = 0
         for p0 in range(0, P, step):
             p1 = min(P, p0 + step)
             nws = capi.size("smx_spectral_panel_workspace", tc["n_slots"], p1 - p0)
             ws = torch.empty(max(nws, 1), dtype=torch.uint8, device=x.device)
+            seg, n_seg = self._segments(p1 - p0)
             call("smx_spectral_panel_tf32", int(tc["dims"].numel()), ptr(tc["dims"]), ptr(tc["dmax"]),
-                 ptr(tc["dsoff"]), tc["n_slots"], ptr(tc["tape"]), tc["K"], ptr(k["fam_a"]), ptr(k["fam_b"]),
-                 ptr(k["fam"]), ptr(x[p0:p1]), p1 - p0, d, ptr(Ah), ptr(Al), ldk, ptr(ws), nws, st)
-            call("smx_gemm_tf32x3", ptr(Ah), ptr(Al), ldk, ptr(tc["Bh"]), ptr(tc["Bl"]), ldk, p1 - p0, d_out,
+                 ptr(tc["dsoff"]), tc["n_slots"], ptr(tc["tape"]), tc["K"], ptr(seg), n_seg, ptr(k["fam_a"]),
+                 ptr(k["fam_b"]), ptr(k["fam"]), ptr(x[p0:p1]), p1 - p0, d, ptr(Ah), ptr(Al), lda, ptr(ws), nws, st)
+            call("smx_gemm_tf32x3", ptr(Ah), ptr(Al), lda, ptr(tc["Bh"]), ptr(tc["Bl"]), ldk, p1 - p0, d_out,
                  tc["K"], ptr(y[p0:p1]), d_out, ptr(tc["bias"]), 0, ptr(tc["err"]), st)
         return y
 

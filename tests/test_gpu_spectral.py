@@ -229,3 +229,51 @@ def test_blocked_evaluator_generic_groups(kind, d, t):
     err = ((y32 - y64).abs().max() / y64.abs().max()).item()
     print("%s d=%d t=%.1f: FP32 error %.2e" % (kind, d, t, err))
     assert err < 1e-6
+
+
+@pytest.mark.parametrize("bf16", [False, True])
+def test_panel_segments_equal_single_walk(bf16):
+    """The tape split into segments at depth-1 entries (one block of points per
+    segment) writes the same panel, bit for bit, as one walk of the whole tape."""
+    import torch
+
+    from smolyax_gb300 import _capi, nodes
+
+    d, d_out = 100, 32
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    ip = _interp(node_gen=nodes.GaussHermite(dim=d), k=k, t=7.723434, d_out=d_out,
+                 f=fns.exponential(d, d_out, seed=0))
+    sp = ip.spectral_plan()
+    tc, kk = sp.tc, sp.keep
+    assert tc is not None
+    P = 300
+    x = torch.as_tensor(np.random.default_rng(6).normal(size=(P, d)), device="cuda")
+    K = tc["K"]
+    ld = (K + 7) // 8 * 8
+    dt = torch.bfloat16 if bf16 else torch.float32
+    name = "smx_spectral_panel_bf16" if bf16 else "smx_spectral_panel_tf32"
+    lvl1 = set(tc["lvl1"].tolist())
+    st = _capi.stream_ptr(torch.cuda.current_stream())
+    nws = _capi.size("smx_spectral_panel_workspace", tc["n_slots"], P)
+    ws = torch.empty(max(nws, 1), dtype=torch.uint8, device="cuda")
+    outs = []
+    for n in (None, 2, 7, 32):
+        if n is None:
+            seg, n_seg = None, 1
+        else:
+            b = sorted(set([0, K] + [int(tc["lvl1"][min(len(lvl1) - 1, i * len(lvl1) // n)]) for i in range(1, n)]))
+            assert all(v in lvl1 for v in b[:-1])
+            seg, n_seg = torch.as_tensor(np.array(b, np.int32), device="cuda"), len(b) - 1
+        Ah = torch.full((P, ld), 7, dtype=dt, device="cuda")
+        Al = torch.full_like(Ah, 7)
+        _capi.call(name, int(tc["dims"].numel()), _capi.ptr(tc["dims"]), _capi.ptr(tc["dmax"]), _capi.ptr(tc["dsoff"]),
+                   tc["n_slots"], _capi.ptr(tc["tape"]), K, _capi.ptr(seg), n_seg, _capi.ptr(kk["fam_a"]),
+                   _capi.ptr(kk["fam_b"]), _capi.ptr(kk["fam"]), _capi.ptr(x), P, d, _capi.ptr(Ah), _capi.ptr(Al), ld,
+                   _capi.ptr(ws), nws, st)
+        outs.append((Ah[:, :K].clone(), Al[:, :K].clone()))
+    for Ah, Al in outs[1:]:
+        assert torch.equal(Ah, outs[0][0]) and torch.equal(Al, outs[0][1])
+    # the segments the plan picks for a launch start at depth-1 entries
+    seg, n_seg = sp._segments(P)
+    if seg is not None:
+        assert all(int(v) in lvl1 for v in seg.cpu().numpy()[:-1]) and int(seg[-1]) == K
