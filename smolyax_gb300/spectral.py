@@ -284,20 +284,21 @@ class SpectralPlan:
         step = max(128, int(self.memory_limit * 1024**3 // (8 * ldk)) // 128 * 128)
         if need_x:
             dx = torch.zeros(P, d, dtype=torch.float64, device=dev)
-            G = torch.empty(min(step, P), ldk, dtype=torch.float32, device=dev)
+            ldg = _round32(K)  # 128-byte rows
+            G = torch.empty(min(step, P), ldg, dtype=torch.float32, device=dev)
             nws = capi.size("smx_spectral_vjp_x_workspace", ops["n_slots"], min(step, P))
             ws = torch.empty(max(nws, 1), dtype=torch.uint8, device=dev)
             for p0 in range(0, P, step):
                 p1 = min(P, p0 + step)
                 call("smx_gemm_tf32x3", ptr(gh[p0:p1]), ptr(gl[p0:p1]), ldo, ptr(ops["Rh"]), ptr(ops["Rl"]), ldo,
-                     p1 - p0, K, ldo, ptr(G), ldk, None, 0, ptr(err), st)
-                call("smx_spectral_vjp_x", *common, ptr(x[p0:p1]), p1 - p0, d, ptr(G), ldk, ptr(dx[p0:p1]), d,
+                     p1 - p0, K, ldo, ptr(G), ldg, None, 0, ptr(err), st)
+                call("smx_spectral_vjp_x", *common, ptr(x[p0:p1]), p1 - p0, d, ptr(G), ldg, ptr(dx[p0:p1]), d,
                      ptr(ws), nws, st)
         if need_coef:
-            ldp = _round4(min(step, P))
+            ldp = _round32(min(step, P))  # 128-byte rows
             ATh = torch.empty(K, ldp, dtype=torch.float32, device=dev)
             ATl = torch.empty_like(ATh)
-            gT = torch.empty(ldo, ldp, dtype=torch.float32, device=dev)
+            gT = torch.zeros(ldo, ldp, dtype=torch.float32, device=dev)
             gTh, gTl = torch.empty_like(gT), torch.empty_like(gT)
             dCrev = torch.zeros(K, d_out, dtype=torch.float32, device=dev)
             nws = capi.size("smx_spectral_panel_t_workspace", ops["n_slots"], min(step, P))
@@ -305,14 +306,13 @@ class SpectralPlan:
             for i, p0 in enumerate(range(0, P, step)):
                 p1 = min(P, p0 + step)
                 n = p1 - p0
-                ATh.zero_()
-                ATl.zero_()
+                # the contraction runs over the chunk's n points: the columns past n
+                # are outside the operands' tensor maps and need no zeros
                 call("smx_spectral_panel_t_tf32", *common, ptr(x[p0:p1]), n, d, ptr(ATh), ptr(ATl), ldp, ptr(ws), nws,
                      st)
-                gT.zero_()
                 gT[:, :n] = g32[p0:p1].t()
-                call("smx_split_tf32", ptr(gT), ldo, ldp, ldp, ptr(gTh), ptr(gTl), ldp, st)
-                call("smx_gemm_tf32x3", ptr(ATh), ptr(ATl), ldp, ptr(gTh), ptr(gTl), ldp, K, d_out, ldp,
+                call("smx_split_tf32", ptr(gT), ldo, n, ldp, ptr(gTh), ptr(gTl), ldp, st)
+                call("smx_gemm_tf32x3", ptr(ATh), ptr(ATl), ldp, ptr(gTh), ptr(gTl), ldp, K, d_out, n,
                      ptr(dCrev), d_out, None, 1 if i else 0, ptr(err), st)
             n_lam = int(self.C64.shape[0])
             dC = torch.zeros(n_lam, d_out, dtype=torch.float64, device=dev)
@@ -451,6 +451,10 @@ class SpectralPlan:
 
 def _round4(v):
     return (int(v) + 3) // 4 * 4
+
+
+def _round32(v):
+    return (int(v) + 31) // 32 * 32
 
 
 class _Runs:
