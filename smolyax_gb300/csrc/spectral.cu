@@ -1052,6 +1052,11 @@ __global__ void __launch_bounds__(128) panel_t_tf32_kernel(int n_dims, const int
 // read 8 entries at a time so their basis values load together.
 constexpr int kVjpTP = 32;
 
+// GB = false: the adjoints bar[slot][point] of the block's 32 points sit in
+// shared memory; GB = true (many basis slots, where that shared memory would
+// leave room for only a few warps per SM): they sit in a global scratch
+// [n_slots][rstride] beside the basis rows, read and updated through L1/L2.
+template <bool GB>
 __global__ void __launch_bounds__(kVjpTP) vjp_x_kernel(int n_dims, const int32_t* __restrict__ dims,
                                                        const int32_t* __restrict__ dmax,
                                                        const int32_t* __restrict__ dsoff, int n_slots,
@@ -1061,19 +1066,21 @@ __global__ void __launch_bounds__(kVjpTP) vjp_x_kernel(int n_dims, const int32_t
                                                        const int32_t* __restrict__ fam, const double* __restrict__ x,
                                                        int64_t P, int64_t ldx, const float* __restrict__ G,
                                                        int64_t ldg, double* __restrict__ dx, int64_t lddx,
-                                                       float* __restrict__ rowg, int64_t rstride) {
+                                                       float* __restrict__ rowg, int64_t rstride,
+                                                       float* __restrict__ barg) {
   extern __shared__ __align__(16) float sm[];
   constexpr int TP = kVjpTP;
-  float* bar = sm;                             // [n_slots][TP] adjoints
-  float* tile = bar + size_t(n_slots) * TP;    // [32][TP + 1]
+  const int64_t BS = GB ? rstride : TP;              // slot stride of the adjoints
+  float* tile = GB ? sm : sm + size_t(n_slots) * TP;  // [32][TP + 1]
   const int tid = threadIdx.x;
   const int64_t p0 = blockIdx.x * int64_t(TP);
   const int64_t p = p0 + tid;
+  float* bar = GB ? barg + p0 : sm;                  // bar[slot * BS + tid]
   const double* xp = x + (p < P ? p : 0) * ldx;
   float* row = rowg + p;
   basis_row(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, xp, row, rstride, 0);
-  for (int s = 0; s < n_slots; ++s) bar[s * TP + tid] = 0.f;
-  int s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0, s6 = 0, s7 = 0, s8 = 0;
+  for (int s = 0; s < n_slots; ++s) bar[s * BS + tid] = 0.f;
+  int64_t s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0, s6 = 0, s7 = 0, s8 = 0;
   float f1 = 1.f, f2 = 1.f, f3 = 1.f, f4 = 1.f, f5 = 1.f, f6 = 1.f, f7 = 1.f, f8 = 1.f;
   float q1 = 1.f, q2 = 1.f, q3 = 1.f, q4 = 1.f, q5 = 1.f, q6 = 1.f, q7 = 1.f;
   for (int jb = 0; jb < K; jb += 32) {
@@ -1095,7 +1102,7 @@ __global__ void __launch_bounds__(kVjpTP) vjp_x_kernel(int n_dims, const int32_t
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int k = min(8, w[u] >> 16);  // 0: padding past the end of the tape
-        const int sl = (w[u] & 0xffff) * TP + tid;
+        const int64_t sl = (w[u] & 0xffff) * BS + tid;
         switch (k) {
           case 1: s1 = sl; f1 = b[u]; q1 = b[u]; break;
           case 2: s2 = sl; f2 = b[u]; q2 = q1 * b[u]; break;
@@ -1137,7 +1144,7 @@ __global__ void __launch_bounds__(kVjpTP) vjp_x_kernel(int n_dims, const int32_t
       pc = pn;
       dm1 = dc;
       dc = dn;
-      acc = fmaf(bar[(so + n) * TP + tid], dc, acc);
+      acc = fmaf(bar[(so + n) * BS + tid], dc, acc);
     }
     dx[p * lddx + dim] = double(fam_a[dim]) * double(acc);
   }
@@ -1208,9 +1215,14 @@ extern "C" int smx_spectral_panel_t_tf32(int n_dims, const int32_t* dims, const 
   return SMX_OK;
 }
 
+// Adjoints in global scratch once their shared memory would exceed 24 KB per
+// 32-point block (fewer than ~8 warps per SM).
+static bool vjp_global_bar(int n_slots) { return (size_t(n_slots) * kVjpTP + 32 * (kVjpTP + 1)) * 4 > 24 * 1024; }
+
 extern "C" size_t smx_spectral_vjp_x_workspace(int n_slots, int64_t P) {
   if (n_slots < 0 || P < 0) return 0;
-  return size_t(n_slots) * size_t((P + kVjpTP - 1) / kVjpTP * kVjpTP) * sizeof(float);
+  const size_t rows = size_t(n_slots) * size_t((P + kVjpTP - 1) / kVjpTP * kVjpTP) * sizeof(float);
+  return vjp_global_bar(n_slots) ? 2 * rows : rows;
 }
 
 extern "C" int smx_spectral_vjp_x(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff,
@@ -1221,19 +1233,25 @@ extern "C" int smx_spectral_vjp_x(int n_dims, const int32_t* dims, const int32_t
   if (P == 0) return SMX_OK;
   SMX_REQUIRE(dims && dmax && dsoff && tape && fam_a && fam_b && fam && x && G && dx, "smx_spectral_vjp_x: null");
   SMX_REQUIRE(ws && ws_bytes >= smx_spectral_vjp_x_workspace(n_slots, P), "smx_spectral_vjp_x: workspace too small");
-  const size_t smem = (size_t(n_slots) * kVjpTP + 32 * (kVjpTP + 1)) * sizeof(float);
-  SMX_REQUIRE(smem <= 220 * 1024, "smx_spectral_vjp_x: too many basis slots");
+  const bool gb = vjp_global_bar(n_slots);
+  const size_t smem = ((gb ? 0 : size_t(n_slots) * kVjpTP) + 32 * (kVjpTP + 1)) * sizeof(float);
   int rc = upload_consts();
   if (rc) return rc;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(vjp_x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    cudaFuncSetAttribute(vjp_x_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     attr = true;
   }
   const int64_t rstride = (P + kVjpTP - 1) / kVjpTP * kVjpTP;
-  vjp_x_kernel<<<smx::grid_for(P, kVjpTP), kVjpTP, smem, smx::as_stream(stream)>>>(
-      n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, G, ldg, dx, lddx,
-      static_cast<float*>(ws), rstride);
+  float* rowg = static_cast<float*>(ws);
+  if (gb)
+    vjp_x_kernel<true><<<smx::grid_for(P, kVjpTP), kVjpTP, smem, smx::as_stream(stream)>>>(
+        n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, G, ldg, dx, lddx, rowg, rstride,
+        rowg + size_t(n_slots) * rstride);
+  else
+    vjp_x_kernel<false><<<smx::grid_for(P, kVjpTP), kVjpTP, smem, smx::as_stream(stream)>>>(
+        n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, G, ldg, dx, lddx, rowg, rstride,
+        nullptr);
   SMX_LAUNCH_CHECK("smx_spectral_vjp_x");
   return SMX_OK;
 }
