@@ -397,6 +397,14 @@ int smx_blocked_eval_batch(const smx_blocked* plans_host, int n_plans, const smx
 int smx_gemm_tf32x3(const float* A_hi, const float* A_lo, int64_t lda, const float* B_hi, const float* B_lo,
                     int64_t ldb, int M, int N, int K, float* D, int64_t ldd, const float* bias, int accumulate, int* err,
                     void* stream);
+/* Same product with the K range split into up to `splits` slices that run side
+ * by side (for small M x N with long K, e.g. the backward's dL/dC over all
+ * points); the slices' FP32 results go to `ws` and are added in slice order
+ * (deterministic).  ws: smx_gemm_tf32x3_splitk_workspace bytes. */
+size_t smx_gemm_tf32x3_splitk_workspace(int M, int N, int K, int splits);
+int smx_gemm_tf32x3_splitk(const float* A_hi, const float* A_lo, int64_t lda, const float* B_hi, const float* B_lo,
+                           int64_t ldb, int M, int N, int K, float* D, int64_t ldd, const float* bias, int accumulate,
+                           int splits, void* ws, size_t ws_bytes, int* err, void* stream);
 
 /* Split-BF16 form of the same contraction (kind::f16, both operands BF16,
  * FP32 accumulation): D = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T with

@@ -167,6 +167,9 @@ SIGNATURES = {
     "smx_spectral_eval_batch_workspace": (_sz, [_int, _int, _int]),
     "smx_spectral_eval_batch": (_int, [_p, _int, _p, _int, _p, _sz, _p]),
     "smx_gemm_tf32x3": (_int, [_p, _p, _i64, _p, _p, _i64, _int, _int, _int, _p, _i64, _p, _int, _p, _p]),
+    "smx_gemm_tf32x3_splitk_workspace": (_sz, [_int, _int, _int, _int]),
+    "smx_gemm_tf32x3_splitk": (_int, [_p, _p, _i64, _p, _p, _i64, _int, _int, _int, _p, _i64, _p, _int, _int, _p, _sz,
+                                       _p, _p]),
     "smx_spectral_panel_t_workspace": (_sz, [_int, _i64]),
     "smx_spectral_panel_t_tf32": (_int, [_int, _p, _p, _p, _int, _p, _int, _p, _p, _p, _p, _i64, _i64, _p, _p,
                                           _i64, _p, _sz, _p]),

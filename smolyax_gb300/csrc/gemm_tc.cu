@@ -131,8 +131,13 @@ struct GemmArgs {
   int64_t ldd;
   const float* bias;
   int* err;
-  int accumulate;  // D += A B^T instead of D = A B^T
+  int accumulate;   // D += A B^T instead of D = A B^T
+  int kt_per_z;     // split-K: K-tiles per blockIdx.z slice (0: one slice)
+  int64_t zstride;  // split-K: floats between the slices' outputs
 };
+
+constexpr int kEpiLd = 132;  // epilogue staging row stride (floats): 16-byte rows, conflict-free
+static_assert(4 * 32 * kEpiLd * 4 <= Smem::kTiles, "epilogue staging must fit the pipeline stages");
 
 // BF16 = false: kind::tf32 on FP32 operands (32 per 128-byte slice); true:
 // kind::f16 on BF16 operands (64 per slice).  Same slices, stages and MMAs.
@@ -154,8 +159,11 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
-  const int KT = (g.K + EK - 1) / EK;
+  const int KT_all = (g.K + EK - 1) / EK;
+  const int kt_base = g.kt_per_z ? int(blockIdx.z) * g.kt_per_z : 0;
+  const int KT = g.kt_per_z ? min(KT_all - kt_base, g.kt_per_z) : KT_all;  // >= 1 (host)
   const int NCH = (KT + kChunk - 1) / kChunk;
+  float* const D = g.D + int64_t(blockIdx.z) * g.zstride;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -193,7 +201,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         }
         uint8_t* st = base + s * L::kStage;
         mbar_expect_tx(&full[s], L::kStage);
-        const int k = kt * EK;
+        const int k = (kt_base + kt) * EK;
         tma_load_2d(st, &tmAh, k, m0, &full[s]);
         tma_load_2d(st + L::kA, &tmAl, k, m0, &full[s]);
         tma_load_2d(st + 2 * L::kA, &tmBh, k, n0, &full[s]);
@@ -280,13 +288,36 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
       if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[b])) : "memory");
     }
     if (ok) {
-      const int row = m0 + warp * 32 + lane;
-      if (row < g.M) {
-        float* dr = g.D + int64_t(row) * g.ldd;
+      // The last accumulator has been read, so every MMA and every copy into the
+      // pipeline stages is complete: the warp stages its 32 rows there
+      // (T[row][col], stride kEpiLd) and writes them back row by row, 512
+      // contiguous bytes per store instruction.
+      float* T = reinterpret_cast<float*>(base) + warp * (32 * kEpiLd);
 #pragma unroll
-        for (int j = 0; j < kBN; ++j) {
-          const int col = n0 + j;
-          if (col < g.N) dr[col] = acc[j] + (g.bias ? g.bias[col] : 0.f) + (g.accumulate ? dr[col] : 0.f);
+      for (int q = 0; q < kBN; q += 4)
+        *reinterpret_cast<float4*>(T + lane * kEpiLd + q) = make_float4(acc[q], acc[q + 1], acc[q + 2], acc[q + 3]);
+      __syncwarp();
+      const int c0 = n0 + 4 * lane;
+      const bool vec = (g.ldd % 4) == 0 && (reinterpret_cast<uintptr_t>(D) & 15) == 0 && c0 + 3 < g.N;
+      float bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) bv[i] = g.bias && c0 + i < g.N ? g.bias[c0 + i] : 0.f;
+      for (int r = 0; r < 32; ++r) {
+        const int row = m0 + warp * 32 + r;
+        if (row >= g.M) break;
+        const float4 t = *reinterpret_cast<const float4*>(T + r * kEpiLd + 4 * lane);
+        float v[4] = {t.x + bv[0], t.y + bv[1], t.z + bv[2], t.w + bv[3]};
+        float* dr = D + int64_t(row) * g.ldd + c0;
+        if (vec) {
+          if (g.accumulate) {
+            const float4 o = *reinterpret_cast<const float4*>(dr);
+            v[0] += o.x, v[1] += o.y, v[2] += o.z, v[3] += o.w;
+          }
+          *reinterpret_cast<float4*>(dr) = make_float4(v[0], v[1], v[2], v[3]);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            if (c0 + i < g.N) dr[i] = v[i] + (g.accumulate ? dr[i] : 0.f);
         }
       }
     }
@@ -356,7 +387,8 @@ int make_map(CUtensorMap* tm, const void* ptr, int64_t rows, int64_t cols, int64
 
 template <bool BF16>
 int launch(const void* Ah, const void* Al, int64_t lda, const void* Bh, const void* Bl, int64_t ldb, int M, int N,
-           int K, float* D, int64_t ldd, const float* bias, int* err, int accumulate, cudaStream_t st) {
+           int K, float* D, int64_t ldd, const float* bias, int* err, int accumulate, cudaStream_t st,
+           int splits = 1) {
   CUtensorMap tAh, tAl, tBh, tBl;
   int rc;
   if ((rc = make_map(&tAh, Ah, M, K, lda, kBM, BF16)) || (rc = make_map(&tAl, Al, M, K, lda, kBM, BF16)) ||
@@ -367,8 +399,13 @@ int launch(const void* Ah, const void* Al, int64_t lda, const void* Bh, const vo
     cudaFuncSetAttribute(gemm_tf32x3_kernel<BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, Smem::kTotal);
     attr = true;
   }
-  GemmArgs g{M, N, K, D, ldd, bias, err, accumulate};
-  dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM);
+  // split-K: slice z runs K-tiles [z * kt_per_z, ...) into D + z * zstride
+  const int EK = BF16 ? 2 * kBK : kBK;
+  const int KT = (K + EK - 1) / EK;
+  const int kt_per_z = splits > 1 ? (KT + splits - 1) / splits : 0;
+  const int nz = splits > 1 ? (KT + kt_per_z - 1) / kt_per_z : 1;
+  GemmArgs g{M, N, K, D, ldd, bias, err, accumulate, kt_per_z, int64_t(M) * ldd};
+  dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM, nz);
   gemm_tf32x3_kernel<BF16><<<grid, kThreadsTC, Smem::kTotal, st>>>(tAh, tAl, tBh, tBl, g);
   SMX_LAUNCH_CHECK(BF16 ? "smx_gemm_bf16x3" : "smx_gemm_tf32x3");
   return SMX_OK;
@@ -422,6 +459,57 @@ extern "C" int smx_gemm_bf16x3(const uint16_t* A_hi, const uint16_t* A_lo, int64
   if (rc) return rc;
   return launch<true>(A_hi, A_lo, lda, B_hi, B_lo, ldb, M, N, K, D, ldd, bias, err, accumulate,
                       smx::as_stream(stream));
+}
+
+namespace {
+// D = sum over z of the split-K slices (fixed order) + bias (+ D)
+__global__ void splitk_reduce_kernel(const float* __restrict__ part, int nz, int M, int N, float* __restrict__ D,
+                                     int64_t ldd, const float* __restrict__ bias, int accumulate) {
+  const int64_t n = int64_t(M) * N;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t r = i / N, c = i - r * N;
+    float v = 0.f;
+    for (int z = 0; z < nz; ++z) v += part[z * n + r * N + c];
+    if (bias) v += bias[c];
+    float* d = D + r * ldd + c;
+    *d = v + (accumulate ? *d : 0.f);
+  }
+}
+
+int splitk_slices(int K, int splits) {
+  const int KT = (K + kBK - 1) / kBK;
+  const int per = (KT + splits - 1) / splits;
+  return (KT + per - 1) / per;
+}
+}  // namespace
+
+extern "C" size_t smx_gemm_tf32x3_splitk_workspace(int M, int N, int K, int splits) {
+  if (M <= 0 || N <= 0 || K <= 0 || splits < 1) return 0;
+  return size_t(splitk_slices(K, splits)) * size_t(M) * size_t(N) * sizeof(float);
+}
+
+extern "C" int smx_gemm_tf32x3_splitk(const float* A_hi, const float* A_lo, int64_t lda, const float* B_hi,
+                                      const float* B_lo, int64_t ldb, int M, int N, int K, float* D, int64_t ldd,
+                                      const float* bias, int accumulate, int splits, void* ws, size_t ws_bytes,
+                                      int* err, void* stream) {
+  SMX_REQUIRE(M >= 0 && N >= 0 && K >= 0 && lda >= K && ldb >= K && ldd >= N && splits >= 1 && splits <= 65535,
+              "smx_gemm_tf32x3_splitk: bad sizes");
+  if (M == 0 || N == 0) return SMX_OK;
+  SMX_REQUIRE(K >= 1 && A_hi && A_lo && B_hi && B_lo && D && err, "smx_gemm_tf32x3_splitk: null pointer");
+  if (splits == 1 || splitk_slices(K, splits) == 1)
+    return smx_gemm_tf32x3(A_hi, A_lo, lda, B_hi, B_lo, ldb, M, N, K, D, ldd, bias, accumulate, err, stream);
+  SMX_REQUIRE(ws && ws_bytes >= smx_gemm_tf32x3_splitk_workspace(M, N, K, splits),
+              "smx_gemm_tf32x3_splitk: workspace too small");
+  int rc = get_encode();
+  if (rc) return rc;
+  cudaStream_t st = smx::as_stream(stream);
+  float* part = static_cast<float*>(ws);
+  rc = launch<false>(A_hi, A_lo, lda, B_hi, B_lo, ldb, M, N, K, part, N, nullptr, err, 0, st, splits);
+  if (rc) return rc;
+  splitk_reduce_kernel<<<smx::grid_for(int64_t(M) * N, 256), 256, 0, st>>>(part, splitk_slices(K, splits), M, N, D,
+                                                                          ldd, bias, accumulate);
+  SMX_LAUNCH_CHECK("smx_gemm_tf32x3_splitk");
+  return SMX_OK;
 }
 
 extern "C" int smx_split_bf16(const float* src, int64_t rows, int64_t cols, int64_t lds, uint16_t* hi, uint16_t* lo,

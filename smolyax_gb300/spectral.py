@@ -303,6 +303,12 @@ class SpectralPlan:
             dCrev = torch.zeros(K, d_out, dtype=torch.float32, device=dev)
             nws = capi.size("smx_spectral_panel_t_workspace", ops["n_slots"], min(step, P))
             ws = torch.empty(max(nws, 1), dtype=torch.uint8, device=dev)
+            # the [K x d_out] product has few tiles and a long contraction over the
+            # points: split the contraction so that the slices fill the SMs
+            tiles = -(-K // 128) * -(-d_out // 128)
+            splits = max(1, min(64, (2 * ops["sms"]) // tiles))
+            nsk = capi.size("smx_gemm_tf32x3_splitk_workspace", K, d_out, min(step, P), splits)
+            wsk = torch.empty(max(nsk, 1), dtype=torch.uint8, device=dev)
             for i, p0 in enumerate(range(0, P, step)):
                 p1 = min(P, p0 + step)
                 n = p1 - p0
@@ -312,8 +318,8 @@ class SpectralPlan:
                      st)
                 gT[:, :n] = g32[p0:p1].t()
                 call("smx_split_tf32", ptr(gT), ldo, n, ldp, ptr(gTh), ptr(gTl), ldp, st)
-                call("smx_gemm_tf32x3", ptr(ATh), ptr(ATl), ldp, ptr(gTh), ptr(gTl), ldp, K, d_out, n,
-                     ptr(dCrev), d_out, None, 1 if i else 0, ptr(err), st)
+                call("smx_gemm_tf32x3_splitk", ptr(ATh), ptr(ATl), ldp, ptr(gTh), ptr(gTl), ldp, K, d_out, n,
+                     ptr(dCrev), d_out, None, 1 if i else 0, splits, ptr(wsk), nsk, ptr(err), st)
             n_lam = int(self.C64.shape[0])
             dC = torch.zeros(n_lam, d_out, dtype=torch.float64, device=dev)
             ent = ops["ent"]
