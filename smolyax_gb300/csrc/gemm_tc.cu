@@ -20,7 +20,11 @@
 namespace {
 
 constexpr int kBM = 128;
-constexpr int kBK = 32;  // fp32 elements per 128-byte row slice (64 for bf16)
+// K slice of one stage: kRowBytes per operand row (the TMA swizzle span), i.e.
+// kBK fp32 (2 kBK bf16) elements; smaller slices give more pipeline stages in
+// the same shared memory (more copies in flight against the L2 latency).
+constexpr int kRowBytes = 128;
+constexpr int kBK = kRowBytes / 4;
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on every wait
 
 __device__ __forceinline__ uint64_t global_ns() {
@@ -66,15 +70,16 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, in
       : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
-// 1024 bytes apart (tcgen05 descriptor format, version field = 1).
-__device__ __forceinline__ uint64_t make_desc_sw128(uint32_t saddr) {
+// Shared-memory matrix descriptor: K-major, kRowBytes swizzle (128 or 64
+// bytes), 8-row groups 8 * kRowBytes apart (tcgen05 descriptor format,
+// version field = 1; layout field 2 = SWIZZLE_128B, 4 = SWIZZLE_64B).
+__device__ __forceinline__ uint64_t make_desc_sw(uint32_t saddr) {
   uint64_t d = 0;
-  d |= uint64_t((saddr & 0x3FFFF) >> 4);        // start address
-  d |= uint64_t(1) << 16;                        // leading byte offset (unused for swizzled K-major)
-  d |= uint64_t(1024 >> 4) << 32;                // stride byte offset
-  d |= uint64_t(1) << 46;                        // version
-  d |= uint64_t(2) << 61;                        // SWIZZLE_128B
+  d |= uint64_t((saddr & 0x3FFFF) >> 4);          // start address
+  d |= uint64_t(1) << 16;                          // leading byte offset (unused for swizzled K-major)
+  d |= uint64_t((8 * kRowBytes) >> 4) << 32;       // stride byte offset
+  d |= uint64_t(1) << 46;                          // version
+  d |= uint64_t(kRowBytes == 128 ? 2 : 4) << 61;   // swizzle mode
   return d;
 }
 
@@ -109,12 +114,15 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 // Tiles: 128 x 128 outputs per CTA; the FP32 accumulator of the tensor cores
 // truncates when it adds, so one accumulator must not run over long
 // stretches of K: the MMA thread alternates between two accumulators in
-// tensor memory (columns [0,128) and [128,256)) every kChunk K-tiles, and the
+// tensor memory (columns [0,128) and [128,256)) every few K-tiles, and the
 // four drain warps add each finished accumulator into FP32 registers (one row
 // of 128 outputs per thread, round-to-nearest adds), then release it.
 constexpr int kBN = 128;
-constexpr int kStages = 3;
-constexpr int kChunk = 2;  // K-tiles (of 32) per accumulator use
+constexpr int kStages = 3 * 128 / kRowBytes;
+// K-tiles per accumulator use: 64 products for the 3xTF32 form (its error
+// bound), 256 for the split-BF16 form, whose error the 16-bit split sets
+constexpr int kChunkTf32 = 64 / kBK;
+constexpr int kChunkBf16 = 256 / (2 * kBK);
 constexpr int kThreadsTC = 192;  // warps 0-3 drain/epilogue, warp 4 TMA, warp 5 MMA
 
 struct Smem {
@@ -146,6 +154,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                        const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl, GemmArgs g) {
   constexpr int EK = BF16 ? 2 * kBK : kBK;  // elements per K-tile
+  constexpr int kChunk = BF16 ? kChunkBf16 : kChunkTf32;
   using L = Smem;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -239,10 +248,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
           const uint32_t b_hi = a_hi + 2 * L::kA;
           const uint32_t b_lo = b_hi + L::kB;
 #pragma unroll
-          for (int k8 = 0; k8 < 4; ++k8) {  // 32 bytes (8 tf32 or 16 bf16) of K per MMA
+          for (int k8 = 0; k8 < kRowBytes / 32; ++k8) {  // 32 bytes (8 tf32 or 16 bf16) of K per MMA
             const uint32_t off = k8 * 32;
-            const uint64_t dah = make_desc_sw128(a_hi + off), dal = make_desc_sw128(a_lo + off);
-            const uint64_t dbh = make_desc_sw128(b_hi + off), dbl = make_desc_sw128(b_lo + off);
+            const uint64_t dah = make_desc_sw(a_hi + off), dal = make_desc_sw(a_lo + off);
+            const uint64_t dbh = make_desc_sw(b_hi + off), dbl = make_desc_sw(b_lo + off);
             mma_op<BF16>(acc, dah, dbh, idesc, first ? 0u : 1u);
             first = false;
             mma_op<BF16>(acc, dah, dbl, idesc, 1u);
@@ -378,9 +387,9 @@ int make_map(CUtensorMap* tm, const void* ptr, int64_t rows, int64_t cols, int64
   cuuint32_t box[2] = {cuuint32_t(bf16 ? 2 * kBK : kBK), cuuint32_t(box_rows)};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = g_encode(tm, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
-                        const_cast<void*>(ptr), dims, strides, box, estr,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                        const_cast<void*>(ptr), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        kRowBytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return smx::set_error(SMX_ERR_CUDA, "cuTensorMapEncodeTiled failed");
   return SMX_OK;
 }
