@@ -378,21 +378,15 @@ class SpectralPlan:
         return self.tc_chunks(P) * (3 if scratch else 2)
 
     def _segments(self, n):
-        """Tape segments of one panel launch over n points: enough (point block,
-        segment) blocks for ~12 per SM, segments of >= 256 entries, each
-        starting at a depth-1 entry.  Returns (bounds on the device or None, count)."""
+        """Tape segments of one panel launch over n points (see segment_bounds).
+        Returns (bounds on the device or None, count)."""
         tc = self.tc
-        K, pos = tc["K"], tc["lvl1"]
-        n_pb = -(-int(n) // 128)
-        want = max(1, min(32, -(-12 * tc["sms"] // max(n_pb, 1)), K // 256, int(pos.size)))
+        want = segment_count(tc["K"], tc["lvl1"].size, n, tc["sms"])
         if want <= 1:
             return None, 1
         cache = tc.setdefault("segs", {})
         if want not in cache:
-            targets = (np.arange(1, want) * K) // want
-            b = pos[np.minimum(np.searchsorted(pos, targets), pos.size - 1)]
-            bounds = np.unique(np.concatenate([[0], b, [K]])).astype(np.int32)
-            cache[want] = torch.as_tensor(bounds, device=tc["tape"].device)
+            cache[want] = torch.as_tensor(segment_bounds(tc["lvl1"], tc["K"], want), device=tc["tape"].device)
         t = cache[want]
         return t, int(t.numel()) - 1
 
@@ -453,6 +447,24 @@ class SpectralPlan:
             call("smx_gemm_tf32x3", ptr(Ah), ptr(Al), lda, ptr(tc["Bh"]), ptr(tc["Bl"]), ldk, p1 - p0, d_out,
                  tc["K"], ptr(y[p0:p1]), d_out, ptr(tc["bias"]), 0, ptr(tc["err"]), st)
         return y
+
+
+def segment_count(K, n_lvl1, n_points, sms):
+    """Segments per panel launch: enough (segment, 128-point block) blocks for
+    ~12 per SM, at most 32 segments, segments of >= 256 entries on average, and
+    no more than there are depth-1 entries to start them."""
+    n_pb = max(-(-int(n_points) // 128), 1)
+    return max(1, min(32, -(-12 * int(sms) // n_pb), int(K) // 256, int(n_lvl1)))
+
+
+def segment_bounds(lvl1, K, want):
+    """Segment bounds [0, ..., K] (int32) near equal splits of the tape: every
+    bound but the last is the tape position of a depth-1 entry, so that each
+    segment holds whole subtrees (lvl1: sorted positions, lvl1[0] = 0)."""
+    lvl1 = np.asarray(lvl1)
+    targets = (np.arange(1, want) * int(K)) // want
+    b = lvl1[np.minimum(np.searchsorted(lvl1, targets), lvl1.size - 1)]
+    return np.unique(np.concatenate([[0], b, [int(K)]])).astype(np.int32)
 
 
 def _round4(v):

@@ -277,3 +277,39 @@ def test_panel_segments_equal_single_walk(bf16):
     seg, n_seg = sp._segments(P)
     if seg is not None:
         assert all(int(v) in lvl1 for v in seg.cpu().numpy()[:-1]) and int(seg[-1]) == K
+
+
+def test_blocked_tables_in_shared_memory_equal_global_tables():
+    """The blocked evaluator's per-block shared-memory copy of its tables gives
+    the same values, bit for bit, as reading the tables from global memory
+    (the path of plans whose tables do not fit beside the tile arrays)."""
+    import ctypes
+
+    import torch
+
+    from smolyax_gb300 import _capi, nodes
+
+    d, t = 60, 7.0
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    ip = _interp(node_gen=nodes.Leja(dim=d), k=k, t=t, d_out=1, f=fns.rational_vec(d, 1, seed=11))
+    sp = ip.spectral_plan()
+    b = sp.blocked
+    assert b is not None and b.n_ent > 0 and b.n_w > 0
+    P = 5000
+    x = torch.as_tensor(np.random.default_rng(12).uniform(-1, 1, (P, d)), device="cuda")
+    st = _capi.stream_ptr(torch.cuda.current_stream())
+    nws = _capi.size("smx_blocked_eval_workspace", ctypes.byref(b), P)
+    ws = torch.empty(max(nws, 1), dtype=torch.uint8, device="cuda")
+    out = []
+    n_ent = b.n_ent
+    try:
+        for ne in (n_ent, 0):  # n_ent = 0: sizes not given, tables read from global memory
+            b.n_ent = ne
+            y = torch.empty(P, 1, dtype=torch.float32, device="cuda")
+            _capi.call("smx_blocked_eval", ctypes.byref(b), _capi.ptr(x), P, d, _capi.ptr(y), _capi.ptr(ws), nws, st)
+            out.append(y)
+    finally:
+        b.n_ent = n_ent
+    assert torch.equal(out[0], out[1])
+    y64 = ip(x, precision="fp64")
+    assert (out[0].double() - y64).abs().max().item() <= 1e-6 * y64.abs().max().item()
