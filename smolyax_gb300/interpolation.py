@@ -82,6 +82,7 @@ class SmolyakBarycentricInterpolator:
             raise ValueError("precision must be 'fp64' or 'fp32'")
         self._precision = precision
         self._spectral = None
+        self._side_streams = {}  # device -> the two streams of chunked host-input evaluation
         self._d_in = len(k)
         self._d_out = int(d_out)
         self._node_gen = node_gen
@@ -355,7 +356,10 @@ class SmolyakBarycentricInterpolator:
         xd = torch.empty(Pn, self._d_in, dtype=torch.float64, device=dev)
         y = torch.empty(Pn, self._d_out, dtype=torch.float32, device=dev)
         cur = torch.cuda.current_stream(dev)
-        streams = [torch.cuda.Stream(device=dev) for _ in range(2)]
+        # two side streams, created once per device
+        streams = self._side_streams.get(dev)
+        if streams is None:
+            streams = self._side_streams[dev] = [torch.cuda.Stream(device=dev) for _ in range(2)]
         n_chunks = max(2, min(8, Pn // (_OVERLAP_MIN_ROWS // 2)))
         step = -(-Pn // n_chunks)
         for i, p0 in enumerate(range(0, Pn, step)):

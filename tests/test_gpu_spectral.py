@@ -313,3 +313,34 @@ def test_blocked_tables_in_shared_memory_equal_global_tables():
     assert torch.equal(out[0], out[1])
     y64 = ip(x, precision="fp64")
     assert (out[0].double() - y64).abs().max().item() <= 1e-6 * y64.abs().max().item()
+
+
+@pytest.mark.parametrize("P", [1, 130, 128 * 9 + 37, 128 * 70])
+def test_blocked_small_batches_split_over_blocks(P):
+    """With at most half as many 128-point tiles as SMs, each tile is shared by
+    several blocks (fixed-order sum of their partial results): same values as
+    one block per tile (no workspace) to FP32 rounding."""
+    import ctypes
+
+    import torch
+
+    from smolyax_gb300 import _capi, nodes
+
+    d, t = 40, 6.5
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    ip = _interp(node_gen=nodes.Leja(dim=d), k=k, t=t, d_out=1, f=fns.rational_vec(d, 1, seed=13))
+    sp = ip.spectral_plan()
+    b = sp.blocked
+    assert b is not None
+    x = torch.as_tensor(np.random.default_rng(14).uniform(-1, 1, (P, d)), device="cuda")
+    st = _capi.stream_ptr(torch.cuda.current_stream())
+    nws = _capi.size("smx_blocked_eval_workspace", ctypes.byref(b), P)
+    ws = torch.empty(nws, dtype=torch.uint8, device="cuda")
+    y_split = torch.empty(P, 1, dtype=torch.float32, device="cuda")
+    y_one = torch.empty(P, 1, dtype=torch.float32, device="cuda")
+    _capi.call("smx_blocked_eval", ctypes.byref(b), _capi.ptr(x), P, d, _capi.ptr(y_split), _capi.ptr(ws), nws, st)
+    _capi.call("smx_blocked_eval", ctypes.byref(b), _capi.ptr(x), P, d, _capi.ptr(y_one), None, 0, st)
+    y64 = ip(x, precision="fp64")
+    scale = y64.abs().max().item()
+    assert (y_split.double() - y_one.double()).abs().max().item() <= 2e-6 * scale
+    assert (y_split.double() - y64).abs().max().item() <= 1e-6 * scale
