@@ -474,9 +474,8 @@ __global__ void __launch_bounds__(kThr, 1)
   }
   const int64_t n_tiles = (P + 32 * NP - 1) / (32 * NP);
   const int64_t G = gridDim.x, rounds = n_tiles / G, rem = n_tiles - rounds * G;
-  // last round (the only one when there are fewer tiles than blocks): each
-  // remaining tile is shared by S blocks
-  const int S = rem > 0 && part != nullptr ? int(G / rem < kMaxSplit ? G / rem : kMaxSplit) : 1;
+  // last round: each remaining tile is shared by S blocks (S = 1 without a full round before it)
+  const int S = rounds > 0 && part != nullptr ? int(G / rem < kMaxSplit ? G / rem : kMaxSplit) : 1;
   const int64_t t = rem > 0 ? blockIdx.x / S : rem;
   const int64_t last = t < rem ? rounds * G + t : -1;  // this block's share of the last round
   double xpre[kHotPass];
@@ -656,14 +655,13 @@ extern "C" int smx_blocked_eval(const smx_blocked* b, const double* x, int64_t P
   // 128-point tiles (96-point tiles measured slower even where they cut the
   // last round of blocks: most per-item work does not scale with the points)
   const int64_t tiles = (P + 127) / 128;
-  // scratch of the last-round tile split: partial sums and counters; used
-  // after full rounds, or when there are at most half as many tiles as SMs
-  // (then every SM gets a block and each tile is shared by several)
-  const bool split = ws && ws_bytes >= smx_blocked_eval_workspace(b, P) && (tiles > sms || 2 * tiles <= sms);
-  const unsigned grid = static_cast<unsigned>(tiles < sms && !split ? tiles : sms);
+  const unsigned grid = static_cast<unsigned>(tiles < sms ? tiles : sms);
+  // scratch of the last-round tile split: partial sums and counters.  (Launches
+  // with fewer tiles than SMs are not split: their results must equal the
+  // multi-plan batch kernel's, which gives every tile to one block.)
   float* part = nullptr;
   unsigned int* ctr = nullptr;
-  if (split) {
+  if (ws && ws_bytes >= smx_blocked_eval_workspace(b, P) && tiles > sms) {
     part = static_cast<float*>(ws);
     ctr = reinterpret_cast<unsigned int*>(static_cast<char*>(ws) + size_t(sms) * 2 * kMaxSplit * kT * sizeof(float));
     if (cudaMemsetAsync(ctr, 0, size_t(sms) * sizeof(unsigned int), smx::as_stream(stream)) != cudaSuccess)
