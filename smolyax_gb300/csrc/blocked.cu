@@ -10,7 +10,10 @@
 //                         block, 16 FFMA per shared load), then
 //                         y += sum_s T[.][s] * phi_s(x)            (x read once)
 //   phase 3  per-point sum over the warps in a fixed order, y = c_0 + sum.
-// Coefficients and descriptors are read with warp-uniform loads (L1-resident);
+// Coefficients and descriptors are read with warp-uniform loads: from the
+// block's own copy of the tables in shared memory when they fit beside the
+// tile arrays (copied once per launch), else from global memory through L1.
+// The lane's 4 points are processed as two FP32 pairs (packed FFMA2/FMUL2).
 // x is streamed with L1-bypassing loads (a software L2 prefetch measured slower:
 // its per-row requests load the L1 pipeline more than the latency it hides).
 // The cancellation-free orthogonal form is summed with Kahan compensation per
