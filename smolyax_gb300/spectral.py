@@ -188,7 +188,7 @@ class SpectralPlan:
         slot = dsoff[idx[tr["dim"][ent]]] + tr["deg"][ent] - 1
         tape = (slot | (tr["level"][ent] << 16)).astype(np.int32)
         K = int(ent.size)
-        ldk = _round4(max(K, 1))
+        ldk = _round32(max(K, 1))  # 128-byte rows: whole cache lines per TMA row of B
         d_out = C32.shape[1]
         B = np.zeros((d_out, ldk), dtype=np.float32)
         B[:, :K] = C32[ent[::-1]].T  # the panel stores the entries in reversed pre-order
@@ -391,16 +391,15 @@ class SpectralPlan:
         return t, int(t.numel()) - 1
 
     def _bf16_operands(self):
-        """Coefficient matrix B split to BF16 hi/lo, rows padded to 8 entries."""
+        """Coefficient matrix B split to BF16 hi/lo (built on first use), rows
+        padded to 64 entries (128 bytes)."""
         tc = self.tc
         if "Bh16" not in tc:
-            d_out = int(tc["Bd"].shape[0])
-            ld16 = (tc["K"] + 7) // 8 * 8
-            Bd = torch.zeros(d_out, ld16, dtype=torch.float32, device=tc["Bd"].device)
-            Bd[:, : tc["ldk"]] = tc["Bd"]
-            Bh, Bl = torch.empty(d_out, ld16, dtype=torch.bfloat16, device=Bd.device), torch.empty(
-                d_out, ld16, dtype=torch.bfloat16, device=Bd.device)
-            call("smx_split_bf16", ptr(Bd), d_out, ld16, ld16, ptr(Bh), ptr(Bl), ld16,
+            d_out, K = int(tc["Bd"].shape[0]), tc["K"]
+            ld16 = (K + 63) // 64 * 64
+            Bh = torch.zeros(d_out, ld16, dtype=torch.bfloat16, device=tc["Bd"].device)
+            Bl = torch.zeros_like(Bh)
+            call("smx_split_bf16", ptr(tc["Bd"]), d_out, K, tc["ldk"], ptr(Bh), ptr(Bl), ld16,
                  capi.stream_ptr(torch.cuda.current_stream()))
             tc.update(Bh16=Bh, Bl16=Bl, ld16=ld16)
         return tc["Bh16"], tc["Bl16"], tc["ld16"]
