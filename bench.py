@@ -69,8 +69,8 @@ def ncu_traffic():
 
 
 class NvmlClockSampler:
-    """SM clock and clock-event reasons read through NVML (the driver's
-    libnvidia-ml, read-only queries) every ~1 ms while the timed region runs."""
+    """SM clock and clock-event reasons read through NVML (libnvidia-ml of the
+    NVIDIA GPU driver, read-only queries) every ~1 ms while the timed region runs."""
 
     REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
                0x80: "hw_power_brake_slowdown"}
@@ -131,7 +131,7 @@ class NvmlClockSampler:
 
 
 def ClockSampler(index):
-    """NVML sampler when the driver library loads, else nvidia-smi."""
+    """NVML sampler when libnvidia-ml loads, else nvidia-smi."""
     try:
         return NvmlClockSampler(index)
     except Exception:
