@@ -1,0 +1,90 @@
+"""Admission policy of the serving loop, on the CPU: a scheduler-only server
+(no streams or kernels; launches are recorded) over requests of known sizes."""
+import collections
+import threading
+
+import numpy as np
+import pytest
+
+from smolyax_gb300 import serving
+
+
+class _Scheduler(serving.Server):
+    """Server state without CUDA: request sizes and launch kinds are given,
+    launches are recorded instead of run."""
+
+    def __init__(self, budget, n_streams, kinds, bytes_per_point, failing=()):
+        self.budget = budget
+        self.in_use = 0
+        self.streams = ["s%d" % i for i in range(n_streams)]
+        self.free_streams = collections.deque(self.streams)
+        self.waiting = collections.deque()
+        self.inflight = []
+        self.lock = threading.Lock()
+        self.completed, self.rejected = [], []
+        self.batch_launches = self.launches = self.admitted = 0
+        self.ips = {name: type("IP", (), {"d_in": 3})() for name in kinds}
+        self._kinds, self._bpp, self._failing = kinds, bytes_per_point, set(failing)
+        self.launched = []
+
+    def request_bytes(self, req):
+        return self._bpp[req.name] * req.points
+
+    def _kind(self, req):
+        return self._kinds[req.name]
+
+    def _launch_batch(self, kind, batch, stream, now):
+        self.launched.append((kind, [r.id for r, _ in batch], stream))
+
+    def _launch_single(self, req, nb, stream, now):
+        if req.name in self._failing:
+            raise RuntimeError("the plan cannot serve this request")
+        self.launched.append((None, [req.id], stream))
+
+
+def _req(name, points, op="eval"):
+    return serving.Request(name, np.zeros((points, 3)), op=op)
+
+
+def test_over_budget_request_is_rejected_and_the_rest_served():
+    s = _Scheduler(budget=1000, n_streams=4, kinds={"a": None}, bytes_per_point={"a": 10})
+    big, small = s.submit(_req("a", 101)), s.submit(_req("a", 5))
+    s._admit()
+    assert big.error is not None and big.done.is_set() and big in s.rejected
+    assert [ids for _, ids, _ in s.launched] == [[small.id]]
+    assert s.in_use == 50
+
+
+def test_requests_wait_in_order_at_the_budget():
+    s = _Scheduler(budget=1000, n_streams=8, kinds={"a": None}, bytes_per_point={"a": 10})
+    r = [s.submit(_req("a", n)) for n in (60, 30, 20, 5)]
+    s._admit()
+    # 600 + 300 fit; the third (200) does not, and the fourth may not overtake it
+    assert [ids for _, ids, _ in s.launched] == [[r[0].id], [r[1].id]]
+    assert list(s.waiting) == [r[2], r[3]] and s.in_use == 900
+
+
+def test_merged_launch_per_kind_and_stream_limit():
+    s = _Scheduler(budget=10**9, n_streams=2, kinds={"b": "blocked", "c": None, "t": "stream"},
+                   bytes_per_point={"b": 1, "c": 1, "t": 1})
+    r = [s.submit(_req(n, 10)) for n in ("b", "b", "t", "b", "c")]
+    s._admit()
+    # two streams: one merged launch of the three 'b' requests, one of 't'; 'c' waits for a stream
+    kinds = {k: ids for k, ids, _ in s.launched}
+    assert kinds == {"blocked": [r[0].id, r[1].id, r[3].id], "stream": [r[2].id]}
+    assert list(s.waiting) == [r[4]] and not s.free_streams
+
+
+def test_failed_launch_returns_its_stream_and_memory():
+    s = _Scheduler(budget=1000, n_streams=1, kinds={"f": None}, bytes_per_point={"f": 10}, failing={"f"})
+    bad = s.submit(_req("f", 10, op="grad"))
+    s._admit()
+    assert bad.error and bad in s.rejected and s.in_use == 0 and list(s.free_streams) == ["s0"]
+
+
+def test_submit_checks_name_and_width():
+    s = _Scheduler(budget=1000, n_streams=1, kinds={"a": None}, bytes_per_point={"a": 1})
+    with pytest.raises(KeyError):
+        s.submit(_req("zz", 1))
+    with pytest.raises(ValueError):
+        s.submit(serving.Request("a", np.zeros((2, 4))))
