@@ -344,3 +344,61 @@ def test_blocked_small_batches_one_block_per_tile(P):
     scale = y64.abs().max().item()
     assert torch.equal(y_split, y_one)
     assert (y_split.double() - y64).abs().max().item() <= 1e-6 * scale
+
+
+@pytest.mark.parametrize("d", [31, 40])
+def test_blocked_row_pitch_and_alignment(d):
+    """x rows with any pitch and 8-byte alignment: the evaluator's 32-byte,
+    16-byte and scalar load paths give the same values, bit for bit."""
+    import ctypes
+
+    import torch
+
+    from smolyax_gb300 import _capi, nodes
+
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    ip = _interp(node_gen=nodes.Leja(dim=d), k=k, t=6.0, d_out=1, f=fns.rational_vec(d, 1, seed=15))
+    sp = ip.spectral_plan()
+    b = sp.blocked
+    assert b is not None
+    P = 128 * 5 + 3
+    x0 = np.random.default_rng(16).uniform(-1, 1, (P, d))
+    st = _capi.stream_ptr(torch.cuda.current_stream())
+    outs = []
+    # (row pitch, first column): pitch % 4 == 0 and 32-byte rows (32-byte loads),
+    # 16-byte rows (16-byte loads), odd pitch or 8-byte offset (scalar loads)
+    for cols, c0 in ((d, 0), (44, 0), (44, 2), (42, 0), (43, 0), (44, 1)):
+        buf = np.zeros((P, cols))
+        buf[:, c0:c0 + d] = x0
+        xb = torch.as_tensor(buf, device="cuda")
+        y = torch.empty(P, 1, dtype=torch.float32, device="cuda")
+        _capi.call("smx_blocked_eval", ctypes.byref(b), ctypes.c_void_p(xb.data_ptr() + 8 * c0), P, cols,
+                   _capi.ptr(y), None, 0, st)
+        outs.append(y)
+    for y in outs[1:]:
+        assert torch.equal(outs[0], y)
+    y64 = ip(torch.as_tensor(x0, device="cuda"), precision="fp64")
+    assert (outs[0].double() - y64).abs().max().item() <= 1e-6 * y64.abs().max().item()
+
+
+def test_fp32_and_bf16x3_input_edge_cases():
+    """Empty and 1-D inputs and a wrong width on the mixed-precision paths, as
+    the reference's __call__ handles them (interpolation.py:253-262)."""
+    from smolyax_gb300 import nodes
+
+    d = 10
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    one = _interp(node_gen=nodes.Leja(dim=d), k=k, t=5.0, d_out=1, f=fns.rational(d, seed=0))
+    many = _interp(node_gen=nodes.GaussHermite(dim=d), k=k, t=5.0, d_out=20, f=fns.exponential(d, 20, seed=0))
+    for ip, precs in ((one, ("fp32",)), (many, ("fp32", "bf16x3"))):
+        for prec in precs:
+            y0 = ip(np.zeros((0, d)), precision=prec)
+            assert tuple(y0.shape) == (0, ip.d_out)
+            x1 = np.random.default_rng(17).normal(size=d) * 0.5
+            y1 = ip(x1, precision=prec)
+            assert tuple(y1.shape) == (1, ip.d_out)
+            y64 = ip(x1[None, :]).cpu().numpy()
+            tol = 1e-4 if prec == "bf16x3" else 2e-6
+            assert np.max(np.abs(y1.cpu().numpy() - y64)) <= tol * max(1.0, np.max(np.abs(y64)))
+            with pytest.raises(AssertionError):
+                ip(np.zeros((3, d + 1)), precision=prec)
