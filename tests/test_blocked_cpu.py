@@ -41,6 +41,12 @@ def test_blocked_tables_match_direct_sum(d, t, fam_id):
     node = lay["node"].reshape(-1, 12)
     assert np.array_equal(hot, np.nonzero(node[:, 1] > 0)[0])
     assert lay["smem"] == (lay["n_hs"] + lay["k_c"]) * 512 + 2 * N_WARPS * 512
+    # the kernel's 16- and 32-byte x loads of a "fast" group start at its first
+    # dimension: it must be a multiple of 4, the dimensions consecutive, degree 1
+    grp = lay["grp"].reshape(-1, 12)
+    for g in grp[grp[:, 2] != 0]:
+        dims, degs = g[4:8], g[8:12]
+        assert dims[0] % 4 == 0 and np.array_equal(dims, dims[0] + np.arange(4)) and np.all(degs == 1)
 
 
 def test_blocked_balance_at_high_dimension():
