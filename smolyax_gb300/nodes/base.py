@@ -1,7 +1,10 @@
-"""Node-generator interface (mirrors ``src/smolyax/nodes/base.py``).
+"""Node-generator interface (the API of ``src/smolyax/nodes/base.py``).
 
-Node generation is FP64 set-up data computed on the host, exactly as in the
-reference; the device only ever sees the resulting node tables.
+Node rules are FP64 set-up data computed on the host; the device only sees
+the node and weight tables built from them.  A one-dimensional rule
+(`Generator1D`) yields the first n+1 nodes of its sequence, maps points
+between its reference domain and its custom domain, samples its measure and
+gives quadrature weights; a `Generator` holds one rule per dimension.
 """
 from __future__ import annotations
 
@@ -12,7 +15,7 @@ import numpy as np
 
 
 class Generator1D(ABC):
-    """One-dimensional node sequence (``base.py:8-128``)."""
+    """One-dimensional node sequence (interface of ``base.py:8-128``)."""
 
     def __init__(self, is_nested: bool) -> None:
         self._is_nested = bool(is_nested)
@@ -23,7 +26,7 @@ class Generator1D(ABC):
 
     @abstractmethod
     def __call__(self, n: int) -> np.ndarray:
-        """The first n+1 nodes."""
+        """The first n+1 nodes on the custom domain."""
 
     @abstractmethod
     def scale(self, x):
@@ -35,15 +38,15 @@ class Generator1D(ABC):
 
     @abstractmethod
     def get_random(self, n: int = 1):
-        """Samples from the measure associated with the domain."""
+        """n samples of the measure associated with the domain."""
 
     @abstractmethod
     def get_quadrature_weights(self, n: int) -> np.ndarray:
         """Quadrature weights of the first n+1 nodes."""
 
     def spectral_map(self):
-        """(family, a, b): orthogonal family used by the mixed-precision path and the
-        affine map z = a*x + b to its reference variable.  Generators that do not
+        """(family, a, b): the orthogonal polynomial family of the mixed-precision
+        path and the affine map z = a*x + b to its variable.  Rules that do not
         override it get Legendre polynomials on the hull of their first nodes."""
         pts = np.asarray(self(8), dtype=float)
         lo, hi = float(pts.min()), float(pts.max())
@@ -54,17 +57,24 @@ class Generator1D(ABC):
 
 
 class Generator:
-    """Container of per-dimension generators (``base.py:131-262``)."""
+    """One rule per dimension (interface of ``base.py:131-262``).
+
+    All rules must agree on nestedness (AssertionError otherwise), since the
+    index set and the node-reuse cache depend on it."""
 
     def __init__(self, node_gens: List[Generator1D]):
-        assert all(g.is_nested == node_gens[0].is_nested for g in node_gens)
-        self._gens = list(node_gens)
-        self._is_nested = node_gens[0].is_nested
-        self._dim = len(node_gens)
+        gens = list(node_gens)
+        if not gens:
+            raise AssertionError("a generator needs at least one one-dimensional rule")
+        nested = {g.is_nested for g in gens}
+        if len(nested) != 1:
+            raise AssertionError("mixing nested and non-nested rules in one generator is not supported")
+        self._gens = gens
+        self._is_nested = nested.pop()
 
     @property
     def dim(self) -> int:
-        return self._dim
+        return len(self._gens)
 
     @property
     def is_nested(self) -> bool:
@@ -74,26 +84,35 @@ class Generator:
         return self._gens[i]
 
     def __iter__(self) -> Iterator[Generator1D]:
-        for i in range(self._dim):
-            yield self._gens[i]
+        return iter(list(self._gens))
 
     def __len__(self) -> int:
-        return self._dim
+        return len(self._gens)
 
     def get_random(self, n: int = 0):
-        """n = 0 returns one point of shape (d,), otherwise (n, d)."""
-        if n == 0:
-            return np.squeeze([g.get_random() for g in self._gens])
-        return np.array([g.get_random(n) for g in self._gens]).T
+        """Samples of the product measure: n = 0 gives one point of shape (d,),
+        n >= 1 gives an array of shape (n, d)."""
+        rows = max(int(n), 1)
+        pts = np.empty((rows, self.dim))
+        for j, g in enumerate(self._gens):
+            pts[:, j] = np.reshape(g.get_random(rows), rows)
+        if n:
+            return pts
+        return pts[0] if self.dim > 1 else pts[0, 0]
+
+    def _per_column(self, x, method):
+        x = np.asarray(x)
+        if x.ndim == 0 or x.shape[-1] != self.dim:
+            raise AssertionError("points of shape %s do not have %d coordinates" % (x.shape, self.dim))
+        out = np.empty(x.shape)
+        for j, g in enumerate(self._gens):
+            out[..., j] = getattr(g, method)(x[..., j])
+        return out
 
     def scale(self, x):
-        assert x.shape[-1] == self.dim
-        if x.ndim == 1:
-            return np.array([g.scale(v) for g, v in zip(self._gens, x)])
-        return np.array([g.scale(col) for g, col in zip(self._gens, x.T)]).T
+        """Reference domain -> custom domain, coordinate by coordinate."""
+        return self._per_column(x, "scale")
 
     def scale_back(self, x):
-        assert x.shape[-1] == self.dim
-        if x.ndim == 1:
-            return np.array([g.scale_back(v) for g, v in zip(self._gens, x)])
-        return np.array([g.scale_back(col) for g, col in zip(self._gens, x.T)]).T
+        """Custom domain -> reference domain, coordinate by coordinate."""
+        return self._per_column(x, "scale_back")

@@ -1,152 +1,144 @@
-"""Leja nodes (mirrors ``src/smolyax/nodes/leja.py``)."""
-from __future__ import annotations
+"""Leja nodes (the API of ``src/smolyax/nodes/leja.py``).
 
-from functools import lru_cache
+The nested Leja sequence on [-1, 1] starts 0, 1, -1, 1/sqrt(2), -1/sqrt(2);
+after that, node j is the mirror -node[j-1] for even j and
+sqrt((node[(j+1)/2] + 1) / 2) for odd j (``leja.py:17,48-57``).  The same
+sequence gives the same interpolant, so these values are reproduced exactly.
+Custom domains are reached by an affine map of each coordinate
+(``nodes/_box.py``).
+"""
+from __future__ import annotations
 
 import numpy as np
 
+from ._box import UNIT_INTERVAL, as_box, map_points
 from .base import Generator, Generator1D
 
-
-class _LejaSequence:
-    """Leja points on [-1, 1]: 0, 1, -1, 1/sqrt2, -1/sqrt2, then x_j = -x_{j-1}
-    for even j and sqrt((x_{(j+1)/2} + 1) / 2) for odd j (``leja.py:17,48-57``)."""
-
-    values = np.array([0.0, 1.0, -1.0, 1 / np.sqrt(2), -1 / np.sqrt(2)])
-
-    @classmethod
-    def upto(cls, n: int) -> np.ndarray:
-        have = cls.values.shape[0]
-        if n >= have:
-            ext = np.empty(n + 1)
-            ext[:have] = cls.values
-            for j in range(have, n + 1):
-                ext[j] = -ext[j - 1] if j % 2 == 0 else np.sqrt((ext[(j + 1) // 2] + 1) / 2)
-            cls.values = ext
-        return cls.values[: n + 1]
+_SEQUENCE = np.array([0.0, 1.0, -1.0, 1 / np.sqrt(2), -1 / np.sqrt(2)])
 
 
-def _affine(x, src, dst):
-    """Map x from interval src to interval dst in the reference's two-step form."""
-    x = (x - src[0]) / (src[1] - src[0])
-    return x * (dst[1] - dst[0]) + dst[0]
+def leja_points(n: int) -> np.ndarray:
+    """The first n+1 points of the Leja sequence on [-1, 1] (a copy)."""
+    global _SEQUENCE
+    have = _SEQUENCE.size
+    if n >= have:
+        grown = np.concatenate([_SEQUENCE, np.zeros(n + 1 - have)])
+        for j in range(have, n + 1):
+            grown[j] = np.sqrt((grown[(j + 1) // 2] + 1) / 2) if j & 1 else -grown[j - 1]
+        _SEQUENCE = grown
+    return _SEQUENCE[: n + 1].copy()
+
+
+def _uniform_quadrature(n: int) -> np.ndarray:
+    """Weights q with sum_j q_j p(x_j) = (1/2) int_{-1}^{1} p for every
+    polynomial p of degree <= n, x = the first n+1 Leja points (``leja.py:83-93``):
+    the moment equations sum_j q_j x_j^i = mean of x^i over [-1, 1], i = 0..n."""
+    pts = leja_points(n)
+    powers = np.arange(n + 1)
+    moments = np.where(powers % 2 == 0, 1.0 / (powers + 1.0), 0.0)
+    return np.linalg.solve(pts[None, :] ** powers[:, None], moments)
 
 
 class Leja1D(Generator1D):
-    """Nested Leja nodes on [-1, 1] or a custom interval."""
+    """Nested Leja nodes on [-1, 1], or mapped to the interval `domain`."""
 
     def __init__(self, domain=None) -> None:
         super().__init__(is_nested=True)
         self._domain = None if domain is None else np.asarray(domain)
-        self._ref = None if domain is None else (-1, 1)
-        self._nodes = lru_cache(maxsize=None)(self._make_nodes)
-        self._qw = lru_cache(maxsize=None)(self._make_qw)
+        self._nodes = {}
+        self._weights = {}
 
     @property
     def domain(self):
         return self._domain
 
-    def _make_nodes(self, n):
-        return self.scale(_LejaSequence.upto(n).copy())
-
-    def _make_qw(self, n):
-        # Vandermonde solve against the moments of the uniform probability
-        # measure on [-1, 1] (``leja.py:83-93``); not rescaled by the domain.
-        pts = _LejaSequence.upto(n)
-        vm = np.vstack([pts**i for i in range(n + 1)])
-        rhs = np.array([(1 + (-1) ** i) / (2.0 * (i + 1)) for i in range(n + 1)])
-        return np.linalg.solve(vm, rhs)
-
     def __call__(self, n: int) -> np.ndarray:
-        return self._nodes(int(n))
+        n = int(n)
+        if n not in self._nodes:
+            self._nodes[n] = self.scale(leja_points(n))
+        return self._nodes[n]
 
     def get_quadrature_weights(self, n: int) -> np.ndarray:
-        return self._qw(int(n))
+        """Weights of the uniform probability measure on the reference interval
+        (they do not depend on the domain)."""
+        n = int(n)
+        if n not in self._weights:
+            self._weights[n] = _uniform_quadrature(n)
+        return self._weights[n]
 
     def scale(self, x, d1=None, d2=None):
-        d1 = self._ref if d1 is None else d1
-        d2 = self._domain if d2 is None else d2
-        assert (d1 is None) == (d2 is None)
-        if d1 is None:
+        """Affine map from interval d1 (default [-1, 1]) to d2 (default: the domain).
+        Without a domain and without explicit intervals, x is returned as is."""
+        src = d1 if d1 is not None else (None if self._domain is None else UNIT_INTERVAL)
+        dst = d2 if d2 is not None else self._domain
+        if src is None and dst is None:
             return x
-        d1, d2 = np.squeeze(d1), np.squeeze(d2)
-        assert d1.shape == d2.shape == (2,), f"shapes {d1.shape} and {d2.shape} do not match (2, )"
-        assert d1[0] < d1[1]
-        assert d2[0] < d2[1]
-        shape = x.shape
-        x = np.squeeze(x)
-        assert x.ndim <= 1
-        lo_ok = (x >= d1[0]) | np.isclose(x, d1[0])
-        hi_ok = (x <= d1[1]) | np.isclose(x, d1[1])
-        assert np.all(lo_ok), f"Assertion failed: Some values are below lower bounds\n{x[~lo_ok]}"
-        assert np.all(hi_ok), f"Assertion failed: Some values are above upper bounds\n{x[~hi_ok]}"
-        return _affine(x, d1, d2).reshape(shape)
+        if src is None or dst is None:
+            raise AssertionError("Leja1D.scale: a source interval needs a target interval and vice versa")
+        if as_box(src).shape[0] != 1 or as_box(dst).shape[0] != 1:
+            raise AssertionError("Leja1D.scale: intervals must be single (lower, upper) pairs")
+        return map_points(x, src, dst)
 
     def scale_back(self, x):
-        return self.scale(x, d1=self._domain, d2=self._ref)
+        """Domain -> [-1, 1]."""
+        return self.scale(x, d1=self._domain, d2=None if self._domain is None else UNIT_INTERVAL)
 
     def get_random(self, n: int = 1):
-        return self.scale(np.random.uniform(-1, 1, n))
+        """n points uniform on the domain (numpy's global generator)."""
+        return self.scale(np.random.uniform(-1.0, 1.0, n))
 
     def spectral_map(self):
         if self._domain is None:
             return ("legendre", 1.0, 0.0)
-        lo, hi = float(self._domain[0]), float(self._domain[1])
+        lo, hi = (float(v) for v in np.ravel(self._domain)[:2])
         a = 2.0 / (hi - lo)
         return ("legendre", a, -1.0 - a * lo)
 
     def __repr__(self) -> str:
-        return f"Leja (domain = {self._domain})"
+        where = "[-1, 1]" if self._domain is None else str(np.ravel(self._domain).tolist())
+        return "Leja1D(domain=%s)" % where
 
 
 class Leja(Generator):
-    """Leja nodes in every dimension, optionally on per-dimension intervals."""
+    """Leja nodes in every dimension: give `dim` for [-1, 1]^dim, or `domains`
+    (one (lower, upper) pair per dimension)."""
 
     def __init__(self, *, domains=None, dim: int = None):
-        self._domains = None
-        self._refs = None
         if domains is not None:
-            Generator.__init__(self, [Leja1D(dom) for dom in domains])
-            self._domains = np.asarray(domains)
-            self._refs = np.array([[-1, 1]] * len(domains))
+            boxes = as_box(domains, "Leja domains")
+            super().__init__([Leja1D(row) for row in np.asarray(domains)])
+            self._domains = boxes
         elif dim is not None:
-            Generator.__init__(self, [Leja1D()] * dim)
+            super().__init__([Leja1D() for _ in range(int(dim))])
+            self._domains = None
         else:
-            raise ValueError("Must specify one of 'domains' or 'dim'.")
+            raise ValueError("Leja needs either `dim` or `domains`")
+
+    def _resolve(self, d1, d2, forward):
+        unit = None if self._domains is None else np.repeat(UNIT_INTERVAL, self.dim, axis=0)
+        src = d1 if d1 is not None else (unit if forward else self._domains)
+        dst = d2 if d2 is not None else (self._domains if forward else unit)
+        return src, dst
+
+    def _map(self, x, src, dst):
+        if src is None and dst is None:
+            return x
+        if src is None or dst is None:
+            raise AssertionError("Leja.scale: a source box needs a target box and vice versa")
+        return map_points(x, src, dst)
 
     def scale(self, x, d1=None, d2=None):
-        d1 = self._refs if d1 is None else d1
-        d2 = self._domains if d2 is None else d2
-        assert (d1 is None) == (d2 is None)
-        if d1 is None:
-            return x
-        d1, d2 = np.asarray(d1), np.asarray(d2)
-        assert d1.shape == d2.shape, f"shapes {d1.shape} and {d2.shape} do not match"
-        if d1.ndim == 1:
-            d1, d2 = d1.reshape(1, 2), d2.reshape(1, 2)
-        d = d1.shape[0]
-        for i in range(d):
-            assert d1[i, 0] < d1[i, 1]
-            assert d2[i, 0] < d2[i, 1]
-        x = np.asarray(x)
-        shape = x.shape
-        if shape == ():
-            x = np.array([[x]])
-        elif x.ndim == 1:
-            x = x.reshape((1, len(x))) if x.shape[0] == d else x.reshape((len(x), 1))
-        lo_ok = (x >= d1[:, 0]) | np.isclose(x, d1[:, 0])
-        hi_ok = (x <= d1[:, 1]) | np.isclose(x, d1[:, 1])
-        assert np.all(lo_ok), f"Assertion failed: Some values are below lower bounds\n{x[~lo_ok]}"
-        assert np.all(hi_ok), f"Assertion failed: Some values are above upper bounds\n{x[~hi_ok]}"
-        assert x.ndim == 2 and x.shape[1] == d1.shape[0] == d2.shape[0]
-        x = (x - d1[:, 0]) / (d1[:, 1] - d1[:, 0])
-        x = x * (d2[:, 1] - d2[:, 0]) + d2[:, 0]
-        return x.reshape(shape)
+        """Affine map of each coordinate from box d1 (default [-1, 1]^d) to box
+        d2 (default: the domains); x has shape (d,) or (n, d)."""
+        src, dst = self._resolve(d1, d2, forward=True)
+        return self._map(x, src, dst)
 
     def scale_back(self, x):
-        return self.scale(x, d1=self._domains, d2=self._refs)
+        """Domains -> [-1, 1]^d."""
+        src, dst = self._resolve(None, None, forward=False)
+        return self._map(x, src, dst)
 
     def __repr__(self) -> str:
-        if self._domains is not None:
-            return f"Leja (d = {self.dim}, domains = {self._domains.tolist()})"
-        return f"Leja (d = {self.dim})"
+        if self._domains is None:
+            return "Leja(dim=%d)" % self.dim
+        return "Leja(dim=%d, domains=%s)" % (self.dim, self._domains.tolist())
