@@ -235,10 +235,20 @@ __device__ __forceinline__ void kahan_add(float& sum, float& comp, float v) {
   sum = t;
 }
 
+// x coordinate in FP32; infinities become NaN, so that a non-finite
+// coordinate makes the point's value NaN as in the FP64 path (whose
+// barycentric weights 1/(x - node) then vanish and normalise to 0/0).
+__device__ __forceinline__ float x32(double v) {
+  const float f = static_cast<float>(v);
+  return fabsf(f) == __int_as_float(0x7f800000) ? __int_as_float(0x7fc00000) : f;
+}
+
 __constant__ float c_alpha[2][kMaxRec];
 __constant__ float c_beta[2][kMaxRec];
 
-// s[q] += sum over the run's slots of coef * row value.
+// s[q] = sum over the run's slots of coef * row value (runs are at most 32
+// slots long, so each is a short FP32 chain; callers add the run sums with
+// compensation).
 template <int DO>
 __device__ __forceinline__ void dot_run(const float* __restrict__ Rw, const float* __restrict__ coef, int4 r,
                                         int dstride, int o0, float (&s)[DO]) {
@@ -256,8 +266,10 @@ __device__ __forceinline__ void dot_run(const float* __restrict__ Rw, const floa
       s0 = fmaf(c.z, t.z, s0);
       s1 = fmaf(c.w, t.w, s1);
     }
-    s[0] += s0 + s1;
+    s[0] = s0 + s1;
   } else {
+#pragma unroll
+    for (int q = 0; q < DO; ++q) s[q] = 0.f;
     const float* Cb = coef + r.z + o0;
     for (int k = 0; k < n4; ++k) {
       const float4 t = T[k];
@@ -295,7 +307,7 @@ __device__ __forceinline__ void spectral_eval_tile(const SpecArgs& a, const doub
   for (int h = seg; h < a.n_hot_dims; h += kSeg) {
     const int dim = a.hot_dim[h], g = a.hot_deg[h], so = a.hot_soff[h];
     const int fm = a.fam[dim];
-    const float z = fmaf(a.fam_a[dim], float(xp[dim]), a.fam_b[dim]);
+    const float z = fmaf(a.fam_a[dim], x32(xp[dim]), a.fam_b[dim]);
     float pm1 = 0.f, pc = 1.f;
     for (int n = 0; n < g; ++n) {
       const float pn = c_alpha[fm][n] * z * pc - c_beta[fm][n] * pm1;
@@ -338,12 +350,20 @@ __device__ __forceinline__ void spectral_eval_tile(const SpecArgs& a, const doub
         }
       }
       if (nd.y >= 0) Rw[nd.y] = v;
-      float s[DO];
+      float s[DO], sc[DO];
 #pragma unroll
-      for (int q = 0; q < DO; ++q) s[q] = (q < a.dout - o0) ? __ldg(a.node_c + size_t(i) * a.dstride + o0 + q) : 0.f;
-      for (int r = nd.z; r < nd.w; ++r) dot_run<DO>(Rw, a.coef, __ldg(a.run + r), a.dstride, o0, s);
+      for (int q = 0; q < DO; ++q) {
+        s[q] = (q < a.dout - o0) ? __ldg(a.node_c + size_t(i) * a.dstride + o0 + q) : 0.f;
+        sc[q] = 0.f;
+      }
+      for (int r = nd.z; r < nd.w; ++r) {
+        float t[DO];
+        dot_run<DO>(Rw, a.coef, __ldg(a.run + r), a.dstride, o0, t);
 #pragma unroll
-      for (int q = 0; q < DO; ++q) kahan_add(acc[q], comp[q], v * s[q]);
+        for (int q = 0; q < DO; ++q) kahan_add(s[q], sc[q], t[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < DO; ++q) kahan_add(acc[q], comp[q], v * (s[q] - sc[q]));
     }
   }
   __syncthreads();  // prefix products complete
@@ -386,10 +406,10 @@ __device__ __forceinline__ void spectral_eval_tile(const SpecArgs& a, const doub
         u0 = fmaf(c2.x, t.z, u0); u1 = fmaf(c2.y, t.z, u1); u2 = fmaf(c2.z, t.z, u2); u3 = fmaf(c2.w, t.z, u3);
         u0 = fmaf(c3.x, t.w, u0); u1 = fmaf(c3.y, t.w, u1); u2 = fmaf(c3.z, t.w, u2); u3 = fmaf(c3.w, t.w, u3);
       }
-      float v = fmaf(ca.x, float(x0), cb.x) * u0;
-      v = fmaf(fmaf(ca.y, float(x1), cb.y), u1, v);
-      v = fmaf(fmaf(ca.z, float(x2), cb.z), u2, v);
-      v = fmaf(fmaf(ca.w, float(x3), cb.w), u3, v);
+      float v = fmaf(ca.x, x32(x0), cb.x) * u0;
+      v = fmaf(fmaf(ca.y, x32(x1), cb.y), u1, v);
+      v = fmaf(fmaf(ca.z, x32(x2), cb.z), u2, v);
+      v = fmaf(fmaf(ca.w, x32(x3), cb.w), u3, v);
       bsum += v;
       if (((bi - b0) & 3) == 3) {
         kahan_add(acc[0], comp[0], bsum);
@@ -423,7 +443,7 @@ __device__ __forceinline__ void spectral_eval_tile(const SpecArgs& a, const doub
         xn = xp[cg.x];
       }
       const int fm = cur.w >> 8;
-      const float z = fmaf(ab.x, float(xv), ab.y);
+      const float z = fmaf(ab.x, x32(xv), ab.y);
       float pm1 = 0.f, pc = 1.f;
       int gcur = 0;
       for (int r = cur.y; r < cur.z; ++r) {
@@ -435,8 +455,6 @@ __device__ __forceinline__ void spectral_eval_tile(const SpecArgs& a, const doub
           ++gcur;
         }
         float s[DO];
-#pragma unroll
-        for (int q = 0; q < DO; ++q) s[q] = 0.f;
         dot_run<DO>(Rw, a.coef, rr, a.dstride, o0, s);
 #pragma unroll
         for (int q = 0; q < DO; ++q) blk[q] = fmaf(pc, s[q], blk[q]);
@@ -781,7 +799,7 @@ __global__ void __launch_bounds__(128) panel_basis_kernel(int n_dims, const int3
   for (int h = 0; h < n_dims; ++h) {
     const int dim = dims[h], g = dmax[h], so = dsoff[h];
     const int fm = fam[dim];
-    const float z = fmaf(fam_a[dim], float(xp[dim]), fam_b[dim]);
+    const float z = fmaf(fam_a[dim], x32(xp[dim]), fam_b[dim]);
     float pm1 = 0.f, pc = 1.f;
     for (int n = 0; n < g; ++n) {
       const float pn = c_alpha[fm][n] * z * pc - c_beta[fm][n] * pm1;
@@ -824,7 +842,7 @@ __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32
     for (int h = 0; h < n_dims; ++h) {
       const int dim = dims[h], g = dmax[h], so = dsoff[h];
       const int fm = fam[dim];
-      const float z = fmaf(fam_a[dim], float(xp[dim]), fam_b[dim]);
+      const float z = fmaf(fam_a[dim], x32(xp[dim]), fam_b[dim]);
       float pm1 = 0.f, pc = 1.f;
       for (int n = 0; n < g; ++n) {
         const float pn = c_alpha[fm][n] * z * pc - c_beta[fm][n] * pm1;
@@ -976,7 +994,7 @@ __device__ __forceinline__ void basis_row(int n_dims, const int32_t* __restrict_
   for (int h = 0; h < n_dims; ++h) {
     const int dim = dims[h], g = dmax[h], so = dsoff[h];
     const int fm = fam[dim];
-    const float z = fmaf(fam_a[dim], float(xp[dim]), fam_b[dim]);
+    const float z = fmaf(fam_a[dim], x32(xp[dim]), fam_b[dim]);
     float pm1 = 0.f, pc = 1.f;
     for (int n = 0; n < g; ++n) {
       const float pn = c_alpha[fm][n] * z * pc - c_beta[fm][n] * pm1;
@@ -1134,7 +1152,7 @@ __global__ void __launch_bounds__(kVjpTP) vjp_x_kernel(int n_dims, const int32_t
   for (int h = 0; h < n_dims; ++h) {
     const int dim = dims[h], g = dmax[h], so = dsoff[h];
     const int fm = fam[dim];
-    const float z = fmaf(fam_a[dim], float(xp[dim]), fam_b[dim]);
+    const float z = fmaf(fam_a[dim], x32(xp[dim]), fam_b[dim]);
     float pm1 = 0.f, pc = 1.f, dm1 = 0.f, dc = 0.f, acc = 0.f;
     for (int n = 0; n < g; ++n) {
       const float al = c_alpha[fm][n], be = c_beta[fm][n];

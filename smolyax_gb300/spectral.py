@@ -483,16 +483,18 @@ class _Runs:
         self.coef = []
         self.ncoef = 0
 
-    def add(self, slots, coefs, max_gap=4, degree=0):
-        """slots: increasing row slots; coefs: [len(slots), d_out]. Returns (r0, r1)."""
+    def add(self, slots, coefs, max_gap=4, degree=0, max_len=32):
+        """slots: increasing row slots; coefs: [len(slots), d_out]. Returns (r0, r1).
+        A run spans at most max_len slots: the evaluator sums each run in plain
+        FP32 and adds the run sums with compensation."""
         r0 = len(self.tab)
         i = 0
         n = len(slots)
         while i < n:
             j = i + 1
-            while j < n and slots[j] - slots[j - 1] <= max_gap:
-                j += 1
             a0 = int(slots[i]) & ~3
+            while j < n and slots[j] - slots[j - 1] <= max_gap and slots[j] - a0 < max_len:
+                j += 1
             length = _round4(int(slots[j - 1]) + 1 - a0)
             blk = np.zeros((length, self.dstride), dtype=np.float32)
             blk[np.asarray(slots[i:j]) - a0, : coefs.shape[1]] = coefs[i:j]

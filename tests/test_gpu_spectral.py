@@ -2,9 +2,21 @@
 
 Pins: (1) the FP64 coefficients reproduce the FP64 combination sum (host
 evaluation of the orthogonal form, 1e-9 relative); (2) the FP32 GPU values
-against the extended-precision values of the same data, with the relative
-error bound written per workload; (3) interpolation of polynomials in the
-index set stays exact to FP32 accuracy.
+against the extended-precision values of the same data, or against the FP64
+path, at 1e-6; (3) interpolation of polynomials in the index set stays exact
+to FP32 accuracy.
+
+Norms (bound 1e-6 in every case, printed per test):
+* element-wise relative error, max_(p,o) |y32 - y64| / |y64| -- the Leja
+  configurations and the per-point evaluator's Gauss-Hermite configurations;
+* per-point norm-wise, max_p max_o |y32 - y64| / max_o |y64| -- the
+  tensor-core Gauss-Hermite configurations, where some outputs are much smaller
+  than the terms c_m phi_m(x) they are the sum of (condition numbers
+  sum_m |c_m phi_m(x)| / |y| up to ~100 at N(0, I) points): FP32 arithmetic,
+  whose rounding is relative to those terms, cannot give them 1e-6 element-wise
+  accuracy.  For these the element-wise error is printed, and every element is
+  also checked against 1e-6 * sum_m |c_m phi_m(x)| (error relative to the size
+  of what is summed).
 """
 import numpy as np
 import pytest
@@ -38,9 +50,10 @@ def _phi(fam, z, n):
     return out
 
 
-def host_orthogonal_eval(ip, x):
+def host_basis_products(ip, x):
+    """[P, n_lambda] table of prod_j phi_{m_j}(z_j) over the index set (FP64,
+    host), in the order of the plan's coefficient rows."""
     sp = ip.spectral_plan()
-    C = sp.C64.cpu().numpy()
     tree = ip._tree
     tuples = tree.host_tuples(np.arange(tree.size))
     fam = sp.fam.cpu().numpy()
@@ -48,13 +61,29 @@ def host_orthogonal_eval(ip, x):
     z = x * a + b
     maxdeg = ip._maxdeg
     phis = {j: _phi(fam[j], z[:, j], int(maxdeg[j])) for j in range(x.shape[1]) if maxdeg[j] > 0}
-    y = np.zeros((x.shape[0], C.shape[1]))
+    out = np.ones((x.shape[0], len(tuples)))
     for e, nu in enumerate(tuples):
-        v = np.ones(x.shape[0])
         for dd, g in nu:
-            v = v * phis[dd][g]
-        y += v[:, None] * C[e][None, :]
-    return y
+            out[:, e] *= phis[dd][g]
+    return out
+
+
+def host_orthogonal_eval(ip, x):
+    return host_basis_products(ip, x) @ ip.spectral_plan().C64.cpu().numpy()
+
+
+def fp32_errors(y32, y64):
+    """(element-wise max relative, per-point norm-wise max relative) errors."""
+    y32, y64 = np.asarray(y32, dtype=float), np.asarray(y64, dtype=float)
+    ew = float(np.max(np.abs(y32 - y64) / np.abs(y64)))
+    pn = float(np.max(np.max(np.abs(y32 - y64), axis=1) / np.max(np.abs(y64), axis=1)))
+    return ew, pn
+
+
+def term_relative_error(ip, x, y32, y64):
+    """max over elements of |y32 - y64| / sum_m |c_m phi_m(x)|."""
+    S = np.abs(host_basis_products(ip, x)) @ np.abs(ip.spectral_plan().C64.cpu().numpy())
+    return float(np.max(np.abs(np.asarray(y32, dtype=float) - y64) / S))
 
 
 @pytest.mark.parametrize("name", [str(n) for n in INTERP["names"]][:8])
@@ -72,40 +101,85 @@ def test_small_cases_fp32(name):
 
 
 CASES = {
-    # tag: (d, t, kind, d_out, f, x, bound on the max relative FP32 error)
-    "cfg1": (10, 8.831421, "leja", 1, fns.rational(10, seed=0), np.random.default_rng(1).uniform(-1, 1, (10000, 10)), 1e-6),
+    # tag: (d, t, kind, d_out, f, x); element-wise bound 1e-6 for all
+    "cfg1": (10, 8.831421, "leja", 1, fns.rational(10, seed=0), np.random.default_rng(1).uniform(-1, 1, (10000, 10))),
     "cfg2": (1000, 8.224520, "leja", 1, fns.rational(1000, seed=0),
-             np.random.default_rng(1).uniform(-1, 1, (256, 1000)), 1e-6),
+             np.random.default_rng(1).uniform(-1, 1, (256, 1000))),
     # d_out = 64: tensor-core contraction (3xTF32, FP32 accumulation in tensor memory)
     "cfg4": (200, 7.853604, "leja", 64, fns.rational_vec(200, 64, seed=0),
-             np.random.default_rng(1).uniform(-1, 1, (64, 200)), 5e-5),
+             np.random.default_rng(1).uniform(-1, 1, (64, 200))),
+    # d_out = 8: per-point evaluator
     "cfg3alt": (100, 7.723434, "gh", 8, fns.exponential(100, 8, seed=0),
-                np.random.default_rng(1).normal(size=(32, 100)), 1e-5),
-    "cfg3": (100, 9.464636, "gh", 8, fns.exponential(100, 8, seed=0), np.random.default_rng(1).normal(size=(32, 100)),
-             1e-5),
+                np.random.default_rng(1).normal(size=(32, 100))),
+    "cfg3": (100, 9.464636, "gh", 8, fns.exponential(100, 8, seed=0), np.random.default_rng(1).normal(size=(32, 100))),
 }
 
 
 @pytest.mark.parametrize("tag", list(CASES))
 def test_fp32_error_bound(tag):
+    """Element-wise relative error <= 1e-6 against the extended-precision values."""
     from smolyax_gb300 import nodes
 
-    d, t, kind, d_out, f, x, bound = CASES[tag]
+    d, t, kind, d_out, f, x = CASES[tag]
     k = np.log((2 + np.arange(d)) / np.log(2))
     gen = nodes.Leja(dim=d) if kind == "leja" else nodes.GaussHermite(dim=d)
     ip = _interp(node_gen=gen, k=k, t=t, d_out=d_out, f=f)
     y32 = ip(x, precision="fp32").cpu().numpy().astype(float)
     exact = EXACT[tag + "/y"]
     err = rel_err(y32, exact)
-    print("%s: FP32 max relative error vs FP64 exact %.3e (bound %.0e)" % (tag, err, bound))
-    assert err < bound
+    print("%s: FP32 element-wise max relative error vs FP64 exact %.3e (bound 1e-06)" % (tag, err))
+    assert err < 1e-6
     if x.shape[0] <= 256:
         np.testing.assert_allclose(host_orthogonal_eval(ip, x[:16]), exact[:16], rtol=1e-9)
 
 
+@pytest.mark.parametrize("points", [256, 1000])
+def test_fp32_leja_d200_dout64_tensor_core(points):
+    """Leja d_in=200, d_out=64, |Lambda|=5000 (t=7.853604) on the tensor-core
+    path: element-wise relative error <= 1e-6 against the FP64 path."""
+    from smolyax_gb300 import nodes
+
+    d = 200
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    f = fns.rational_vec(d, 64, seed=0)
+    f.vectorized = True
+    ip = _interp(node_gen=nodes.Leja(dim=d), k=k, t=7.853604, d_out=64, f=f)
+    assert ip.spectral_plan().tc is not None
+    x = np.random.default_rng(11).uniform(-1, 1, (points, d))
+    ew, pn = fp32_errors(ip(x, precision="fp32").cpu().numpy(), ip(x).cpu().numpy())
+    print("Leja d=200 d_out=64 (%d points): element-wise %.3e, per-point norm-wise %.3e (bound 1e-06 element-wise)"
+          % (points, ew, pn))
+    assert ew < 1e-6
+
+
+def test_fp32_gauss_hermite_d100_dout2048_tensor_core():
+    """Gauss-Hermite d_in=100, d_out=2048, |Lambda|=20010 (t=9.464636, 159540
+    nodes), 256 points ~ N(0, I): the tcgen05 3xTF32 path against the FP64
+    path.  Per-point norm-wise error <= 1e-6; every element within 1e-6 of
+    sum_m |c_m phi_m(x)|; element-wise error printed."""
+    from smolyax_gb300 import nodes
+
+    d, d_out = 100, 2048
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    f = fns.exponential(d, d_out, seed=0)
+    f.vectorized = True
+    ip = _interp(node_gen=nodes.GaussHermite(dim=d), k=k, t=9.464636, d_out=d_out, f=f, memory_limit=8.0)
+    assert ip.n_f_evals == 159540 and ip.spectral_plan().tc is not None
+    x = np.random.default_rng(1).normal(size=(256, d))
+    y64 = ip(x).cpu().numpy()
+    y32 = ip(x, precision="fp32").cpu().numpy()
+    ew, pn = fp32_errors(y32, y64)
+    tr = term_relative_error(ip, x, y32, y64)
+    print("GH d=100 d_out=2048: per-point norm-wise %.3e (bound 1e-06), relative to sum|terms| %.3e (bound 1e-06), "
+          "element-wise %.3e" % (pn, tr, ew))
+    assert pn < 1e-6 and tr < 1e-6
+
+
 @pytest.mark.parametrize("t,d_out", [(7.723434, 32), (7.723434, 300)])
 def test_tensor_core_path_gauss_hermite(t, d_out):
-    """Gauss-Hermite, d_in = 100, vector output: the tcgen05 path against our FP64 path."""
+    """Gauss-Hermite, d_in = 100, vector output: the tcgen05 path against our
+    FP64 path.  Per-point norm-wise error <= 1e-6 and every element within
+    1e-6 of sum_m |c_m phi_m(x)|; element-wise error printed."""
     from smolyax_gb300 import nodes
 
     d = 100
@@ -115,12 +189,11 @@ def test_tensor_core_path_gauss_hermite(t, d_out):
     assert ip.spectral_plan().tc is not None
     y64 = ip(x).cpu().numpy()
     y32 = ip(x, precision="fp32").cpu().numpy().astype(float)
-    # per point, relative to the largest output of that point (a few outputs are
-    # 20x smaller than the others; FP32 cannot resolve them to 1e-6 pointwise)
-    err = float(np.max(np.max(np.abs(y32 - y64), axis=1) / np.max(np.abs(y64), axis=1)))
-    print("GH d_out=%d: tensor-core FP32 per-point norm-wise error vs FP64 %.3e" % (d_out, err))
-    assert err < 2e-6
-
+    ew, pn = fp32_errors(y32, y64)
+    tr = term_relative_error(ip, x, y32, y64)
+    print("GH d_out=%d: tensor-core FP32 per-point norm-wise %.3e, relative to sum|terms| %.3e, element-wise %.3e"
+          % (d_out, pn, tr, ew))
+    assert pn < 1e-6 and tr < 1e-6
 
 
 def test_bf16x3_contraction_gauss_hermite():
