@@ -406,6 +406,15 @@ int smx_gemm_tf32x3_splitk(const float* A_hi, const float* A_lo, int64_t lda, co
                            int64_t ldb, int M, int N, int K, float* D, int64_t ldd, const float* bias, int accumulate,
                            int splits, void* ws, size_t ws_bytes, int* err, void* stream);
 
+/* Test of the contraction's failure detection (no counterpart in the
+ * reference): runs smx_gemm_tf32x3's kernel with its copy producer switched
+ * off, so the first pipeline wait times out after wait_ns (<= 2 s); the
+ * kernel then sets *err = 2 and returns without writing D.  Every other
+ * entry point uses the 2 s bound. */
+int smx_gemm_tf32x3_timeout_selftest(const float* A_hi, const float* A_lo, int64_t lda, const float* B_hi,
+                                     const float* B_lo, int64_t ldb, int M, int N, int K, float* D, int64_t ldd,
+                                     int* err, uint64_t wait_ns, void* stream);
+
 /* Split-BF16 form of the same contraction (kind::f16, both operands BF16,
  * FP32 accumulation): D = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T with
  * A = A_hi + A_lo, B = B_hi + B_lo in BF16 (2-byte bit patterns; leading
@@ -432,13 +441,13 @@ int smx_split_tf32(const float* src, int64_t rows, int64_t cols, int64_t lds, fl
  * library until the process exits); nothing is allocated.  Calls whose table
  * (n_values * P doubles) does not fit return SMX_ERR_WORKSPACE: split the
  * points.  The first call on a device looks up the array's address with that
- * device current -- make it before any stream capture.  All calls share the
- * array, so calls that overlap on the GPU race: serialise them. */
+ * device current -- make it before any stream capture; the address is looked
+ * up again when the device's context changes (after a device reset).  All
+ * calls share the array, so calls that overlap on the GPU race: serialise them. */
 #define SMX_STATIC_SCRATCH_BYTES (32u << 20)
 int smx_eval_f64_noalloc(const smx_plan* plan_host, const double* x, int64_t P, int64_t ldx, double* y,
                          void* stream);
 
-/* Human-readable description of the last error on this thread (host string). */
 /* Device address of page-locked (pinned) host memory, for kernels that read
  * host inputs directly over the host link instead of copying them first;
  * SMX_ERR_ARG if `host` is not page-locked host memory, SMX_ERR_UNSUPPORTED
@@ -446,6 +455,7 @@ int smx_eval_f64_noalloc(const smx_plan* plan_host, const double* x, int64_t P, 
  * reference: its inputs are copied to the device by JAX, interpolation.py:257.) */
 int smx_host_device_pointer(const void* host, void** dev);
 
+/* Human-readable description of the last error on this thread (host string). */
 const char* smx_last_error_string(void);
 
 /* Library version string (host). */

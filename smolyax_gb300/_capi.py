@@ -167,6 +167,8 @@ SIGNATURES = {
     "smx_spectral_eval_batch_workspace": (_sz, [_int, _int, _int]),
     "smx_spectral_eval_batch": (_int, [_p, _int, _p, _int, _p, _sz, _p]),
     "smx_gemm_tf32x3": (_int, [_p, _p, _i64, _p, _p, _i64, _int, _int, _int, _p, _i64, _p, _int, _p, _p]),
+    "smx_gemm_tf32x3_timeout_selftest": (_int, [_p, _p, _i64, _p, _p, _i64, _int, _int, _int, _p, _i64, _p,
+                                                 C.c_uint64, _p]),
     "smx_gemm_tf32x3_splitk_workspace": (_sz, [_int, _int, _int, _int]),
     "smx_gemm_tf32x3_splitk": (_int, [_p, _p, _i64, _p, _p, _i64, _int, _int, _int, _p, _i64, _p, _int, _int, _p, _sz,
                                        _p, _p]),

@@ -25,7 +25,7 @@ constexpr int kBM = 128;
 // the same shared memory (more copies in flight against the L2 latency).
 constexpr int kRowBytes = 128;
 constexpr int kBK = kRowBytes / 4;
-constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on every wait
+constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on every wait (the default of GemmArgs::wait_ns)
 
 __device__ __forceinline__ uint64_t global_ns() {
   uint64_t t;
@@ -45,8 +45,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 
-// Bounded parity wait; returns false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort_flag) {
+// Bounded parity wait; returns false on timeout (after `limit_ns`) or when
+// the abort flag is raised.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort_flag,
+                                          uint64_t limit_ns = kWaitNs) {
   const uint32_t a = smem_u32(bar);
   const uint64_t t0 = global_ns();
   for (uint32_t it = 0;; ++it) {
@@ -58,7 +60,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const 
         : "memory");
     if (done) return true;
     if (abort_flag && *abort_flag) return false;
-    if ((it & 255) == 255 && global_ns() - t0 > kWaitNs) return false;
+    if ((it & 255) == 255 && global_ns() - t0 > limit_ns) return false;
   }
 }
 
@@ -142,6 +144,8 @@ struct GemmArgs {
   int accumulate;   // D += A B^T instead of D = A B^T
   int kt_per_z;     // split-K: K-tiles per blockIdx.z slice (0: one slice)
   int64_t zstride;  // split-K: floats between the slices' outputs
+  uint64_t wait_ns; // bound on each pipeline wait (kWaitNs; shorter only in the self-test)
+  int no_loads;     // self-test only: the producer issues no copies, so the first wait must time out
 };
 
 constexpr int kEpiLd = 132;  // epilogue staging row stride (floats): 16-byte rows, conflict-free
@@ -162,7 +166,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
   uint64_t* empty = full + kStages;
   uint64_t* acc_full = empty + kStages;  // [2] MMA -> drain
   uint64_t* acc_empty = acc_full + 2;    // [2] drain -> MMA
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+  uint64_t* flush = acc_empty + 2;       // MMA thread, on failure: its own MMAs complete
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(flush + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   volatile int* armed_slot = abort_flag + 1;
 
@@ -183,6 +188,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
       mbar_init(&acc_full[b], 1);
       mbar_init(&acc_empty[b], 4);  // one arrival per drain warp
     }
+    mbar_init(flush, 1);
     *abort_flag = 0;
     *armed_slot = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -200,10 +206,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
   if (warp == 4) {
     if (lane == 0) {  // ---- TMA producer
       int armed_upto = 0;
-      for (int kt = 0; kt < KT; ++kt) {
+      for (int kt = 0; kt < (g.no_loads ? 0 : KT); ++kt) {
         const int s = kt % kStages;
         const uint32_t ph = (kt / kStages) & 1;
-        if (kt >= kStages && !mbar_wait(&empty[s], ph ^ 1, abort_flag)) {
+        if (kt >= kStages && !mbar_wait(&empty[s], ph ^ 1, abort_flag, g.wait_ns)) {
           atomicExch(g.err, 1);
           *abort_flag = 1;
           break;
@@ -227,7 +233,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
       int kt = 0;
       for (int c = 0; c < NCH && ok; ++c) {
         const int b = c & 1;
-        if (c >= 2 && !mbar_wait(&acc_empty[b], ((c >> 1) & 1) ^ 1, abort_flag)) {
+        if (c >= 2 && !mbar_wait(&acc_empty[b], ((c >> 1) & 1) ^ 1, abort_flag, g.wait_ns)) {
           ok = false;
           break;
         }
@@ -238,7 +244,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         for (; kt < kt_end; ++kt) {
           const int s = kt % kStages;
           const uint32_t ph = (kt / kStages) & 1;
-          if (!mbar_wait(&full[s], ph, abort_flag)) {
+          if (!mbar_wait(&full[s], ph, abort_flag, g.wait_ns)) {
             ok = false;
             break;
           }
@@ -259,9 +265,16 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
           }
           mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
         }
-        mma_commit(&acc_full[b]);  // accumulator b complete (or abandoned on abort)
+        if (ok) mma_commit(&acc_full[b]);  // accumulator b complete
       }
       if (!ok) {
+        // A wait ran out (or the producer gave up): the abandoned accumulator
+        // is never signalled, so no drain warp reads it; this thread waits
+        // (bounded) until its own MMAs have completed, then raises the abort
+        // flag, on which the other warps stop waiting, skip the epilogue and
+        // the block frees its tensor memory.
+        mma_commit(flush);
+        mbar_wait(flush, 0, nullptr);
         atomicExch(g.err, 2);
         *abort_flag = 1;
       }
@@ -276,7 +289,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     const uint32_t lane_base = tmem + (uint32_t(warp * 32) << 16);
     for (int c = 0; c < NCH; ++c) {
       const int b = c & 1;
-      ok = __all_sync(0xffffffffu, ok && mbar_wait(&acc_full[b], (c >> 1) & 1, abort_flag) && !*abort_flag);
+      ok = __all_sync(0xffffffffu,
+                      ok && mbar_wait(&acc_full[b], (c >> 1) & 1, abort_flag, g.wait_ns) && !*abort_flag);
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll
@@ -397,7 +411,7 @@ int make_map(CUtensorMap* tm, const void* ptr, int64_t rows, int64_t cols, int64
 template <bool BF16>
 int launch(const void* Ah, const void* Al, int64_t lda, const void* Bh, const void* Bl, int64_t ldb, int M, int N,
            int K, float* D, int64_t ldd, const float* bias, int* err, int accumulate, cudaStream_t st,
-           int splits = 1) {
+           int splits = 1, uint64_t wait_ns = kWaitNs, int no_loads = 0) {
   CUtensorMap tAh, tAl, tBh, tBl;
   int rc;
   if ((rc = make_map(&tAh, Ah, M, K, lda, kBM, BF16)) || (rc = make_map(&tAl, Al, M, K, lda, kBM, BF16)) ||
@@ -413,7 +427,7 @@ int launch(const void* Ah, const void* Al, int64_t lda, const void* Bh, const vo
   const int KT = (K + EK - 1) / EK;
   const int kt_per_z = splits > 1 ? (KT + splits - 1) / splits : 0;
   const int nz = splits > 1 ? (KT + kt_per_z - 1) / kt_per_z : 1;
-  GemmArgs g{M, N, K, D, ldd, bias, err, accumulate, kt_per_z, int64_t(M) * ldd};
+  GemmArgs g{M, N, K, D, ldd, bias, err, accumulate, kt_per_z, int64_t(M) * ldd, wait_ns, no_loads};
   dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM, nz);
   gemm_tf32x3_kernel<BF16><<<grid, kThreadsTC, Smem::kTotal, st>>>(tAh, tAl, tBh, tBl, g);
   SMX_LAUNCH_CHECK(BF16 ? "smx_gemm_bf16x3" : "smx_gemm_tf32x3");
@@ -456,6 +470,24 @@ extern "C" int smx_gemm_tf32x3(const float* A_hi, const float* A_lo, int64_t lda
   if (rc) return rc;
   return launch<false>(A_hi, A_lo, lda, B_hi, B_lo, ldb, M, N, K, D, ldd, bias, err, accumulate,
                        smx::as_stream(stream));
+}
+
+// Self-test of the timeout path: the same kernel with its producer issuing no
+// copies, so the MMA thread's first wait cannot complete; after `wait_ns` it
+// records error code 2 in *err, raises the abort flag, the drain warps skip
+// the epilogue and the block frees its tensor memory.  Nothing is in flight
+// when it gives up (no copy, no MMA), and D is not written.
+extern "C" int smx_gemm_tf32x3_timeout_selftest(const float* A_hi, const float* A_lo, int64_t lda, const float* B_hi,
+                                                const float* B_lo, int64_t ldb, int M, int N, int K, float* D,
+                                                int64_t ldd, int* err, uint64_t wait_ns, void* stream) {
+  SMX_REQUIRE(M >= 1 && N >= 1 && K >= 1 && lda >= K && ldb >= K && ldd >= N,
+              "smx_gemm_tf32x3_timeout_selftest: bad sizes");
+  SMX_REQUIRE(A_hi && A_lo && B_hi && B_lo && D && err, "smx_gemm_tf32x3_timeout_selftest: null pointer");
+  SMX_REQUIRE(wait_ns <= kWaitNs, "smx_gemm_tf32x3_timeout_selftest: wait bound above the default");
+  int rc = get_encode();
+  if (rc) return rc;
+  return launch<false>(A_hi, A_lo, lda, B_hi, B_lo, ldb, M, N, K, D, ldd, nullptr, err, 0, smx::as_stream(stream), 1,
+                       wait_ns, 1);
 }
 
 extern "C" int smx_gemm_bf16x3(const uint16_t* A_hi, const uint16_t* A_lo, int64_t lda, const uint16_t* B_hi,

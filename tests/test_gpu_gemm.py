@@ -1,7 +1,8 @@
 """tcgen05 3xTF32 contraction (``smx_gemm_tf32x3``) against an FP64 product.
 
-Bound: norm-wise relative error 1e-8 K + 2e-6 (22-bit products; the tensor cores accumulate
-in FP32 with truncation, so the bound grows with K <= 5000).
+Bound: norm-wise relative error 2e-6 for K up to 5000 (hi + lo keeps ~22 bits of
+each operand; the tensor cores accumulate in FP32 with truncation, in chunks of
+64 products that are added in registers; measured 4e-7 .. 8e-7 at every K).
 """
 import numpy as np
 import pytest
@@ -50,7 +51,7 @@ def test_gemm_tf32x3(M, N, K):
     ref = A.astype(np.float64) @ B.astype(np.float64).T + bias
     err = np.max(np.abs(D - ref)) / np.max(np.abs(ref))
     print("M=%d N=%d K=%d norm-wise rel err %.2e" % (M, N, K, err))
-    assert err < 1e-8 * K + 2e-6
+    assert err < 2e-6
 
 
 def _gemm_bf16(A, B, bias=None):
@@ -108,7 +109,7 @@ def test_gemm_bf16x3(M, N, K):
     err = np.max(np.abs(D - ref)) / scale
     err3 = np.max(np.abs(D - ref3)) / scale
     print("M=%d N=%d K=%d bf16x3 norm-wise rel err %.2e (vs its own three products %.2e)" % (M, N, K, err, err3))
-    assert err3 < 1e-8 * K + 2e-6
+    assert err3 < 2e-6
     assert err < 1e-4
 
 
@@ -153,5 +154,34 @@ def test_gemm_tf32x3_splitk(M, N, K, splits):
     ref = A.astype(np.float64) @ B.astype(np.float64).T + bias + D0
     e = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
     print("split-K M=%d N=%d K=%d splits=%d: norm-wise rel err %.2e" % (M, N, K, splits, e))
-    assert e < 1e-8 * K + 2e-6
+    assert e < 2e-6
     assert torch.all(D[:, N:] == 0)  # the pitch padding is untouched
+
+
+def test_gemm_timeout_path_reports_and_recovers():
+    """Failure detection of the tensor-core contraction: with its copy producer
+    switched off, the kernel's first pipeline wait runs out after 1 ms; it must
+    record error code 2, leave D untouched and return, and the next ordinary
+    contraction on the same context must be correct."""
+    import torch
+
+    from smolyax_gb300 import _capi
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    st = _capi.stream_ptr(torch.cuda.current_stream())
+    M, N, K = 256, 128, 64
+    A = torch.zeros(M, K, dtype=torch.float32, device=dev)
+    B = torch.zeros(N, K, dtype=torch.float32, device=dev)
+    D = torch.full((M, N), 7.0, dtype=torch.float32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    _capi.call("smx_gemm_tf32x3_timeout_selftest", _capi.ptr(A), _capi.ptr(A), K, _capi.ptr(B), _capi.ptr(B), K, M, N,
+               K, _capi.ptr(D), N, _capi.ptr(err), 1_000_000, st)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 2
+    assert bool((D == 7.0).all())
+    rng = np.random.default_rng(5)
+    A2 = rng.normal(size=(300, 200)).astype(np.float32)
+    B2 = rng.normal(size=(150, 200)).astype(np.float32)
+    got = _gemm(A2, B2)
+    ref = A2.astype(np.float64) @ B2.astype(np.float64).T
+    assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) < 2e-6
