@@ -17,7 +17,12 @@
 //    before any stream capture;
 //  * all calls share the one array: calls that overlap on the GPU (different
 //    streams, or threads) race; serialise them.  The basis kernel overwrites
-//    every slot it later reads, so nothing needs clearing between calls.
+//    every slot it later reads, so nothing needs clearing between calls;
+//  * the address is cached per device together with the CUDA context it was
+//    looked up in; after a device reset (a new primary context) the next call
+//    looks it up again instead of using the old context's address.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "common.cuh"
@@ -31,6 +36,30 @@ static __device__ __align__(256) double g_static_scratch[kScratchDoubles];
 std::mutex g_mu;
 constexpr int kMaxDevices = 256;
 void* g_scratch_addr[kMaxDevices] = {};
+CUcontext g_scratch_ctx[kMaxDevices] = {};
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+
+// The driver's cuCtxGetCurrent, through the runtime's entry-point query (the
+// library links only the CUDA runtime); null if unavailable.
+CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return static_cast<CtxGetCurrentFn>(nullptr);
+    return reinterpret_cast<CtxGetCurrentFn>(p);
+  }();
+  return fn;
+}
+
+CUcontext current_context() {
+  CUcontext c = nullptr;
+  const CtxGetCurrentFn fn = ctx_get_current();
+  if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+  return c;
+}
 
 }  // namespace
 
@@ -53,13 +82,15 @@ extern "C" int smx_eval_f64_noalloc(const smx_plan* pl, const double* x, int64_t
   void* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_addr[dev]) {
+    const CUcontext ctx = current_context();
+    if (!g_scratch_addr[dev] || !ctx || ctx != g_scratch_ctx[dev]) {
       void* addr = nullptr;
       const cudaError_t e = cudaGetSymbolAddress(&addr, g_static_scratch);
       if (e != cudaSuccess || addr == nullptr)
         return smx::set_error(SMX_ERR_CUDA, std::string("smx_eval_f64_noalloc: cudaGetSymbolAddress failed: ") +
                                                 cudaGetErrorString(e));
       g_scratch_addr[dev] = addr;
+      g_scratch_ctx[dev] = current_context();  // the lookup made the device's context current if it was not
     }
     scratch = g_scratch_addr[dev];
   }

@@ -10,12 +10,21 @@ scratch array; its results must equal those of the workspace-taking
 This file is collected last on purpose; it builds its own interpolant so that
 it also passes alone in a fresh process.
 """
-import ctypes
+import os
+import re
 
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+
+def _static_scratch_bytes():
+    """SMX_STATIC_SCRATCH_BYTES as the public header defines it."""
+    hdr = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "include", "smolyax_gb300.h")
+    m = re.search(r"#define\s+SMX_STATIC_SCRATCH_BYTES\s+\((\d+)u\s*<<\s*(\d+)\)", open(hdr).read())
+    assert m, "SMX_STATIC_SCRATCH_BYTES not found in the header"
+    return int(m.group(1)) << int(m.group(2))
 
 
 def test_noalloc_matches_workspace_entry_point():
@@ -43,8 +52,19 @@ def test_noalloc_matches_workspace_entry_point():
         _capi.call("smx_eval_f64_noalloc", plan.ref(), _capi.ptr(x), P, d, _capi.ptr(y_na), stream)
         torch.cuda.synchronize()
         np.testing.assert_allclose(y_na.cpu().numpy(), y_ws.cpu().numpy(), rtol=1e-12, atol=0.0)
-    # a batch whose basis table exceeds the static scratch is rejected before any launch
-    too_many = (32 << 20) // (8 * plan.c.n_values) + 1
-    rc = lib.smx_eval_f64_noalloc(plan.ref(), _capi.ptr(x), too_many, d, _capi.ptr(y_na), stream)
+    # the largest batch that fits the static scratch is evaluated like smx_eval
+    most = _static_scratch_bytes() // (8 * plan.c.n_values)
+    x = torch.as_tensor(rng.uniform(-1, 1, (most + 1, d)), device=dev)
+    y_ws = torch.empty(most, 2, dtype=torch.float64, device=dev)
+    y_na = torch.full((most + 1, 2), float("nan"), dtype=torch.float64, device=dev)
+    ws = torch.empty(_capi.size("smx_eval_workspace", plan.ref(), most, 64), dtype=torch.uint8, device=dev)
+    _capi.call("smx_eval", plan.ref(), 64, _capi.ptr(x), most, d, _capi.ptr(y_ws), _capi.ptr(ws), ws.numel(), stream)
+    _capi.call("smx_eval_f64_noalloc", plan.ref(), _capi.ptr(x), most, d, _capi.ptr(y_na), stream)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(y_na[:most].cpu().numpy(), y_ws.cpu().numpy(), rtol=1e-12, atol=0.0)
+    # one point more is rejected before any launch, and the message names the limit
+    rc = lib.smx_eval_f64_noalloc(plan.ref(), _capi.ptr(x), most + 1, d, _capi.ptr(y_na), stream)
     assert rc == -2
-    assert b"static scratch" in lib.smx_last_error_string()
+    msg = lib.smx_last_error_string().decode()
+    assert "static scratch" in msg and ("at most %d points" % most) in msg
+    assert bool(torch.isnan(y_na[most]).all())
