@@ -270,7 +270,9 @@ def gen_configs(interp_mod, nodes, out):
 
 
 def main():
-    ref_src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src"
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <reference source dir (the folder holding smolyax/)> [indices|interp|configs ...]")
+    ref_src = sys.argv[1]
     sys.path.insert(0, ref_src)
     from smolyax import indices, nodes
     from smolyax import interpolation as interp_mod
