@@ -217,19 +217,32 @@ def dist_setup():
     return rank_info()
 
 
+def headline_config(world, P):
+    """The `config` of the headline line (both arms print the same one)."""
+    return {"workload": WORKLOAD, "points": P, "d_in": D_IN, "d_out": D_OUT, "lambda": 9999,
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "inputs larger than L2 (x is %d MB FP64)" % (P * D_IN * 8 // 2**20)}
+
+
 def run_reference(args):
+    """The reference's evaluation algorithm on the host cores (the oracle's
+    numpy restatement of its JAX path: JAX itself is not installed), on the
+    headline workload.  Each step evaluates a bounded sample of the workload's
+    points (~2 s of work on all cores); the step time printed is that measured
+    time, with the points it covered."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    per_step = []
-    sample_pts = 0
+    per_ms, per_pts = [], []
     for i in range(args.warmup + args.steps):
-        rate, n = cpu_reference_rate(10**9, threads, seconds=4.0, seed=100 + i)
+        t0 = time.perf_counter()
+        rate, n = cpu_reference_rate(10**9, threads, seconds=2.0, seed=100 + i)
+        dt = time.perf_counter() - t0
         if i >= args.warmup:
-            per_step.append(rate)
-            sample_pts += n
-    value = statistics.median(per_step)
+            per_ms.append(1e3 * dt)
+            per_pts.append(n)
+    value = sum(per_pts) * D_OUT / (1e-3 * sum(per_ms))
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -238,16 +251,17 @@ def run_reference(args):
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": 1e3 * POINTS * D_OUT / value,
+        "ms_per_step": statistics.mean(per_ms),
+        "points_per_step": statistics.mean(per_pts),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "points": POINTS, "d_in": D_IN, "d_out": D_OUT},
+        "config": headline_config(world, args.points),
         "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
-                         "sample": "%d points of the workload over %d steps of ~4 s (numpy restatement of the "
-                                   "reference's evaluation; JAX is not installed)" % (sample_pts, args.steps)},
+                         "sample": "%d points of the workload over %d steps of ~2 s (numpy restatement of the "
+                                   "reference's evaluation; JAX is not installed)" % (sum(per_pts), args.steps)},
         "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -276,14 +290,14 @@ WORKLOADS = {
 }
 
 
-def run_tensor_workload(args):
-    """Vector-valued workloads served by the tensor-core contraction (one JSON line)."""
+def tensor_workload(name, steps, warmup, points=None):
+    """Vector-valued workloads served by the tensor-core contraction: one result dict."""
     import torch
 
     from smolyax_gb300 import SmolyakBarycentricInterpolator, nodes
 
-    kind, d, t, d_out, P, fbuild, desc = WORKLOADS[args.workload]
-    P = args.points if args.points != POINTS else P
+    kind, d, t, d_out, P, fbuild, desc = WORKLOADS[name]
+    P = points or P
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
     k = np.log((2 + np.arange(d)) / np.log(2))
@@ -300,10 +314,10 @@ def run_tensor_workload(args):
         x = torch.randn(P, d, dtype=torch.float64, device=dev, generator=gen_t)
     y = torch.empty(P, d_out, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
-    for _ in range(max(3, args.warmup)):
+    for _ in range(max(3, warmup)):
         sp.evaluate(x, y)
     torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     with ClockSampler(0) as clk:
         for a, b in ev:
             a.record(stream)
@@ -314,7 +328,9 @@ def run_tensor_workload(args):
     ms = statistics.mean(per)
     sub = 256
     y64 = ip(x[:sub]).cpu().numpy()
-    err = float(np.max(np.max(np.abs(y[:sub].double().cpu().numpy() - y64), axis=1) / np.max(np.abs(y64), axis=1)))
+    y32 = y[:sub].double().cpu().numpy()
+    err = float(np.max(np.max(np.abs(y32 - y64), axis=1) / np.max(np.abs(y64), axis=1)))
+    err_ew = float(np.max(np.abs(y32 - y64) / np.abs(y64)))
     bf16 = None
     if sp.tc is not None:
         # the split-BF16 form of the same contraction: timed alike, error on the same points
@@ -322,18 +338,19 @@ def run_tensor_workload(args):
             sp.evaluate(x, y, mode="bf16x3")
         torch.cuda.synchronize()
         ev16 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-                for _ in range(args.steps)]
+                for _ in range(steps)]
         for a, b in ev16:
             a.record(stream)
             sp.evaluate(x, y, mode="bf16x3")
             b.record(stream)
         torch.cuda.synchronize()
         ms16 = statistics.mean(a.elapsed_time(b) for a, b in ev16)
-        e16 = float(np.max(np.max(np.abs(y[:sub].double().cpu().numpy() - y64), axis=1)
-                           / np.max(np.abs(y64), axis=1)))
+        y16 = y[:sub].double().cpu().numpy()
+        e16 = float(np.max(np.max(np.abs(y16 - y64), axis=1) / np.max(np.abs(y64), axis=1)))
         bf16 = {"ms_per_step": ms16, "value": P * d_out / (ms16 * 1e-3),
                 "tflops": 2.0 * P * d_out * sp.tc["K"] / (ms16 * 1e-3) / 1e12,
                 "per_point_normwise_vs_fp64": e16,
+                "elementwise_max_rel_vs_fp64": float(np.max(np.abs(y16 - y64) / np.abs(y64))),
                 "note": "3 kind::f16 BF16 passes (hi*hi + hi*lo + lo*hi), FP32 accumulation"}
     K = sp.tc["K"] if sp.tc is not None else None
     # algorithmic flops: one multiply-add per (point, entry, output); the
@@ -344,12 +361,16 @@ def run_tensor_workload(args):
         pk = "measured bf16 dense"
     except Exception:
         peak, pk = 1900.0, "fallback bf16 dense"
+    tf32_peak = peak / 2  # kind::tf32 issues at half the bf16 dense rate
     line = {
-        "metric": METRIC, "workload": args.workload, "value": P * d_out / (ms * 1e-3), "unit": "evals/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "metric": METRIC, "workload": name, "value": P * d_out / (ms * 1e-3), "unit": "evals/s",
+        "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": ms, "higher_is_better": True,
         "dtype": "fp32 (3xTF32 tensor contraction)", "data": "synthetic",
         "config": {"workload": desc, "points": P, "d_in": d, "d_out": d_out, "lambda": K + 1 if K else None},
-        "error": {"fp32_per_point_normwise_vs_fp64": err, "points_checked": sub},
+        "error": {"fp32_per_point_normwise_vs_fp64": err, "fp32_elementwise_max_rel_vs_fp64": err_ew,
+                  "points_checked": sub, "bound": 1e-6, "bound_norm": "per-point norm-wise"},
+        "tflops_algorithmic": tensor_flops / (ms * 1e-3) / 1e12 if K else None,
+        "frac_of_tf32_peak": tensor_flops / (ms * 1e-3) / 1e12 / tf32_peak if K else None,
         "roofline": {"bound": "tensor", "achieved": tensor_flops / (ms * 1e-3) / 1e12 if K else None, "peak": peak,
                      "unit": "TFLOP/s", "frac": tensor_flops / (ms * 1e-3) / 1e12 / peak if K else None,
                      "peak_kind": pk, "flops_per_step": tensor_flops,
@@ -359,13 +380,25 @@ def run_tensor_workload(args):
         "setup_s": setup_s, "clocks": clk.summary(),
         # per step: per chunk of points a panel (+ its basis rows) and a tensor-core GEMM, or one
         # evaluator launch per 4 outputs
-        "gpu_launches": args.steps * (sp.tc_launches(P) if sp.tc is not None else (d_out + 3) // 4),
+        "gpu_launches": steps * (sp.tc_launches(P) if sp.tc is not None else (d_out + 3) // 4),
     }
-    print(json.dumps(line))
+    del ip, sp, x, y
+    torch.cuda.empty_cache()
+    return line
+
+
+def run_tensor_workload(args):
+    print(json.dumps(tensor_workload(args.workload, args.steps, args.warmup,
+                                     args.points if args.points != POINTS else None)))
     return 0
 
 
 def run_backward_workload(args):
+    print(json.dumps(backward_workload(args.steps, args.warmup, args.points if args.points != POINTS else None)))
+    return 0
+
+
+def backward_workload(steps, warmup, points=None):
     """Forward + hand-written backward through torch.autograd (dL/dx and dL/d
     nodal values) at d_in=200, d_out=64, |Lambda|=5000, 1e5 points, with a
     random FP32 cotangent (one JSON line)."""
@@ -375,7 +408,7 @@ def run_backward_workload(args):
     from smolyax_gb300.autograd import interpolate
 
     d, t, d_out, P = 200, 7.853604, 64, 100_000
-    P = args.points if args.points != POINTS else P
+    P = points or P
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
     k = np.log((2 + np.arange(d)) / np.log(2))
@@ -398,11 +431,11 @@ def run_backward_workload(args):
         y.backward(g)
         return x.grad, fu.grad
 
-    for _ in range(max(3, args.warmup)):
+    for _ in range(max(3, warmup)):
         step()
     torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    evf = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    evf = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     with ClockSampler(0) as clk:
         for (a, b), (fa, fb) in zip(ev, evf):
             a.record(stream)
@@ -416,15 +449,16 @@ def run_backward_workload(args):
     ms = statistics.mean(a.elapsed_time(b) for a, b in ev) - ms_fwd
     line = {
         "metric": METRIC, "workload": "leja64bwd", "value": P * d_out / (ms * 1e-3), "unit": "evals/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": ms, "higher_is_better": True,
         "dtype": "fp32 (3xTF32 tensor contractions, FP64 coefficient adjoint)", "data": "synthetic",
         "config": {"workload": "Leja d_in=200 d_out=64 |Lambda|=5000 (t=7.853604) rational f, 1e5 points U[-1,1]^200,"
                                " forward + backward (dL/dx and dL/d nodal values), FP32 cotangent N(0,1)",
                    "points": P, "d_in": d, "d_out": d_out},
         "forward_ms": ms_fwd, "backward_ms": ms - ms_fwd, "setup_s": setup_s, "clocks": clk.summary(),
     }
-    print(json.dumps(line))
-    return 0
+    del ip, fu, x0, g
+    torch.cuda.empty_cache()
+    return line
 
 
 def serving_fleet(seed=0):
@@ -442,7 +476,12 @@ def serving_fleet(seed=0):
 
 
 def run_serving(args):
-    """Poisson stream of eval/gradient requests over the 16-interpolant fleet."""
+    print(json.dumps(serving_workload(args.requests, args.rate)))
+    return 0
+
+
+def serving_workload(n_req, rate):
+    """Poisson stream of eval/gradient requests over the 16-interpolant fleet: one result dict."""
     import torch
 
     from smolyax_gb300 import SmolyakBarycentricInterpolator, indices, nodes
@@ -465,8 +504,7 @@ def run_serving(args):
         kind = "leja" if isinstance(ip._node_gen, nodes.Leja) else "gh"
         xs = rng.uniform(-1, 1, (65536, ip.d_in)) if kind == "leja" else rng.normal(size=(65536, ip.d_in)) / np.sqrt(2)
         pools[name] = xs
-    n_req = args.requests
-    reqs, arrivals = [], np.cumsum(rng.exponential(1.0 / args.rate, n_req))
+    reqs, arrivals = [], np.cumsum(rng.exponential(1.0 / rate, n_req))
     names = sorted(ips)
     for j in range(n_req):
         name = names[rng.integers(len(names))]
@@ -485,7 +523,7 @@ def run_serving(args):
         "higher_is_better": True, "dtype": "fp32", "data": "synthetic",
         "config": {"workload": "16 resident interpolants (d_in 4-1000, d_out 1-1024, |Lambda| 1e2-1e5, Leja/GH, seed 0);"
                                " Poisson stream, 80% eval / 20% gradient, batch log-uniform [1, 65536]",
-                   "requests": n_req, "rate_per_s": args.rate},
+                   "requests": n_req, "rate_per_s": rate},
         "latency_ms": {"p50": float(np.percentile(lat_e, 50)), "p99": float(np.percentile(lat_e, 99)),
                        "grad_p50": float(np.percentile(lat_g, 50)) if lat_g.size else None,
                        "grad_p99": float(np.percentile(lat_g, 99)) if lat_g.size else None},
@@ -494,8 +532,9 @@ def run_serving(args):
         "fleet": [dict(d_in=d, d_out=o, lam=l, kind=kd, K=int(ips["ip%02d" % i]._tree.size),
                        tensor=ips["ip%02d" % i].spectral_plan().tc is not None) for i, d, o, l, kd in fleet],
     }
-    print(json.dumps(line))
-    return 0
+    del server, ips
+    torch.cuda.empty_cache()
+    return line
 
 
 def run_ours(args):
@@ -588,9 +627,7 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "fp32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "points": P, "d_in": D_IN, "d_out": D_OUT, "lambda": 9999,
-                   "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (x is %d MB FP64)" % (P * D_IN * 8 // 2**20)},
+        "config": headline_config(world, P),
         "latency_ms": {"p50": statistics.median(per32), "p99": p99, "max": max(per32)},
         "fp64": {"value": world * P * D_OUT / (ms64 * 1e-3), "ms_per_step": ms64, "steps": fp64_steps},
         "speedup_vs_fp64": ms64 / ms32,
@@ -605,10 +642,35 @@ def run_ours(args):
         "gpu_launches": launches,
         "wall_s_timed_region": wall32,
     }
+    if world == 1 and not args.no_extras:
+        # the other benchmark configurations, each measured by its own timed loop
+        # after the headline (not part of the headline's value)
+        del x, y32, y64, xh, yh, ip, sp
+        torch.cuda.empty_cache()
+        line["extras"] = extras()
     print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def extras():
+    """Tensor-core (GH d_in=100 d_out=2048), forward + backward (Leja d_in=200
+    d_out=64), quadrature and serving (16-interpolant fleet) results."""
+    out = {}
+    for key, fn in (("gh2048_tensor_core", lambda: tensor_workload("gh2048", 5, 3)),
+                    ("leja64_forward_backward", lambda: backward_workload(5, 3)),
+                    ("serving", lambda: serving_workload(300, 200.0))):
+        t0 = time.perf_counter()
+        try:
+            r = fn()
+        except Exception as exc:  # recorded, so that the headline line is still printed
+            r = {"error": "%s: %s" % (type(exc).__name__, exc)}
+        r["bench_wall_s"] = time.perf_counter() - t0
+        for drop in ("metric", "fleet"):
+            r.pop(drop, None)
+        out[key] = r
+    return out
 
 
 def main():
@@ -622,6 +684,7 @@ def main():
                     choices=["leja1000", "serving", "leja64bwd"] + sorted(WORKLOADS))
     ap.add_argument("--requests", type=int, default=300)
     ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--no-extras", action="store_true", help="headline only (skip the other configurations)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
