@@ -1,29 +1,49 @@
 """Continuous-batching request loop over many resident interpolants.
 
-A :class:`Server` keeps built interpolants (plans, coefficients) resident on
-the device and serves evaluation and gradient requests of different
-interpolants and batch sizes:
+A :class:`Server` keeps built interpolants (plans, coefficients, backward
+operands) resident on the device and serves evaluation and gradient requests
+of different interpolants and batch sizes:
 
-* admission -- requests wait in FIFO order and are admitted while a stream
-  slot is free and their device memory (inputs, outputs, scratch) fits the
-  budget; a request that can never fit is rejected;
-* batching  -- at every scheduling step, the admitted FP32 evaluations whose
-  plans use a CUDA-core evaluator are merged into one persistent launch per
-  evaluator kind (``smx_blocked_eval_batch`` for one-output plans with blocked
-  tables, ``smx_spectral_eval_batch`` for the others: blocks take 128-point
-  tiles of any request from a shared counter); tensor-core evaluations, FP64
-  evaluations and gradients run on their own streams, so their work overlaps
-  on the device;
-* completion -- each admission group records a CUDA event; the loop polls the
-  events, copies results to the host, frees memory and slots, and admits
-  requests that arrived meanwhile.
+* admission -- requests wait in FIFO order and are admitted while a stream is
+  free and their device memory (inputs, outputs, the scratch of the kernels
+  that will run) fits the budget; a request that can never fit the budget is
+  rejected;
+* batching  -- at every scheduling step the admitted requests are merged by
+  kind, one launch (and one stream) per kind:
 
-Results are identical to evaluating each request alone (same kernels per
-128-point tile).  Gradient requests return the vector-Jacobian product
-dL/dx for a cotangent (default: ones), shape [P, d_in].
+  - FP32 evaluations of one-output plans with blocked tables and of plans on
+    the per-point evaluator: one persistent multi-plan launch each
+    (``smx_blocked_eval_batch``, ``smx_spectral_eval_batch``: blocks take
+    128-point tiles of any request from a shared counter);
+  - every other request (tensor-core evaluations, FP64 evaluations, gradients)
+    merges with the admitted requests of the same interpolant, operation and
+    precision: their points are copied into one device array and evaluated
+    (or differentiated) by one call, whose rows are then handed back per
+    request.  These paths compute every point independently of the others,
+    so a request's rows are the same alone and in the merged call.  (A blocked
+    one-output request large enough to fill the GPU alone runs alone: its
+    tiles of the last round may be shared by several blocks.)
+
+  Launches of different kinds run on different streams, so their work
+  overlaps on the device;
+* staging   -- inputs are copied from the request's numpy array into a pinned
+  host arena allocated once (no page-locking per request), then to the device
+  without blocking the host; results come back into the arena the same way.
+  When the arena is full, a launch takes a one-off pinned buffer instead
+  (counted in ``stats()["staging_spills"]``);
+* completion -- each launch records a CUDA event; the loop polls the events,
+  hands results to the requests, frees device memory, stream and staging
+  space, and admits requests that arrived meanwhile.  A launch that fails
+  (an error raised while it is prepared) fails its requests with the message
+  and gives back everything it took.
+
+Results are identical to evaluating each request alone.  Gradient requests
+return the vector-Jacobian product dL/dx for a cotangent (default: ones),
+shape [P, d_in].
 """
 from __future__ import annotations
 
+import bisect
 import collections
 import itertools
 import threading
@@ -34,6 +54,8 @@ import torch
 
 from . import _capi as capi
 from ._capi import call, ptr
+
+_ALIGN = 256
 
 
 class Request:
@@ -70,6 +92,56 @@ class Request:
         return None if self.t_done is None else self.t_done - self.t_submit
 
 
+class PinnedArena:
+    """First-fit allocator over one page-locked host buffer (allocated once).
+
+    ``alloc`` returns an offset (bytes, 256-aligned) or None when no free
+    range is large enough; ``free`` returns a range and merges it with its
+    free neighbours."""
+
+    def __init__(self, nbytes, pinned=True):
+        self.size = int(nbytes) // _ALIGN * _ALIGN
+        self.buf = torch.empty(self.size, dtype=torch.uint8, pin_memory=pinned and self.size > 0)
+        self.free_list = [(0, self.size)] if self.size else []  # sorted (offset, length)
+        self.used = {}
+
+    def alloc(self, nbytes):
+        n = max(_ALIGN, (int(nbytes) + _ALIGN - 1) // _ALIGN * _ALIGN)
+        for i, (off, ln) in enumerate(self.free_list):
+            if ln >= n:
+                if ln == n:
+                    self.free_list.pop(i)
+                else:
+                    self.free_list[i] = (off + n, ln - n)
+                self.used[off] = n
+                return off
+        return None
+
+    def free(self, off):
+        n = self.used.pop(off)
+        i = bisect.bisect_left(self.free_list, (off, 0))
+        self.free_list.insert(i, (off, n))
+        if i + 1 < len(self.free_list) and off + n == self.free_list[i + 1][0]:  # merge with the next range
+            self.free_list[i] = (off, n + self.free_list[i + 1][1])
+            self.free_list.pop(i + 1)
+        if i > 0 and self.free_list[i - 1][0] + self.free_list[i - 1][1] == off:  # and with the previous one
+            self.free_list[i - 1] = (self.free_list[i - 1][0], self.free_list[i - 1][1] + self.free_list[i][1])
+            self.free_list.pop(i)
+
+    def view(self, off, shape, dtype):
+        """Host tensor over [off, off + nbytes) of the arena."""
+        n = int(np.prod(shape)) * torch.tensor([], dtype=dtype).element_size()
+        return self.buf[off : off + n].view(dtype).view(*shape)
+
+    @property
+    def in_use(self):
+        return sum(self.used.values())
+
+
+def _staged_bytes(n):
+    return max(_ALIGN, (int(n) + _ALIGN - 1) // _ALIGN * _ALIGN)
+
+
 class _Group:
     """Requests launched together: one stream, one completion event."""
 
@@ -79,13 +151,18 @@ class _Group:
         self.nbytes = nbytes
         self.event = torch.cuda.Event()
         self.keep = []
-        self.outputs = []
+        self.host = []      # per request: pinned host view of its result
+        self.staged = []    # arena offsets held by this group
+        self.spill = []     # one-off pinned tensors (the arena was full)
 
 
 class Server:
-    """Request loop over resident interpolants (see the module docstring)."""
+    """Request loop over resident interpolants (see the module docstring).
 
-    def __init__(self, interpolants: dict, memory_budget: float = 8.0, n_streams: int = 8):
+    ``memory_budget`` (GiB) bounds the device memory of the requests in
+    flight; ``staging`` (GiB) is the size of the pinned host arena."""
+
+    def __init__(self, interpolants: dict, memory_budget: float = 8.0, n_streams: int = 8, staging: float = 1.0):
         self.dev = torch.device("cuda", torch.cuda.current_device())
         self.sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
         self.ips = dict(interpolants)
@@ -96,6 +173,7 @@ class Server:
             self.spec[name]._backward_ops()  # gradient operands built before serving starts
         self.budget = int(memory_budget * 1024**3)
         self.in_use = 0
+        self.arena = PinnedArena(int(staging * 1024**3))
         self.streams = [torch.cuda.Stream(device=self.dev) for _ in range(n_streams)]
         self.free_streams = collections.deque(self.streams)
         self.waiting = collections.deque()
@@ -103,9 +181,11 @@ class Server:
         self.lock = threading.Lock()
         self.completed = []
         self.rejected = []
+        self.failed = []
         self.batch_launches = 0
         self.launches = 0
         self.admitted = 0
+        self.spilled = 0
 
     # ------------------------------------------------------------------ interface
     def submit(self, req: Request) -> Request:
@@ -123,7 +203,7 @@ class Server:
             return not self.waiting and not self.inflight
 
     def step(self):
-        """One scheduling step: complete finished groups, then admit and launch."""
+        """One scheduling step: complete finished launches, then admit and launch."""
         self._poll()
         self._admit()
 
@@ -135,35 +215,53 @@ class Server:
                 raise TimeoutError("server did not drain")
             time.sleep(0.0002)
 
-    # ------------------------------------------------------------------ internals
+    # ------------------------------------------------------------------ sizes
     def request_bytes(self, req):
+        """Device bytes of one request: input, output and the scratch the
+        kernels of its path allocate (from the library's workspace queries and
+        the tensors the paths create)."""
         ip = self.ips[req.name]
         P, d_in, d_out = req.points, ip.d_in, ip.d_out
-        b = P * d_in * 8 + P * d_out * (4 if req.precision == "fp32" else 8)
         sp = self.spec[req.name]
+        b = P * d_in * 8
         if req.op == "grad":
-            bwd = sp._bwd or {}
-            K = bwd.get("ldk", ip._tree.size)
-            b += P * d_in * 8 + P * K * 4 + P * 4 * ((d_out + 3) // 4 * 4) * 3 + P * 4 * bwd.get("n_slots", d_in)
+            bwd = sp._bwd
+            ldo, ldk = bwd["ldo"], bwd["ldk"]
+            step = min(P, max(128, int(sp.memory_limit * 1024**3 // (8 * ldk)) // 128 * 128))
+            b += P * d_out * 4 + 3 * P * ldo * 4 + P * d_in * 8  # cotangent, its TF32 split, dL/dx
+            b += step * (ldk + 31) // 32 * 32 * 4 + capi.size("smx_spectral_vjp_x_workspace", bwd["n_slots"], step)
         elif req.precision == "fp64":
-            b += P * ip._plan.c.n_values * 8
-        elif sp.tc is not None:
-            b += min(P, 1 << 20) * sp.tc["ldk"] * 8
-        return b
+            per_point = capi.size("smx_eval_workspace", ip._plan.ref(), 1, 64)
+            b += P * d_out * 8 + capi.size("smx_eval_workspace", ip._plan.ref(), min(P, max(1, ip._chunk(per_point))),
+                                           64)
+        else:
+            b += P * d_out * 4
+            if sp.tc is not None:
+                step = sp._tc_step(P)
+                b += 2 * step * (sp.tc["K"] + 31) // 32 * 32 * 4 + capi.size("smx_spectral_panel_workspace",
+                                                                               sp.tc["n_slots"], step)
+            elif sp.blocked is not None:
+                b += self.sms * 2 * 16 * 128 * 4 + 4 * self.sms
+        return int(b)
 
     def _kind(self, req):
-        """'blocked' / 'stream': merged into a persistent multi-plan launch; None: own launch."""
+        """Launch kind: 'blocked' / 'stream' (persistent multi-plan launches), or
+        ('plan', name, op, precision[, id]) for requests evaluated by one call
+        per interpolant."""
         sp = self.spec[req.name]
-        if req.op != "eval" or req.precision != "fp32" or sp.tc is not None:
-            return None
-        if sp.blocked is not None:
-            # a request of a full round of tiles or more fills the GPU alone (and
-            # is then evaluated exactly as alone, with the last-round split)
-            return None if req.points > 128 * self.sms else "blocked"
-        return "stream"
+        if req.op == "eval" and req.precision == "fp32" and sp.tc is None:
+            if sp.blocked is None:
+                return "stream"
+            if req.points <= 128 * self.sms:
+                return "blocked"
+            # a blocked request of a full round of tiles or more fills the GPU
+            # alone and is evaluated exactly as alone (last-round split)
+            return ("plan", req.name, req.op, req.precision, req.id)
+        return ("plan", req.name, req.op, req.precision)
 
+    # ------------------------------------------------------------------ admission
     def _admit(self):
-        batches, singles = {}, []
+        batches = {}
         with self.lock:
             avail = len(self.free_streams)  # streams not yet promised in this step
             while self.waiting:
@@ -179,44 +277,87 @@ class Server:
                 if self.in_use + nb > self.budget:
                     break
                 kind = self._kind(req)
-                if kind is None or kind not in batches:
+                if kind not in batches:
                     if avail < 1:
                         break
-                    avail -= 1  # an own launch, or the first request of a merged launch
+                    avail -= 1  # one stream per launch
                 self.waiting.popleft()
-                if kind is None:
-                    singles.append((req, nb, self.free_streams.popleft()))
-                else:
-                    batches.setdefault(kind, []).append((req, nb))
+                batches.setdefault(kind, []).append((req, nb))
                 self.in_use += nb
                 self.admitted += 1
             streams = {kind: self.free_streams.popleft() for kind in batches}
         now = time.perf_counter()
         for kind, batch in batches.items():
-            self._launch_batch(kind, batch, streams[kind], now)
-        for req, nb, stream in singles:
             try:
-                self._launch_single(req, nb, stream, now)
-            except (RuntimeError, ValueError) as e:  # the plan cannot serve this request
-                req.error = str(e)
-                req.t_done = time.perf_counter()
-                req.done.set()
-                with self.lock:
-                    self.rejected.append(req)
-                    self.in_use -= nb
-                    self.free_streams.append(stream)
+                self._launch_batch(kind, batch, streams[kind], now)
+            except Exception as e:  # the launch could not be prepared: fail its requests, give back what it took
+                self._fail(kind, batch, streams[kind], e)
 
-    def _h2d(self, req, stream):
-        xh = torch.from_numpy(req.x).pin_memory()
-        with torch.cuda.stream(stream):
-            xd = torch.empty(req.x.shape, dtype=torch.float64, device=self.dev)
-            xd.copy_(xh, non_blocking=True)
-        return xh, xd
+    def _fail(self, kind, batch, stream, exc):
+        msg = "%s: %s" % (type(exc).__name__, exc)
+        for req, _ in batch:
+            req.error = msg
+            req.t_done = time.perf_counter()
+            req.done.set()
+        g = getattr(self, "_building", None)
+        if g is not None and g.stream is stream and g.staged:
+            stream.synchronize()  # copies already queued from or into its staging ranges have finished
+        with self.lock:
+            if g is not None and g.stream is stream:
+                for off in g.staged:
+                    self.arena.free(off)
+                self._building = None
+            self.failed.extend(r for r, _ in batch)
+            self.in_use -= sum(nb for _, nb in batch)
+            self.free_streams.append(stream)
 
+    # ------------------------------------------------------------------ staging
+    def _stage(self, g, nbytes):
+        """Pinned host range of nbytes: from the arena, else a one-off pinned tensor."""
+        with self.lock:
+            off = self.arena.alloc(nbytes)
+            if off is not None:
+                g.staged.append(off)
+        if off is not None:
+            return lambda shape, dtype: self.arena.view(off, shape, dtype)
+        t = torch.empty(_staged_bytes(nbytes), dtype=torch.uint8, pin_memory=True)
+        g.spill.append(t)
+        self.spilled += 1
+        return lambda shape, dtype: t[: int(np.prod(shape)) * torch.tensor([], dtype=dtype).element_size()].view(
+            dtype).view(*shape)
+
+    def _h2d_into(self, g, req, dst):
+        """Copy the request's input into the device rows dst (stream-ordered)."""
+        view = self._stage(g, req.x.nbytes)(req.x.shape, torch.float64)
+        view.numpy()[...] = req.x
+        dst.copy_(view, non_blocking=True)
+
+    def _d2h(self, g, y):
+        h = self._stage(g, y.numel() * y.element_size())(tuple(y.shape), y.dtype)
+        h.copy_(y, non_blocking=True)
+        g.host.append(h)
+
+    # ------------------------------------------------------------------ launches
     def _launch_batch(self, kind, batch, stream, now):
         g = _Group(stream, [r for r, _ in batch], sum(nb for _, nb in batch))
-        plan_idx = {}
-        plans = []
+        self._building = g
+        with torch.cuda.stream(stream):
+            for req, _ in batch:
+                req.t_admit = now
+            if kind in ("blocked", "stream"):
+                self._launch_multiplan(kind, batch, g)
+                self.batch_launches += 1
+            else:
+                self._launch_plan(kind, batch, g)
+                if len(batch) > 1:
+                    self.batch_launches += 1
+            g.event.record(stream)
+        self._building = None
+        self.launches += 1
+        self.inflight.append(g)
+
+    def _launch_multiplan(self, kind, batch, g):
+        plan_idx, plans = {}, []
         for req, _ in batch:
             if req.name not in plan_idx:
                 plan_idx[req.name] = len(plans)
@@ -225,56 +366,56 @@ class Server:
         struct = capi.SmxBlocked if kind == "blocked" else capi.SmxSpectral
         arr = (struct * len(plans))(*plans)
         items = (capi.SmxWork * len(batch))()
-        with torch.cuda.stream(stream):
-            for i, (req, _) in enumerate(batch):
-                req.t_admit = now
-                xh, xd = self._h2d(req, stream)
-                y = torch.empty(req.points, self.ips[req.name].d_out, dtype=torch.float32, device=self.dev)
-                g.keep += [xh, xd]
-                g.outputs.append(y)
-                items[i].plan = plan_idx[req.name]
-                items[i].x = xd.data_ptr()
-                items[i].P = req.points
-                items[i].ldx = req.x.shape[1]
-                items[i].y = y.data_ptr()
-            if kind == "blocked":
-                nws = capi.size("smx_blocked_eval_batch_workspace", len(plans), len(batch))
-            else:
-                max_dout = max(p.d_out for p in plans)
-                nws = capi.size("smx_spectral_eval_batch_workspace", len(plans), len(batch), max_dout)
-            ws = torch.empty(nws, dtype=torch.uint8, device=self.dev)
-            g.keep.append(ws)
-            fn = "smx_blocked_eval_batch" if kind == "blocked" else "smx_spectral_eval_batch"
-            call(fn, arr, len(plans), items, len(batch), ptr(ws), ws.numel(), capi.stream_ptr(stream))
-            g.host = [torch.empty(y.shape, dtype=y.dtype, pin_memory=True) for y in g.outputs]
-            for h, y in zip(g.host, g.outputs):
-                h.copy_(y, non_blocking=True)
-            g.event.record(stream)
-        self.batch_launches += 1
-        self.launches += 1
-        self.inflight.append(g)
+        outs = []
+        for i, (req, _) in enumerate(batch):
+            xd = torch.empty(req.x.shape, dtype=torch.float64, device=self.dev)
+            self._h2d_into(g, req, xd)
+            y = torch.empty(req.points, self.ips[req.name].d_out, dtype=torch.float32, device=self.dev)
+            g.keep += [xd, y]
+            outs.append(y)
+            items[i].plan = plan_idx[req.name]
+            items[i].x = xd.data_ptr()
+            items[i].P = req.points
+            items[i].ldx = req.x.shape[1]
+            items[i].y = y.data_ptr()
+        if kind == "blocked":
+            nws = capi.size("smx_blocked_eval_batch_workspace", len(plans), len(batch))
+        else:
+            nws = capi.size("smx_spectral_eval_batch_workspace", len(plans), len(batch), max(p.d_out for p in plans))
+        ws = torch.empty(nws, dtype=torch.uint8, device=self.dev)
+        g.keep.append(ws)
+        fn = "smx_blocked_eval_batch" if kind == "blocked" else "smx_spectral_eval_batch"
+        call(fn, arr, len(plans), items, len(batch), ptr(ws), ws.numel(), capi.stream_ptr(g.stream))
+        for y in outs:
+            self._d2h(g, y)
 
-    def _launch_single(self, req, nb, stream, now):
-        g = _Group(stream, [req], nb)
-        ip = self.ips[req.name]
-        req.t_admit = now
-        with torch.cuda.stream(stream):
-            xh, xd = self._h2d(req, stream)
-            g.keep += [xh, xd]
-            if req.op == "eval":
-                y = ip(xd, precision=req.precision)
-            else:
-                cot = req.cotangent
-                cot = torch.ones(req.points, ip.d_out, dtype=torch.float32, device=self.dev) if cot is None else \
-                    torch.as_tensor(np.asarray(cot), dtype=torch.float32, device=self.dev)
-                y, _ = self.spec[req.name].vjp(xd, cot, need_x=True, need_coef=False, check=False)
-            g.outputs.append(y)
-            g.host = [torch.empty(y.shape, dtype=y.dtype, pin_memory=True)]
-            g.host[0].copy_(y, non_blocking=True)
-            g.event.record(stream)
-        self.launches += 1
-        self.inflight.append(g)
+    def _launch_plan(self, kind, batch, g):
+        """Requests of one interpolant, operation and precision: one call over
+        their concatenated points."""
+        name, op, prec = kind[1], kind[2], kind[3]
+        ip = self.ips[name]
+        sizes = [req.points for req, _ in batch]
+        offs = np.concatenate([[0], np.cumsum(sizes)])
+        xd = torch.empty(int(offs[-1]), ip.d_in, dtype=torch.float64, device=self.dev)
+        for (req, _), a, b in zip(batch, offs[:-1], offs[1:]):
+            self._h2d_into(g, req, xd[a:b])
+        g.keep.append(xd)
+        if op == "eval":
+            y = ip(xd, precision=prec)
+        else:
+            cot = torch.empty(int(offs[-1]), ip.d_out, dtype=torch.float32, device=self.dev)
+            for (req, _), a, b in zip(batch, offs[:-1], offs[1:]):
+                if req.cotangent is None:
+                    cot[a:b] = 1.0
+                else:
+                    cot[a:b] = torch.as_tensor(np.asarray(req.cotangent, dtype=np.float32)).to(self.dev)
+            y, _ = self.spec[name].vjp(xd, cot, need_x=True, need_coef=False, check=False)
+            g.keep.append(cot)
+        g.keep.append(y)
+        for a, b in zip(offs[:-1], offs[1:]):
+            self._d2h(g, y[a:b])
 
+    # ------------------------------------------------------------------ completion
     def _poll(self):
         done = [g for g in self.inflight if g.event.query()]
         if not done:
@@ -283,11 +424,13 @@ class Server:
         for g in done:
             self.inflight.remove(g)
             for req, h in zip(g.reqs, g.host):
-                req.result = h.numpy()
+                req.result = h.numpy().copy()
                 req.t_done = now
                 req.done.set()
                 self.completed.append(req)
             with self.lock:
+                for off in g.staged:
+                    self.arena.free(off)
                 self.in_use -= g.nbytes
                 self.free_streams.append(g.stream)
 
@@ -296,9 +439,9 @@ class Server:
         lat = np.array([r.latency for r in self.completed]) if self.completed else np.zeros(1)
         evals = sum(r.points * self.ips[r.name].d_out for r in self.completed if r.op == "eval")
         return dict(
-            completed=len(self.completed), rejected=len(self.rejected), launches=self.launches,
-            batch_launches=self.batch_launches, p50_ms=float(np.percentile(lat, 50) * 1e3),
-            p99_ms=float(np.percentile(lat, 99) * 1e3), evals=int(evals),
+            completed=len(self.completed), rejected=len(self.rejected), failed=len(self.failed),
+            launches=self.launches, batch_launches=self.batch_launches, staging_spills=self.spilled,
+            p50_ms=float(np.percentile(lat, 50) * 1e3), p99_ms=float(np.percentile(lat, 99) * 1e3), evals=int(evals),
         )
 
 

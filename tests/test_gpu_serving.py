@@ -84,3 +84,40 @@ def test_burst_and_rejection(fleet):
     assert big.error is not None and big.result is None
     for r in reqs:
         np.testing.assert_array_equal(r.result, _alone(fleet, r))
+
+
+def test_merged_gradients_tensor_core_and_fp64_equal_alone(fleet):
+    """A burst of gradient requests and tensor-core evaluations of one
+    interpolant and FP64 evaluations of another, submitted together: each
+    group is served by one merged call (one launch per interpolant, operation
+    and precision), and every request's rows equal its result alone.  The
+    pinned staging arena is made too small for some inputs (one-off pinned
+    buffers are then used)."""
+    from smolyax_gb300.serving import Request, Server
+
+    rng = np.random.default_rng(21)
+    reqs = []
+    for P in (1, 17, 300, 129, 64, 2000):
+        reqs.append(Request("d", rng.uniform(-0.9, 0.9, (P, fleet["d"].d_in)), op="grad",
+                            cotangent=rng.normal(size=(P, fleet["d"].d_out)).astype(np.float32)))
+    for P in (5, 700, 33, 128):
+        reqs.append(Request("d", rng.uniform(-0.9, 0.9, (P, fleet["d"].d_in))))
+    for P in (3, 90, 400):
+        reqs.append(Request("b", rng.uniform(-0.9, 0.9, (P, fleet["b"].d_in)), precision="fp64"))
+    server = Server(fleet, memory_budget=4.0, n_streams=8, staging=1e-5)  # 10 KiB arena
+    for r in reqs:
+        server.submit(r)
+    server.drain()
+    st = server.stats()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["launches"] == 3 and st["batch_launches"] == 3 and st["staging_spills"] > 0
+    for r in reqs:
+        assert r.error is None
+        x = torch.as_tensor(r.x, device="cuda")
+        ip = fleet[r.name]
+        if r.op == "grad":
+            g = torch.as_tensor(r.cotangent, device="cuda")
+            alone = ip.spectral_plan().vjp(x, g, need_x=True, need_coef=False)[0].cpu().numpy()
+        else:
+            alone = ip(x, precision=r.precision).cpu().numpy()
+        np.testing.assert_array_equal(r.result, alone)

@@ -21,7 +21,7 @@ class _Scheduler(serving.Server):
         self.waiting = collections.deque()
         self.inflight = []
         self.lock = threading.Lock()
-        self.completed, self.rejected = [], []
+        self.completed, self.rejected, self.failed = [], [], []
         self.batch_launches = self.launches = self.admitted = 0
         self.ips = {name: type("IP", (), {"d_in": 3})() for name in kinds}
         self._kinds, self._bpp, self._failing = kinds, bytes_per_point, set(failing)
@@ -34,12 +34,9 @@ class _Scheduler(serving.Server):
         return self._kinds[req.name]
 
     def _launch_batch(self, kind, batch, stream, now):
-        self.launched.append((kind, [r.id for r, _ in batch], stream))
-
-    def _launch_single(self, req, nb, stream, now):
-        if req.name in self._failing:
+        if any(r.name in self._failing for r, _ in batch):
             raise RuntimeError("the plan cannot serve this request")
-        self.launched.append((None, [req.id], stream))
+        self.launched.append((kind, [r.id for r, _ in batch], stream))
 
 
 def _req(name, points, op="eval"):
@@ -59,8 +56,9 @@ def test_requests_wait_in_order_at_the_budget():
     s = _Scheduler(budget=1000, n_streams=8, kinds={"a": None}, bytes_per_point={"a": 10})
     r = [s.submit(_req("a", n)) for n in (60, 30, 20, 5)]
     s._admit()
-    # 600 + 300 fit; the third (200) does not, and the fourth may not overtake it
-    assert [ids for _, ids, _ in s.launched] == [[r[0].id], [r[1].id]]
+    # 600 + 300 fit (one merged launch of the same kind); the third (200) does
+    # not, and the fourth may not overtake it
+    assert [ids for _, ids, _ in s.launched] == [[r[0].id, r[1].id]]
     assert list(s.waiting) == [r[2], r[3]] and s.in_use == 900
 
 
@@ -79,7 +77,18 @@ def test_failed_launch_returns_its_stream_and_memory():
     s = _Scheduler(budget=1000, n_streams=1, kinds={"f": None}, bytes_per_point={"f": 10}, failing={"f"})
     bad = s.submit(_req("f", 10, op="grad"))
     s._admit()
-    assert bad.error and bad in s.rejected and s.in_use == 0 and list(s.free_streams) == ["s0"]
+    assert bad.error and bad.done.is_set() and bad in s.failed and s.in_use == 0 and list(s.free_streams) == ["s0"]
+
+
+def test_failed_merged_launch_fails_every_request_and_returns_everything():
+    s = _Scheduler(budget=1000, n_streams=2, kinds={"f": "blocked", "a": None}, bytes_per_point={"f": 10, "a": 1},
+                   failing={"f"})
+    bad = [s.submit(_req("f", 10)) for _ in range(3)]
+    ok = s.submit(_req("a", 10))
+    s._admit()
+    assert all(r.error and r.done.is_set() and r in s.failed for r in bad)
+    assert [ids for _, ids, _ in s.launched] == [[ok.id]]
+    assert s.in_use == 10 and len(s.free_streams) == 1  # only the good launch holds memory and a stream
 
 
 def test_submit_checks_name_and_width():
@@ -88,3 +97,23 @@ def test_submit_checks_name_and_width():
         s.submit(_req("zz", 1))
     with pytest.raises(ValueError):
         s.submit(serving.Request("a", np.zeros((2, 4))))
+
+
+def test_pinned_arena_first_fit_and_merging():
+    import torch
+
+    from smolyax_gb300.serving import PinnedArena
+
+    a = PinnedArena(4096, pinned=False)  # the allocator logic; page-locking needs a GPU
+    x, y, z = a.alloc(1000), a.alloc(256), a.alloc(1)
+    assert (x, y, z) == (0, 1024, 1280) and a.in_use == 1536
+    assert a.alloc(4096) is None
+    a.free(y)
+    assert a.alloc(200) == 1024  # first fit reuses the hole
+    a.free(x)
+    a.free(1024)
+    a.free(z)
+    assert a.free_list == [(0, 4096)] and a.in_use == 0
+    v = a.view(a.alloc(80), (10,), torch.float64)
+    v[:] = 3.0
+    assert float(v.sum()) == 30.0
