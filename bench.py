@@ -268,6 +268,25 @@ def run_reference(args):
     return 0
 
 
+def _vec_target_device(kind, d, d_out, seed):
+    """The function of _vec_target (same seeded weights) as a torch function of
+    device tensors, evaluated on the GPU at set-up (``f.on_device``)."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    if kind == "leja":
+        W = rng.uniform(0, 1, (d_out, d)) / (np.arange(d) + 1) ** 2
+        W *= 0.5 / W.sum(axis=1, keepdims=True)
+        Wd = torch.as_tensor(W, device="cuda")
+        f = lambda X: 1.0 / (1.0 + X @ Wd.T)
+    else:
+        A = rng.normal(0.0, 0.3, (d_out, d)) / (np.arange(d) + 1) ** 1.5
+        Ad = torch.as_tensor(A, device="cuda")
+        f = lambda X: torch.exp(-(X @ Ad.T))
+    f.on_device = True
+    return f
+
+
 def _vec_target(kind, d, d_out, seed):
     rng = np.random.default_rng(seed)
     if kind == "leja":
@@ -495,7 +514,8 @@ def serving_workload(n_req, rate):
         t = indices.find_approximate_threshold(k, lam, nested=True, accuracy=0.01)
         gen = nodes.Leja(dim=d) if kind == "leja" else nodes.GaussHermite(dim=d)
         ips["ip%02d" % i] = SmolyakBarycentricInterpolator(node_gen=gen, k=k, t=t, d_out=d_out,
-                                                            f=_vec_target(kind, d, d_out, i), memory_limit=2.0)
+                                                            f=_vec_target_device(kind, d, d_out, i),
+                                                            memory_limit=2.0)
     server = Server(ips, memory_budget=48.0, n_streams=8)
     setup_s = time.perf_counter() - t0
     rng = np.random.default_rng(1)

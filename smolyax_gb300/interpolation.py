@@ -100,7 +100,16 @@ class SmolyakBarycentricInterpolator:
     # ------------------------------------------------------------------ set-up
     def set_f(self, *, f: Callable, f_evals: dict = None) -> dict:
         """Evaluate (or reuse) f at the interpolation nodes and build the device plan
-        (``interpolation.py:115-239``).  Returns the updated f-evaluation dictionary."""
+        (``interpolation.py:115-239``).  Returns the updated f-evaluation dictionary.
+
+        By default f is called on the host as in the reference: with one point
+        of shape (d_in,) at a time, or, if f has a true attribute
+        ``vectorized``, once with the stacked [n, d_in] array of the missing
+        nodes.  If f has a true attribute ``on_device``, it is called with CUDA
+        tensors [n, d_in] (FP64) of node points, in chunks, and must return
+        [n, d_out] tensors on the device; the nodal values then stay on the
+        device and are not added to ``f_evals`` (the dictionary is returned
+        unchanged and its entries are not reused)."""
         if f_evals is None:
             f_evals = {}
         dev = indices.device()
@@ -124,11 +133,15 @@ class SmolyakBarycentricInterpolator:
             cache0 = f_evals
         else:
             cache0 = f_evals.get((), {})
+        on_device = bool(getattr(f, "on_device", False))
         if zeta0 != 0:
-            if () not in cache0:
+            if on_device:
+                cache0 = {(): f(torch.as_tensor(zero[None, :], device=dev)).reshape(-1).double().cpu().numpy()}
+                self._n_f_evals_new += 1
+            elif () not in cache0:
                 cache0[()] = f(zero.copy())
                 self._n_f_evals_new += 1
-            if not self._is_nested:
+            if not self._is_nested and not on_device:
                 f_evals[()] = cache0
             offset = zeta0 * self._as_out(cache0[()])
         else:
@@ -179,9 +192,13 @@ class SmolyakBarycentricInterpolator:
         P.set("sum_pairs", sum_pairs)
         P.set("sum_eoff", sum_eoff)
 
-        # nodal values: host calls of f with the reference's cache keys, device gather
-        fu, umap = self._evaluate_nodes(f, f_evals, zero, sum_poff.cpu().numpy(), sum_pairs.cpu().numpy(),
-                                        pair_dim_h, pair_deg_h, pair_voff_h, node_h, R)
+        # nodal values: calls of f with the reference's cache keys, device gather
+        if on_device:
+            fu_d, umap = self._evaluate_nodes_on_device(f, zero, sum_poff.cpu().numpy(), sum_pairs.cpu().numpy(),
+                                                        pair_dim_h, pair_deg_h, pair_voff_h, node_h, R, dev)
+        else:
+            fu, umap = self._evaluate_nodes(f, f_evals, zero, sum_poff.cpu().numpy(), sum_pairs.cpu().numpy(),
+                                            pair_dim_h, pair_deg_h, pair_voff_h, node_h, R)
         P.set("F64", torch.empty(max(R * d_out, 1), dtype=torch.float64, device=dev))
         P.set("F32", torch.empty(max(R * d_out, 1), dtype=torch.float32, device=dev))
         c = P.c
@@ -194,7 +211,7 @@ class SmolyakBarycentricInterpolator:
         P.keep["umap"] = T(umap, torch.int64)
         P.keep["offset0"] = T(offset, torch.float64)  # zeta_0 f(zero) as the reference computes it
         self._plan = P
-        self._assemble_rows(T(fu, torch.float64))
+        self._assemble_rows(fu_d if on_device else T(fu, torch.float64))
         P.keep["ent"] = ent
         self._spectral = None
         self._tree = tree
@@ -317,6 +334,66 @@ class SmolyakBarycentricInterpolator:
                 vals.append(self._as_out(cache[key]))
             umap[r] = idx
         fu = np.array(vals, dtype=float).reshape(-1, self._d_out) if vals else np.zeros((1, self._d_out))
+        return fu, umap
+
+    def _evaluate_nodes_on_device(self, f, zero, sum_poff, sum_pairs, pdim, pdeg, pvoff, node, R, dev,
+                                  chunk=1 << 16):
+        """Unique nodal values computed by a device function f, and the row ->
+        value map.  The unique nodes are found with the same keys as
+        ``_evaluate_nodes`` (one per sparse node multi-index for nested rules,
+        per multi-index nu and node otherwise), each recorded sparsely as the
+        (dimension, node value) pairs of its summand; dense [chunk, d_in] point
+        arrays are then assembled on the device (the zero point, with those
+        coordinates scattered in) and passed to f."""
+        nested = self._is_nested
+        index = {}
+        umap = np.empty(R, dtype=np.int64)
+        pt_len, pt_dims, pt_vals = [], [], []
+        r = 0
+        for s in range(len(sum_poff) - 1):
+            prs = sum_pairs[sum_poff[s] : sum_poff[s + 1]]
+            dims = [int(pdim[u]) for u in prs]
+            degs = [int(pdeg[u]) for u in prs]
+            offs = [int(pvoff[u]) for u in prs]
+            nu = None if nested else tuple(zip(dims, degs))
+            n = len(dims)
+            mu = [0] * n
+            for _ in range(int(np.prod([g + 1 for g in degs]))):
+                gk = (nu, tuple((dims[i], mu[i]) for i in range(n) if mu[i] > 0))
+                idx = index.get(gk)
+                if idx is None:
+                    idx = index[gk] = len(pt_len)
+                    pt_len.append(n)
+                    pt_dims.extend(dims)
+                    pt_vals.extend(node[offs[i] + mu[i]] for i in range(n))
+                umap[r] = idx
+                r += 1
+                for i in range(n - 1, -1, -1):
+                    mu[i] += 1
+                    if mu[i] <= degs[i]:
+                        break
+                    mu[i] = 0
+        U = len(pt_len)
+        self._n_f_evals_new += U
+        fu = torch.empty(max(U, 1), self._d_out, dtype=torch.float64, device=dev)
+        if U == 0:
+            fu.zero_()
+            return fu, umap
+        lens = np.asarray(pt_len, dtype=np.int64)
+        starts = np.concatenate([[0], np.cumsum(lens)])
+        pt_dims = torch.as_tensor(np.asarray(pt_dims, dtype=np.int64), device=dev)
+        pt_vals = torch.as_tensor(np.asarray(pt_vals, dtype=np.float64), device=dev)
+        zero_d = torch.as_tensor(zero, dtype=torch.float64, device=dev)
+        for u0 in range(0, U, chunk):
+            u1 = min(U, u0 + chunk)
+            a, b = int(starts[u0]), int(starts[u1])
+            X = zero_d.repeat(u1 - u0, 1)
+            rows = torch.as_tensor(np.repeat(np.arange(u1 - u0), lens[u0:u1]), device=dev)
+            X[rows, pt_dims[a:b]] = pt_vals[a:b]
+            out = torch.as_tensor(f(X), device=dev).to(torch.float64).reshape(u1 - u0, -1)
+            if out.shape[1] != self._d_out:
+                raise ValueError("f returned %d outputs per point, expected d_out = %d" % (out.shape[1], self._d_out))
+            fu[u0:u1] = out
         return fu, umap
 
     # ------------------------------------------------------------------ evaluation
