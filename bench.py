@@ -480,6 +480,50 @@ def backward_workload(steps, warmup, points=None):
     return line
 
 
+def quadrature_workload(max_samples=1 << 26):
+    """The reference's quadrature study (notebooks/smolyak_quadrature.ipynb) on
+    the GPU: Gauss-Hermite d_in=100, k_j = log((j+2)^2 / 0.1), f(x) = 1/(1 + 0.1
+    sum_j (j+2)^-2 x_j); integrals of the interpolants of 10 thresholds up to
+    |Lambda| ~ 1000, then Monte-Carlo means of the second-finest interpolant
+    over N = 2^14 .. max_samples samples, against its integral."""
+    import torch
+
+    from smolyax_gb300 import SmolyakBarycentricInterpolator, indices, nodes
+    from smolyax_gb300.quadrature import integral_sweep, monte_carlo
+
+    d, r, theta = 100, 2.0, 0.1
+    wj = theta * (np.arange(d) + 2.0) ** (-r)
+
+    def f(x):
+        return np.atleast_1d(1.0 / (1.0 + np.asarray(x) @ wj))
+
+    gen = nodes.GaussHermite(dim=d)
+    k = np.log((np.arange(d) + 2.0) ** r / theta)
+    t_max = indices.find_approximate_threshold(k, 1000, gen.is_nested)
+    ts = np.linspace(1.0, t_max, 10)
+    t0 = time.perf_counter()
+    sweep = integral_sweep(gen, k, f, ts, d_out=1)
+    sweep_s = time.perf_counter() - t0
+    ip = SmolyakBarycentricInterpolator(node_gen=gen, k=k, t=float(ts[-2]), d_out=1, f=f)
+    q = float(ip.integral().cpu().numpy()[0])
+    mc = []
+    n = 1 << 14
+    while n <= max_samples:
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        mean, se = monte_carlo(ip, n, seed=n)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t1
+        mc.append({"N": n, "rel_err": float(abs(mean[0] - q) / abs(q)), "std_err_rel": float(se[0] / abs(q)),
+                   "seconds": dt, "samples_per_s": n / dt})
+        n <<= 2
+    return {"workload": "quadrature", "config": {"d_in": d, "rule": "gauss-hermite", "r": r, "theta": theta,
+                                                 "thresholds": [float(t) for t in ts]},
+            "sweep": [{"t": x["t"], "n_f_evals": x["n_f_evals"], "integral": float(x["integral"][0]),
+                       "err_vs_finest": x["err"], "integral_ms": 1e3 * x["seconds"]} for x in sweep],
+            "sweep_seconds": sweep_s, "integral_second_finest": q, "monte_carlo": mc}
+
+
 def serving_fleet(seed=0):
     """16 interpolants: d_in log-uniform [4, 1000], d_out in {1, 16, 256, 1024},
     |Lambda| log-uniform [1e2, 1e5], Leja or Gauss-Hermite at random (seed 0)."""
@@ -680,6 +724,7 @@ def extras():
     out = {}
     for key, fn in (("gh2048_tensor_core", lambda: tensor_workload("gh2048", 5, 3)),
                     ("leja64_forward_backward", lambda: backward_workload(5, 3)),
+                    ("quadrature", lambda: quadrature_workload(1 << 24)),
                     ("serving", lambda: serving_workload(300, 200.0))):
         t0 = time.perf_counter()
         try:
@@ -701,7 +746,7 @@ def main():
     ap.add_argument("--points", type=int, default=POINTS)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="leja1000",
-                    choices=["leja1000", "serving", "leja64bwd"] + sorted(WORKLOADS))
+                    choices=["leja1000", "serving", "leja64bwd", "quadrature"] + sorted(WORKLOADS))
     ap.add_argument("--requests", type=int, default=300)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--no-extras", action="store_true", help="headline only (skip the other configurations)")
@@ -710,6 +755,9 @@ def main():
         return run_reference(args)
     if args.workload == "serving":
         return run_serving(args)
+    if args.workload == "quadrature":
+        print(json.dumps(quadrature_workload()))
+        return 0
     if args.workload == "leja64bwd":
         return run_backward_workload(args)
     if args.workload != "leja1000":
