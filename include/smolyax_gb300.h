@@ -431,6 +431,31 @@ int smx_split_bf16(const float* src, int64_t rows, int64_t cols, int64_t lds, ui
 int smx_split_tf32(const float* src, int64_t rows, int64_t cols, int64_t lds, float* hi, float* lo, int64_t ldo,
                    void* stream);
 
+/* ---- host-side layout builders of the FP32 evaluators ------------------------------
+ * The tables of the blocked one-output evaluator (smx_blocked), of the
+ * per-point evaluator (smx_spectral) and the entry tape of the tensor-core
+ * panel, built on the host from host copies of the index-set tree (entry 0 =
+ * root, parent[0] = -1; level = number of non-zero entries; rank = DFS
+ * pre-order rank, as smx_lambda_ranks writes it in SMX_MODE_PREORDER) and the
+ * FP32 coefficients C[n][d_out] of every entry.  They re-express the
+ * reference's evaluation (interpolation.py:264-304) as the smx_spectral /
+ * smx_blocked comments describe; smx_fp32_plan_create uses them.  Tables are
+ * read back by name (the field names of smx_blocked / smx_spectral, plus
+ * "dims", "dmax", "dsoff", "tape", "ent", "lvl1" of the tape). */
+#define SMX_LAYOUT_BLOCKED 0
+#define SMX_LAYOUT_PERPOINT 1
+#define SMX_LAYOUT_TAPE 2
+typedef struct smx_host_tables smx_host_tables;
+int smx_layout_build(int kind, int64_t n, const int32_t* parent_host, const int32_t* dim_host,
+                     const int32_t* deg_host, const int32_t* level_host, const int64_t* rank_host,
+                     const double* rem_host, const float* C_host, int d_out, const int64_t* maxdeg_host, int d,
+                     const int32_t* fam_host, const double* fam_a_host, const double* fam_b_host,
+                     smx_host_tables** out);
+int smx_layout_i32(const smx_host_tables* tables, const char* name, const int32_t** data_host, int64_t* count);
+int smx_layout_f32(const smx_host_tables* tables, const char* name, const float** data_host, int64_t* count);
+int smx_layout_scalar(const smx_host_tables* tables, const char* name, double* value);
+void smx_layout_free(smx_host_tables* tables);
+
 /* ---- allocation-free FP64 evaluation -------------------------------------------------
  * No counterpart in the reference: an added entry point for callers that
  * cannot allocate device memory while evaluating (FFI hosts without a CUDA

@@ -180,6 +180,12 @@ SIGNATURES = {
                                    _p, _sz, _p]),
     "smx_spectral_coefficients_adjoint": (_int, [_p, _p, _p, _p, _p, _p, _p]),
     "smx_split_tf32": (_int, [_p, _i64, _i64, _i64, _p, _p, _i64, _p]),
+    "smx_layout_build": (_int, [_int, _i64, _p, _p, _p, _p, _p, _p, _p, _int, _p, _int, _p, _p, _p,
+                                 C.POINTER(_p)]),
+    "smx_layout_i32": (_int, [_p, C.c_char_p, C.POINTER(_p), C.POINTER(_i64)]),
+    "smx_layout_f32": (_int, [_p, C.c_char_p, C.POINTER(_p), C.POINTER(_i64)]),
+    "smx_layout_scalar": (_int, [_p, C.c_char_p, C.POINTER(_dbl)]),
+    "smx_layout_free": (None, [_p]),
     "smx_last_error_string": (C.c_char_p, []),
     "smx_version": (C.c_char_p, []),
 }
@@ -230,3 +236,48 @@ def ptr(t):
 
 def stream_ptr(stream):
     return C.c_void_p(stream.cuda_stream) if stream is not None else None
+
+
+LAYOUT_KINDS = {"blocked": 0, "perpoint": 1, "tape": 2}
+
+
+def host_layout(kind, tree, coef, d_out, maxdeg, fam, fa, fb, i32=(), f32=(), scalars=()):
+    """Tables of the library's host-side layout builder (``smx_layout_build``)
+    as numpy copies: {name: array or float}.  ``tree`` holds host arrays
+    parent, dim, deg, level, rank, rem; coef is FP32 [n, d_out] (unused for
+    the tape).  Returns None if the plan is outside the evaluator's limits."""
+    import numpy as np
+
+    lib = load()
+    n = int(tree["parent"].shape[0])
+    d = int(np.asarray(maxdeg).shape[0])
+    arr = lambda a, dt: np.ascontiguousarray(np.asarray(a), dtype=dt)
+    keep = [arr(tree["parent"], np.int32), arr(tree["dim"], np.int32), arr(tree["deg"], np.int32),
+            arr(tree["level"], np.int32), arr(tree["rank"], np.int64), arr(tree["rem"], np.float64),
+            arr(coef if coef is not None else np.zeros((n, d_out)), np.float32), arr(maxdeg, np.int64),
+            arr(fam, np.int32), arr(fa, np.float64), arr(fb, np.float64)]
+    ptrs = [k.ctypes.data_as(C.c_void_p) for k in keep]
+    h = C.c_void_p()
+    rc = lib.smx_layout_build(LAYOUT_KINDS[kind], n, *ptrs[:7], int(d_out), ptrs[7], d, *ptrs[8:], C.byref(h))
+    if rc == -5:
+        return None
+    if rc != SMX_OK:
+        raise RuntimeError("smx_layout_build failed (%d): %s" % (rc, lib.smx_last_error_string().decode()))
+    out = {}
+    try:
+        for names, fn, ct, dt in ((i32, lib.smx_layout_i32, C.c_int32, np.int32),
+                                  (f32, lib.smx_layout_f32, C.c_float, np.float32)):
+            for name in names:
+                p, cnt = C.c_void_p(), _i64()
+                if fn(h, name.encode(), C.byref(p), C.byref(cnt)) != SMX_OK:
+                    raise KeyError(name)
+                out[name] = np.zeros(0, dt) if cnt.value == 0 else \
+                    np.ctypeslib.as_array(C.cast(p, C.POINTER(ct)), shape=(cnt.value,)).astype(dt).copy()
+        for name in scalars:
+            v = _dbl()
+            if lib.smx_layout_scalar(h, name.encode(), C.byref(v)) != SMX_OK:
+                raise KeyError(name)
+            out[name] = v.value
+    finally:
+        lib.smx_layout_free(h)
+    return out

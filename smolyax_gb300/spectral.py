@@ -174,19 +174,10 @@ class SpectralPlan:
         """Operands of the tensor-core contraction: tape over all non-root entries
         (pre-order), coefficient matrix B = C^T split into TF32 hi/lo."""
         self.tree_np, self.maxdeg = tr, maxdeg
-        dims = np.nonzero(maxdeg > 0)[0]
-        dmax = maxdeg[dims]
-        dsoff = np.concatenate([[0], np.cumsum(dmax)[:-1]]) if dims.size else np.zeros(0, np.int64)
-        n_slots = int(dmax.sum())
-        if int(tr["level"].max()) > 8:
+        tp = build_tape(tr, maxdeg)
+        if tp is None:
             return  # the FP32 stream evaluator serves this plan
-        idx = np.full(maxdeg.shape[0], -1, dtype=np.int64)
-        idx[dims] = np.arange(dims.size)
-        n = tr["parent"].shape[0]
-        ent = np.arange(1, n)
-        ent = ent[np.argsort(tr["rank"][ent], kind="stable")]
-        slot = dsoff[idx[tr["dim"][ent]]] + tr["deg"][ent] - 1
-        tape = (slot | (tr["level"][ent] << 16)).astype(np.int32)
+        dims, dmax, dsoff, n_slots, tape, ent = (tp[key] for key in ("dims", "dmax", "dsoff", "n_slots", "tape", "ent"))
         K = int(ent.size)
         ldk = _round32(max(K, 1))  # 128-byte rows: whole cache lines per TMA row of B
         d_out = C32.shape[1]
@@ -446,6 +437,28 @@ class SpectralPlan:
             call("smx_gemm_tf32x3", ptr(Ah), ptr(Al), lda, ptr(tc["Bh"]), ptr(tc["Bl"]), ldk, p1 - p0, d_out,
                  tc["K"], ptr(y[p0:p1]), d_out, ptr(tc["bias"]), 0, ptr(tc["err"]), st)
         return y
+
+
+def build_tape(tr, maxdeg):
+    """Tape of the tensor-core panel: the non-root entries in DFS pre-order,
+    word = basis slot | depth << 16, the slots of dimension j (max degree
+    m_j > 0) being dsoff[j] .. dsoff[j] + m_j - 1.  None when an entry is
+    deeper than 8 (the panel's register product stack)."""
+    maxdeg = np.asarray(maxdeg)
+    if int(tr["level"].max()) > 8:
+        return None
+    dims = np.nonzero(maxdeg > 0)[0]
+    dmax = maxdeg[dims]
+    dsoff = np.concatenate([[0], np.cumsum(dmax)[:-1]]) if dims.size else np.zeros(0, np.int64)
+    idx = np.full(maxdeg.shape[0], -1, dtype=np.int64)
+    idx[dims] = np.arange(dims.size)
+    n = tr["parent"].shape[0]
+    ent = np.arange(1, n)
+    ent = ent[np.argsort(tr["rank"][ent], kind="stable")]
+    slot = dsoff[idx[tr["dim"][ent]]] + tr["deg"][ent] - 1
+    tape = (slot | (tr["level"][ent] << 16)).astype(np.int32)
+    return dict(dims=dims, dmax=dmax, dsoff=dsoff, n_slots=int(dmax.sum()), tape=tape, ent=ent,
+                lvl1=np.nonzero(tr["level"][ent] == 1)[0])
 
 
 def segment_count(K, n_lvl1, n_points, sms):
