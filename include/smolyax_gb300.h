@@ -4,8 +4,10 @@
  *
  * Conventions
  *  - Every pointer argument is a DEVICE pointer owned by the caller unless the
- *    comment says "host".  The library allocates no device memory: scratch
- *    space is passed in by the caller (`ws`, `ws_bytes`).
+ *    comment says "host".  Scratch space is passed in by the caller (`ws`,
+ *    `ws_bytes`); the only entry point that allocates device memory is
+ *    smx_fp32_plan_create (the FP32 plan's tables, released by
+ *    smx_fp32_plan_destroy).
  *  - `stream` is a cudaStream_t passed as void*; all work is stream-ordered and
  *    asynchronous unless the comment says the call synchronises.
  *  - Every entry point returns SMX_OK (0) or one of the negative SMX_ERR_*
@@ -121,6 +123,8 @@ typedef struct smx_plan {
   const double* F64;           /* [n_entries * d_out] zeta * f(node)               */
   const float* F32;            /* [n_entries * d_out] FP32 rounding of F64 (or NULL)*/
   const double* offset;        /* [d_out] zeta_0 * f(zero point)                   */
+  const struct smx_fp32_plan* fp32; /* FP32 form (smx_fp32_plan_create), or NULL:
+                                       smx_eval(plan, 32, ...) evaluates through it */
 } smx_plan;
 
 /* Barycentric weights of every pair: w_b = prod_a 1/(xi_a - xi_b) with zero
@@ -164,9 +168,11 @@ int smx_basis_f64(const smx_plan* plan_host, const double* x, int64_t P, int64_t
  * (barycentric.py:69-123, interpolation.py:264-304). */
 int smx_contract_f64(const smx_plan* plan_host, const double* Lt, int64_t P, double* y, void* stream);
 
-/* One call of the FP64 path: basis table into `ws`, then the contraction.
- * ws_bytes must be at least smx_eval_workspace(plan, P, 64); y is FP64
- * [P, d_out] (interpolation.py:264-304). */
+/* One evaluation call (interpolation.py:264-304).  precision 64: the FP64
+ * path (basis table into `ws`, then the contraction; y is FP64 [P, d_out]).
+ * precision 32: the FP32 form plan->fp32 (SMX_ERR_UNSUPPORTED if NULL; y is
+ * FP32 [P, d_out]), as smx_fp32_eval.  ws_bytes >= smx_eval_workspace(plan,
+ * P, precision). */
 size_t smx_eval_workspace(const smx_plan* plan_host, int64_t P, int precision);
 int smx_eval(const smx_plan* plan_host, int precision, const double* x, int64_t P, int64_t ldx, void* y, void* ws,
              size_t ws_bytes, void* stream);
@@ -455,6 +461,58 @@ int smx_layout_i32(const smx_host_tables* tables, const char* name, const int32_
 int smx_layout_f32(const smx_host_tables* tables, const char* name, const float** data_host, int64_t* count);
 int smx_layout_scalar(const smx_host_tables* tables, const char* name, double* value);
 void smx_layout_free(smx_host_tables* tables);
+
+/* ---- FP32 form of a plan behind the C ABI -------------------------------------------
+ * smx_fp32_plan_create builds the orthogonal-polynomial form of an FP64 plan
+ * (coefficients in FP64 on the device: smx_spectral_pairs and
+ * smx_spectral_coefficients; pair degrees up to 23) and the tables of the
+ * evaluator that serves it: the blocked evaluator for one output, the
+ * per-point evaluator for 2..15 outputs, the tcgen05 3xTF32 contraction for
+ * 16 or more outputs (or rows too large for the per-point evaluator).  It is
+ * what the Python package builds for precision="fp32" (the same host layout
+ * builders), replacing interpolation.py:264-304 in FP32.  The tree is the
+ * index set built by smx_lambda_* in SMX_MODE_NONZERO (device arrays); fam /
+ * fam_a / fam_b (host, [d_in]) are each dimension's polynomial family (0
+ * Legendre, 1 Hermite) and affine map z = a x + b of its node rule.  The
+ * handle keeps `plan_host` (which must outlive it) and owns device memory for
+ * its tables (allocated here, released by smx_fp32_plan_destroy);
+ * memory_limit_gib bounds the points per tensor-core chunk.  The call
+ * synchronises `stream`. */
+typedef struct smx_tree {
+  int64_t n;                  /* entries, root first                            */
+  const int32_t* parent;      /* [n] (-1 for the root)                          */
+  const int32_t* dim;         /* [n] last non-zero entry (dim, deg)             */
+  const int32_t* deg;         /* [n]                                            */
+  const double* rem;          /* [n] remaining budget                           */
+  const int64_t* first_child; /* [n] children range (smx_lambda_expand order)  */
+  const int64_t* n_child;     /* [n]                                            */
+} smx_tree;
+typedef struct smx_fp32_plan smx_fp32_plan;
+#define SMX_FP32_BLOCKED 0
+#define SMX_FP32_PERPOINT 1
+#define SMX_FP32_TENSOR 2
+int smx_fp32_plan_create(const smx_plan* plan_host, const smx_tree* tree_host, const int32_t* fam_host,
+                         const double* fam_a_host, const double* fam_b_host, double memory_limit_gib,
+                         smx_fp32_plan** out, void* stream);
+void smx_fp32_plan_destroy(smx_fp32_plan* fp32);
+/* Evaluator (SMX_FP32_*), |Lambda| and the device FP64 coefficients [n_lambda][d_out]. */
+int smx_fp32_plan_info(const smx_fp32_plan* fp32, int* evaluator, int64_t* n_lambda, const double** coef);
+/* y[P, d_out] (FP32) at x[P, ldx] (FP64). */
+size_t smx_fp32_workspace(const smx_fp32_plan* fp32, int64_t P);
+int smx_fp32_eval(const smx_fp32_plan* fp32, const double* x, int64_t P, int64_t ldx, float* y, void* ws,
+                  size_t ws_bytes, void* stream);
+/* SMX_OK, or SMX_ERR_CUDA if a tensor-core pipeline wait of an earlier call
+ * timed out (those results are invalid); resets the flag; synchronises. */
+int smx_fp32_plan_check(const smx_fp32_plan* fp32, void* stream);
+/* Vector-Jacobian products of y = I(x) (the FP32 form) at the cotangent
+ * g[P, ldg] (FP32): dx[P, lddx] = dL/dx (FP64; NULL to skip) and
+ * dF[n_entries, d_out] = dL/d(plan rows F64) (FP64; NULL to skip).  The
+ * reference has no hand-written derivative w.r.t. the nodal values; dL/dx is
+ * the transpose of its Jacobian (barycentric.py:126-229,
+ * interpolation.py:306-345) applied to g.  Needs index-set depth <= 8. */
+size_t smx_vjp_workspace(const smx_fp32_plan* fp32, int64_t P);
+int smx_vjp(const smx_fp32_plan* fp32, const double* x, int64_t P, int64_t ldx, const float* g, int64_t ldg,
+            double* dx, int64_t lddx, double* dF, void* ws, size_t ws_bytes, void* stream);
 
 /* ---- allocation-free FP64 evaluation -------------------------------------------------
  * No counterpart in the reference: an added entry point for callers that

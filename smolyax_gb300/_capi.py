@@ -49,6 +49,21 @@ class SmxPlan(C.Structure):
         ("F64", _p),
         ("F32", _p),
         ("offset", _p),
+        ("fp32", _p),
+    ]
+
+
+class SmxTree(C.Structure):
+    """Mirror of ``struct smx_tree``."""
+
+    _fields_ = [
+        ("n", _i64),
+        ("parent", _p),
+        ("dim", _p),
+        ("deg", _p),
+        ("rem", _p),
+        ("first_child", _p),
+        ("n_child", _p),
     ]
 
 
@@ -186,6 +201,14 @@ SIGNATURES = {
     "smx_layout_f32": (_int, [_p, C.c_char_p, C.POINTER(_p), C.POINTER(_i64)]),
     "smx_layout_scalar": (_int, [_p, C.c_char_p, C.POINTER(_dbl)]),
     "smx_layout_free": (None, [_p]),
+    "smx_fp32_plan_create": (_int, [_p, _p, _p, _p, _p, _dbl, C.POINTER(_p), _p]),
+    "smx_fp32_plan_destroy": (None, [_p]),
+    "smx_fp32_plan_info": (_int, [_p, C.POINTER(_int), C.POINTER(_i64), C.POINTER(_p)]),
+    "smx_fp32_workspace": (_sz, [_p, _i64]),
+    "smx_fp32_eval": (_int, [_p, _p, _i64, _i64, _p, _p, _sz, _p]),
+    "smx_fp32_plan_check": (_int, [_p, _p]),
+    "smx_vjp_workspace": (_sz, [_p, _i64]),
+    "smx_vjp": (_int, [_p, _p, _i64, _i64, _p, _i64, _p, _i64, _p, _p, _sz, _p]),
     "smx_last_error_string": (C.c_char_p, []),
     "smx_version": (C.c_char_p, []),
 }

@@ -409,7 +409,7 @@ extern "C" int smx_contract_f64(const smx_plan* pl, const double* Lt, int64_t P,
 
 extern "C" size_t smx_eval_workspace(const smx_plan* pl, int64_t P, int precision) {
   if (!pl || P < 0) return 0;
-  (void)precision;
+  if (precision == 32) return pl->fp32 ? smx_fp32_workspace(pl->fp32, P) : 0;
   return size_t(pl->n_values) * size_t(P) * sizeof(double) + 256;
 }
 
@@ -417,7 +417,13 @@ extern "C" int smx_eval(const smx_plan* pl, int precision, const double* x, int6
                         size_t ws_bytes, void* stream) {
   int rc = check_plan(pl, "smx_eval");
   if (rc) return rc;
-  SMX_REQUIRE(precision == 64, "smx_eval: only precision 64 is served by the combination path");
+  SMX_REQUIRE(precision == 64 || precision == 32, "smx_eval: precision must be 64 or 32");
+  if (precision == 32) {
+    if (!pl->fp32)
+      return smx::set_error(SMX_ERR_UNSUPPORTED, "smx_eval: precision 32 needs the plan's FP32 form (plan->fp32, "
+                                                 "built by smx_fp32_plan_create)");
+    return smx_fp32_eval(pl->fp32, x, P, ldx, static_cast<float*>(y), ws, ws_bytes, stream);
+  }
   SMX_REQUIRE(ws_bytes >= smx_eval_workspace(pl, P, precision), "smx_eval: workspace too small");
   double* Lt = static_cast<double*>(ws);
   rc = smx_basis_f64(pl, x, P, ldx, Lt, nullptr, stream);
