@@ -113,23 +113,29 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                : "memory");
 }
 
-// Tiles: 128 x 128 outputs per CTA; the FP32 accumulator of the tensor cores
-// truncates when it adds, so one accumulator must not run over long
-// stretches of K: the MMA thread alternates between two accumulators in
-// tensor memory (columns [0,128) and [128,256)) every few K-tiles, and the
-// four drain warps add each finished accumulator into FP32 registers (one row
-// of 128 outputs per thread, round-to-nearest adds), then release it.
-constexpr int kBN = 128;
-constexpr int kStages = 3 * 128 / kRowBytes;
+// Tiles: 128 x BN outputs per CTA (BN = 128, or 256 for wide products: A is
+// then read once per 256 columns and B streams past L2 half as often).  The
+// FP32 accumulator of the tensor cores truncates when it adds, so one
+// accumulator must not run over long stretches of K: the MMA thread
+// alternates between two accumulators in tensor memory (columns [0, BN) and
+// [BN, 2 BN)) every few K-tiles, and the drain warps add each finished
+// accumulator into FP32 registers, then release it.  Drain warp w reads the
+// TMEM lane quadrant w % 4 (rows 32 (w % 4) .. +31) and columns 128 (w / 4) ..
+// +127: one row of 128 outputs per thread.
 // K-tiles per accumulator use: 64 products for the 3xTF32 form (its error
 // bound), 256 for the split-BF16 form, whose error the 16-bit split sets
 constexpr int kChunkTf32 = 64 / kBK;
 constexpr int kChunkBf16 = 256 / (2 * kBK);
-constexpr int kThreadsTC = 192;  // warps 0-3 drain/epilogue, warp 4 TMA, warp 5 MMA
 
-struct Smem {
+template <int BN>
+struct Tile {
+  static constexpr int kN = BN;
+  static constexpr int kDrainWarps = 4 * (BN / 128);
+  static constexpr int kWarpTMA = kDrainWarps, kWarpMMA = kDrainWarps + 1;
+  static constexpr int kThreads = 32 * (kDrainWarps + 2);
+  static constexpr int kStages = BN == 128 ? 3 : 2;  // 64 KB or 96 KB stages in ~192 KB
   static constexpr int kA = kBM * kBK * 4;
-  static constexpr int kB = kBN * kBK * 4;
+  static constexpr int kB = BN * kBK * 4;
   static constexpr int kStage = 2 * kA + 2 * kB;
   static constexpr int kTiles = kStages * kStage;
   static constexpr int kTotal = kTiles + 1024 /*align*/ + 256 /*barriers*/;
@@ -149,17 +155,20 @@ struct GemmArgs {
 };
 
 constexpr int kEpiLd = 132;  // epilogue staging row stride (floats): 16-byte rows, conflict-free
-static_assert(4 * 32 * kEpiLd * 4 <= Smem::kTiles, "epilogue staging must fit the pipeline stages");
+static_assert(Tile<128>::kDrainWarps * 32 * kEpiLd * 4 <= Tile<128>::kTiles, "epilogue staging must fit");
+static_assert(Tile<256>::kDrainWarps * 32 * kEpiLd * 4 <= Tile<256>::kTiles, "epilogue staging must fit");
 
 // BF16 = false: kind::tf32 on FP32 operands (32 per 128-byte slice); true:
 // kind::f16 on BF16 operands (64 per slice).  Same slices, stages and MMAs.
-template <bool BF16>
-__global__ void __launch_bounds__(kThreadsTC, 1)
+template <bool BF16, int BN>
+__global__ void __launch_bounds__(Tile<BN>::kThreads, 1)
     gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                        const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl, GemmArgs g) {
   constexpr int EK = BF16 ? 2 * kBK : kBK;  // elements per K-tile
   constexpr int kChunk = BF16 ? kChunkBf16 : kChunkTf32;
-  using L = Smem;
+  using L = Tile<BN>;
+  constexpr int kBN = BN;
+  constexpr int kStages = L::kStages;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(base + L::kTiles);
@@ -186,7 +195,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], 4);  // one arrival per drain warp
+      mbar_init(&acc_empty[b], L::kDrainWarps);  // one arrival per drain warp
     }
     mbar_init(flush, 1);
     *abort_flag = 0;
@@ -203,7 +212,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 4) {
+  if (warp == L::kWarpTMA) {
     if (lane == 0) {  // ---- TMA producer
       int armed_upto = 0;
       for (int kt = 0; kt < (g.no_loads ? 0 : KT); ++kt) {
@@ -226,7 +235,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
       *armed_slot = armed_upto;
     }
     __syncwarp();
-  } else if (warp == 5) {
+  } else if (warp == L::kWarpMMA) {
     if (lane == 0) {  // ---- MMA issuer
       constexpr uint32_t idesc = idesc_mma(kBM, kBN, BF16);
       bool ok = true;
@@ -281,12 +290,14 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     }
     __syncwarp();
   } else {
-    // ---- drain warps 0-3: warp w owns TMEM lanes 32w .. 32w+31 (rows m0 + 32w + lane)
-    float acc[kBN];
+    // ---- drain warps: warp w owns TMEM lanes 32 (w % 4) .. +31 (rows m0 + 32 (w % 4) + lane)
+    // and the 128 columns cw .. cw + 127 of the tile
+    const int quad = warp & 3, cw = (warp >> 2) * 128;
+    float acc[128];
 #pragma unroll
-    for (int j = 0; j < kBN; ++j) acc[j] = 0.f;
+    for (int j = 0; j < 128; ++j) acc[j] = 0.f;
     bool ok = true;
-    const uint32_t lane_base = tmem + (uint32_t(warp * 32) << 16);
+    const uint32_t lane_base = tmem + (uint32_t(quad * 32) << 16);
     for (int c = 0; c < NCH; ++c) {
       const int b = c & 1;
       ok = __all_sync(0xffffffffu,
@@ -294,14 +305,14 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll
-      for (int q = 0; q < kBN; q += 16) {
+      for (int q = 0; q < 128; q += 16) {
         uint32_t r[16];
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
             "%14, %15}, [%16];"
             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
               "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-            : "r"(lane_base + uint32_t(b * kBN + q)));
+            : "r"(lane_base + uint32_t(b * kBN + cw + q)));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
         for (int j = 0; j < 16; ++j) acc[q + j] += __uint_as_float(r[j]);
@@ -317,16 +328,16 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
       // contiguous bytes per store instruction.
       float* T = reinterpret_cast<float*>(base) + warp * (32 * kEpiLd);
 #pragma unroll
-      for (int q = 0; q < kBN; q += 4)
+      for (int q = 0; q < 128; q += 4)
         *reinterpret_cast<float4*>(T + lane * kEpiLd + q) = make_float4(acc[q], acc[q + 1], acc[q + 2], acc[q + 3]);
       __syncwarp();
-      const int c0 = n0 + 4 * lane;
+      const int c0 = n0 + cw + 4 * lane;
       const bool vec = (g.ldd % 4) == 0 && (reinterpret_cast<uintptr_t>(D) & 15) == 0 && c0 + 3 < g.N;
       float bv[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) bv[i] = g.bias && c0 + i < g.N ? g.bias[c0 + i] : 0.f;
       for (int r = 0; r < 32; ++r) {
-        const int row = m0 + warp * 32 + r;
+        const int row = m0 + quad * 32 + r;
         if (row >= g.M) break;
         const float4 t = *reinterpret_cast<const float4*>(T + r * kEpiLd + 4 * lane);
         float v[4] = {t.x + bv[0], t.y + bv[1], t.z + bv[2], t.w + bv[3]};
@@ -346,7 +357,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     }
   }
   // after an abort, wait (bounded) for the last copy armed on every stage
-  if (warp == 4 && lane == 0 && *abort_flag) {
+  if (warp == L::kWarpTMA && lane == 0 && *abort_flag) {
     const int armed = *armed_slot;
     for (int kt = max(0, armed - kStages); kt < armed; ++kt)
       mbar_wait(&full[kt % kStages], (kt / kStages) & 1, nullptr);
@@ -408,18 +419,17 @@ int make_map(CUtensorMap* tm, const void* ptr, int64_t rows, int64_t cols, int64
   return SMX_OK;
 }
 
-template <bool BF16>
-int launch(const void* Ah, const void* Al, int64_t lda, const void* Bh, const void* Bl, int64_t ldb, int M, int N,
-           int K, float* D, int64_t ldd, const float* bias, int* err, int accumulate, cudaStream_t st,
-           int splits = 1, uint64_t wait_ns = kWaitNs, int no_loads = 0) {
-  CUtensorMap tAh, tAl, tBh, tBl;
+template <bool BF16, int BN>
+int launch_tile(const CUtensorMap& tAh, const CUtensorMap& tAl, const void* Bh, const void* Bl, int64_t ldb, int M,
+                int N, int K, float* D, int64_t ldd, const float* bias, int* err, int accumulate, cudaStream_t st,
+                int splits, uint64_t wait_ns, int no_loads) {
+  using L = Tile<BN>;
+  CUtensorMap tBh, tBl;
   int rc;
-  if ((rc = make_map(&tAh, Ah, M, K, lda, kBM, BF16)) || (rc = make_map(&tAl, Al, M, K, lda, kBM, BF16)) ||
-      (rc = make_map(&tBh, Bh, N, K, ldb, kBN, BF16)) || (rc = make_map(&tBl, Bl, N, K, ldb, kBN, BF16)))
-    return rc;
+  if ((rc = make_map(&tBh, Bh, N, K, ldb, BN, BF16)) || (rc = make_map(&tBl, Bl, N, K, ldb, BN, BF16))) return rc;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(gemm_tf32x3_kernel<BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, Smem::kTotal);
+    cudaFuncSetAttribute(gemm_tf32x3_kernel<BF16, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::kTotal);
     attr = true;
   }
   // split-K: slice z runs K-tiles [z * kt_per_z, ...) into D + z * zstride
@@ -428,10 +438,25 @@ int launch(const void* Ah, const void* Al, int64_t lda, const void* Bh, const vo
   const int kt_per_z = splits > 1 ? (KT + splits - 1) / splits : 0;
   const int nz = splits > 1 ? (KT + kt_per_z - 1) / kt_per_z : 1;
   GemmArgs g{M, N, K, D, ldd, bias, err, accumulate, kt_per_z, int64_t(M) * ldd, wait_ns, no_loads};
-  dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM, nz);
-  gemm_tf32x3_kernel<BF16><<<grid, kThreadsTC, Smem::kTotal, st>>>(tAh, tAl, tBh, tBl, g);
+  dim3 grid((N + BN - 1) / BN, (M + kBM - 1) / kBM, nz);
+  gemm_tf32x3_kernel<BF16, BN><<<grid, L::kThreads, L::kTotal, st>>>(tAh, tAl, tBh, tBl, g);
   SMX_LAUNCH_CHECK(BF16 ? "smx_gemm_bf16x3" : "smx_gemm_tf32x3");
   return SMX_OK;
+}
+
+// Products wider than 192 columns use 128 x 256 tiles, the others 128 x 128.
+template <bool BF16>
+int launch(const void* Ah, const void* Al, int64_t lda, const void* Bh, const void* Bl, int64_t ldb, int M, int N,
+           int K, float* D, int64_t ldd, const float* bias, int* err, int accumulate, cudaStream_t st,
+           int splits = 1, uint64_t wait_ns = kWaitNs, int no_loads = 0) {
+  CUtensorMap tAh, tAl;
+  int rc;
+  if ((rc = make_map(&tAh, Ah, M, K, lda, kBM, BF16)) || (rc = make_map(&tAl, Al, M, K, lda, kBM, BF16))) return rc;
+  if (N > 192)
+    return launch_tile<BF16, 256>(tAh, tAl, Bh, Bl, ldb, M, N, K, D, ldd, bias, err, accumulate, st, splits, wait_ns,
+                                  no_loads);
+  return launch_tile<BF16, 128>(tAh, tAl, Bh, Bl, ldb, M, N, K, D, ldd, bias, err, accumulate, st, splits, wait_ns,
+                                no_loads);
 }
 
 // ---- BF16 split: hi = x rounded to BF16 (round to nearest even), lo = BF16(x - hi)
