@@ -134,9 +134,12 @@ class SmolyakBarycentricInterpolator:
         else:
             cache0 = f_evals.get((), {})
         on_device = bool(getattr(f, "on_device", False))
+        zero_val = None
         if zeta0 != 0:
             if on_device:
-                cache0 = {(): f(torch.as_tensor(zero[None, :], device=dev)).reshape(-1).double().cpu().numpy()}
+                zero_val = torch.as_tensor(f(torch.as_tensor(zero[None, :], device=dev)), device=dev).to(
+                    torch.float64).reshape(-1)
+                cache0 = {(): zero_val.cpu().numpy()}
                 self._n_f_evals_new += 1
             elif () not in cache0:
                 cache0[()] = f(zero.copy())
@@ -195,7 +198,8 @@ class SmolyakBarycentricInterpolator:
         # nodal values: calls of f with the reference's cache keys, device gather
         if on_device:
             fu_d, umap = self._evaluate_nodes_on_device(f, zero, sum_poff.cpu().numpy(), sum_pairs.cpu().numpy(),
-                                                        pair_dim_h, pair_deg_h, pair_voff_h, node_h, R, dev)
+                                                        pair_dim_h, pair_deg_h, pair_voff_h, node_h, R, dev,
+                                                        zero_val if self._is_nested else None)
         else:
             fu, umap = self._evaluate_nodes(f, f_evals, zero, sum_poff.cpu().numpy(), sum_pairs.cpu().numpy(),
                                             pair_dim_h, pair_deg_h, pair_voff_h, node_h, R)
@@ -337,14 +341,17 @@ class SmolyakBarycentricInterpolator:
         return fu, umap
 
     def _evaluate_nodes_on_device(self, f, zero, sum_poff, sum_pairs, pdim, pdeg, pvoff, node, R, dev,
-                                  chunk=1 << 16):
+                                  zero_val=None, chunk=1 << 16):
         """Unique nodal values computed by a device function f, and the row ->
         value map.  The unique nodes are found with the same keys as
         ``_evaluate_nodes`` (one per sparse node multi-index for nested rules,
         per multi-index nu and node otherwise), each recorded sparsely as the
         (dimension, node value) pairs of its summand; dense [chunk, d_in] point
         arrays are then assembled on the device (the zero point, with those
-        coordinates scattered in) and passed to f."""
+        coordinates scattered in) and passed to f.  ``zero_val``: f at the zero
+        point, already evaluated for the offset (nested rules, where the node
+        with key () is that point): reused and not counted again, as the host
+        path finds it in its cache."""
         nested = self._is_nested
         index = {}
         umap = np.empty(R, dtype=np.int64)
@@ -374,7 +381,8 @@ class SmolyakBarycentricInterpolator:
                         break
                     mu[i] = 0
         U = len(pt_len)
-        self._n_f_evals_new += U
+        reuse = index.get((None, ())) if zero_val is not None else None
+        self._n_f_evals_new += U - (1 if reuse is not None else 0)
         fu = torch.empty(max(U, 1), self._d_out, dtype=torch.float64, device=dev)
         if U == 0:
             fu.zero_()
@@ -394,6 +402,8 @@ class SmolyakBarycentricInterpolator:
             if out.shape[1] != self._d_out:
                 raise ValueError("f returned %d outputs per point, expected d_out = %d" % (out.shape[1], self._d_out))
             fu[u0:u1] = out
+        if reuse is not None:
+            fu[reuse] = zero_val
         return fu, umap
 
     # ------------------------------------------------------------------ evaluation

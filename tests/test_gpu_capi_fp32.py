@@ -54,7 +54,7 @@ def test_fp32_form_and_vjp_through_the_c_abi(kind, d, t, d_out, evaluator):
         sp = ip.spectral_plan()
 
         class _Dev:  # the library's device array of coefficients, viewed through the CUDA array interface
-            __cuda_array_interface__ = {"shape": (nl.value, d_out), "typestr": "<f8", "data": (coef.value, True),
+            __cuda_array_interface__ = {"shape": (nl.value, d_out), "typestr": "<f8", "data": (coef.value, False),
                                         "version": 3}
 
         torch.cuda.synchronize()
