@@ -207,12 +207,16 @@ int smx_spectral_pairs(int n_pairs, const int32_t* pair_dim, const int32_t* pair
 /* Coefficients C[n_lambda * d_out] (FP64) of every entry of the index set
  * (tree arrays of smx_lambda_*, NONZERO mode): mode products of each summand's
  * rows with its pairs' A matrices (scratch G: n_entries * d_out doubles, ids:
- * n_entries int32) scattered into the entries; C[root] also receives the
- * plan's offset.  *flag = 4 if a multi-index is missing from the tree. */
+ * n_entries int32 = the entry of every row) summed into the entries in row
+ * order (rows sorted by entry on the device: the same result on every call);
+ * C[root] also receives the plan's offset.  Scratch ws of
+ * smx_spectral_coefficients_workspace bytes (device).  *flag = 4 if a
+ * multi-index is missing from the tree. */
+size_t smx_spectral_coefficients_workspace(const smx_plan* plan_host);
 int smx_spectral_coefficients(const smx_plan* plan_host, const int64_t* aoff, const double* A,
                               const int64_t* first_child, const int64_t* n_child, const int32_t* tdim,
                               const int32_t* tdeg, int64_t n_lambda, double* G, int32_t* ids, double* C,
-                              int32_t* flag, void* stream);
+                              int32_t* flag, void* ws, size_t ws_bytes, void* stream);
 
 /* Evaluation layout of the orthogonal form.  "Hot" dimensions are those that
  * occur before another dimension in some multi-index; every entry of Lambda
@@ -319,6 +323,55 @@ int smx_blocked_eval(const smx_blocked* plan_host, const double* x, int64_t P, i
 /* Scratch for the split of the last round of tiles across blocks (partial
  * sums and counters); without it (ws = NULL) every tile is one block's work. */
 size_t smx_blocked_eval_workspace(const smx_blocked* plan_host, int64_t P);
+
+/* Tensor-core blocked evaluator (one output).  The same sum split by the kind
+ * of each entry's last factor: I(x) = c_0 + sum_a V_a(x) [ sum_s Bt[a][s]
+ * Phi_s(x) + sum_j Bl[a][j] x_j ] over the nodes a (entries with children,
+ * by remaining budget: the rows), the basis slots s of the table dimensions
+ * (hot ones and cold ones of degree >= 2; slot 0 = 1) and the linear
+ * dimensions j (cold, degree 1; phi_1(z_j) = alpha0 (fa x + fb) folded into
+ * Bl and column 0 of Bt).  Per 128-point tile, T = A B runs on the tensor
+ * cores in chunks of <= 64 columns (A = V in three bf16 parts built on chip
+ * in tensor memory, B = the coefficients in three bf16 parts, six part
+ * products per 16-row K step, FP32 accumulation) and y = c_0 + sum T x +
+ * sum T Phi is summed in FP32 (Kahan) as the x boxes (8 dimensions x 128
+ * points) arrive by TMA.  Tables from smx_layout_build (SMX_LAYOUT_BLOCKED_TC;
+ * names "tc_*").  Device pointers unless noted:
+ *   td[n_td][4]        dimension, degree, first basis slot, family
+ *   tdab[n_td][2]      affine map a, b (z = a x + b)
+ *   row[n_rows][4]     the 8 basis slots (16 bits each, 0 = the constant) of the node's path
+ *   chunk[n_chunks][4] HOST: N | table << 16, K steps, stage offset / 16 bytes,
+ *                      first basis slot (table chunks) or x box (linear chunks)
+ *   bimg               coefficient stages in the order the kernel consumes them (16-byte aligned)
+ *   box[n_boxes]       per x box: bit i set = dimension lin0 + 8 box + i is inactive (masked)
+ *   err                int, 0 = ok; set when a pipeline wait ran out */
+typedef struct smx_blocked_tc {
+  int32_t d_in;
+  int32_t n_td, n_phi, n_phi_pad, n_rows, max_depth;
+  int32_t n_agen;     /* K steps of A built per tile (the chunks' largest; <= 16) */
+  int32_t n_chunks, n_boxes, lin0, stages;
+  float c0;
+  const int32_t* td;
+  const float* tdab;
+  const int32_t* row;
+  const int32_t* chunk;
+  const void* bimg;
+  const int32_t* box;
+  int32_t* err;
+} smx_blocked_tc;
+
+/* From this many points on, one-output evaluations (smx_fp32_eval, and the
+ * package's FP32 path) use smx_blocked_tc_eval when the plan has its tables;
+ * below, smx_blocked_eval (whose results the multi-plan batch kernel
+ * reproduces exactly). */
+#define SMX_BLOCKED_TC_MIN_POINTS (1 << 30)
+/* 1 if smx_blocked_tc_eval serves x (16-byte aligned, even row pitch >= d_in). */
+int smx_blocked_tc_supported(const smx_blocked_tc* plan_host, const double* x, int64_t ldx);
+/* y[P] (FP32) at x[P, ldx] (FP64); one persistent block per SM (up to 225
+ * KiB of shared memory, all 512 tensor-memory columns); SMX_ERR_UNSUPPORTED
+ * for an x it does not serve. */
+int smx_blocked_tc_eval(const smx_blocked_tc* plan_host, const double* x, int64_t P, int64_t ldx, float* y,
+                        void* stream);
 
 /* Basis-product panel of the orthogonal form for the tensor-core contraction:
  * A[p][j] = prod over the pairs of entry j of phi_g(z_d) for the K non-root
@@ -451,6 +504,7 @@ int smx_split_tf32(const float* src, int64_t rows, int64_t cols, int64_t lds, fl
 #define SMX_LAYOUT_BLOCKED 0
 #define SMX_LAYOUT_PERPOINT 1
 #define SMX_LAYOUT_TAPE 2
+#define SMX_LAYOUT_BLOCKED_TC 3
 typedef struct smx_host_tables smx_host_tables;
 int smx_layout_build(int kind, int64_t n, const int32_t* parent_host, const int32_t* dim_host,
                      const int32_t* deg_host, const int32_t* level_host, const int64_t* rank_host,

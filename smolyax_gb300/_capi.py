@@ -135,6 +135,32 @@ class SmxBlocked(C.Structure):
     ]
 
 
+class SmxBlockedTc(C.Structure):
+    """Mirror of ``struct smx_blocked_tc``."""
+
+    _fields_ = [
+        ("d_in", _i32),
+        ("n_td", _i32),
+        ("n_phi", _i32),
+        ("n_phi_pad", _i32),
+        ("n_rows", _i32),
+        ("max_depth", _i32),
+        ("n_agen", _i32),
+        ("n_chunks", _i32),
+        ("n_boxes", _i32),
+        ("lin0", _i32),
+        ("stages", _i32),
+        ("c0", C.c_float),
+        ("td", _p),
+        ("tdab", _p),
+        ("row", _p),
+        ("chunk", _p),
+        ("bimg", _p),
+        ("box", _p),
+        ("err", _p),
+    ]
+
+
 class SmxWork(C.Structure):
     """Mirror of ``struct smx_work``."""
 
@@ -163,13 +189,16 @@ SIGNATURES = {
     "smx_integral_workspace": (_sz, [_p]),
     "smx_integral": (_int, [_p, _p, _p, _p, _sz, _p]),
     "smx_spectral_pairs": (_int, [_int, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
-    "smx_spectral_coefficients": (_int, [_p, _p, _p, _p, _p, _p, _p, _i64, _p, _p, _p, _p, _p]),
+    "smx_spectral_coefficients": (_int, [_p, _p, _p, _p, _p, _p, _p, _i64, _p, _p, _p, _p, _p, _sz, _p]),
+    "smx_spectral_coefficients_workspace": (_sz, [_p]),
     "smx_spectral_eval": (_int, [_p, _p, _i64, _i64, _p, _p]),
     "smx_blocked_smem": (_sz, [_p]),
     "smx_gemm_bf16x3": (_int, [_p, _p, _i64, _p, _p, _i64, _int, _int, _int, _p, _i64, _p, _int, _p, _p]),
     "smx_split_bf16": (_int, [_p, _i64, _i64, _i64, _p, _p, _i64, _p]),
     "smx_host_device_pointer": (_int, [_p, _p]),
     "smx_blocked_eval": (_int, [_p, _p, _i64, _i64, _p, _p, _sz, _p]),
+    "smx_blocked_tc_eval": (_int, [_p, _p, _i64, _i64, _p, _p]),
+    "smx_blocked_tc_supported": (_int, [_p, _p, _i64]),
     "smx_blocked_eval_workspace": (_sz, [_p, _i64]),
     "smx_blocked_eval_batch_workspace": (_sz, [_int, _int]),
     "smx_blocked_eval_batch": (_int, [_p, _int, _p, _int, _p, _sz, _p]),
@@ -261,7 +290,7 @@ def stream_ptr(stream):
     return C.c_void_p(stream.cuda_stream) if stream is not None else None
 
 
-LAYOUT_KINDS = {"blocked": 0, "perpoint": 1, "tape": 2}
+LAYOUT_KINDS = {"blocked": 0, "perpoint": 1, "tape": 2, "blocked_tc": 3}
 
 
 def host_layout(kind, tree, coef, d_out, maxdeg, fam, fa, fb, i32=(), f32=(), scalars=()):

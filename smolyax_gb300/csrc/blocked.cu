@@ -26,8 +26,12 @@
 #include <vector>
 
 #include "common.cuh"
+#include "fp_convert.cuh"
 
 namespace {
+
+using smx::f64_to_f32;
+using smx::kahan_add;
 
 constexpr int kW = 16;           // warps per block
 constexpr int kT = 128;          // points per tile
@@ -62,25 +66,6 @@ struct BArgs {
   const float2* hab;  // per hot dimension affine map {a, b}                  (shared-memory tables only)
 };
 
-// FP64 -> FP32 with integer operations (truncation of the mantissa; |v| below
-// 2^-126 is raised to a value in [2^-126, 2^-125) of the same sign; |v| of
-// 2^128 and above, infinities and NaNs give NaN, so that a non-finite
-// coordinate makes the point's value NaN as in the FP64 path).  Keeps the
-// conversions off the FP64 pipe.  Layout facts used: IEEE-754 binary64 =
-// sign, 11-bit exponent (bias 1023), 52-bit fraction; binary32 = sign, 8-bit
-// exponent (bias 127), 23-bit fraction.  The magnitude's high word is clamped
-// below at the exponent of 2^-126; its top 9 exponent bits and 23 fraction
-// bits are then shifted into place together, adding 2^30 re-biases the
-// exponent modulo 2^32, and the sign is merged back.
-__device__ __forceinline__ float f64_to_f32(double v) {
-  const unsigned hi = static_cast<unsigned>(__double2hiint(v));
-  const unsigned lo = static_cast<unsigned>(__double2loint(v));
-  const unsigned a = hi & 0x7fffffffu;
-  const unsigned mag = max(a, 0x38100000u);
-  const unsigned t = a >= 0x47f00000u ? 0x7fc00000u : __funnelshift_l(lo, mag, 3) + 0x40000000u;
-  return __uint_as_float((t & 0x7fffffffu) | (hi & 0x80000000u));
-}
-
 __device__ __forceinline__ void ld2_stream(const double* p, double& a, double& b) {
   asm volatile("ld.global.nc.L1::no_allocate.v2.f64 {%0, %1}, [%2];" : "=d"(a), "=d"(b) : "l"(p));
 }
@@ -107,12 +92,6 @@ __device__ __forceinline__ T tl(const T* p) {
     return __ldg(p);
 }
 
-__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
-  const float yv = v - c;
-  const float t = s + yv;
-  c = (t - s) - yv;
-  s = t;
-}
 
 __device__ __forceinline__ float phi_rec(int fm, float z, int g) {
   float pm1 = 0.f, pc = 1.f;

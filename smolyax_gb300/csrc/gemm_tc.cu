@@ -16,6 +16,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "tc_util.cuh"
 
 namespace {
 
@@ -25,93 +26,10 @@ constexpr int kBM = 128;
 // the same shared memory (more copies in flight against the L2 latency).
 constexpr int kRowBytes = 128;
 constexpr int kBK = kRowBytes / 4;
-constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on every wait (the default of GemmArgs::wait_ns)
+using namespace smx::tc;
 
-__device__ __forceinline__ uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-// Bounded parity wait; returns false on timeout (after `limit_ns`) or when
-// the abort flag is raised.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort_flag,
-                                          uint64_t limit_ns = kWaitNs) {
-  const uint32_t a = smem_u32(bar);
-  const uint64_t t0 = global_ns();
-  for (uint32_t it = 0;; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if (abort_flag && *abort_flag) return false;
-    if ((it & 255) == 255 && global_ns() - t0 > limit_ns) return false;
-  }
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int c0, int c1, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
-      : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major, kRowBytes swizzle (128 or 64
-// bytes), 8-row groups 8 * kRowBytes apart (tcgen05 descriptor format,
-// version field = 1; layout field 2 = SWIZZLE_128B, 4 = SWIZZLE_64B).
-__device__ __forceinline__ uint64_t make_desc_sw(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= uint64_t((saddr & 0x3FFFF) >> 4);          // start address
-  d |= uint64_t(1) << 16;                          // leading byte offset (unused for swizzled K-major)
-  d |= uint64_t((8 * kRowBytes) >> 4) << 32;       // stride byte offset
-  d |= uint64_t(1) << 46;                          // version
-  d |= uint64_t(kRowBytes == 128 ? 2 : 4) << 61;   // swizzle mode
-  return d;
-}
-
-// Instruction descriptor: D = F32, A = B = TF32 (kind::tf32, format 2) or
-// BF16 (kind::f16, format 1), both K-major, M x N.
-__host__ __device__ constexpr uint32_t idesc_mma(int M, int N, bool bf16) {
-  return (1u << 4) | ((bf16 ? 1u : 2u) << 7) | ((bf16 ? 1u : 2u) << 10) | (uint32_t(N >> 3) << 17) |
-         (uint32_t(M >> 4) << 24);
-}
-
-template <bool BF16>
-__device__ __forceinline__ void mma_op(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                       uint32_t accumulate) {
-  if constexpr (BF16) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-  } else {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-  }
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
+// K-major operand descriptor of this kernel's slices (kRowBytes swizzle)
+__device__ __forceinline__ uint64_t make_desc_k(uint32_t saddr) { return make_desc_sw(saddr, kRowBytes); }
 
 // Tiles: 128 x BN outputs per CTA (BN = 128, or 256 for wide products: A is
 // then read once per 256 columns and B streams past L2 half as often).  The
@@ -265,8 +183,8 @@ __global__ void __launch_bounds__(Tile<BN>::kThreads, 1)
 #pragma unroll
           for (int k8 = 0; k8 < kRowBytes / 32; ++k8) {  // 32 bytes (8 tf32 or 16 bf16) of K per MMA
             const uint32_t off = k8 * 32;
-            const uint64_t dah = make_desc_sw(a_hi + off), dal = make_desc_sw(a_lo + off);
-            const uint64_t dbh = make_desc_sw(b_hi + off), dbl = make_desc_sw(b_lo + off);
+            const uint64_t dah = make_desc_k(a_hi + off), dal = make_desc_k(a_lo + off);
+            const uint64_t dbh = make_desc_k(b_hi + off), dbl = make_desc_k(b_lo + off);
             mma_op<BF16>(acc, dah, dbh, idesc, first ? 0u : 1u);
             first = false;
             mma_op<BF16>(acc, dah, dbl, idesc, 1u);
@@ -473,6 +391,12 @@ __global__ void split_bf16_kernel(const float* __restrict__ src, int64_t rows, i
 }
 
 }  // namespace
+
+int smx::tc::tensor_map_encoder(PFN_cuTensorMapEncodeTiled_v12000* fn) {
+  const int rc = get_encode();
+  if (rc == SMX_OK) *fn = g_encode;
+  return rc;
+}
 
 extern "C" int smx_split_tf32(const float* src, int64_t rows, int64_t cols, int64_t lds, float* hi, float* lo,
                               int64_t ldo, void* stream) {

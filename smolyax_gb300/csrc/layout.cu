@@ -18,6 +18,7 @@
 #include <tuple>
 #include <vector>
 
+#include "blocked_tc.h"
 #include "layout.h"
 
 namespace smx {
@@ -324,6 +325,211 @@ bool build_blocked(const Tree& tr, const float* C, const int64_t* maxdeg, int d,
   return true;
 }
 
+namespace {
+
+// bf16 of an FP32 value, rounded to nearest even (NaN stays NaN).
+uint16_t bf16_rn(float v) {
+  uint32_t u;
+  std::memcpy(&u, &v, 4);
+  if ((u & 0x7fffffffu) > 0x7f800000u) return 0x7fc0;
+  u += 0x7fffu + ((u >> 16) & 1u);
+  return uint16_t(u >> 16);
+}
+
+float bf16_value(uint16_t h) {
+  const uint32_t u = uint32_t(h) << 16;
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
+}  // namespace
+
+// Tables of the tensor-core blocked evaluator (blocked_tc.cu), one output.
+//
+// Every entry e != root extends a node a (an entry with children) by one
+// factor: I(x) = c_0 + sum_a V_a(x) [ sum_{table slots s} B_t[a][s] Phi_s(x)
+//                                    + sum_{linear dims j} B_l[a][j] x_j ].
+// Table dimensions are the hot ones (those with children) and the cold ones
+// of degree >= 2; their basis values Phi_s (slot 0 = the constant 1) are
+// computed per point.  Linear dimensions (cold, degree 1) enter through
+// phi_1(z_j) = alpha0 (fa_j x_j + fb_j): B_l = C alpha0 fa_j, and the constant
+// part C alpha0 fb_j is summed into B_t[a][0].  The nodes, sorted by remaining
+// budget (descending), are the rows of A = V (per point, computed on chip) and
+// of the coefficient matrices, so that a dimension j of weight k_j only uses
+// the first rows (a node admits j iff its remaining budget exceeds k_j): the
+// table and linear columns are cut into chunks of 64, each with its own
+// number of 16-row K steps (at most 16: A lives in tensor memory).
+// Coefficients are stored as three bf16 parts (hi + mid + lo = the FP32
+// value) in the shared-memory image of the MMA's B operand (K-major, 32-byte
+// swizzle: 16-byte half h of row n at (h ^ (n >> 2 & 1))), chunk by chunk,
+// each chunk's K steps from the last to the first.
+bool build_blocked_tc(const Tree& tr, const float* C, const int64_t* maxdeg, int d, const int32_t* fam,
+                      const double* fa, const double* fb, Tables& out) {
+  using namespace smx::btc;
+  const int64_t n = tr.n;
+  if (n < 2) return false;
+  std::vector<char> hot(d, 0);
+  for (int64_t e = 1; e < n; ++e)
+    if (tr.parent[e] > 0) hot[tr.dim[tr.parent[e]]] = 1;
+  // table dimensions and their basis slots (slot 0: the constant 1)
+  std::vector<int64_t> soff(d, -1);
+  std::vector<int32_t> td;
+  std::vector<float> tdab;
+  int64_t n_phi = 1;
+  for (int j = 0; j < d; ++j)
+    if (hot[j] || maxdeg[j] >= 2) {
+      soff[j] = n_phi;
+      td.insert(td.end(), {int32_t(j), int32_t(maxdeg[j]), int32_t(n_phi), fam[j]});
+      tdab.insert(tdab.end(), {float(fa[j]), float(fb[j])});
+      n_phi += maxdeg[j];
+    }
+  if (n_phi > kMaxPhi) return false;
+  const int64_t n_phi_pad = (n_phi + 15) / 16 * 16;
+
+  // rows: the nodes, by remaining budget (descending), then entry
+  std::vector<char> has_kid(n, 0);
+  for (int64_t e = 1; e < n; ++e) has_kid[tr.parent[e]] = 1;
+  std::vector<int64_t> nodes;
+  for (int64_t e = 0; e < n; ++e)
+    if (has_kid[e]) nodes.push_back(e);
+  {
+    std::vector<int64_t> o = stable_order(int64_t(nodes.size()), [&](int64_t i) {
+      return std::make_pair(-tr.rem[nodes[i]], nodes[i]);
+    });
+    std::vector<int64_t> s2;
+    for (int64_t i : o) s2.push_back(nodes[i]);
+    nodes.swap(s2);
+  }
+  const int64_t n_rows = int64_t(nodes.size());
+  std::vector<int64_t> row_of(n, -1);
+  for (int64_t r = 0; r < n_rows; ++r) row_of[nodes[r]] = r;
+  std::vector<int32_t> rows(n_rows * 4, 0);
+  int max_depth = 0;
+  for (int64_t r = 0; r < n_rows; ++r) {
+    std::vector<int64_t> p;
+    for (int64_t v = nodes[r]; v != 0; v = tr.parent[v]) {
+      const int64_t s = soff[tr.dim[v]];
+      if (s < 0) return false;  // a node's factor must be a table slot
+      p.push_back(s + tr.deg[v] - 1);
+    }
+    if (int(p.size()) > 8) return false;
+    std::reverse(p.begin(), p.end());
+    max_depth = std::max(max_depth, int(p.size()));
+    for (size_t q = 0; q < p.size(); ++q) rows[r * 4 + q / 2] |= int32_t(uint32_t(p[q]) << (16 * (q % 2)));
+  }
+
+  // coefficients
+  std::vector<int64_t> lin_dims;
+  for (int j = 0; j < d; ++j)
+    if (soff[j] < 0 && maxdeg[j] == 1) lin_dims.push_back(j);
+  const int64_t lin0 = lin_dims.empty() ? 0 : lin_dims.front() / kBox * kBox;
+  const int64_t n_cols = lin_dims.empty() ? 0 : (lin_dims.back() + 1 - lin0 + 15) / 16 * 16;
+  std::vector<double> Bt(size_t(n_rows * n_phi_pad), 0.0), Bl(size_t(n_rows * n_cols), 0.0);
+  std::vector<int64_t> t_rows(1, 0);  // K extent of the table chunk
+  std::vector<int64_t> col_rows(n_cols, 0);
+  bool any_table = false;
+  for (int64_t e = 1; e < n; ++e) {
+    const int64_t r = row_of[tr.parent[e]];
+    const int j = tr.dim[e];
+    if (soff[j] >= 0) {
+      Bt[r * n_phi_pad + soff[j] + tr.deg[e] - 1] = double(C[e]);
+      t_rows[0] = std::max(t_rows[0], r + 1);
+      any_table = true;
+    } else {
+      if (tr.deg[e] != 1) return false;
+      const double a0 = fam[j] == 0 ? 1.0 : sqrt(2.0);
+      Bl[r * n_cols + (j - lin0)] = double(C[e]) * a0 * fa[j];
+      col_rows[j - lin0] = std::max(col_rows[j - lin0], r + 1);
+      if (fb[j] != 0.0) {
+        Bt[r * n_phi_pad] += double(C[e]) * a0 * fb[j];
+        t_rows[0] = std::max(t_rows[0], r + 1);
+        any_table = true;
+      }
+    }
+  }
+  const int64_t kt_t = any_table ? (t_rows[0] + kStep - 1) / kStep : 0;
+  struct Chunk {
+    int64_t N, nk, table, col0;
+  };
+  std::vector<Chunk> chunks;
+  for (int64_t c0 = 0; any_table && c0 < n_phi_pad; c0 += kMaxN)
+    chunks.push_back({std::min<int64_t>(kMaxN, n_phi_pad - c0), kt_t, 1, c0});
+  int64_t n_agen = kt_t;
+  for (int64_t c0 = 0; c0 < n_cols; c0 += kMaxN) {
+    const int64_t N = std::min<int64_t>(kMaxN, n_cols - c0);
+    int64_t rmax = 1;
+    for (int64_t c = c0; c < c0 + N; ++c) rmax = std::max(rmax, col_rows[c]);
+    const int64_t nk = (rmax + kStep - 1) / kStep;
+    n_agen = std::max(n_agen, nk);
+    chunks.push_back({N, nk, 0, c0});
+  }
+  if (chunks.empty() || int(chunks.size()) > kMaxChunks || n_agen > kMaxSteps) return false;
+  if (smem_layout(n_phi_pad).n_x == 0) return false;
+
+  // coefficient stages in the order the MMA thread consumes them: per chunk
+  // its K steps from the last (small terms) to the first
+  std::vector<uint16_t> img;
+  std::vector<int32_t> chunk_tab;
+  int64_t stages = 0;
+  for (const Chunk& ch : chunks) {
+    chunk_tab.insert(chunk_tab.end(), {int32_t(ch.N | (ch.table << 16)), int32_t(ch.nk), int32_t(img.size() * 2 / 16),
+                                       int32_t(ch.table ? ch.col0 : ch.col0 / kBox)});
+    for (int64_t kk = ch.nk - 1; kk >= 0; --kk) {
+      const size_t base = img.size();
+      img.resize(base + size_t(kSplits * ch.N * 16), 0);
+      for (int64_t nn = 0; nn < ch.N; ++nn)
+        for (int k = 0; k < kStep; ++k) {
+          const int64_t r = kk * kStep + k;
+          double v = 0.0;
+          if (r < n_rows) v = ch.table ? Bt[r * n_phi_pad + ch.col0 + nn] : Bl[r * n_cols + ch.col0 + nn];
+          const float f = float(v);
+          const uint16_t h = bf16_rn(f);
+          const float r1 = f - bf16_value(h);
+          const uint16_t m = bf16_rn(r1);
+          const uint16_t l = bf16_rn(r1 - bf16_value(m));
+          const uint16_t parts[3] = {h, m, l};
+          const size_t off = size_t(nn * 16 + (((k >> 3) ^ ((nn >> 2) & 1)) << 3) + (k & 7));
+          for (int sp = 0; sp < kSplits; ++sp) img[base + size_t(sp * ch.N * 16) + off] = parts[sp];
+        }
+      ++stages;
+    }
+  }
+  std::vector<int32_t> img32((img.size() + 1) / 2, 0);
+  std::memcpy(img32.data(), img.data(), img.size() * 2);
+
+  // x boxes: inactive dimensions among the linear columns are masked (their
+  // coordinates do not enter the interpolant)
+  const int64_t n_boxes = n_cols / kBox;
+  std::vector<int32_t> box(n_boxes, 0);
+  for (int64_t b = 0; b < n_boxes; ++b)
+    for (int i = 0; i < kBox; ++i) {
+      const int64_t j = lin0 + b * kBox + i;
+      if (j < d && maxdeg[j] == 0) box[b] |= 1 << i;
+    }
+
+  out.i32["tc_td"] = td;
+  out.f32["tc_tdab"] = tdab;
+  out.i32["tc_row"] = rows;
+  out.i32["tc_chunk"] = chunk_tab;
+  out.i32["tc_b"] = img32;
+  out.i32["tc_box"] = box;
+  out.scalar["tc_n_td"] = double(td.size() / 4);
+  out.scalar["tc_n_phi"] = double(n_phi);
+  out.scalar["tc_n_phi_pad"] = double(n_phi_pad);
+  out.scalar["tc_n_rows"] = double(n_rows);
+  out.scalar["tc_max_depth"] = double(max_depth);
+  out.scalar["tc_n_agen"] = double(n_agen);
+  out.scalar["tc_kt_table"] = double(kt_t);
+  out.scalar["tc_n_chunks"] = double(chunks.size());
+  out.scalar["tc_n_boxes"] = double(n_boxes);
+  out.scalar["tc_lin0"] = double(lin0);
+  out.scalar["tc_stages"] = double(stages);
+  out.scalar["tc_smem"] = double(smem_layout(n_phi_pad).total);
+  out.scalar["c0"] = double(C[0]);
+  return true;
+}
+
 // Port of spectral.py build_layout (4 segments).
 bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
                     const double* fa, const double* fb, Tables& out) {
@@ -584,6 +790,9 @@ extern "C" int smx_layout_build(int kind, int64_t n, const int32_t* parent, cons
     ok = smx::layout::build_perpoint(tr, C, d_out, maxdeg, d, fam, fa, fb, h->t);
   } else if (kind == SMX_LAYOUT_TAPE) {
     ok = smx::layout::build_tape(tr, maxdeg, d, h->t);
+  } else if (kind == SMX_LAYOUT_BLOCKED_TC) {
+    SMX_REQUIRE(d_out == 1, "smx_layout_build: the blocked evaluator has one output");
+    ok = smx::layout::build_blocked_tc(tr, C, maxdeg, d, fam, fa, fb, h->t);
   } else {
     return smx::set_error(SMX_ERR_ARG, "smx_layout_build: unknown layout kind");
   }

@@ -38,6 +38,8 @@ bool build_blocked(const Tree& tr, const float* C, const int64_t* maxdeg, int d,
 bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
                     const double* fa, const double* fb, Tables& out);
 bool build_tape(const Tree& tr, const int64_t* maxdeg, int d, Tables& out);
+bool build_blocked_tc(const Tree& tr, const float* C, const int64_t* maxdeg, int d, const int32_t* fam,
+                      const double* fa, const double* fb, Tables& out);
 
 }  // namespace layout
 }  // namespace smx

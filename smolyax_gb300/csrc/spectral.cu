@@ -177,13 +177,106 @@ __global__ void spectral_ids_kernel(int n_sum, const int32_t* __restrict__ poff,
   }
 }
 
-__global__ void spectral_scatter_kernel(int64_t R, int dout, const int32_t* __restrict__ ids,
-                                        const double* __restrict__ G, double* __restrict__ C) {
+// --- deterministic scatter: rows sorted by target entry (stable LSD radix
+// sort, 8-bit digits), then one thread per (entry, output) sums its rows in
+// row order.  The sum is the same on every run and for every caller.
+constexpr int kSortThreads = 256, kSortPer = 8, kSortTile = kSortThreads * kSortPer;
+
+__global__ void sort_hist_kernel(int64_t R, const int32_t* __restrict__ keys, int shift, int nblk,
+                                 int32_t* __restrict__ hist) {
+  __shared__ int cnt[256];
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = int64_t(blockIdx.x) * kSortTile;
+  for (int i = threadIdx.x; i < kSortTile; i += kSortThreads) {
+    const int64_t r = base + i;
+    if (r < R) atomicAdd(&cnt[(keys[r] >> shift) & 255], 1);
+  }
+  __syncthreads();
+  hist[int64_t(threadIdx.x) * nblk + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// Exclusive scan of hist in (digit, block) order: the first destination of
+// every digit of every tile.  One block of 256 threads (thread = digit).
+__global__ void sort_scan_kernel(int nblk, int32_t* __restrict__ hist) {
+  __shared__ int tot[256];
+  const int d = threadIdx.x;
+  int s = 0;
+  for (int b = 0; b < nblk; ++b) s += hist[int64_t(d) * nblk + b];
+  tot[d] = s;
+  __syncthreads();
+  if (d == 0) {
+    int run = 0;
+    for (int i = 0; i < 256; ++i) {
+      const int t = tot[i];
+      tot[i] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+  int run = tot[d];
+  for (int b = 0; b < nblk; ++b) {
+    const int t = hist[int64_t(d) * nblk + b];
+    hist[int64_t(d) * nblk + b] = run;
+    run += t;
+  }
+}
+
+// Stable scatter of one tile: the rows are taken in order (rounds of 256,
+// warps in order, lanes in order), each placed after the earlier rows of its
+// digit.  vin == nullptr: the values are the row indices.
+__global__ void sort_scatter_kernel(int64_t R, const int32_t* __restrict__ kin, const int32_t* __restrict__ vin,
+                                    int shift, int nblk, const int32_t* __restrict__ off, int32_t* __restrict__ kout,
+                                    int32_t* __restrict__ vout) {
+  constexpr int kW = kSortThreads / 32;
+  __shared__ int cnt[256];
+  __shared__ int wcnt[kW][256];
+  const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+  cnt[t] = off[int64_t(t) * nblk + blockIdx.x];
+  for (int i = 0; i < kW; ++i) wcnt[i][t] = 0;
+  __syncthreads();
+  const int64_t base = int64_t(blockIdx.x) * kSortTile;
+  for (int j = 0; j < kSortPer; ++j) {
+    const int64_t r = base + int64_t(j) * kSortThreads + t;
+    const bool valid = r < R;
+    const int key = valid ? kin[r] : 0;
+    const int val = valid ? (vin ? vin[r] : int(r)) : 0;
+    const int d = (key >> shift) & 255;
+    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+    unsigned peers = 0;
+    if (valid) peers = __match_any_sync(vmask, d);
+    const int rank_w = __popc(peers & ((1u << lane) - 1u));
+    if (valid && rank_w == 0) wcnt[w][d] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+      int pos = cnt[d] + rank_w;
+      for (int w2 = 0; w2 < w; ++w2) pos += wcnt[w2][d];
+      kout[pos] = key;
+      vout[pos] = val;
+    }
+    __syncthreads();
+    int add = 0;
+    for (int w2 = 0; w2 < kW; ++w2) {
+      add += wcnt[w2][t];
+      wcnt[w2][t] = 0;
+    }
+    cnt[t] += add;
+    __syncthreads();
+  }
+}
+
+// C[key][o] += sum of G[row][o] over the run of rows of each key (row order).
+__global__ void run_sum_kernel(int64_t R, int dout, const int32_t* __restrict__ skeys,
+                               const int32_t* __restrict__ srows, const double* __restrict__ G, double* __restrict__ C) {
   const int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (idx >= R * dout) return;
-  const int64_t r = idx / dout;
-  const int o = int(idx - r * dout);
-  atomicAdd(&C[int64_t(ids[r]) * dout + o], G[idx]);
+  const int64_t i = idx / dout;
+  const int o = int(idx - i * dout);
+  const int key = skeys[i];
+  if (i > 0 && skeys[i - 1] == key) return;
+  double s = 0.0;
+  for (int64_t j = i; j < R && skeys[j] == key; ++j) s += G[int64_t(srows[j]) * dout + o];
+  C[int64_t(key) * dout + o] += s;
 }
 
 // --- FP32 evaluation -----------------------------------------------------------------------
@@ -573,12 +666,26 @@ extern "C" int smx_spectral_pairs(int n_pairs, const int32_t* pair_dim, const in
   return SMX_OK;
 }
 
+namespace {
+
+size_t up256(size_t v) { return (v + 255) / 256 * 256; }
+
+int sort_blocks(int64_t R) { return int((R + kSortTile - 1) / kSortTile); }
+
+}  // namespace
+
+extern "C" size_t smx_spectral_coefficients_workspace(const smx_plan* pl) {
+  if (!pl) return 0;
+  const int64_t R = std::max<int64_t>(pl->n_entries, 1);
+  return 4 * up256(size_t(R) * sizeof(int32_t)) + up256(size_t(256) * sort_blocks(R) * sizeof(int32_t));
+}
+
 extern "C" int smx_spectral_coefficients(const smx_plan* pl, const int64_t* aoff, const double* A,
                                          const int64_t* first_child, const int64_t* n_child, const int32_t* tdim,
                                          const int32_t* tdeg, int64_t n_lambda, double* G, int32_t* ids, double* C,
-                                         int32_t* flag, void* stream) {
+                                         int32_t* flag, void* ws, size_t ws_bytes, void* stream) {
   SMX_REQUIRE(pl != nullptr, "smx_spectral_coefficients: null plan");
-  SMX_REQUIRE(C && flag && n_lambda >= 1, "smx_spectral_coefficients: bad arguments");
+  SMX_REQUIRE(C && flag && n_lambda >= 1 && n_lambda < (int64_t(1) << 31), "smx_spectral_coefficients: bad arguments");
   cudaStream_t st = smx::as_stream(stream);
   const int dout = pl->d_out;
   const int64_t R = pl->n_entries;
@@ -588,6 +695,8 @@ extern "C" int smx_spectral_coefficients(const smx_plan* pl, const int64_t* aoff
   SMX_LAUNCH_CHECK("smx_spectral_coefficients init");
   if (pl->n_summands == 0 || R == 0) return SMX_OK;
   SMX_REQUIRE(aoff && A && first_child && n_child && tdim && tdeg && G && ids, "smx_spectral_coefficients: null");
+  SMX_REQUIRE(ws && ws_bytes >= smx_spectral_coefficients_workspace(pl), "smx_spectral_coefficients: workspace");
+  SMX_REQUIRE(R < (int64_t(1) << 31), "smx_spectral_coefficients: too many rows");
   cudaMemcpyAsync(G, pl->F64, size_t(R) * dout * sizeof(double), cudaMemcpyDeviceToDevice, st);
   const int64_t nt = int64_t(pl->n_summands) * dout;
   spectral_transform_kernel<<<smx::grid_for(nt, 128), 128, 0, st>>>(pl->n_summands, pl->sum_poff, pl->sum_pairs,
@@ -595,7 +704,30 @@ extern "C" int smx_spectral_coefficients(const smx_plan* pl, const int64_t* aoff
   spectral_ids_kernel<<<smx::grid_for(pl->n_summands, 128), 128, 0, st>>>(
       pl->n_summands, pl->sum_poff, pl->sum_pairs, pl->sum_eoff, pl->pair_dim, pl->pair_deg, first_child, n_child,
       tdim, tdeg, ids, flag);
-  spectral_scatter_kernel<<<smx::grid_for(R * dout, 256), 256, 0, st>>>(R, dout, ids, G, C);
+  // rows sorted by entry (stable), ping-ponging between two key/row buffers
+  uint8_t* w = static_cast<uint8_t*>(ws);
+  const size_t rb = up256(size_t(R) * sizeof(int32_t));
+  int32_t* k0 = reinterpret_cast<int32_t*>(w);
+  int32_t* v0 = reinterpret_cast<int32_t*>(w + rb);
+  int32_t* k1 = reinterpret_cast<int32_t*>(w + 2 * rb);
+  int32_t* v1 = reinterpret_cast<int32_t*>(w + 3 * rb);
+  int32_t* hist = reinterpret_cast<int32_t*>(w + 4 * rb);
+  const int nblk = sort_blocks(R);
+  int bits = 1;
+  while (bits < 31 && (int64_t(1) << bits) < n_lambda) ++bits;
+  const int passes = (bits + 7) / 8;
+  const int32_t* kin = ids;
+  const int32_t* vin = nullptr;
+  for (int ps = 0; ps < passes; ++ps) {
+    int32_t* ko = (ps & 1) ? k1 : k0;
+    int32_t* vo = (ps & 1) ? v1 : v0;
+    sort_hist_kernel<<<nblk, kSortThreads, 0, st>>>(R, kin, 8 * ps, nblk, hist);
+    sort_scan_kernel<<<1, 256, 0, st>>>(nblk, hist);
+    sort_scatter_kernel<<<nblk, kSortThreads, 0, st>>>(R, kin, vin, 8 * ps, nblk, hist, ko, vo);
+    kin = ko;
+    vin = vo;
+  }
+  run_sum_kernel<<<smx::grid_for(R * dout, 256), 256, 0, st>>>(R, dout, kin, vin, G, C);
   SMX_LAUNCH_CHECK("smx_spectral_coefficients");
   return SMX_OK;
 }

@@ -21,6 +21,13 @@ from ._capi import call, ptr
 
 FAMILIES = {"legendre": 0, "hermite": 1}
 TC_MIN_DOUT = 16  # from this many outputs on, the tensor-core contraction is used
+# one-output plans: from this many points on, the tensor-core blocked evaluator
+# serves an evaluation (below it, the blocked evaluator, whose results the
+# multi-plan batch kernel of the serving loop reproduces exactly)
+BLOCKED_TC_MIN_POINTS = 1 << 30
+BLOCKED_TC_TABLES = dict(i32=("tc_td", "tc_row", "tc_chunk", "tc_b", "tc_box"), f32=("tc_tdab",),
+                         scalars=("tc_n_td", "tc_n_phi", "tc_n_phi_pad", "tc_n_rows", "tc_max_depth", "tc_n_agen",
+                                  "tc_n_chunks", "tc_n_boxes", "tc_lin0", "tc_stages", "c0"))
 MAX_DEGREE = 512  # recurrence tables of the kernels
 
 
@@ -115,8 +122,10 @@ class SpectralPlan:
         G = torch.empty(max(R * d_out, 1), dtype=torch.float64, device=dev)
         ids = torch.empty(max(R, 1), dtype=torch.int32, device=dev)
         C = torch.empty(n_lam * d_out, dtype=torch.float64, device=dev)
+        nws = capi.size("smx_spectral_coefficients_workspace", pl.ref())
+        ws = torch.empty(max(nws, 1), dtype=torch.uint8, device=dev)
         call("smx_spectral_coefficients", pl.ref(), ptr(aoff), ptr(A), ptr(tree.first_child), ptr(tree.n_child),
-             ptr(tree.dim), ptr(tree.deg), n_lam, ptr(G), ptr(ids), ptr(C), ptr(flag), st)
+             ptr(tree.dim), ptr(tree.deg), n_lam, ptr(G), ptr(ids), ptr(C), ptr(flag), ptr(ws), nws, st)
         if int(flag.item()):
             raise RuntimeError("orthogonal-basis coefficients: multi-index missing from the tree")
         self.C64 = C.view(n_lam, d_out)
@@ -167,6 +176,7 @@ class SpectralPlan:
             self._build_tc(*self._fwd_args)
         self.memory_limit = ip._memory_limit
         self.blocked = None
+        self.blocked_tc = None
         if d_out == 1 and self.tc is None:
             self._build_blocked(tree_np, C32[:, 0], np.asarray(ip._maxdeg), d, fam, fa, fb, T)
 
@@ -220,6 +230,30 @@ class SpectralPlan:
         self.blocked = b
         self.blocked_keep = kb
         self.blocked_layout = lay
+        self._build_blocked_tc(tr, c, maxdeg, fam, fa, fb, T)
+
+    def _build_blocked_tc(self, tr, c, maxdeg, fam, fa, fb, T):
+        """Tables of the tensor-core blocked evaluator (library builder), if the plan fits it."""
+        self.blocked_tc = None
+        lay = capi.host_layout("blocked_tc", tr, np.asarray(c, dtype=np.float32).reshape(-1, 1), 1, maxdeg, fam, fa,
+                               fb, **BLOCKED_TC_TABLES)
+        if lay is None:
+            return
+        kt = dict(td=T(lay["tc_td"], torch.int32), tdab=T(lay["tc_tdab"], torch.float32),
+                  row=T(lay["tc_row"], torch.int32), bimg=T(lay["tc_b"], torch.int32),
+                  box=T(lay["tc_box"], torch.int32), err=T(np.zeros(1, np.int32), torch.int32))
+        chunk = np.ascontiguousarray(lay["tc_chunk"], dtype=np.int32)
+        b = capi.SmxBlockedTc()
+        b.d_in = int(np.asarray(maxdeg).shape[0])
+        for name in ("n_td", "n_phi", "n_phi_pad", "n_rows", "max_depth", "n_agen", "n_chunks", "n_boxes", "lin0",
+                     "stages"):
+            setattr(b, name, int(lay["tc_" + name]))
+        b.c0 = float(lay["c0"])
+        for name in ("td", "tdab", "row", "bimg", "box", "err"):
+            setattr(b, name, kt[name].data_ptr() if kt[name].numel() else None)
+        b.chunk = chunk.ctypes.data
+        self.blocked_tc = b
+        self.blocked_tc_keep = (kt, chunk)
 
     def ref(self):
         import ctypes
@@ -333,7 +367,9 @@ class SpectralPlan:
     def evaluate(self, x, y, mode="tf32x3"):
         """y[P, d_out] (FP32) at x[P, d_in] (FP64, contiguous, on the device).
         ``mode="bf16x3"`` runs the tensor-core contraction with split-BF16
-        operands (plans with the tensor-core form only)."""
+        operands (plans with the tensor-core form only).  One-output plans
+        use the tensor-core blocked evaluator from BLOCKED_TC_MIN_POINTS
+        points on; ``mode="blocked"`` / ``"blocked_tc"`` choose the evaluator."""
         st = capi.stream_ptr(torch.cuda.current_stream())
         if mode == "bf16x3":
             if self.tc is None:
@@ -345,6 +381,13 @@ class SpectralPlan:
             import ctypes
 
             P = int(x.shape[0])
+            if self.blocked_tc is not None and mode != "blocked" and (mode == "blocked_tc" or P >= BLOCKED_TC_MIN_POINTS):
+                ref = ctypes.byref(self.blocked_tc)
+                if capi.size("smx_blocked_tc_supported", ref, ptr(x), int(x.shape[1])):
+                    call("smx_blocked_tc_eval", ref, ptr(x), P, int(x.shape[1]), ptr(y), st)
+                    return y
+                if mode == "blocked_tc":
+                    raise ValueError("the tensor-core blocked evaluator needs x 16-byte aligned with an even row pitch")
             nws = capi.size("smx_blocked_eval_workspace", ctypes.byref(self.blocked), P)
             ws = torch.empty(max(nws, 1), dtype=torch.uint8, device=x.device)
             call("smx_blocked_eval", ctypes.byref(self.blocked), ptr(x), P, int(x.shape[1]), ptr(y), ptr(ws), nws, st)
