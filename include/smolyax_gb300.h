@@ -324,7 +324,10 @@ int smx_blocked_eval(const smx_blocked* plan_host, const double* x, int64_t P, i
  * sums and counters); without it (ws = NULL) every tile is one block's work. */
 size_t smx_blocked_eval_workspace(const smx_blocked* plan_host, int64_t P);
 
-/* Tensor-core blocked evaluator (one output).  The same sum split by the kind
+/* Tensor-core blocked evaluator (one output): an alternative to
+ * smx_blocked_eval with ~2.5x smaller rounding error (max element-wise
+ * 1.5e-7 against 3.9e-7 at d_in = 1000, |Lambda| = 9999) at ~1.6x its time;
+ * no evaluation path selects it by itself.  The same sum split by the kind
  * of each entry's last factor: I(x) = c_0 + sum_a V_a(x) [ sum_s Bt[a][s]
  * Phi_s(x) + sum_j Bl[a][j] x_j ] over the nodes a (entries with children,
  * by remaining budget: the rows), the basis slots s of the table dimensions
@@ -334,22 +337,25 @@ size_t smx_blocked_eval_workspace(const smx_blocked* plan_host, int64_t P);
  * cores in chunks of <= 64 columns (A = V in three bf16 parts built on chip
  * in tensor memory, B = the coefficients in three bf16 parts, six part
  * products per 16-row K step, FP32 accumulation) and y = c_0 + sum T x +
- * sum T Phi is summed in FP32 (Kahan) as the x boxes (8 dimensions x 128
- * points) arrive by TMA.  Tables from smx_layout_build (SMX_LAYOUT_BLOCKED_TC;
- * names "tc_*").  Device pointers unless noted:
+ * sum T Phi is summed in FP32 (Kahan) as x streams in (read once, units of 8
+ * coordinates per point, prefetched to L2 chunks ahead).  Tables from
+ * smx_layout_build (SMX_LAYOUT_BLOCKED_TC; names "tc_*").  Device pointers
+ * unless noted:
  *   td[n_td][4]        dimension, degree, first basis slot, family
  *   tdab[n_td][2]      affine map a, b (z = a x + b)
  *   row[n_rows][4]     the 8 basis slots (16 bits each, 0 = the constant) of the node's path
  *   chunk[n_chunks][4] HOST: N | table << 16, K steps, stage offset / 16 bytes,
  *                      first basis slot (table chunks) or x box (linear chunks)
  *   bimg               coefficient stages in the order the kernel consumes them (16-byte aligned)
- *   box[n_boxes]       per x box: bit i set = dimension lin0 + 8 box + i is inactive (masked)
+ *   box[n_boxes]       per unit of 8 linear columns: bit i set = dimension lin0 + 8 unit + i is
+ *                      inactive or past d_in (masked: never read)
  *   err                int, 0 = ok; set when a pipeline wait ran out */
 typedef struct smx_blocked_tc {
   int32_t d_in;
   int32_t n_td, n_phi, n_phi_pad, n_rows, max_depth;
   int32_t n_agen;     /* K steps of A built per tile (the chunks' largest; <= 16) */
   int32_t n_chunks, n_boxes, lin0, stages;
+  int32_t td_col, td_bytes; /* x row segment of the table dimensions: first column, bytes (L2 prefetch) */
   float c0;
   const int32_t* td;
   const float* tdab;
@@ -360,16 +366,12 @@ typedef struct smx_blocked_tc {
   int32_t* err;
 } smx_blocked_tc;
 
-/* From this many points on, one-output evaluations (smx_fp32_eval, and the
- * package's FP32 path) use smx_blocked_tc_eval when the plan has its tables;
- * below, smx_blocked_eval (whose results the multi-plan batch kernel
- * reproduces exactly). */
-#define SMX_BLOCKED_TC_MIN_POINTS (1 << 30)
-/* 1 if smx_blocked_tc_eval serves x (16-byte aligned, even row pitch >= d_in). */
+/* 1 if smx_blocked_tc_eval serves x (16-byte aligned, even row pitch >= d_in;
+ * 32-byte loads when x is 32-byte aligned and the pitch a multiple of 4). */
 int smx_blocked_tc_supported(const smx_blocked_tc* plan_host, const double* x, int64_t ldx);
-/* y[P] (FP32) at x[P, ldx] (FP64); one persistent block per SM (up to 225
- * KiB of shared memory, all 512 tensor-memory columns); SMX_ERR_UNSUPPORTED
- * for an x it does not serve. */
+/* y[P] (FP32) at x[P, ldx] (FP64); one persistent block per SM (~140 KiB of
+ * shared memory, all 512 tensor-memory columns); SMX_ERR_UNSUPPORTED for an
+ * x it does not serve. */
 int smx_blocked_tc_eval(const smx_blocked_tc* plan_host, const double* x, int64_t P, int64_t ldx, float* y,
                         void* stream);
 

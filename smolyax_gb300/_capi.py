@@ -150,6 +150,8 @@ class SmxBlockedTc(C.Structure):
         ("n_boxes", _i32),
         ("lin0", _i32),
         ("stages", _i32),
+        ("td_col", _i32),
+        ("td_bytes", _i32),
         ("c0", C.c_float),
         ("td", _p),
         ("tdab", _p),

@@ -14,18 +14,22 @@
 //                       cores (kind::f16, A from tensor memory, B from shared
 //                       memory, six part products per 16-row K step, FP32
 //                       accumulation in tensor memory, two accumulators);
-//   producer thread     x boxes (8 dimensions x 128 points, FP64) by TMA, with
-//                       L2 prefetch ahead, and the chunks' coefficient stages
-//                       (bulk copies from the L2-resident image);
-//   compute warps       y_p += sum_j T[p][j] x_pj (x converted to FP32 as it
-//                       leaves shared memory) and sum_s T[p][s] Phi_s, Kahan-
-//                       compensated, then a fixed-order sum over the 4 column
-//                       groups.
-// The x stream is read once; everything else stays on chip or in L2.  Every
-// wait is bounded: on a timeout the block records an error, stops waiting and
-// finishes its loops without work, so that every barrier is still reached.
-#include <cuda.h>
-#include <cudaTypedefs.h>
+//   producer thread     the chunks' coefficient stages (bulk copies from the
+//                       L2-resident image) and L2 prefetches of the x rows a
+//                       few chunks ahead of their use (bulk prefetch of each
+//                       point's row segment);
+//   compute warps       y_p += sum_j T[p][j] x_pj -- x read once, straight
+//                       from global memory (32-byte streaming loads, two units
+//                       of 8 coordinates ahead in registers), converted to FP32
+//                       on the integer pipes -- and sum_s T[p][s] Phi_s,
+//                       Kahan-compensated, then a fixed-order sum over the 4
+//                       column groups.
+// (Measured and replaced: a TMA tile stream of the x rows, 8 coordinates x
+// 128 points per box, reached at most ~2.45 TB/s however many boxes were in
+// flight; per-row bulk L2 prefetches through the TMA unit delayed the
+// coefficient stages queued behind them.)  Every wait is bounded: on a timeout the block records
+// an error, stops waiting and finishes its loops without work, so that every
+// barrier is still reached.
 #include <cuda_bf16.h>
 
 #include <mutex>
@@ -44,7 +48,7 @@ using smx::f64_to_f32;
 using smx::kahan_add;
 
 constexpr int kRec = 512;
-constexpr int kPrefetch = 16;  // x boxes prefetched to L2 ahead of the loads (128 KB per block)
+constexpr int kPfChunks = 4;  // linear chunks of x prefetched to L2 ahead of the producer (64 KB each per block)
 constexpr int kWarpProducer = kComputeWarps, kWarpMMA = kComputeWarps + 1;
 
 __constant__ float t_alpha[2][kRec];
@@ -54,7 +58,10 @@ struct TcArgs {
   int64_t P, ldx;
   const double* x;
   float* y;
-  int n_td, n_phi, n_phi_pad, n_rows, max_depth, n_agen, n_chunks, n_boxes, lin0, stages, n_x;
+  int n_td, n_phi, n_phi_pad, n_rows, max_depth, n_agen, n_chunks, n_tchunks, n_boxes, lin0, stages;
+  int nbuf, acol;  // accumulators in tensor memory, first column of A
+  int8_t lin_idx[kMaxChunks];  // the linear chunks' positions in the chunk order
+  int td_col, td_bytes;  // x row segment of the table dimensions (L2 prefetch)
   float c0;
   const int4* td;
   const float2* tdab;
@@ -63,13 +70,12 @@ struct TcArgs {
   const int32_t* box;
   int* err;
   uint64_t wait_ns;
-  int4 chunk[kMaxChunks];  // {N | table << 16, K steps, stage image offset / 16, first slot or x box}
+  int4 chunk[kMaxChunks];  // {N | table << 16, K steps, stage image offset / 16, first slot or unit}
 };
 
 struct Bars {
-  uint64_t x_full[kXMax], x_empty[kXMax];
   uint64_t b_full[kBStages], b_empty[kBStages];
-  uint64_t acc_full[2], acc_empty[2];
+  uint64_t acc_full[3], acc_empty[3];
   uint64_t a_full, flush;
   uint32_t tmem;
   int abort_flag;
@@ -87,9 +93,9 @@ __device__ __forceinline__ void mma_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_
       "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
-__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&v)[8]) {
-  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
-               "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+__device__ __forceinline__ void tmem_st4(uint32_t taddr, const uint32_t (&v)[4]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(taddr), "r"(v[0]), "r"(v[1]),
+               "r"(v[2]), "r"(v[3])
                : "memory");
 }
 
@@ -107,18 +113,40 @@ __device__ __forceinline__ void split3(float a, float b, uint32_t (&w)[3]) {
   w[2] = *reinterpret_cast<uint32_t*>(&l);
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
-    blocked_tc_kernel(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ TcArgs g) {
+// x loads of one unit (8 coordinates of one point): 32-byte (X32) or 16-byte
+// streaming loads, or guarded scalar loads when some coordinates are masked.
+template <bool X32>
+__device__ __forceinline__ void load_unit(const double* __restrict__ p, int mask, double (&v)[8]) {
+  if (mask == 0) {
+    if constexpr (X32) {
+      asm volatile("ld.global.nc.L1::no_allocate.v4.f64 {%0, %1, %2, %3}, [%4];"
+                   : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3])
+                   : "l"(p));
+      asm volatile("ld.global.nc.L1::no_allocate.v4.f64 {%0, %1, %2, %3}, [%4];"
+                   : "=d"(v[4]), "=d"(v[5]), "=d"(v[6]), "=d"(v[7])
+                   : "l"(p + 4));
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; j += 2)
+        asm volatile("ld.global.nc.L1::no_allocate.v2.f64 {%0, %1}, [%2];" : "=d"(v[j]), "=d"(v[j + 1]) : "l"(p + j));
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = ((mask >> j) & 1) ? 0.0 : __ldg(p + j);
+  }
+}
+
+template <bool X32>
+__global__ void __launch_bounds__(kThreads, 1) blocked_tc_kernel(const __grid_constant__ TcArgs g) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const Smem L = smem_layout(g.n_phi_pad);
   float* phi = reinterpret_cast<float*>(base + L.phi);
+  int4* rowtab = reinterpret_cast<int4*>(base + L.row);
   uint8_t* bst = base + L.b;
-  uint8_t* xst = base + L.x;
   float* rs = reinterpret_cast<float*>(base + L.rs);
   Bars* bars = reinterpret_cast<Bars*>(base + L.bar);
   volatile int* abort_flag = &bars->abort_flag;
-  const int n_x = g.n_x;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t n_tiles = (g.P + kTile - 1) / kTile;
@@ -126,15 +154,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int nt = blockIdx.x < n_tiles ? int((n_tiles - blockIdx.x + G - 1) / G) : 0;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < n_x; ++s) {
-      mbar_init(&bars->x_full[s], 1);
-      mbar_init(&bars->x_empty[s], 4);  // the 4 warps of the column group that reads the box
-    }
     for (int s = 0; s < kBStages; ++s) {
       mbar_init(&bars->b_full[s], 1);
       mbar_init(&bars->b_empty[s], 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < 3; ++b) {
       mbar_init(&bars->acc_full[b], 1);
       mbar_init(&bars->acc_empty[b], kComputeWarps);
     }
@@ -143,11 +167,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     bars->abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // constant slot 0 and the padding slots of Phi (never rewritten)
+  // constant slot 0 and the padding slots of Phi (never rewritten); the rows' paths
   for (int i = threadIdx.x; i < kTile; i += blockDim.x) {
     phi[i] = 1.f;
     for (int s = g.n_phi; s < g.n_phi_pad; ++s) phi[s * kTile + i] = 0.f;
   }
+  for (int r = threadIdx.x; r < g.n_agen * kStep; r += blockDim.x)
+    rowtab[r] = r < g.n_rows ? __ldg(&g.row[r]) : make_int4(0, 0, 0, 0);
   if (warp == kWarpMMA) {  // all of tensor memory: accumulators and A
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&bars->tmem)),
                  "r"(512));
@@ -159,60 +185,80 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tmem = bars->tmem;
 
   if (warp == kWarpProducer) {
-    if (lane == 0) {
-      // ---- producer: x boxes and coefficient stages, two independent queues
-      const uint64_t total_x = uint64_t(nt) * g.n_boxes, total_b = uint64_t(nt) * g.stages;
-      uint64_t ix = 0, ib = 0, pf = 0;
-      int cb = 0, jb = 0;
-      uint64_t t_last = global_ns();
-      while ((ix < total_x || ib < total_b) && !*abort_flag) {
-        for (; pf < total_x && pf < ix + kPrefetch; ++pf) {
-          const int64_t tile = blockIdx.x + int64_t(pf / g.n_boxes) * G;
-          tma_prefetch_2d(&tmx, g.lin0 + kBox * int(pf % g.n_boxes), int(tile * kTile));
-        }
-        bool prog = false;
-        if (ix < total_x) {
-          const int s = int(ix % n_x);
-          if (ix < uint64_t(n_x) || mbar_test(&bars->x_empty[s], uint32_t((ix / n_x) & 1) ^ 1u)) {
-            const int64_t tile = blockIdx.x + int64_t(ix / g.n_boxes) * G;
-            mbar_expect_tx(&bars->x_full[s], kBoxBytes);
-            tma_load_2d(xst + s * kBoxBytes, &tmx, g.lin0 + kBox * int(ix % g.n_boxes), int(tile * kTile),
-                        &bars->x_full[s]);
-            ++ix;
-            prog = true;
-          }
-        }
-        if (ib < total_b) {
-          const int s = int(ib % kBStages);
-          if (ib < kBStages || mbar_test(&bars->b_empty[s], uint32_t((ib / kBStages) & 1) ^ 1u)) {
-            const int4 ch = g.chunk[cb];
-            const uint32_t bytes = uint32_t(ch.x & 0xFFFF) * (kSplits * 32);
-            mbar_expect_tx(&bars->b_full[s], bytes);
-            bulk_load(bst + s * kBStageMax, g.bimg + int64_t(ch.z) * 16 + int64_t(jb) * bytes, bytes,
-                      &bars->b_full[s]);
-            ++ib;
-            if (++jb == ch.y) {
-              jb = 0;
-              if (++cb == g.n_chunks) cb = 0;
-            }
-            prog = true;
-          }
-        }
-        if (prog) {
-          t_last = global_ns();
-        } else if (global_ns() - t_last > g.wait_ns) {
-          atomicExch(g.err, 1);
-          *abort_flag = 1;
-        }
+    // ---- producer warp: coefficient stages by 16-byte asynchronous copies
+    // through L1 (all lanes; a stage is handed to the MMA thread once the
+    // kBInflight later ones are issued and its own copies have landed), and L2
+    // prefetches of the x row segments of the table dimensions (one tile
+    // ahead) and of the linear chunks (kPfChunks chunks ahead)
+    const int n_lin = g.n_chunks - g.n_tchunks;
+    auto prefetch_rows = [&](int64_t tile, int64_t col, int bytes) {  // within each row: [col, ldx)
+      const int64_t room = (g.ldx - col) * 8;
+      bytes = int(room < bytes ? room : int64_t(bytes));
+      if (bytes <= 0) return;
+      const int64_t p0 = tile * kTile;
+      const int rows = int(g.P - p0 < kTile ? g.P - p0 : int64_t(kTile));
+      const double* xp = g.x + p0 * g.ldx + col;
+      // one prefetch per 128-byte line of every row segment (all inside the row),
+      // lanes over (row, line)
+      const int lmax = (bytes + 127) / 128 + 1;
+      for (int q = lane; q < rows * lmax; q += 32) {
+        const int r = q / lmax, l = q - r * lmax;
+        const uintptr_t a = reinterpret_cast<uintptr_t>(xp + r * g.ldx);
+        const uintptr_t first = a & ~uintptr_t(127), last = (a + bytes - 1) & ~uintptr_t(127);
+        if (first + 128 * uintptr_t(l) <= last)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(first + 128 * uintptr_t(l)));
       }
-      if (*abort_flag) {
-        // wait (bounded) until the copies already issued have landed
-        for (uint64_t u = ix > uint64_t(n_x) ? ix - n_x : 0; u < ix; ++u)
-          mbar_wait(&bars->x_full[u % n_x], uint32_t((u / n_x) & 1), nullptr, g.wait_ns);
-        for (uint64_t u = ib > kBStages ? ib - kBStages : 0; u < ib; ++u)
-          mbar_wait(&bars->b_full[u % kBStages], uint32_t((u / kBStages) & 1), nullptr, g.wait_ns);
+    };
+    auto prefetch_lin = [&](int64_t k) {  // the k-th linear chunk of this block's sequence
+      const int i = int(k / n_lin), c = g.lin_idx[k % n_lin];
+      if (i >= nt) return;
+      const int4 ch = g.chunk[c];
+      prefetch_rows(blockIdx.x + int64_t(i) * G, g.lin0 + int64_t(kBox) * ch.w, (ch.x & 0xFFFF) * 8);
+    };
+    int64_t pf = 0;
+    if (nt > 0 && g.td_bytes > 0) prefetch_rows(blockIdx.x, g.td_col, g.td_bytes);
+    for (; n_lin > 0 && pf < kPfChunks; ++pf) prefetch_lin(pf);
+    uint64_t ib = 0, handed = 0;
+    bool ok = true;
+    auto hand_over = [&](uint64_t upto) {  // stages [handed, upto) have landed: fence, signal
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0)
+        for (; handed < upto; ++handed) mbar_arrive(&bars->b_full[handed % kBStages]);
+      handed = upto;
+    };
+    for (int i = 0; i < nt && ok; ++i) {
+      if (i + 1 < nt && g.td_bytes > 0) prefetch_rows(blockIdx.x + int64_t(i + 1) * G, g.td_col, g.td_bytes);
+      for (int c = 0; c < g.n_chunks && ok; ++c) {
+        const int4 ch = g.chunk[c];
+        if (ch.x >> 16 == 0 && n_lin > 0) prefetch_lin(pf++);
+        const int bytes = (ch.x & 0xFFFF) * (kSplits * 32);
+        for (int jb = 0; jb < ch.y; ++jb, ++ib) {
+          const int s = int(ib % kBStages);
+          bool got = true;
+          if (lane == 0 && ib >= kBStages)
+            got = mbar_wait(&bars->b_empty[s], uint32_t((ib / kBStages) & 1) ^ 1u, abort_flag, g.wait_ns);
+          if (!__shfl_sync(0xffffffffu, got ? 1 : 0, 0)) {
+            if (lane == 0) {
+              atomicExch(g.err, 1);
+              *abort_flag = 1;
+            }
+            ok = false;
+            break;
+          }
+          const uint8_t* src = g.bimg + int64_t(ch.z) * 16 + int64_t(jb) * bytes;
+          const uint32_t dst = smem_u32(bst + s * kBStageMax);
+          for (int q = lane; q < bytes / 16; q += 32)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16 * q), "l"(src + 16 * q)
+                         : "memory");
+          asm volatile("cp.async.commit_group;" ::: "memory");
+          asm volatile("cp.async.wait_group %0;" ::"n"(kBInflight) : "memory");
+          if (ib + 1 > uint64_t(kBInflight)) hand_over(ib + 1 - kBInflight);
+        }
       }
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    if (ok) hand_over(ib);
     __syncwarp();
   } else if (warp == kWarpMMA) {
     if (lane == 0) {
@@ -227,8 +273,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int c = 0; c < g.n_chunks && ok; ++c, ++gc) {
           const int4 ch = g.chunk[c];
           const int N = ch.x & 0xFFFF, nk = ch.y;
-          const int b = int(gc & 1);
-          if (gc >= 2 && !mbar_wait(&bars->acc_empty[b], uint32_t((gc >> 1) & 1) ^ 1u, abort_flag, g.wait_ns)) {
+          const int b = int(gc % g.nbuf);
+          if (gc >= uint64_t(g.nbuf) &&
+              !mbar_wait(&bars->acc_empty[b], uint32_t((gc / g.nbuf) & 1) ^ 1u, abort_flag, g.wait_ns)) {
             ok = false;
             break;
           }
@@ -245,7 +292,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t b_addr = smem_u32(bst + bs * kBStageMax);
             const uint32_t bsz = uint32_t(N) * 32;
-            const uint32_t a0 = tmem + uint32_t(kAcol + kSplits * 8 * kk);
+            const uint32_t a0 = tmem + uint32_t(g.acol + kSplits * 8 * kk);
             uint64_t db[3];
 #pragma unroll
             for (int s = 0; s < 3; ++s) db[s] = make_desc_sw(b_addr + s * bsz, 32);
@@ -275,7 +322,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncwarp();
   } else {
     // ---- compute warps: warp (quadrant qd = warp % 4: points 32 qd .. +31 =
-    // tensor-memory lanes, column group grp = warp / 4)
+    // tensor-memory lanes, column group grp = warp / 4: units grp, grp + 4, ...)
     const int tid = threadIdx.x;
     const int qd = warp & 3, grp = warp >> 2, pt = 32 * qd + lane;
     const uint32_t lane_base = tmem + (uint32_t(32 * qd) << 16);
@@ -294,6 +341,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     };
     for (int i = 0; i < nt; ++i) {
       const int64_t p0 = (blockIdx.x + int64_t(i) * G) * kTile;
+      const double* xrow = g.x + min(p0 + pt, g.P - 1) * g.ldx + g.lin0;
 
       // phase 0: basis values of the table dimensions (thread: point q, dimensions hb, hb + 4, ...)
       {
@@ -323,30 +371,31 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
       }
+      // the first two units of x of this warp's column group, in flight during A
+      double xn0[8], xn1[8];
+      if (grp < g.n_boxes) load_unit<X32>(xrow + kBox * grp, __ldg(g.box + grp), xn0);
+      if (grp + 4 < g.n_boxes) load_unit<X32>(xrow + kBox * (grp + 4), __ldg(g.box + grp + 4), xn1);
       compute_sync();
 
-      // A = V in tensor memory: warp (qd, grp) writes the K steps grp, grp + 4, ...
-      // of its 32 points (lanes), 16 rows per step, three bf16 parts
-      for (int kk = grp; kk < g.n_agen; kk += 4) {
-        float v[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int r = kk * kStep + j;
-          float pv = 0.f;
-          if (r < g.n_rows) {
-            const int4 rw = __ldg(&g.row[r]);
-            const int wv[4] = {rw.x, rw.y, rw.z, rw.w};
-            pv = 1.f;
-            for (int qq = 0; qq < g.max_depth; ++qq) {
-              const int slot = (unsigned(wv[qq >> 1]) >> (16 * (qq & 1))) & 0xFFFF;
-              pv *= phi[slot * kTile + pt];
-            }
-          }
-          v[j] = pv;
-        }
-        uint32_t w[3][8];
+      // A = V in tensor memory: warp (qd, grp) writes the half steps (8 rows)
+      // grp, grp + 4, ... of its 32 points (lanes), three bf16 parts each
+      for (int hs = grp; hs < 2 * g.n_agen; hs += 4) {
+        const int kk = hs >> 1, half = hs & 1;
+        float v[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
+          const int r = kk * kStep + 8 * half + j;
+          const int4 rw = rowtab[r];
+          const unsigned wv[4] = {unsigned(rw.x), unsigned(rw.y), unsigned(rw.z), unsigned(rw.w)};
+          float pv = 1.f;
+#pragma unroll
+          for (int qq = 0; qq < 8; ++qq)
+            if (qq < g.max_depth) pv *= phi[((wv[qq >> 1] >> (16 * (qq & 1))) & 0xFFFFu) * kTile + pt];
+          v[j] = r < g.n_rows ? pv : 0.f;
+        }
+        uint32_t w[3][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
           uint32_t t3[3];
           split3(v[2 * j], v[2 * j + 1], t3);
           w[0][j] = t3[0];
@@ -354,20 +403,20 @@ __global__ void __launch_bounds__(kThreads, 1)
           w[2][j] = t3[2];
         }
 #pragma unroll
-        for (int s = 0; s < 3; ++s) tmem_st8(lane_base + uint32_t(kAcol + kSplits * 8 * kk + 8 * s), w[s]);
+        for (int s = 0; s < 3; ++s) tmem_st4(lane_base + uint32_t(g.acol + kSplits * 8 * kk + 8 * s + 4 * half), w[s]);
       }
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;");
       compute_sync();
       if (tid == 0) mbar_arrive(&bars->a_full);
 
-      // contraction of the accumulators: column units of 8 (u = grp, grp + 4, ...)
+      // contraction of the accumulators: units of 8 columns (u = grp, grp + 4, ...)
       float s_acc = 0.f, c_acc = 0.f;
       for (int c = 0; c < g.n_chunks; ++c, ++gc) {
         const int4 ch = g.chunk[c];
         const int N = ch.x & 0xFFFF, table = ch.x >> 16;
-        const int b = int(gc & 1);
-        wait_ok(&bars->acc_full[b], uint32_t((gc >> 1) & 1));
+        const int b = int(gc % g.nbuf);
+        wait_ok(&bars->acc_full[b], uint32_t((gc / g.nbuf) & 1));
         ok = __all_sync(0xffffffffu, ok);
         asm volatile("tcgen05.fence::after_thread_sync;");
         for (int u = grp; u < N / 8; u += 4) {
@@ -376,34 +425,24 @@ __global__ void __launch_bounds__(kThreads, 1)
                        : "=r"(T[0]), "=r"(T[1]), "=r"(T[2]), "=r"(T[3]), "=r"(T[4]), "=r"(T[5]), "=r"(T[6]),
                          "=r"(T[7])
                        : "r"(lane_base + uint32_t(b * kMaxN + 8 * u)));
-          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
           float v;
           if (table) {
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             const float* ph = phi + (ch.w + 8 * u) * kTile + pt;
             v = __uint_as_float(T[0]) * ph[0];
 #pragma unroll
             for (int j = 1; j < 8; ++j) v = fmaf(__uint_as_float(T[j]), ph[j * kTile], v);
           } else {
-            const int box = ch.w + u;
-            const uint64_t gb = uint64_t(i) * g.n_boxes + box;
-            const int s = int(gb % n_x);
-            wait_ok(&bars->x_full[s], uint32_t((gb / n_x) & 1));
-            const uint8_t* row = xst + s * kBoxBytes + pt * 64;
+            // this unit's x arrived in xn0; the unit two ahead in the group is loaded now
             double xv[8];
 #pragma unroll
-            for (int c4 = 0; c4 < 4; ++c4) {
-              const double2 d2 = *reinterpret_cast<const double2*>(row + ((c4 ^ ((pt >> 1) & 3)) << 4));
-              xv[2 * c4] = d2.x;
-              xv[2 * c4 + 1] = d2.y;
+            for (int j = 0; j < 8; ++j) {
+              xv[j] = xn0[j];
+              xn0[j] = xn1[j];
             }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&bars->x_empty[s]);
-            const int mask = __ldg(g.box + box);
-            if (mask) {
-#pragma unroll
-              for (int j = 0; j < 8; ++j)
-                if ((mask >> j) & 1) xv[j] = 0.0;
-            }
+            const int nb = ch.w + u + 8;
+            if (nb < g.n_boxes) load_unit<X32>(xrow + kBox * nb, __ldg(g.box + nb), xn1);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             v = __uint_as_float(T[0]) * f64_to_f32(xv[0]);
 #pragma unroll
             for (int j = 1; j < 8; ++j) v = fmaf(__uint_as_float(T[j]), f64_to_f32(xv[j]), v);
@@ -456,8 +495,10 @@ int prepare(int* sms) {
       }
     if (cudaMemcpyToSymbol(t_alpha, al, sizeof(al)) != cudaSuccess ||
         cudaMemcpyToSymbol(t_beta, be, sizeof(be)) != cudaSuccess ||
-        cudaFuncSetAttribute(blocked_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemLimit)) !=
+        cudaFuncSetAttribute(blocked_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemLimit)) !=
             cudaSuccess ||
+        cudaFuncSetAttribute(blocked_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(kSmemLimit)) != cudaSuccess ||
         cudaDeviceGetAttribute(&g_sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
       return smx::set_error(SMX_ERR_CUDA, "smx_blocked_tc_eval: device set-up failed");
     g_ready[dev] = true;
@@ -484,8 +525,12 @@ int check_plan(const smx_blocked_tc* b) {
     stages += nk;
   }
   if (stages != b->stages) return smx::set_error(SMX_ERR_ARG, "smx_blocked_tc_eval: stage count");
-  if (smem_layout(b->n_phi_pad).n_x == 0)
+  if (acc_buffers(b->n_agen) * kMaxN + kSplits * 8 * b->n_agen > 512)
+    return smx::set_error(SMX_ERR_ARG, "smx_blocked_tc_eval: A does not fit tensor memory");
+  if (smem_layout(b->n_phi_pad).total > kSmemLimit)
     return smx::set_error(SMX_ERR_UNSUPPORTED, "smx_blocked_tc_eval: shared memory");
+  if (b->td_col < 0 || b->td_col % 2 || b->td_bytes < 0 || b->td_bytes % 16)
+    return smx::set_error(SMX_ERR_ARG, "smx_blocked_tc_eval: bad table-dimension segment");
   return SMX_OK;
 }
 
@@ -508,17 +553,6 @@ extern "C" int smx_blocked_tc_eval(const smx_blocked_tc* b, const double* x, int
   SMX_REQUIRE(P <= (int64_t(1) << 31) - kTile, "smx_blocked_tc_eval: too many points");
   int sms = 0;
   if ((rc = prepare(&sms))) return rc;
-  PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-  if ((rc = smx::tc::tensor_map_encoder(&encode))) return rc;
-  CUtensorMap tmx;
-  cuuint64_t dims[2] = {cuuint64_t(b->d_in), cuuint64_t(P)};
-  cuuint64_t strides[1] = {cuuint64_t(ldx) * 8};
-  cuuint32_t box[2] = {cuuint32_t(kBox), cuuint32_t(kTile)};
-  cuuint32_t estr[2] = {1, 1};
-  if (encode(&tmx, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double*>(x), dims, strides, box, estr,
-             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-    return smx::set_error(SMX_ERR_CUDA, "smx_blocked_tc_eval: tensor map encoding failed");
   TcArgs a{};
   a.P = P;
   a.ldx = ldx;
@@ -534,7 +568,17 @@ extern "C" int smx_blocked_tc_eval(const smx_blocked_tc* b, const double* x, int
   a.n_boxes = b->n_boxes;
   a.lin0 = b->lin0;
   a.stages = b->stages;
-  a.n_x = smem_layout(b->n_phi_pad).n_x;
+  a.n_tchunks = 0;
+  for (int c = 0, k = 0; c < b->n_chunks; ++c) {
+    if (b->chunk[4 * c] >> 16)
+      ++a.n_tchunks;
+    else
+      a.lin_idx[k++] = int8_t(c);
+  }
+  a.nbuf = acc_buffers(b->n_agen);
+  a.acol = a.nbuf * kMaxN;
+  a.td_col = b->td_col;
+  a.td_bytes = b->td_bytes;
   a.c0 = b->c0;
   a.td = reinterpret_cast<const int4*>(b->td);
   a.tdab = reinterpret_cast<const float2*>(b->tdab);
@@ -548,7 +592,11 @@ extern "C" int smx_blocked_tc_eval(const smx_blocked_tc* b, const double* x, int
   const int64_t tiles = (P + kTile - 1) / kTile;
   const unsigned grid = unsigned(tiles < sms ? tiles : sms);
   const size_t smem = size_t(smem_layout(b->n_phi_pad).total);
-  blocked_tc_kernel<<<grid, kThreads, smem, smx::as_stream(stream)>>>(tmx, a);
+  const bool x32 = (reinterpret_cast<uintptr_t>(x) & 31) == 0 && ldx % 4 == 0;
+  if (x32)
+    blocked_tc_kernel<true><<<grid, kThreads, smem, smx::as_stream(stream)>>>(a);
+  else
+    blocked_tc_kernel<false><<<grid, kThreads, smem, smx::as_stream(stream)>>>(a);
   SMX_LAUNCH_CHECK("smx_blocked_tc_eval");
   return SMX_OK;
 }

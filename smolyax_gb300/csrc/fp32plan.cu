@@ -122,12 +122,6 @@ struct smx_fp32_plan {
   DevBuf<float> tf;
   smx_blocked blocked{};
   smx_spectral spectral{};
-  // tensor-core blocked evaluator (one output; large point counts)
-  bool have_btc = false;
-  smx_blocked_tc btc{};
-  DevBuf<int32_t> btc_td, btc_row, btc_img, btc_box, btc_err;
-  DevBuf<float> btc_tdab;
-  std::vector<int32_t> btc_chunk;
   // tape of the tensor-core panel (forward on the tensor cores, and the VJP of every evaluator)
   bool have_tape = false;
   int K = 0, ldk = 0, ldo = 0, n_slots = 0, n_dims = 0;
@@ -401,37 +395,6 @@ extern "C" int smx_fp32_plan_create(const smx_plan* pl, const smx_tree* tree, co
       s.fam = h->fam.p;
       s.n_ent = int(size_of(t, "hot_ent"));
       s.n_w = int(size_of(t, "W") / 4);
-      smx::layout::Tables tt;
-      if (smx::layout::build_blocked_tc(tr, C32.data(), maxdeg.data(), d, fam_v.data(), fa_v.data(), fb_v.data(),
-                                        tt)) {
-        if ((rc = h->btc_td.upload(tt.i32["tc_td"], st)) || (rc = h->btc_row.upload(tt.i32["tc_row"], st)) ||
-            (rc = h->btc_img.upload(tt.i32["tc_b"], st)) || (rc = h->btc_box.upload(tt.i32["tc_box"], st)) ||
-            (rc = h->btc_err.upload(std::vector<int32_t>{0}, st)) ||
-            (rc = h->btc_tdab.upload(tt.f32["tc_tdab"], st)))
-          return rc;
-        h->btc_chunk = tt.i32["tc_chunk"];
-        smx_blocked_tc& q = h->btc;
-        q.d_in = d;
-        q.n_td = int(tt.scalar["tc_n_td"]);
-        q.n_phi = int(tt.scalar["tc_n_phi"]);
-        q.n_phi_pad = int(tt.scalar["tc_n_phi_pad"]);
-        q.n_rows = int(tt.scalar["tc_n_rows"]);
-        q.max_depth = int(tt.scalar["tc_max_depth"]);
-        q.n_agen = int(tt.scalar["tc_n_agen"]);
-        q.n_chunks = int(tt.scalar["tc_n_chunks"]);
-        q.n_boxes = int(tt.scalar["tc_n_boxes"]);
-        q.lin0 = int(tt.scalar["tc_lin0"]);
-        q.stages = int(tt.scalar["tc_stages"]);
-        q.c0 = float(tt.scalar["c0"]);
-        q.td = h->btc_td.p;
-        q.tdab = h->btc_tdab.p;
-        q.row = h->btc_row.p;
-        q.chunk = h->btc_chunk.data();
-        q.bimg = h->btc_img.p;
-        q.box = h->btc_box.p;
-        q.err = h->btc_err.p;
-        h->have_btc = true;
-      }
     } else {
       h->evaluator = SMX_FP32_PERPOINT;
       smx_spectral& s = h->spectral;
@@ -503,11 +466,7 @@ extern "C" int smx_fp32_eval(const smx_fp32_plan* h, const double* x, int64_t P,
   SMX_REQUIRE(x && y, "smx_fp32_eval: null pointer");
   const size_t need = smx_fp32_workspace(h, P);
   SMX_REQUIRE(ws_bytes >= need && (ws || need == 0), "smx_fp32_eval: workspace too small");
-  if (h->evaluator == SMX_FP32_BLOCKED) {
-    if (h->have_btc && P >= SMX_BLOCKED_TC_MIN_POINTS && smx_blocked_tc_supported(&h->btc, x, ldx))
-      return smx_blocked_tc_eval(&h->btc, x, P, ldx, y, stream);
-    return smx_blocked_eval(&h->blocked, x, P, ldx, y, ws, ws_bytes, stream);
-  }
+  if (h->evaluator == SMX_FP32_BLOCKED) return smx_blocked_eval(&h->blocked, x, P, ldx, y, ws, ws_bytes, stream);
   if (h->evaluator == SMX_FP32_PERPOINT) return smx_spectral_eval(&h->spectral, x, P, ldx, y, stream);
   // tensor core: per chunk of points a basis-product panel (TF32 hi/lo) and the contraction
   const int64_t step = tc_step(h, P);
@@ -536,16 +495,13 @@ extern "C" int smx_fp32_eval(const smx_fp32_plan* h, const double* x, int64_t P,
 
 extern "C" int smx_fp32_plan_check(const smx_fp32_plan* h, void* stream) {
   SMX_REQUIRE(h, "smx_fp32_plan_check: null plan");
-  int32_t e = 0, e2 = 0;
+  int32_t e = 0;
   cudaStream_t st = smx::as_stream(stream);
   if (cudaMemcpyAsync(&e, h->err.p, sizeof(e), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      (h->have_btc && cudaMemcpyAsync(&e2, h->btc_err.p, sizeof(e2), cudaMemcpyDeviceToHost, st) != cudaSuccess) ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return smx::set_error(SMX_ERR_CUDA, "smx_fp32_plan_check: read failed");
-  if (e == 0 && e2 == 0) return SMX_OK;
+  if (e == 0) return SMX_OK;
   cudaMemsetAsync(h->err.p, 0, sizeof(int32_t), st);
-  if (h->have_btc) cudaMemsetAsync(h->btc_err.p, 0, sizeof(int32_t), st);
-  if (e == 0) e = e2;
   return smx::set_error(SMX_ERR_CUDA, "tensor-core contraction: a pipeline wait timed out (code " + std::to_string(e) +
                                           "); its results are invalid");
 }

@@ -452,9 +452,10 @@ bool build_blocked_tc(const Tree& tr, const float* C, const int64_t* maxdeg, int
   struct Chunk {
     int64_t N, nk, table, col0;
   };
-  std::vector<Chunk> chunks;
-  for (int64_t c0 = 0; any_table && c0 < n_phi_pad; c0 += kMaxN)
-    chunks.push_back({std::min<int64_t>(kMaxN, n_phi_pad - c0), kt_t, 1, c0});
+  // chunk order: linear chunks (their contraction starts the x stream) with
+  // the table chunks spread among them, so that the table chunks' longer
+  // products run while earlier linear chunks are summed
+  std::vector<Chunk> lin, tab, chunks;
   int64_t n_agen = kt_t;
   for (int64_t c0 = 0; c0 < n_cols; c0 += kMaxN) {
     const int64_t N = std::min<int64_t>(kMaxN, n_cols - c0);
@@ -462,10 +463,17 @@ bool build_blocked_tc(const Tree& tr, const float* C, const int64_t* maxdeg, int
     for (int64_t c = c0; c < c0 + N; ++c) rmax = std::max(rmax, col_rows[c]);
     const int64_t nk = (rmax + kStep - 1) / kStep;
     n_agen = std::max(n_agen, nk);
-    chunks.push_back({N, nk, 0, c0});
+    lin.push_back({N, nk, 0, c0});
+  }
+  for (int64_t c0 = 0; any_table && c0 < n_phi_pad; c0 += kMaxN)
+    tab.push_back({std::min<int64_t>(kMaxN, n_phi_pad - c0), kt_t, 1, c0});
+  for (size_t q = 0, t = 0; q <= lin.size(); ++q) {
+    // table chunk t goes after (t + 1) * n_lin / (n_tab + 1) linear chunks
+    while (t < tab.size() && q == (t + 1) * lin.size() / (tab.size() + 1)) chunks.push_back(tab[t++]);
+    if (q < lin.size()) chunks.push_back(lin[q]);
   }
   if (chunks.empty() || int(chunks.size()) > kMaxChunks || n_agen > kMaxSteps) return false;
-  if (smem_layout(n_phi_pad).n_x == 0) return false;
+  if (smem_layout(n_phi_pad).total > kSmemLimit) return false;
 
   // coefficient stages in the order the MMA thread consumes them: per chunk
   // its K steps from the last (small terms) to the first
@@ -498,14 +506,14 @@ bool build_blocked_tc(const Tree& tr, const float* C, const int64_t* maxdeg, int
   std::vector<int32_t> img32((img.size() + 1) / 2, 0);
   std::memcpy(img32.data(), img.data(), img.size() * 2);
 
-  // x boxes: inactive dimensions among the linear columns are masked (their
-  // coordinates do not enter the interpolant)
+  // units of 8 linear columns: inactive dimensions and those past d are
+  // masked (never read; their coordinates do not enter the interpolant)
   const int64_t n_boxes = n_cols / kBox;
   std::vector<int32_t> box(n_boxes, 0);
   for (int64_t b = 0; b < n_boxes; ++b)
     for (int i = 0; i < kBox; ++i) {
       const int64_t j = lin0 + b * kBox + i;
-      if (j < d && maxdeg[j] == 0) box[b] |= 1 << i;
+      if (j >= d || maxdeg[j] == 0) box[b] |= 1 << i;
     }
 
   out.i32["tc_td"] = td;
@@ -524,6 +532,13 @@ bool build_blocked_tc(const Tree& tr, const float* C, const int64_t* maxdeg, int
   out.scalar["tc_n_chunks"] = double(chunks.size());
   out.scalar["tc_n_boxes"] = double(n_boxes);
   out.scalar["tc_lin0"] = double(lin0);
+  {
+    int64_t lo = d, hi = 0;
+    for (size_t q = 0; q < td.size(); q += 4) lo = std::min<int64_t>(lo, td[q]), hi = std::max<int64_t>(hi, td[q] + 1);
+    lo = lo / 2 * 2;
+    out.scalar["tc_td_col"] = double(td.empty() ? 0 : lo);
+    out.scalar["tc_td_bytes"] = double(td.empty() ? 0 : ((hi - lo) * 8 + 15) / 16 * 16);
+  }
   out.scalar["tc_stages"] = double(stages);
   out.scalar["tc_smem"] = double(smem_layout(n_phi_pad).total);
   out.scalar["c0"] = double(C[0]);

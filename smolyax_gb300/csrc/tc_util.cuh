@@ -74,13 +74,6 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, in
       : "memory");
 }
 
-// L2 prefetch of one 2-D box (no shared memory, no completion).
-__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* tm, int c0, int c1) {
-  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(reinterpret_cast<uint64_t>(tm)),
-               "r"(c0), "r"(c1)
-               : "memory");
-}
-
 // Contiguous bulk copy global -> shared (16-byte aligned addresses, size a
 // multiple of 16), completion counted on `bar`.
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {

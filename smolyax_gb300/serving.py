@@ -54,7 +54,6 @@ import torch
 
 from . import _capi as capi
 from ._capi import call, ptr
-from .spectral import BLOCKED_TC_MIN_POINTS
 
 _ALIGN = 256
 
@@ -253,12 +252,10 @@ class Server:
         if req.op == "eval" and req.precision == "fp32" and sp.tc is None:
             if sp.blocked is None:
                 return "stream"
-            if req.points <= 128 * self.sms and not (sp.blocked_tc is not None and
-                                                     req.points >= BLOCKED_TC_MIN_POINTS):
+            if req.points <= 128 * self.sms:
                 return "blocked"
-            # a request of a full round of tiles or more fills the GPU alone, and
-            # one the tensor-core blocked evaluator serves is evaluated by it:
-            # either way exactly as alone
+            # a blocked request of a full round of tiles or more fills the GPU
+            # alone and is evaluated exactly as alone (last-round split)
             return ("plan", req.name, req.op, req.precision, req.id)
         return ("plan", req.name, req.op, req.precision)
 

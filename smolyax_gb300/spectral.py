@@ -21,13 +21,10 @@ from ._capi import call, ptr
 
 FAMILIES = {"legendre": 0, "hermite": 1}
 TC_MIN_DOUT = 16  # from this many outputs on, the tensor-core contraction is used
-# one-output plans: from this many points on, the tensor-core blocked evaluator
-# serves an evaluation (below it, the blocked evaluator, whose results the
-# multi-plan batch kernel of the serving loop reproduces exactly)
-BLOCKED_TC_MIN_POINTS = 1 << 30
 BLOCKED_TC_TABLES = dict(i32=("tc_td", "tc_row", "tc_chunk", "tc_b", "tc_box"), f32=("tc_tdab",),
                          scalars=("tc_n_td", "tc_n_phi", "tc_n_phi_pad", "tc_n_rows", "tc_max_depth", "tc_n_agen",
-                                  "tc_n_chunks", "tc_n_boxes", "tc_lin0", "tc_stages", "c0"))
+                                  "tc_n_chunks", "tc_n_boxes", "tc_lin0", "tc_stages", "tc_td_col", "tc_td_bytes",
+                                  "c0"))
 MAX_DEGREE = 512  # recurrence tables of the kernels
 
 
@@ -246,7 +243,7 @@ class SpectralPlan:
         b = capi.SmxBlockedTc()
         b.d_in = int(np.asarray(maxdeg).shape[0])
         for name in ("n_td", "n_phi", "n_phi_pad", "n_rows", "max_depth", "n_agen", "n_chunks", "n_boxes", "lin0",
-                     "stages"):
+                     "stages", "td_col", "td_bytes"):
             setattr(b, name, int(lay["tc_" + name]))
         b.c0 = float(lay["c0"])
         for name in ("td", "tdab", "row", "bimg", "box", "err"):
@@ -367,9 +364,10 @@ class SpectralPlan:
     def evaluate(self, x, y, mode="tf32x3"):
         """y[P, d_out] (FP32) at x[P, d_in] (FP64, contiguous, on the device).
         ``mode="bf16x3"`` runs the tensor-core contraction with split-BF16
-        operands (plans with the tensor-core form only).  One-output plans
-        use the tensor-core blocked evaluator from BLOCKED_TC_MIN_POINTS
-        points on; ``mode="blocked"`` / ``"blocked_tc"`` choose the evaluator."""
+        operands (plans with the tensor-core form only).  ``mode="blocked_tc"``
+        evaluates a one-output plan with the tensor-core blocked evaluator
+        (``csrc/blocked_tc.cu``: ~2.5x smaller error than the blocked
+        evaluator, ~1.6x its time at d_in = 1000)."""
         st = capi.stream_ptr(torch.cuda.current_stream())
         if mode == "bf16x3":
             if self.tc is None:
@@ -381,13 +379,14 @@ class SpectralPlan:
             import ctypes
 
             P = int(x.shape[0])
-            if self.blocked_tc is not None and mode != "blocked" and (mode == "blocked_tc" or P >= BLOCKED_TC_MIN_POINTS):
+            if mode == "blocked_tc":
+                if self.blocked_tc is None:
+                    raise ValueError("the plan is outside the tensor-core blocked evaluator's limits")
                 ref = ctypes.byref(self.blocked_tc)
-                if capi.size("smx_blocked_tc_supported", ref, ptr(x), int(x.shape[1])):
-                    call("smx_blocked_tc_eval", ref, ptr(x), P, int(x.shape[1]), ptr(y), st)
-                    return y
-                if mode == "blocked_tc":
+                if not capi.size("smx_blocked_tc_supported", ref, ptr(x), int(x.shape[1])):
                     raise ValueError("the tensor-core blocked evaluator needs x 16-byte aligned with an even row pitch")
+                call("smx_blocked_tc_eval", ref, ptr(x), P, int(x.shape[1]), ptr(y), st)
+                return y
             nws = capi.size("smx_blocked_eval_workspace", ctypes.byref(self.blocked), P)
             ws = torch.empty(max(nws, 1), dtype=torch.uint8, device=x.device)
             call("smx_blocked_eval", ctypes.byref(self.blocked), ptr(x), P, int(x.shape[1]), ptr(y), ptr(ws), nws, st)

@@ -113,29 +113,32 @@ def test_tables_match_direct_sum(d, t, fam_id):
 
 
 def test_headline_structure():
-    """d = 1000, |Lambda| = 9999: 41 table dimensions (100 slots: two table
-    chunks over every node, 13 K steps), 959 linear ones in 15 chunks of 64
-    whose K steps follow the staircase; A fits tensor memory (<= 16 steps)."""
+    """d = 1000, |Lambda| = 9999: 959 linear dimensions in 15 chunks of 64
+    whose K steps follow the staircase, and 41 table dimensions (100 slots:
+    two table chunks over every node, 13 K steps) placed after the 5th and
+    10th linear chunk; A fits tensor memory with three accumulators."""
     tr, C, maxdeg, fam, fa, fb, lay = _build(1000, 8.22452, 0, seed=0)
     assert int(lay["tc_n_td"]) == 41 and int(lay["tc_n_rows"]) == 208 and int(lay["tc_n_phi"]) == 100
     chunks = lay["tc_chunk"].reshape(-1, 4)
     table = chunks[:, 0] >> 16
-    assert list(table[:2]) == [1, 1] and not table[2:].any()
-    assert list(chunks[:2, 1]) == [13, 13] and list(chunks[:2, 3]) == [0, 64]
-    assert int(lay["tc_n_agen"]) == 13 <= 16
+    assert list(np.nonzero(table)[0]) == [5, 11] and len(chunks) == 17  # after 5 and 10 linear chunks
+    assert list(chunks[table == 1, 1]) == [13, 13] and list(chunks[table == 1, 3]) == [0, 64]
+    assert int(lay["tc_n_agen"]) == 13 and 3 * 64 + 24 * 13 <= 512
     assert int(lay["tc_lin0"]) % 8 == 0 and int(lay["tc_n_boxes"]) * 8 >= 1000 - int(lay["tc_lin0"])
     assert int(lay["tc_smem"]) <= 225 * 1024
     Bt, Bl, stage_ks = decode(lay)
     # staircase: every linear chunk's coefficients lie within its K steps, which shrink along the columns
     nks = []
-    for c, ks in zip(chunks[2:], stage_ks[2:]):
+    for c, ks, t in zip(chunks, stage_ks, table):
+        if t:
+            continue
         col0, N, nk = int(c[3]) * 8, int(c[0]) & 0xFFFF, int(c[1])
         assert not Bl[16 * nk:, col0: col0 + N].any()
         assert ks == list(range(nk - 1, -1, -1))
         nks.append(nk)
     assert nks == sorted(nks, reverse=True) and nks[-1] == 1
     assert int(lay["tc_stages"]) == sum(len(k) for k in stage_ks)
-    assert not lay["tc_box"].any()
+    assert not lay["tc_box"].any()  # 1000 - 40 = 960 linear columns: no unit past d
 
 
 def test_fold_of_the_affine_constant():
@@ -147,14 +150,3 @@ def test_fold_of_the_affine_constant():
     ref = direct(tr, C.astype(np.float64), x, fam, fa, fb)[:, 0]
     assert np.abs(replay(lay, x, fam) - ref).max() <= 1e-6 * max(1.0, np.abs(ref).max())
 
-
-def test_dispatch_threshold_matches_header():
-    """The package and the C FP32 plan switch evaluators at the same point count."""
-    import os
-    import re
-
-    from smolyax_gb300.spectral import BLOCKED_TC_MIN_POINTS
-
-    hdr = open(os.path.join(os.path.dirname(__file__), "..", "include", "smolyax_gb300.h")).read()
-    expr = re.search(r"#define SMX_BLOCKED_TC_MIN_POINTS ([^\n]+)", hdr).group(1)
-    assert eval(expr) == BLOCKED_TC_MIN_POINTS

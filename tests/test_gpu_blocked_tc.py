@@ -7,10 +7,9 @@ evaluators are also compared with each other.  Gauss-Hermite cases are held
 to 1e-6 relative to sum_m |c_m phi_m(x)| (the size of what FP32 sums; the
 element-wise error is printed).  Further cases: a shifted domain (the folded
 constant column), partial and single-point tiles, inactive dimensions
-(masked inside the x boxes: their coordinates never enter, NaN there leaves
-the value unchanged), non-finite active coordinates (NaN rows, the other rows unchanged),
-the dispatch of ip(x) from BLOCKED_TC_MIN_POINTS points on, and the error
-flag staying clear.
+(masked units of 8 columns: their coordinates are never read, NaN there
+leaves the value unchanged), non-finite active coordinates (NaN rows, the
+other rows unchanged), and the error flag staying clear.
 """
 import numpy as np
 import pytest
@@ -156,17 +155,3 @@ def test_inactive_and_nonfinite_coordinates():
     np.testing.assert_array_equal(got[good], clean[good])
     assert _flag(ip) == 0
 
-
-def test_dispatch_by_point_count(cfg2):
-    """ip(x, precision="fp32") uses the tensor-core blocked evaluator from
-    BLOCKED_TC_MIN_POINTS points on, the blocked evaluator below."""
-    from smolyax_gb300.spectral import BLOCKED_TC_MIN_POINTS as N
-
-    if N > 1 << 20:
-        pytest.skip("the tensor-core blocked evaluator is not dispatched by point count")
-    x = np.random.default_rng(9).uniform(-1, 1, (N, 1000))
-    xd = torch.as_tensor(x, device="cuda")
-    big = cfg2(xd, precision="fp32").cpu().numpy()[:, 0].astype(float)
-    np.testing.assert_array_equal(big, _eval(cfg2, x, "blocked_tc"))
-    small = cfg2(xd[: N - 1], precision="fp32").cpu().numpy()[:, 0].astype(float)
-    np.testing.assert_array_equal(small, _eval(cfg2, x[: N - 1], "blocked"))
