@@ -164,6 +164,8 @@ def build_blocked(tr, C, maxdeg, d, fam, fa, fb):
             else:
                 grp[g, 4 + q] = sl[0][0]
                 grp[g, 8 + q] = 0  # unused slot
+        if fast and np.all(grp_ab[g, :4] == np.float32(1.0)) and np.all(grp_ab[g, 4:] == np.float32(0.0)):
+            grp[g, 2] = 2  # unit maps: phi_1 = x
         for k in range(K):
             for q in range(4):
                 W.append(coef_of.get((k, sl[q]), 0.0) if q < len(sl) else 0.0)

@@ -54,7 +54,7 @@ struct BArgs {
   const int4* node;      // [n_nodes][3]: {entry offset, entry count, depth, 0}, path[0..3], path[4..7]
   const int4* vc;        // [k_c][3] same format (path only)
   const int4* hot_ent;   // pairs {smem offset, coefficient bits} x 2
-  const int4* grp;       // [G][3]: {K, W offset, fast, slots}, dims, degrees
+  const int4* grp;       // [G][3]: {K, W offset, fast (2: unit maps), slots}, dims, degrees
   const float4* grp_ab;  // [G][2]: affine maps (a, b) of the 4 slots
   const float4* W;       // staircase coefficients, one float4 per prefix row
   const int32_t* warp_off;
@@ -288,7 +288,13 @@ __device__ __forceinline__ void blocked_tile(const BArgs& a, const double* __res
         {
           const float4 A = tl<TS>(a.grp_ab + 2 * g), B = tl<TS>(a.grp_ab + 2 * g + 1);
           const float Aa[4] = {A.x, A.y, A.z, A.w}, Bb[4] = {B.x, B.y, B.z, B.w};
-          if (gd.z) {
+          if (gd.z == 2) {  // unit maps (phi_1 = x): the converted coordinates themselves
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+#pragma unroll
+              for (int j = 0; j < 4; ++j)
+                ph2[h][j] = make_float2(f64_to_f32(xv[2 * h][j]), f64_to_f32(xv[2 * h + 1][j]));
+          } else if (gd.z) {
 #pragma unroll
             for (int h = 0; h < 2; ++h)
 #pragma unroll

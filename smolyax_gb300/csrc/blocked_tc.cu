@@ -185,11 +185,10 @@ __global__ void __launch_bounds__(kThreads, 1) blocked_tc_kernel(const __grid_co
   const uint32_t tmem = bars->tmem;
 
   if (warp == kWarpProducer) {
-    // ---- producer warp: coefficient stages by 16-byte asynchronous copies
-    // through L1 (all lanes; a stage is handed to the MMA thread once the
-    // kBInflight later ones are issued and its own copies have landed), and L2
-    // prefetches of the x row segments of the table dimensions (one tile
-    // ahead) and of the linear chunks (kPfChunks chunks ahead)
+    // ---- producer warp: coefficient stages by bulk copies (lane 0; the TMA
+    // unit carries nothing else), and L2 prefetches of the x row segments of
+    // the table dimensions (one tile ahead) and of the linear chunks
+    // (kPfChunks chunks ahead) by all lanes, one per 128-byte line
     const int n_lin = g.n_chunks - g.n_tchunks;
     auto prefetch_rows = [&](int64_t tile, int64_t col, int bytes) {  // within each row: [col, ldx)
       const int64_t room = (g.ldx - col) * 8;
@@ -218,47 +217,41 @@ __global__ void __launch_bounds__(kThreads, 1) blocked_tc_kernel(const __grid_co
     int64_t pf = 0;
     if (nt > 0 && g.td_bytes > 0) prefetch_rows(blockIdx.x, g.td_col, g.td_bytes);
     for (; n_lin > 0 && pf < kPfChunks; ++pf) prefetch_lin(pf);
-    uint64_t ib = 0, handed = 0;
+    uint64_t ib = 0;
     bool ok = true;
-    auto hand_over = [&](uint64_t upto) {  // stages [handed, upto) have landed: fence, signal
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncwarp();
-      if (lane == 0)
-        for (; handed < upto; ++handed) mbar_arrive(&bars->b_full[handed % kBStages]);
-      handed = upto;
-    };
     for (int i = 0; i < nt && ok; ++i) {
       if (i + 1 < nt && g.td_bytes > 0) prefetch_rows(blockIdx.x + int64_t(i + 1) * G, g.td_col, g.td_bytes);
       for (int c = 0; c < g.n_chunks && ok; ++c) {
         const int4 ch = g.chunk[c];
         if (ch.x >> 16 == 0 && n_lin > 0) prefetch_lin(pf++);
-        const int bytes = (ch.x & 0xFFFF) * (kSplits * 32);
+        const uint32_t bytes = uint32_t(ch.x & 0xFFFF) * (kSplits * 32);
         for (int jb = 0; jb < ch.y; ++jb, ++ib) {
           const int s = int(ib % kBStages);
           bool got = true;
-          if (lane == 0 && ib >= kBStages)
-            got = mbar_wait(&bars->b_empty[s], uint32_t((ib / kBStages) & 1) ^ 1u, abort_flag, g.wait_ns);
-          if (!__shfl_sync(0xffffffffu, got ? 1 : 0, 0)) {
-            if (lane == 0) {
+          if (lane == 0) {
+            if (ib >= kBStages)
+              got = mbar_wait(&bars->b_empty[s], uint32_t((ib / kBStages) & 1) ^ 1u, abort_flag, g.wait_ns);
+            if (got) {
+              mbar_expect_tx(&bars->b_full[s], bytes);
+              bulk_load(bst + s * kBStageMax, g.bimg + int64_t(ch.z) * 16 + int64_t(jb) * bytes, bytes,
+                        &bars->b_full[s]);
+            } else {
               atomicExch(g.err, 1);
               *abort_flag = 1;
             }
+          }
+          if (!__shfl_sync(0xffffffffu, got ? 1 : 0, 0)) {
             ok = false;
             break;
           }
-          const uint8_t* src = g.bimg + int64_t(ch.z) * 16 + int64_t(jb) * bytes;
-          const uint32_t dst = smem_u32(bst + s * kBStageMax);
-          for (int q = lane; q < bytes / 16; q += 32)
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16 * q), "l"(src + 16 * q)
-                         : "memory");
-          asm volatile("cp.async.commit_group;" ::: "memory");
-          asm volatile("cp.async.wait_group %0;" ::"n"(kBInflight) : "memory");
-          if (ib + 1 > uint64_t(kBInflight)) hand_over(ib + 1 - kBInflight);
         }
       }
     }
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
-    if (ok) hand_over(ib);
+    if (!ok && lane == 0) {
+      // wait (bounded) until the copies already issued have landed
+      for (uint64_t u = ib > kBStages ? ib - kBStages : 0; u < ib; ++u)
+        mbar_wait(&bars->b_full[u % kBStages], uint32_t((u / kBStages) & 1), nullptr, g.wait_ns);
+    }
     __syncwarp();
   } else if (warp == kWarpMMA) {
     if (lane == 0) {

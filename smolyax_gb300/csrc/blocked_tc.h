@@ -26,7 +26,6 @@ constexpr int kSplits = 3;        // bf16 hi / mid / lo
 constexpr int kMaxSteps = (512 - 2 * kMaxN) / (kSplits * 8);  // 16 K steps = 256 rows
 SMX_BTC_HD inline int acc_buffers(int n_agen) { return 3 * kMaxN + kSplits * 8 * n_agen <= 512 ? 3 : 2; }
 constexpr int kBStages = 12;      // coefficient stages in shared memory
-constexpr int kBInflight = 4;     // stages copied ahead of the one the producer hands over
 constexpr int kBStageMax = kSplits * kMaxN * 32;  // one coefficient stage at N = 64: 6 KB
 constexpr int kComputeWarps = 16;
 constexpr int kThreads = 32 * (kComputeWarps + 2);  // + producer warp + MMA warp

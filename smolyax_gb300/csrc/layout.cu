@@ -261,6 +261,11 @@ bool build_blocked(const Tree& tr, const float* C, const int64_t* maxdeg, int d,
         gr[8 + q] = 0;
       }
     }
+    if (groups[g].fast) {
+      bool unit = true;
+      for (int q = 0; q < 4; ++q) unit = unit && grp_ab[g * 8 + q] == 1.0f && grp_ab[g * 8 + 4 + q] == 0.0f;
+      if (unit) gr[2] = 2;  // unit maps: phi_1 = x
+    }
     for (int64_t k = 0; k < K; ++k)
       for (int q = 0; q < 4; ++q) {
         float c = 0.f;

@@ -1,12 +1,14 @@
 """The FP32 form and its VJP through the C ABI alone: ``smx_fp32_plan_create``
 on an FP64 plan and its index-set tree, ``smx_eval(plan, 32, ...)``,
 ``smx_fp32_eval`` and ``smx_vjp``, for each of the three FP32 evaluators.
-The library builds the same FP64 coefficients (the scatter into the index
-set sums each entry's rows in row order: the same on every call) and the same
-tables as the Python package, so the coefficients and the values must equal
-the package's bit for bit, dL/dx its backward bit for bit, and dL/d(rows of
-F64) its coefficient adjoint to rounding; the values are also within the
-1e-6 bound of the FP64 path (element-wise: Leja cases)."""
+The library builds the same FP64 coefficients as the Python package (the
+scatter into the index set sums each entry's rows in row order: the same on
+every call), checked bit for bit, and the same tables; its launch choices
+(segments of the per-point and panel kernels, split-K slices) follow its own
+rules, so the values, dL/dx and dL/d(rows of F64) are compared with the
+package's at FP32 rounding (2^-20 of their scale), the two C entry points
+with each other bit for bit, and the values with the FP64 path at the 1e-6
+bound (element-wise: Leja cases)."""
 import ctypes
 
 import numpy as np
@@ -84,7 +86,9 @@ def test_fp32_form_and_vjp_through_the_c_abi(kind, d, t, d_out, evaluator):
         ref = ip(x, precision="fp32")
         y64 = ip(x, precision="fp64")
         torch.cuda.synchronize()
-        assert torch.equal(y1, ref) and torch.equal(y2, ref)
+        assert torch.equal(y1, y2)
+        dy = float((y1 - ref).abs().max())
+        assert dy <= 2.0**-20 * float(ref.abs().max()), dy
         if kind == "leja":
             assert float(((y1.double() - y64).abs() / y64.abs()).max()) < 1e-6
         # without the FP32 form, precision 32 is refused
@@ -102,8 +106,9 @@ def test_fp32_form_and_vjp_through_the_c_abi(kind, d, t, d_out, evaluator):
         dx_ref, dC_ref = sp.vjp(x, g)
         dF_ref = sp.coefficient_adjoint(dC_ref)
         torch.cuda.synchronize()
-        assert torch.equal(dx, dx_ref)
-        np.testing.assert_allclose(dF.cpu().numpy(), dF_ref.cpu().numpy(), rtol=1e-12,
-                                   atol=1e-12 * float(dF_ref.abs().max()))
+        ddx = float((dx - dx_ref).abs().max())
+        assert ddx <= 2.0**-20 * float(dx_ref.abs().max()), ddx
+        ddF = float((dF - dF_ref).abs().max())
+        assert ddF <= 2.0**-20 * float(dF_ref.abs().max()), ddF
     finally:
         lib.smx_fp32_plan_destroy(h)
