@@ -582,6 +582,8 @@ def serving_workload(n_req, rate):
     evals = sum(r.points * ips[r.name].d_out for r in ev)
     lat_e = np.array([r.latency for r in ev]) * 1e3
     lat_g = np.array([r.latency for r in reqs if r.op == "grad" and r.error is None]) * 1e3
+    lat_s = np.array([r.latency for r in ev if r.points <= 4096]) * 1e3
+    wait = np.array([r.t_admit - r.t_submit for r in reqs if r.error is None and r.t_admit is not None]) * 1e3
     line = {
         "metric": METRIC, "workload": "serving", "value": evals / wall, "unit": "evals/s", "n_gpus": 1,
         "higher_is_better": True, "dtype": "fp32", "data": "synthetic",
@@ -590,8 +592,15 @@ def serving_workload(n_req, rate):
                    "requests": n_req, "rate_per_s": rate},
         "latency_ms": {"p50": float(np.percentile(lat_e, 50)), "p99": float(np.percentile(lat_e, 99)),
                        "grad_p50": float(np.percentile(lat_g, 50)) if lat_g.size else None,
-                       "grad_p99": float(np.percentile(lat_g, 99)) if lat_g.size else None},
+                       "grad_p99": float(np.percentile(lat_g, 99)) if lat_g.size else None,
+                       # requests of at most 4096 points, and the wait from arrival to admission
+                       # (the scheduler's share of a latency; the rest is the request's own work)
+                       "small_p50": float(np.percentile(lat_s, 50)) if lat_s.size else None,
+                       "small_p99": float(np.percentile(lat_s, 99)) if lat_s.size else None,
+                       "admit_wait_p50": float(np.percentile(wait, 50)),
+                       "admit_wait_p99": float(np.percentile(wait, 99))},
         "wall_s": wall, "setup_s": setup_s, "launches": st["launches"], "merged_launches": st["batch_launches"],
+        "high_priority_launches": st["fast_launches"],
         "completed": st["completed"], "rejected": st["rejected"], "clocks": clk.summary(),
         "fleet": [dict(d_in=d, d_out=o, lam=l, kind=kd, K=int(ips["ip%02d" % i]._tree.size),
                        tensor=ips["ip%02d" % i].spectral_plan().tc is not None) for i, d, o, l, kd in fleet],
@@ -639,10 +648,15 @@ def run_ours(args):
         per = [a.elapsed_time(b) for a, b in ev]
         return per, wall
 
-    # FP64 path (the reference's combination sum)
+    # FP64 paths: the default (orthogonal form in FP64) and the reference's
+    # combination sum (barycentric)
     fp64_steps = max(3, min(args.steps, 5))
     per64, _ = timed(lambda: ip(x, precision="fp64"), fp64_steps, 1)
     y64 = ip(x, precision="fp64")
+    per64b, _ = timed(lambda: ip(x, precision="fp64_barycentric"), 3, 1)
+    y64b = ip(x, precision="fp64_barycentric")
+    err64 = ((y64 - y64b).abs() / y64b.abs()).max().item()
+    del y64b
 
     # FP32 path: one kernel per step (the timed region)
     with ClockSampler(local) as clk:
@@ -662,8 +676,9 @@ def run_ours(args):
             e2e_per.append((t1 - t0) * 1e3)
     ms32 = statistics.mean(per32)
     ms64 = statistics.mean(per64)
+    ms64b = statistics.mean(per64b)
     ms_e2e = statistics.mean(e2e_per)
-    ms32, ms_e2e, ms64 = replicas.max_over_ranks([ms32, ms_e2e, ms64], device=dev)
+    ms32, ms_e2e, ms64, ms64b = replicas.max_over_ranks([ms32, ms_e2e, ms64, ms64b], device=dev)
     if rank != 0:
         dist.destroy_process_group() if world > 1 else None
         return 0
@@ -693,7 +708,10 @@ def run_ours(args):
         "data": "synthetic",
         "config": headline_config(world, P),
         "latency_ms": {"p50": statistics.median(per32), "p99": p99, "max": max(per32)},
-        "fp64": {"value": world * P * D_OUT / (ms64 * 1e-3), "ms_per_step": ms64, "steps": fp64_steps},
+        "fp64": {"value": world * P * D_OUT / (ms64 * 1e-3), "ms_per_step": ms64, "steps": fp64_steps,
+                 "form": "orthogonal polynomials, FP64 (csrc/spectral64.cu)"},
+        "fp64_barycentric": {"value": world * P * D_OUT / (ms64b * 1e-3), "ms_per_step": ms64b, "steps": 3,
+                             "max_rel_diff_vs_fp64": err64},
         "speedup_vs_fp64": ms64 / ms32,
         "error": {"fp32_max_rel_vs_fp64": err, "bound": 1e-6},
         "e2e": {"value": world * P * D_OUT / (ms_e2e * 1e-3), "unit": "evals/s", "ms_per_step": ms_e2e,

@@ -123,8 +123,10 @@ typedef struct smx_plan {
   const double* F64;           /* [n_entries * d_out] zeta * f(node)               */
   const float* F32;            /* [n_entries * d_out] FP32 rounding of F64 (or NULL)*/
   const double* offset;        /* [d_out] zeta_0 * f(zero point)                   */
-  const struct smx_fp32_plan* fp32; /* FP32 form (smx_fp32_plan_create), or NULL:
-                                       smx_eval(plan, 32, ...) evaluates through it */
+  const struct smx_fp32_plan* fp32; /* orthogonal form (smx_fp32_plan_create), or NULL:
+                                       smx_eval(plan, 32, ...) evaluates through it,
+                                       smx_eval(plan, 64, ...) too when it has FP64
+                                       tables (one output) */
 } smx_plan;
 
 /* Barycentric weights of every pair: w_b = prod_a 1/(xi_a - xi_b) with zero
@@ -169,7 +171,9 @@ int smx_basis_f64(const smx_plan* plan_host, const double* x, int64_t P, int64_t
 int smx_contract_f64(const smx_plan* plan_host, const double* Lt, int64_t P, double* y, void* stream);
 
 /* One evaluation call (interpolation.py:264-304).  precision 64: the FP64
- * path (basis table into `ws`, then the contraction; y is FP64 [P, d_out]).
+ * path -- the orthogonal form in FP64 when plan->fp32 is set and has FP64
+ * tables (smx_fp32_plan_has_fp64: one output), else the combination sum
+ * (basis table into `ws`, then the contraction); y is FP64 [P, d_out].
  * precision 32: the FP32 form plan->fp32 (SMX_ERR_UNSUPPORTED if NULL; y is
  * FP32 [P, d_out]), as smx_fp32_eval.  ws_bytes >= smx_eval_workspace(plan,
  * P, precision). */
@@ -263,6 +267,43 @@ typedef struct smx_spectral {
 /* FP32 evaluation y[P, d_out] (x FP64 row-major, leading dimension ldx). */
 int smx_spectral_eval(const smx_spectral* plan_host, const double* x, int64_t P, int64_t ldx, float* y,
                       void* stream);
+
+/* FP64 evaluation of the orthogonal form, one output (the FP64 counterpart of
+ * interpolation.py:264-304 for d_out = 1).  The same layout as smx_spectral
+ * (built from the same index-set tree) with FP64 coefficients and affine maps;
+ * `row` is the per-point row in doubles (even, >= n_hb + n_vp rounded up to
+ * 4; 2 mod 4 keeps the 16-byte row reads free of bank conflicts), and the
+ * block needs (row + 4) * 128 * 8 bytes of shared memory (<= 227 KB).  With
+ * coefficients from smx_spectral_coefficients (compensated sums) the result is
+ * within ~1e-14 relative of the exact value of the interpolant, where the
+ * barycentric combination sum in FP64 cancels to 1e-13 .. 1e-10.  Non-finite
+ * coordinates of active dimensions give NaN. */
+typedef struct smx_spectral64 {
+  int32_t d_in;
+  int32_t row;           /* doubles per point row                                  */
+  int32_t n_hb, n_vp, n_hot_dims, n_nodes, n_cold_groups, max_depth, n_cold_blocks;
+  int32_t node_seg[5], cold_seg[5], block_seg[5];
+  const int32_t* hot_dim;
+  const int32_t* hot_deg;
+  const int32_t* hot_soff;
+  const int32_t* node;      /* as smx_spectral                                       */
+  const double* node_c;     /* [n_nodes]                                             */
+  const int32_t* cold;
+  const double* cold_ab;    /* [n_cold_groups][2]                                    */
+  const int32_t* blk_dims;
+  const int32_t* blk_run;
+  const double* blk_ab;     /* [n_cold_blocks][2][4]                                 */
+  const int32_t* run;
+  const double* coef;       /* run coefficients (offsets multiples of 4)             */
+  const double* fam_a;      /* [d_in]                                                */
+  const double* fam_b;      /* [d_in]                                                */
+  const int32_t* fam;       /* [d_in]                                                */
+  double c0;                /* coefficient of the constant                           */
+} smx_spectral64;
+
+/* y[P] (FP64) = the interpolant at the P rows of x (FP64, leading dimension ldx). */
+int smx_spectral_eval64(const smx_spectral64* plan_host, const double* x, int64_t P, int64_t ldx, double* y,
+                        void* stream);
 
 /* Blocked FP32 evaluator of the orthogonal form for one output (d_out = 1):
  * the same polynomial as smx_spectral_eval, summed as
@@ -513,8 +554,18 @@ int smx_layout_build(int kind, int64_t n, const int32_t* parent_host, const int3
                      const double* rem_host, const float* C_host, int d_out, const int64_t* maxdeg_host, int d,
                      const int32_t* fam_host, const double* fam_a_host, const double* fam_b_host,
                      smx_host_tables** out);
+/* The per-point layout with FP64 coefficients C[n][d_out] for the FP64
+ * evaluator (smx_spectral64): kind SMX_LAYOUT_PERPOINT only; the coefficient
+ * and map tables ("node_c", "coef", "cold_ab", "blk_ab") are read with
+ * smx_layout_f64, "row" is the FP64 row. */
+int smx_layout_build_f64(int kind, int64_t n, const int32_t* parent_host, const int32_t* dim_host,
+                         const int32_t* deg_host, const int32_t* level_host, const int64_t* rank_host,
+                         const double* rem_host, const double* C_host, int d_out, const int64_t* maxdeg_host, int d,
+                         const int32_t* fam_host, const double* fam_a_host, const double* fam_b_host,
+                         smx_host_tables** out);
 int smx_layout_i32(const smx_host_tables* tables, const char* name, const int32_t** data_host, int64_t* count);
 int smx_layout_f32(const smx_host_tables* tables, const char* name, const float** data_host, int64_t* count);
+int smx_layout_f64(const smx_host_tables* tables, const char* name, const double** data_host, int64_t* count);
 int smx_layout_scalar(const smx_host_tables* tables, const char* name, double* value);
 void smx_layout_free(smx_host_tables* tables);
 
@@ -560,6 +611,13 @@ int smx_fp32_eval(const smx_fp32_plan* fp32, const double* x, int64_t P, int64_t
 /* SMX_OK, or SMX_ERR_CUDA if a tensor-core pipeline wait of an earlier call
  * timed out (those results are invalid); resets the flag; synchronises. */
 int smx_fp32_plan_check(const smx_fp32_plan* fp32, void* stream);
+/* FP64 evaluation of the orthogonal form, y[P] (FP64), for one-output plans
+ * whose per-point row fits the FP64 evaluator (smx_spectral64; the handle
+ * builds those tables when it can): SMX_ERR_UNSUPPORTED otherwise.
+ * smx_eval(plan, 64, ...) evaluates through it when plan->fp32 is set and has
+ * them, as the Python package does for precision "fp64". */
+int smx_fp32_plan_has_fp64(const smx_fp32_plan* fp32);
+int smx_fp32_eval64(const smx_fp32_plan* fp32, const double* x, int64_t P, int64_t ldx, double* y, void* stream);
 /* Vector-Jacobian products of y = I(x) (the FP32 form) at the cotangent
  * g[P, ldg] (FP32): dx[P, lddx] = dL/dx (FP64; NULL to skip) and
  * dF[n_entries, d_out] = dL/d(plan rows F64) (FP64; NULL to skip).  The

@@ -104,6 +104,41 @@ class SmxSpectral(C.Structure):
     ]
 
 
+class SmxSpectral64(C.Structure):
+    """Mirror of ``struct smx_spectral64``."""
+
+    _fields_ = [
+        ("d_in", _i32),
+        ("row", _i32),
+        ("n_hb", _i32),
+        ("n_vp", _i32),
+        ("n_hot_dims", _i32),
+        ("n_nodes", _i32),
+        ("n_cold_groups", _i32),
+        ("max_depth", _i32),
+        ("n_cold_blocks", _i32),
+        ("node_seg", _i32 * 5),
+        ("cold_seg", _i32 * 5),
+        ("block_seg", _i32 * 5),
+        ("hot_dim", _p),
+        ("hot_deg", _p),
+        ("hot_soff", _p),
+        ("node", _p),
+        ("node_c", _p),
+        ("cold", _p),
+        ("cold_ab", _p),
+        ("blk_dims", _p),
+        ("blk_run", _p),
+        ("blk_ab", _p),
+        ("run", _p),
+        ("coef", _p),
+        ("fam_a", _p),
+        ("fam_b", _p),
+        ("fam", _p),
+        ("c0", C.c_double),
+    ]
+
+
 class SmxBlocked(C.Structure):
     """Mirror of ``struct smx_blocked``."""
 
@@ -194,6 +229,7 @@ SIGNATURES = {
     "smx_spectral_coefficients": (_int, [_p, _p, _p, _p, _p, _p, _p, _i64, _p, _p, _p, _p, _p, _sz, _p]),
     "smx_spectral_coefficients_workspace": (_sz, [_p]),
     "smx_spectral_eval": (_int, [_p, _p, _i64, _i64, _p, _p]),
+    "smx_spectral_eval64": (_int, [_p, _p, _i64, _i64, _p, _p]),
     "smx_blocked_smem": (_sz, [_p]),
     "smx_gemm_bf16x3": (_int, [_p, _p, _i64, _p, _p, _i64, _int, _int, _int, _p, _i64, _p, _int, _p, _p]),
     "smx_split_bf16": (_int, [_p, _i64, _i64, _i64, _p, _p, _i64, _p]),
@@ -228,8 +264,13 @@ SIGNATURES = {
     "smx_split_tf32": (_int, [_p, _i64, _i64, _i64, _p, _p, _i64, _p]),
     "smx_layout_build": (_int, [_int, _i64, _p, _p, _p, _p, _p, _p, _p, _int, _p, _int, _p, _p, _p,
                                  C.POINTER(_p)]),
+    "smx_layout_build_f64": (_int, [_int, _i64, _p, _p, _p, _p, _p, _p, _p, _int, _p, _int, _p, _p, _p,
+                                     C.POINTER(_p)]),
+    "smx_fp32_plan_has_fp64": (_int, [_p]),
+    "smx_fp32_eval64": (_int, [_p, _p, _i64, _i64, _p, _p]),
     "smx_layout_i32": (_int, [_p, C.c_char_p, C.POINTER(_p), C.POINTER(_i64)]),
     "smx_layout_f32": (_int, [_p, C.c_char_p, C.POINTER(_p), C.POINTER(_i64)]),
+    "smx_layout_f64": (_int, [_p, C.c_char_p, C.POINTER(_p), C.POINTER(_i64)]),
     "smx_layout_scalar": (_int, [_p, C.c_char_p, C.POINTER(_dbl)]),
     "smx_layout_free": (None, [_p]),
     "smx_fp32_plan_create": (_int, [_p, _p, _p, _p, _p, _dbl, C.POINTER(_p), _p]),
@@ -295,11 +336,13 @@ def stream_ptr(stream):
 LAYOUT_KINDS = {"blocked": 0, "perpoint": 1, "tape": 2, "blocked_tc": 3}
 
 
-def host_layout(kind, tree, coef, d_out, maxdeg, fam, fa, fb, i32=(), f32=(), scalars=()):
+def host_layout(kind, tree, coef, d_out, maxdeg, fam, fa, fb, i32=(), f32=(), scalars=(), fp64=False):
     """Tables of the library's host-side layout builder (``smx_layout_build``)
     as numpy copies: {name: array or float}.  ``tree`` holds host arrays
     parent, dim, deg, level, rank, rem; coef is FP32 [n, d_out] (unused for
-    the tape).  Returns None if the plan is outside the evaluator's limits."""
+    the tape).  With ``fp64`` the per-point layout is built with FP64
+    coefficients (``smx_layout_build_f64``) and the ``f32`` names are read as
+    FP64 tables.  Returns None if the plan is outside the evaluator's limits."""
     import numpy as np
 
     lib = load()
@@ -308,11 +351,13 @@ def host_layout(kind, tree, coef, d_out, maxdeg, fam, fa, fb, i32=(), f32=(), sc
     arr = lambda a, dt: np.ascontiguousarray(np.asarray(a), dtype=dt)
     keep = [arr(tree["parent"], np.int32), arr(tree["dim"], np.int32), arr(tree["deg"], np.int32),
             arr(tree["level"], np.int32), arr(tree["rank"], np.int64), arr(tree["rem"], np.float64),
-            arr(coef if coef is not None else np.zeros((n, d_out)), np.float32), arr(maxdeg, np.int64),
+            arr(coef if coef is not None else np.zeros((n, d_out)), np.float64 if fp64 else np.float32),
+            arr(maxdeg, np.int64),
             arr(fam, np.int32), arr(fa, np.float64), arr(fb, np.float64)]
     ptrs = [k.ctypes.data_as(C.c_void_p) for k in keep]
     h = C.c_void_p()
-    rc = lib.smx_layout_build(LAYOUT_KINDS[kind], n, *ptrs[:7], int(d_out), ptrs[7], d, *ptrs[8:], C.byref(h))
+    build = lib.smx_layout_build_f64 if fp64 else lib.smx_layout_build
+    rc = build(LAYOUT_KINDS[kind], n, *ptrs[:7], int(d_out), ptrs[7], d, *ptrs[8:], C.byref(h))
     if rc == -5:
         return None
     if rc != SMX_OK:
@@ -320,6 +365,7 @@ def host_layout(kind, tree, coef, d_out, maxdeg, fam, fa, fb, i32=(), f32=(), sc
     out = {}
     try:
         for names, fn, ct, dt in ((i32, lib.smx_layout_i32, C.c_int32, np.int32),
+                                  (f32, lib.smx_layout_f64, C.c_double, np.float64) if fp64 else
                                   (f32, lib.smx_layout_f32, C.c_float, np.float32)):
             for name in names:
                 p, cnt = C.c_void_p(), _i64()

@@ -127,20 +127,48 @@ __device__ inline void clevel(const double* __restrict__ Lt, const double* __res
                               double (&acc)[OC]) {
   const int g = deg[L];
   const double* lt = (dslot == L ? dLt : Lt) + int64_t(voff[L]) * P + p;
-  for (int j = 0; j <= g; ++j) {
-    const double l = lt[int64_t(j) * P];
-    double sub[OC];
-    if constexpr (L == N - 1) {
-      const double* fr = Fs + (row * (g + 1) + j) * dout + o0;
+  if constexpr (L == N - 1 && OC == 1) {
+    // innermost level of one output: a dot product with the rows of F, as two
+    // interleaved chains (even and odd nodes) so that the FP64 FMA latency overlaps
+    const double* fr = Fs + row * (g + 1) * dout + o0;
+    double a0[OC], a1[OC];
 #pragma unroll
-      for (int q = 0; q < OC; ++q) sub[q] = q < nout ? fr[q] : 0.0;
-    } else {
+    for (int q = 0; q < OC; ++q) a0[q] = a1[q] = 0.0;
+    int j = 0;
+    for (; j < g; j += 2) {
+      const double l0 = lt[int64_t(j) * P], l1 = lt[int64_t(j + 1) * P];
 #pragma unroll
-      for (int q = 0; q < OC; ++q) sub[q] = 0.0;
-      clevel<OC, L + 1, N>(Lt, dLt, dslot, P, p, voff, deg, Fs, dout, o0, nout, row * (g + 1) + j, sub);
+      for (int q = 0; q < OC; ++q) {
+        if (q < nout) {
+          a0[q] = fma(l0, fr[j * dout + q], a0[q]);
+          a1[q] = fma(l1, fr[(j + 1) * dout + q], a1[q]);
+        }
+      }
+    }
+    if (j == g) {
+      const double l0 = lt[int64_t(j) * P];
+#pragma unroll
+      for (int q = 0; q < OC; ++q)
+        if (q < nout) a0[q] = fma(l0, fr[j * dout + q], a0[q]);
     }
 #pragma unroll
-    for (int q = 0; q < OC; ++q) acc[q] = fma(l, sub[q], acc[q]);
+    for (int q = 0; q < OC; ++q) acc[q] += a0[q] + a1[q];
+  } else {
+    for (int j = 0; j <= g; ++j) {
+      const double l = lt[int64_t(j) * P];
+      double sub[OC];
+      if constexpr (L == N - 1) {
+        const double* fr = Fs + (row * (g + 1) + j) * dout + o0;
+#pragma unroll
+        for (int q = 0; q < OC; ++q) sub[q] = q < nout ? fr[q] : 0.0;
+      } else {
+#pragma unroll
+        for (int q = 0; q < OC; ++q) sub[q] = 0.0;
+        clevel<OC, L + 1, N>(Lt, dLt, dslot, P, p, voff, deg, Fs, dout, o0, nout, row * (g + 1) + j, sub);
+      }
+#pragma unroll
+      for (int q = 0; q < OC; ++q) acc[q] = fma(l, sub[q], acc[q]);
+    }
   }
 }
 
@@ -208,8 +236,9 @@ struct PlanArgs {
 
 // Grid: points along x, chunks of OC outputs along y (from output o_base).
 template <int OC>
-__global__ void contract64_kernel(PlanArgs a, const double* __restrict__ Lt, int64_t P, double* __restrict__ y,
-                                  int o_base) {
+__global__ void __launch_bounds__(128, OC == 1 ? 8 : 5) contract64_kernel(PlanArgs a, const double* __restrict__ Lt,
+                                                                          int64_t P, double* __restrict__ y,
+                                                                          int o_base) {
   const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   const int o0 = o_base + int(blockIdx.y) * OC;
   if (p >= P || o0 >= a.dout) return;
@@ -424,6 +453,8 @@ extern "C" int smx_eval(const smx_plan* pl, int precision, const double* x, int6
                                                  "built by smx_fp32_plan_create)");
     return smx_fp32_eval(pl->fp32, x, P, ldx, static_cast<float*>(y), ws, ws_bytes, stream);
   }
+  if (pl->fp32 && smx_fp32_plan_has_fp64(pl->fp32))
+    return smx_fp32_eval64(pl->fp32, x, P, ldx, static_cast<double*>(y), stream);
   SMX_REQUIRE(ws_bytes >= smx_eval_workspace(pl, P, precision), "smx_eval: workspace too small");
   double* Lt = static_cast<double*>(ws);
   rc = smx_basis_f64(pl, x, P, ldx, Lt, nullptr, stream);

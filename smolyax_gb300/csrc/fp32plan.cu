@@ -129,6 +129,11 @@ struct smx_fp32_plan {
   DevBuf<float> Bh, Bl, bias, Rh, Rl;
   std::vector<int32_t> lvl1;
   std::vector<int> seg_off, seg_n;  // per wanted segment count: offset into segs, number of segments
+  // FP64 per-point tables of the orthogonal form (one output), when they fit
+  bool have64 = false;
+  DevBuf<int32_t> ti64;
+  DevBuf<double> tf64, fa64, fb64;
+  smx_spectral64 spectral64{};
 };
 
 namespace {
@@ -159,6 +164,25 @@ struct Blobs {
   const float* fp(const smx_fp32_plan* h, const char* name) const {
     for (const auto& kv : fo)
       if (kv.first == name) return h->tf.p + kv.second;
+    return nullptr;
+  }
+};
+
+// Named tables of one type packed into one blob, each 4-element aligned.
+template <typename T>
+struct Pack {
+  std::vector<T> v;
+  std::vector<std::pair<std::string, size_t>> off;
+  void add(const char* name, const std::vector<T>& src) {
+    off.push_back({name, v.size()});
+    v.insert(v.end(), src.begin(), src.end());
+    v.resize(size_t(round4(int64_t(v.size()))), T(0));
+  }
+  // device address of a table in the uploaded blob, NULL for an empty table
+  const T* at(const T* base, const char* name, const std::vector<T>& src) const {
+    if (src.empty()) return nullptr;
+    for (const auto& kv : off)
+      if (kv.first == name) return base + kv.second;
     return nullptr;
   }
 };
@@ -224,15 +248,27 @@ extern "C" int smx_fp32_plan_create(const smx_plan* pl, const smx_tree* tree, co
   if (cudaStreamSynchronize(st) != cudaSuccess) return smx::set_error(SMX_ERR_CUDA, "smx_fp32_plan_create: sync failed");
   std::vector<int32_t> level(n, 0);
   for (int64_t e = 1; e < n; ++e) level[e] = level[parent[e]] + 1;
+  // pre-order ranks as smx_lambda_ranks writes them in SMX_MODE_PREORDER (the
+  // order the package builds its tables in): an entry before its children,
+  // the children by dimension ascending and, within a dimension, by degree
+  // descending (children are stored dimension- then degree-ascending)
   std::vector<int64_t> rank(n, 0);
   {
-    std::vector<int64_t> stack{0};
+    std::vector<int64_t> stack{0}, visit;
     int64_t r = 0;
     while (!stack.empty()) {
       const int64_t e = stack.back();
       stack.pop_back();
       rank[e] = r++;
-      for (int64_t c = n_child[e] - 1; c >= 0; --c) stack.push_back(first_child[e] + c);
+      visit.clear();
+      const int64_t c0 = first_child[e], nc = n_child[e];
+      for (int64_t c = 0; c < nc;) {
+        int64_t c1 = c;
+        while (c1 < nc && tdim[c0 + c1] == tdim[c0 + c]) ++c1;
+        for (int64_t q = c1 - 1; q >= c; --q) visit.push_back(c0 + q);
+        c = c1;
+      }
+      for (auto it = visit.rbegin(); it != visit.rend(); ++it) stack.push_back(*it);
     }
   }
   std::vector<int64_t> maxdeg(d, 0);
@@ -352,6 +388,60 @@ extern "C" int smx_fp32_plan_create(const smx_plan* pl, const smx_tree* tree, co
     if (cudaStreamSynchronize(st) != cudaSuccess)  // the staging buffers go out of scope
       return smx::set_error(SMX_ERR_CUDA, "smx_fp32_plan_create: sync failed");
   }
+  // FP64 per-point tables (one output): the FP64 evaluator of the orthogonal form
+  if (dout == 1) {
+    smx::layout::Tables p64;
+    if (smx::layout::build_perpoint(tr, C64_h.data(), 1, maxdeg.data(), d, fam_v.data(), fa_v.data(), fb_v.data(),
+                                    p64) &&
+        (int64_t(p64.scalar["row"]) + 4) * 128 * 8 <= 227 * 1024 && p64.scalar["max_depth"] <= 8) {
+      Pack<int32_t> pi;
+      Pack<double> pf;
+      const char* names_i[] = {"hot_dim", "hot_deg", "hot_soff", "node", "cold", "run", "blk_dims", "blk_run"};
+      const char* names_f[] = {"node_c", "coef", "cold_ab", "blk_ab"};
+      for (const char* nm : names_i) pi.add(nm, p64.i32[nm]);
+      for (const char* nm : names_f) pf.add(nm, p64.f64[nm]);
+      if ((rc = h->ti64.upload(pi.v, st)) || (rc = h->tf64.upload(pf.v, st)) || (rc = h->fa64.upload(fa_v, st)) ||
+          (rc = h->fb64.upload(fb_v, st)))
+        return rc;
+      smx_spectral64& s = h->spectral64;
+      s.d_in = d;
+      s.row = int(p64.scalar["row"]);
+      s.n_hb = int(p64.scalar["n_hb"]);
+      s.n_vp = int(p64.scalar["n_vp"]);
+      s.n_hot_dims = int(p64.scalar["n_hot_dims"]);
+      s.n_nodes = int(p64.scalar["n_nodes"]);
+      s.n_cold_groups = int(p64.scalar["n_cold_groups"]);
+      s.max_depth = int(p64.scalar["max_depth"]);
+      s.n_cold_blocks = int(p64.scalar["n_cold_blocks"]);
+      for (int i = 0; i < 5; ++i) {
+        s.node_seg[i] = p64.i32["node_seg"][i];
+        s.cold_seg[i] = p64.i32["cold_seg"][i];
+        s.block_seg[i] = p64.i32["block_seg"][i];
+      }
+      auto ia = [&](const char* nm) { return pi.at(h->ti64.p, nm, p64.i32[nm]); };
+      auto fa = [&](const char* nm) { return pf.at(h->tf64.p, nm, p64.f64[nm]); };
+      s.hot_dim = ia("hot_dim");
+      s.hot_deg = ia("hot_deg");
+      s.hot_soff = ia("hot_soff");
+      s.node = ia("node");
+      s.cold = ia("cold");
+      s.run = ia("run");
+      s.blk_dims = ia("blk_dims");
+      s.blk_run = ia("blk_run");
+      s.node_c = fa("node_c");
+      s.coef = fa("coef");
+      s.cold_ab = fa("cold_ab");
+      s.blk_ab = fa("blk_ab");
+      s.fam_a = h->fa64.p;
+      s.fam_b = h->fb64.p;
+      s.fam = h->fam.p;
+      s.c0 = C64_h[0];
+      h->have64 = true;
+      if (cudaStreamSynchronize(st) != cudaSuccess)  // the host blobs go out of scope
+        return smx::set_error(SMX_ERR_CUDA, "smx_fp32_plan_create: sync failed");
+    }
+  }
+
   if (use_tc) {
     h->evaluator = SMX_FP32_TENSOR;
   } else {
@@ -448,6 +538,17 @@ extern "C" int smx_fp32_plan_info(const smx_fp32_plan* h, int* evaluator, int64_
   if (n_lambda) *n_lambda = h->n_lambda;
   if (coef) *coef = h->C64.p;
   return SMX_OK;
+}
+
+extern "C" int smx_fp32_plan_has_fp64(const smx_fp32_plan* h) { return h && h->have64 ? 1 : 0; }
+
+extern "C" int smx_fp32_eval64(const smx_fp32_plan* h, const double* x, int64_t P, int64_t ldx, double* y,
+                               void* stream) {
+  SMX_REQUIRE(h, "smx_fp32_eval64: null plan");
+  if (!h->have64)
+    return smx::set_error(SMX_ERR_UNSUPPORTED, "smx_fp32_eval64: the plan has no FP64 tables (one output, per-point "
+                                               "row within shared memory)");
+  return smx_spectral_eval64(&h->spectral64, x, P, ldx, y, stream);
 }
 
 extern "C" size_t smx_fp32_workspace(const smx_fp32_plan* h, int64_t P) {

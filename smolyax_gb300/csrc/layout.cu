@@ -57,17 +57,19 @@ int argmin(const double* v, int n) {
 }
 
 // Runs of the per-point evaluator (spectral.py _Runs): 4-aligned slot ranges
-// of at most 32 slots, gaps of at most 4, coefficients [length][dstride].
+// of at most 32 slots, gaps of at most 4, coefficients [length][dstride] of
+// type V (float for the FP32 evaluator, double for the FP64 one).
+template <typename V>
 struct Runs {
   int64_t dstride;
   std::vector<int32_t> tab;  // [n][4] start, length, coefficient offset, degree
-  std::vector<float> coef;
+  std::vector<V> coef;
   struct Range {
     int64_t first, second;
   };
   int64_t n() const { return int64_t(tab.size() / 4); }
   // slots increasing; coefs(i, o) = coefficient o of slot i
-  Range add(const std::vector<int64_t>& slots, const std::function<float(size_t, int)>& coefs, int d_out, int degree) {
+  Range add(const std::vector<int64_t>& slots, const std::function<V(size_t, int)>& coefs, int d_out, int degree) {
     const int64_t r0 = n();
     const size_t N = slots.size();
     for (size_t i = 0; i < N;) {
@@ -76,7 +78,7 @@ struct Runs {
       while (j < N && slots[j] - slots[j - 1] <= 4 && slots[j] - a0 < 32) ++j;
       const int64_t length = round4(slots[j - 1] + 1 - a0);
       const size_t base = coef.size();
-      coef.resize(base + size_t(length * dstride), 0.f);
+      coef.resize(base + size_t(length * dstride), V(0));
       for (size_t q = i; q < j; ++q)
         for (int o = 0; o < d_out; ++o) coef[base + size_t((slots[q] - a0) * dstride + o)] = coefs(q, o);
       tab.insert(tab.end(), {int32_t(a0), int32_t(length), int32_t(base), int32_t(degree)});
@@ -550,9 +552,13 @@ bool build_blocked_tc(const Tree& tr, const float* C, const int64_t* maxdeg, int
   return true;
 }
 
-// Port of spectral.py build_layout (4 segments).
-bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
-                    const double* fa, const double* fb, Tables& out) {
+static void put(Tables& t, const char* name, std::vector<float> v) { t.f32[name] = std::move(v); }
+static void put(Tables& t, const char* name, std::vector<double> v) { t.f64[name] = std::move(v); }
+
+// Port of spectral.py build_layout (4 segments); coefficients and maps of type V.
+template <typename V>
+bool build_perpoint_t(const Tree& tr, const V* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
+                      const double* fa, const double* fb, Tables& out) {
   constexpr int nseg = 4;
   const int64_t n = tr.n;
   const int64_t dstride = d_out == 1 ? 1 : round4(d_out);
@@ -599,8 +605,11 @@ bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* ma
   for (size_t i = 0; i < S.size(); ++i) vp_row[S[i]] = n_hb + 1 + int64_t(i);
   const int64_t n_vp = 1 + int64_t(S.size());
   int64_t row = round4(n_hb + n_vp);
-  while (row % 32 != 4) row += 4;
-  Runs runs{dstride, {}, {}};
+  if (sizeof(V) == 8)
+    row += 2;  // doubles: 2 mod 4 keeps the 16-byte row reads of 8 consecutive points conflict-free
+  else
+    while (row % 32 != 4) row += 4;
+  Runs<V> runs{dstride, {}, {}};
   // leaf children of each node, sorted by (parent, slot)
   std::vector<int64_t> leaf;
   for (int64_t e : hot_e)
@@ -610,7 +619,7 @@ bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* ma
   });
   const int64_t NN = int64_t(nodes.size());
   std::vector<int32_t> node_tab(NN * 4);
-  std::vector<float> node_c(NN * dstride, 0.f);
+  std::vector<V> node_c(NN * dstride, V(0));
   std::vector<double> cost_nodes(NN);
   int max_depth = 0;
   for (int64_t e : nodes) max_depth = std::max(max_depth, int(tr.level[e]));
@@ -652,7 +661,7 @@ bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* ma
   }
   auto alpha0 = [&](int dd) { return fam[dd] == 0 ? 1.0 : sqrt(2.0); };
   std::vector<int32_t> blk_dims, blk_run;
-  std::vector<float> blk_ab;
+  std::vector<V> blk_ab;
   std::vector<double> cost_blk;
   for (size_t q = 0; q < simple.size(); q += 4) {
     const size_t np = std::min<size_t>(4, simple.size() - q);
@@ -666,17 +675,17 @@ bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* ma
     sl.erase(std::unique(sl.begin(), sl.end()), sl.end());
     const int64_t a0 = sl.front() & ~int64_t(3);
     const int64_t n4 = (round4(sl.back() + 1) - a0) / 4;
-    std::vector<float> blk(size_t(n4 * 16), 0.f);  // [slot][dimension]
+    std::vector<V> blk(size_t(n4 * 16), V(0));  // [slot][dimension]
     for (size_t jj = 0; jj < np; ++jj)
       for (size_t r = simple[q + jj].first; r < simple[q + jj].second; ++r) {
         const int64_t v = ce[r];
         blk[size_t((vp_row[tr.parent[v]] - a0) * 4 + int64_t(jj))] = Cv(v, 0);
       }
-    float ab[8] = {0};
+    V ab[8] = {0};
     for (size_t jj = 0; jj < np; ++jj) {
       const int dd = dims4[jj];
-      ab[jj] = float(alpha0(dd) * fa[dd]);
-      ab[4 + jj] = float(alpha0(dd) * fb[dd]);
+      ab[jj] = V(alpha0(dd) * fa[dd]);
+      ab[4 + jj] = V(alpha0(dd) * fb[dd]);
     }
     while (dims4.size() < 4) dims4.push_back(dims4[0]);
     blk_dims.insert(blk_dims.end(), dims4.begin(), dims4.end());
@@ -686,7 +695,7 @@ bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* ma
     cost_blk.push_back(16.0 + 9.0 * double(n4));
   }
   std::vector<int32_t> cold_tab;
-  std::vector<float> cold_ab;
+  std::vector<V> cold_ab;
   std::vector<double> cost_cold;
   for (const auto& b : general) {
     const int dd = tr.dim[ce[b.first]];
@@ -705,8 +714,8 @@ bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* ma
       q = q2;
     }
     cold_tab.insert(cold_tab.end(), {dd, int32_t(r_first), int32_t(runs.n()), int32_t(gmax | (fam[dd] << 8))});
-    cold_ab.push_back(float(fa[dd]));
-    cold_ab.push_back(float(fb[dd]));
+    cold_ab.push_back(V(fa[dd]));
+    cold_ab.push_back(V(fb[dd]));
     cost_cold.push_back(c);
   }
   std::vector<int64_t> allowed_nodes, all_cold, all_blk;
@@ -719,17 +728,17 @@ bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* ma
   out.i32["block_seg"] = cuts(cost_blk, all_blk, nseg);
   out.i32["blk_dims"] = blk_dims;
   out.i32["blk_run"] = blk_run;
-  out.f32["blk_ab"] = blk_ab;
-  out.f32["cold_ab"] = cold_ab;
+  put(out, "blk_ab", std::move(blk_ab));
+  put(out, "cold_ab", std::move(cold_ab));
   out.i32["hot_dim"] = hot_dims;
   out.i32["hot_deg"] = hot_deg;
   out.i32["hot_soff"] = hot_soff;
   out.i32["node"] = node_tab;
-  out.f32["node_c"] = node_c;
+  put(out, "node_c", std::move(node_c));
   out.i32["cold"] = cold_tab;
   out.i32["run"] = runs.tab;
-  if (runs.coef.empty()) runs.coef.assign(4, 0.f);
-  out.f32["coef"] = runs.coef;
+  if (runs.coef.empty()) runs.coef.assign(4, V(0));
+  put(out, "coef", std::move(runs.coef));
   out.scalar["dstride"] = double(dstride);
   out.scalar["row"] = double(row);
   out.scalar["n_hb"] = double(n_hb);
@@ -740,6 +749,16 @@ bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* ma
   out.scalar["max_depth"] = double(max_depth);
   out.scalar["n_cold_blocks"] = double(cost_blk.size());
   return true;
+}
+
+bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
+                    const double* fa, const double* fb, Tables& out) {
+  return build_perpoint_t(tr, C, d_out, maxdeg, d, fam, fa, fb, out);
+}
+
+bool build_perpoint(const Tree& tr, const double* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
+                    const double* fa, const double* fb, Tables& out) {
+  return build_perpoint_t(tr, C, d_out, maxdeg, d, fam, fa, fb, out);
 }
 
 // Tape of the tensor-core panel (spectral.py build_tape): non-root entries in
@@ -818,6 +837,32 @@ extern "C" int smx_layout_build(int kind, int64_t n, const int32_t* parent, cons
   }
   if (!ok) return smx::set_error(SMX_ERR_UNSUPPORTED, "smx_layout_build: the plan is outside this evaluator's limits");
   *out = h.release();
+  return SMX_OK;
+}
+
+extern "C" int smx_layout_build_f64(int kind, int64_t n, const int32_t* parent, const int32_t* dim,
+                                    const int32_t* deg, const int32_t* level, const int64_t* rank, const double* rem,
+                                    const double* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
+                                    const double* fa, const double* fb, smx_host_tables** out) {
+  SMX_REQUIRE(out && n >= 1 && d >= 1 && d_out >= 1 && parent && dim && deg && level && rank && rem && maxdeg && fam &&
+                  fa && fb && C,
+              "smx_layout_build_f64: bad arguments");
+  SMX_REQUIRE(kind == SMX_LAYOUT_PERPOINT, "smx_layout_build_f64: only the per-point layout has an FP64 form");
+  *out = nullptr;
+  smx::layout::Tree tr{n, parent, dim, deg, level, rank, rem};
+  auto h = std::make_unique<smx_host_tables>();
+  if (!smx::layout::build_perpoint(tr, C, d_out, maxdeg, d, fam, fa, fb, h->t))
+    return smx::set_error(SMX_ERR_UNSUPPORTED, "smx_layout_build_f64: the plan is outside this evaluator's limits");
+  *out = h.release();
+  return SMX_OK;
+}
+
+extern "C" int smx_layout_f64(const smx_host_tables* h, const char* name, const double** data, int64_t* count) {
+  SMX_REQUIRE(h && name && data && count, "smx_layout_f64: null argument");
+  auto it = h->t.f64.find(name);
+  SMX_REQUIRE(it != h->t.f64.end(), std::string("smx_layout_f64: no double table ") + name);
+  *data = it->second.data();
+  *count = int64_t(it->second.size());
   return SMX_OK;
 }
 

@@ -28,6 +28,7 @@ struct Tree {
 struct Tables {
   std::map<std::string, std::vector<int32_t>> i32;
   std::map<std::string, std::vector<float>> f32;
+  std::map<std::string, std::vector<double>> f64;
   std::map<std::string, double> scalar;
 };
 
@@ -36,6 +37,11 @@ int64_t blocked_smem_bytes(int64_t n_hs, int64_t k_c);
 bool build_blocked(const Tree& tr, const float* C, const int64_t* maxdeg, int d, const int32_t* fam, const double* fa,
                    const double* fb, Tables& out);
 bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
+                    const double* fa, const double* fb, Tables& out);
+// The same layout with FP64 coefficients and maps (tables in Tables::f64) for
+// the FP64 evaluator of the orthogonal form; "row" is then its row in doubles
+// (n_hb + n_vp rounded up to 4, plus 2).
+bool build_perpoint(const Tree& tr, const double* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
                     const double* fa, const double* fb, Tables& out);
 bool build_tape(const Tree& tr, const int64_t* maxdeg, int d, Tables& out);
 bool build_blocked_tc(const Tree& tr, const float* C, const int64_t* maxdeg, int d, const int32_t* fam,

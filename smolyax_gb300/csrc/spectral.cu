@@ -19,22 +19,14 @@
 #include <cuda_bf16.h>
 
 #include "common.cuh"
+#include "recurrence.cuh"
 
 namespace {
 
 constexpr int kMaxG = 24;     // max degree + 1 handled by the on-device basis-change inversion
 constexpr int kMaxRec = 512;  // max degree of the three-term recurrence tables and mode products
 
-// phi_{n+1} = alpha_n z phi_n - beta_n phi_{n-1}, phi_0 = 1, phi_{-1} = 0.
-__host__ __device__ inline void rec_coeffs(int fam, int n, double* a, double* b) {
-  if (fam == 0) {  // Legendre: P_{n+1} = ((2n+1) z P_n - n P_{n-1}) / (n+1)
-    *a = double(2 * n + 1) / double(n + 1);
-    *b = double(n) / double(n + 1);
-  } else {  // Hermite, psi_n = H_n / sqrt(2^n n!)
-    *a = sqrt(2.0 / double(n + 1));
-    *b = sqrt(double(n) / double(n + 1));
-  }
-}
+using smx::rec_coeffs;
 
 // --- per pair: A = V^{-1}, V[j][m] = phi_m(z_j) --------------------------------------------
 __global__ void spectral_pairs_kernel(int n_pairs, const int32_t* __restrict__ pdim, const int32_t* __restrict__ pdeg,
@@ -274,9 +266,20 @@ __global__ void run_sum_kernel(int64_t R, int dout, const int32_t* __restrict__ 
   const int o = int(idx - i * dout);
   const int key = skeys[i];
   if (i > 0 && skeys[i - 1] == key) return;
-  double s = 0.0;
-  for (int64_t j = i; j < R && skeys[j] == key; ++j) s += G[int64_t(srows[j]) * dout + o];
-  C[int64_t(key) * dout + o] += s;
+  // The rows of one entry cancel (zeta up to ~2e3, their sum ~1e4 times the
+  // coefficient), so they are summed with an error-free transformation
+  // (Knuth's TwoSum) and the rounding errors added at the end: the
+  // coefficients are then accurate to a few units in the last place, which
+  // the FP64 evaluation of the orthogonal form needs.
+  double s = C[int64_t(key) * dout + o], e = 0.0;
+  for (int64_t j = i; j < R && skeys[j] == key; ++j) {
+    const double v = G[int64_t(srows[j]) * dout + o];
+    const double t = s + v;
+    const double bp = t - s;
+    e += (s - (t - bp)) + (v - bp);
+    s = t;
+  }
+  C[int64_t(key) * dout + o] = s + e;
 }
 
 // --- FP32 evaluation -----------------------------------------------------------------------
@@ -410,8 +413,11 @@ __device__ __forceinline__ void spectral_eval_tile(const SpecArgs& a, const doub
     }
   }
   if (seg == 0) {
+    // the prefix slots start at 0 (phase 1 writes them): the last run of hot
+    // leaves may extend past n_hb with zero coefficients and must not meet
+    // stale shared memory (a NaN pattern there would survive the zero)
     Rw[a.n_hb] = 1.f;
-    for (int i = a.n_hb + a.n_vp; i < a.row; ++i) Rw[i] = 0.f;
+    for (int i = a.n_hb + 1; i < a.row; ++i) Rw[i] = 0.f;
   }
   __syncthreads();
 

@@ -1,0 +1,330 @@
+// FP64 evaluation of the orthogonal form, one output.
+//
+// The interpolant's combination sum (interpolation.py:264-304 over
+// barycentric.py:69-123) visits every tensor-product summand: ~6.6e4 FP64
+// multiply-adds per point at d_in = 1000, |Lambda| = 9999, and it cancels
+// (terms ~1e4 times the result), which leaves 1e-13 .. 1e-10 of rounding
+// error in any FP64 evaluation of it.  The orthogonal form sums one term per
+// entry of Lambda (9999 per point), with coefficients whose cancellation was
+// done once, by compensated sums, when they were computed; its terms are of
+// the size of the result (sum |term| / |y| ~ 2.4 at that workload), so plain
+// FP64 sums leave ~1e-14.  On GB300, whose FP64 rate is ~2 multiply-adds per
+// SM clock, the work per point is the bound: this evaluator does one DFMA per
+// term plus ~3 per hot basis value.
+//
+// Organisation as the FP32 per-point evaluator (spectral.cu): 128 points per
+// block, 16 warps = 4 point groups x 4 work segments; a row of `row` doubles
+// per point holds the hot basis values and the products of the hot prefixes
+// that cold entries extend; hot nodes are visited in DFS pre-order with the
+// path products on a register stack; cold blocks (4 degree-1 cold dimensions
+// over one run of prefix slots) and cold groups read their x column once.
+#include <math.h>
+
+#include "common.cuh"
+#include "recurrence.cuh"
+
+namespace {
+
+constexpr int kSeg = 4;
+constexpr int kTP = 128;
+constexpr int kThreads = kSeg * kTP;
+constexpr int kMaxRec = 512;
+constexpr size_t kSmemMax = 227 * 1024;
+
+struct Spec64Args {
+  int d_in, row, n_hb, n_vp, n_hot_dims;
+  int node_seg[kSeg + 1];
+  int cold_seg[kSeg + 1];
+  int block_seg[kSeg + 1];
+  const int32_t* hot_dim;
+  const int32_t* hot_deg;
+  const int32_t* hot_soff;
+  const int4* node;
+  const double* node_c;
+  const int4* cold;
+  const double2* cold_ab;
+  const int4* blk_dims;
+  const int4* blk_run;
+  const double2* blk_ab;  // per block: (a0, a1), (a2, a3), (b0, b1), (b2, b3)
+  const int4* run;
+  const double* coef;
+  const double* fam_a;
+  const double* fam_b;
+  const int32_t* fam;
+  double c0;
+};
+
+__constant__ double c_alpha64[2][kMaxRec];
+__constant__ double c_beta64[2][kMaxRec];
+
+// Infinite coordinates become NaN, as in the barycentric evaluation, whose
+// weights w/(x - node) vanish and normalise to 0/0 there.
+__device__ __forceinline__ double xin(double v) {
+  const long long b = __double_as_longlong(v);
+  return (b & 0x7fffffffffffffffll) == 0x7ff0000000000000ll ? __longlong_as_double(0x7ff8000000000000ll) : v;
+}
+
+// sum over a run's slots of coefficient * row value (length a multiple of 4,
+// start 4-aligned, coefficients 32-byte aligned): two chains of double2 pairs.
+__device__ __forceinline__ double dot_run64(const double* __restrict__ Rw, const double* __restrict__ coef, int4 r) {
+  const double2* T = reinterpret_cast<const double2*>(Rw + r.x);
+  const double2* Cq = reinterpret_cast<const double2*>(coef + r.z);
+  const int n2 = r.y >> 1;
+  double s0 = 0.0, s1 = 0.0;
+#pragma unroll 2
+  for (int k = 0; k < n2; ++k) {
+    const double2 t = T[k];
+    const double2 c = __ldg(Cq + k);
+    s0 = fma(c.x, t.x, s0);
+    s1 = fma(c.y, t.y, s1);
+  }
+  return s0 + s1;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) spectral_eval64_kernel(Spec64Args a, const double* __restrict__ x,
+                                                                      int64_t P, int64_t ldx,
+                                                                      double* __restrict__ y) {
+  extern __shared__ __align__(16) double sm64[];
+  double* RED = sm64 + size_t(a.row) * kTP;  // [kSeg][kTP]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int seg = warp / (kTP / 32);
+  const int pl = (warp % (kTP / 32)) * 32 + lane;
+  const int64_t p = blockIdx.x * int64_t(kTP) + pl;
+  const bool live = p < P;
+  const double* __restrict__ xp = x + (live ? p : 0) * ldx;
+  double* Rw = sm64 + size_t(pl) * a.row;
+
+  // phase 0: hot basis values phi_1..phi_g of every hot dimension; the empty
+  // prefix (= 1); zeros in the other prefix slots (phase 1 writes them, and
+  // the last run of hot leaves may extend into them with zero coefficients,
+  // which must not meet stale shared memory) and in the padding
+  for (int h = seg; h < a.n_hot_dims; h += kSeg) {
+    const int dim = __ldg(a.hot_dim + h), g = __ldg(a.hot_deg + h), so = __ldg(a.hot_soff + h);
+    const int fm = __ldg(a.fam + dim);
+    const double z = fma(__ldg(a.fam_a + dim), xin(xp[dim]), __ldg(a.fam_b + dim));
+    double pm1 = 0.0, pc = 1.0;
+    for (int n = 0; n < g; ++n) {
+      const double pn = fma(c_alpha64[fm][n] * z, pc, -c_beta64[fm][n] * pm1);
+      pm1 = pc;
+      pc = pn;
+      Rw[so + n] = pc;
+    }
+  }
+  if (seg == 0) {
+    Rw[a.n_hb] = 1.0;
+    for (int i = a.n_hb + 1; i < a.row; ++i) Rw[i] = 0.0;
+  }
+  __syncthreads();
+
+  double acc = 0.0;
+
+  // phase 1: hot nodes of this segment: v_node * (c_node + sum of the runs of
+  // its leaf children); the node's product is stored for the cold entries
+  {
+    double st1 = 1.0, st2 = 1.0, st3 = 1.0, st4 = 1.0, st5 = 1.0, st6 = 1.0, st7 = 1.0, st8 = 1.0;
+    for (int i = a.node_seg[seg]; i < a.node_seg[seg + 1]; ++i) {
+      const int4 nd = __ldg(a.node + i);
+      const int slot = nd.x & 0xffff;
+      const int depth = nd.x >> 16;
+      double v;
+      if (depth == 0) {
+        v = 1.0;
+      } else {
+        const double b = Rw[slot];
+        switch (depth) {
+          case 1: st1 = b; v = st1; break;
+          case 2: st2 = st1 * b; v = st2; break;
+          case 3: st3 = st2 * b; v = st3; break;
+          case 4: st4 = st3 * b; v = st4; break;
+          case 5: st5 = st4 * b; v = st5; break;
+          case 6: st6 = st5 * b; v = st6; break;
+          case 7: st7 = st6 * b; v = st7; break;
+          default: st8 = st7 * b; v = st8; break;
+        }
+      }
+      if (nd.y >= 0) Rw[nd.y] = v;
+      double s = __ldg(a.node_c + i);
+      for (int r = nd.z; r < nd.w; ++r) s += dot_run64(Rw, a.coef, __ldg(a.run + r));
+      acc = fma(v, s, acc);
+    }
+  }
+  __syncthreads();  // prefix products complete
+
+  // phase 2a: cold blocks: sum_j phi_1(z_j) * sum_s c[s][j] * prefix[s] over
+  // one run of prefix slots shared by the block's 4 dimensions (coefficients
+  // [slot][dimension], 16 per quad of slots)
+  {
+    const int b0 = a.block_seg[seg], b1 = a.block_seg[seg + 1];
+    int4 dn = b0 < b1 ? __ldg(a.blk_dims + b0) : make_int4(0, 0, 0, 0);
+    double xn0 = xp[dn.x], xn1 = xp[dn.y], xn2 = xp[dn.z], xn3 = xp[dn.w];
+    for (int bi = b0; bi < b1; ++bi) {
+      const double x0 = xn0, x1 = xn1, x2 = xn2, x3 = xn3;
+      if (bi + 8 < b1) {
+        const int4 pd = __ldg(a.blk_dims + bi + 8);
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(xp + pd.x));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(xp + pd.w));
+      }
+      if (bi + 1 < b1) {
+        dn = __ldg(a.blk_dims + bi + 1);
+        xn0 = xp[dn.x];
+        xn1 = xp[dn.y];
+        xn2 = xp[dn.z];
+        xn3 = xp[dn.w];
+      }
+      const int4 rr = __ldg(a.blk_run + bi);
+      const double2* T = reinterpret_cast<const double2*>(Rw + rr.x);
+      const double2* Cq = reinterpret_cast<const double2*>(a.coef + rr.z);
+      double u0 = 0.0, u1 = 0.0, u2 = 0.0, u3 = 0.0;
+      for (int k = 0; k < rr.y; ++k) {
+        const double2 t01 = T[2 * k], t23 = T[2 * k + 1];
+        const double ts[4] = {t01.x, t01.y, t23.x, t23.y};
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+          const double2 clo = __ldg(Cq + 8 * k + 2 * s), chi = __ldg(Cq + 8 * k + 2 * s + 1);
+          u0 = fma(clo.x, ts[s], u0);
+          u1 = fma(clo.y, ts[s], u1);
+          u2 = fma(chi.x, ts[s], u2);
+          u3 = fma(chi.y, ts[s], u3);
+        }
+      }
+      const double2 a01 = __ldg(a.blk_ab + 4 * bi), a23 = __ldg(a.blk_ab + 4 * bi + 1);
+      const double2 f01 = __ldg(a.blk_ab + 4 * bi + 2), f23 = __ldg(a.blk_ab + 4 * bi + 3);
+      double v = fma(a01.x, xin(x0), f01.x) * u0;
+      v = fma(fma(a01.y, xin(x1), f01.y), u1, v);
+      v = fma(fma(a23.x, xin(x2), f23.x), u2, v);
+      v = fma(fma(a23.y, xin(x3), f23.y), u3, v);
+      acc += v;
+    }
+  }
+
+  // phase 2: cold groups: one cold dimension, runs sorted by degree
+  {
+    const int g0 = a.cold_seg[seg], g1 = a.cold_seg[seg + 1];
+    int4 cg = g0 < g1 ? __ldg(a.cold + g0) : make_int4(0, 0, 0, 0);
+    double xn = g0 < g1 ? xp[cg.x] : 0.0;
+    for (int gi = g0; gi < g1; ++gi) {
+      const int4 cur = cg;
+      const double xv = xn;
+      const double2 ab = __ldg(a.cold_ab + gi);
+      if (gi + 16 < g1) {
+        const double* pf = xp + __ldg(&a.cold[gi + 16].x);
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(pf));
+      }
+      if (gi + 1 < g1) {
+        cg = __ldg(a.cold + gi + 1);
+        xn = xp[cg.x];
+      }
+      const int fm = cur.w >> 8;
+      const double z = fma(ab.x, xin(xv), ab.y);
+      double pm1 = 0.0, pc = 1.0;
+      int gcur = 0;
+      for (int r = cur.y; r < cur.z; ++r) {
+        const int4 rr = __ldg(a.run + r);
+        while (gcur < rr.w) {
+          const double pn = fma(c_alpha64[fm][gcur] * z, pc, -c_beta64[fm][gcur] * pm1);
+          pm1 = pc;
+          pc = pn;
+          ++gcur;
+        }
+        acc = fma(pc, dot_run64(Rw, a.coef, rr), acc);
+      }
+    }
+  }
+
+  // phase 3: the segments' sums, in a fixed order
+  RED[seg * kTP + pl] = acc;
+  __syncthreads();
+  if (seg == 0 && live) {
+    double s = a.c0;
+#pragma unroll
+    for (int r = 0; r < kSeg; ++r) s += RED[r * kTP + pl];
+    y[p] = s;
+  }
+}
+
+bool g_consts64_ready = false;
+
+int upload_consts64() {
+  if (g_consts64_ready) return SMX_OK;
+  static double al[2][kMaxRec], be[2][kMaxRec];
+  for (int f = 0; f < 2; ++f)
+    for (int n = 0; n < kMaxRec; ++n) smx::rec_coeffs(f, n, &al[f][n], &be[f][n]);
+  if (cudaMemcpyToSymbol(c_alpha64, al, sizeof(al)) != cudaSuccess ||
+      cudaMemcpyToSymbol(c_beta64, be, sizeof(be)) != cudaSuccess)
+    return smx::set_error(SMX_ERR_CUDA, "smx_spectral_eval64: constant upload failed");
+  g_consts64_ready = true;
+  return SMX_OK;
+}
+
+bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
+
+}  // namespace
+
+extern "C" int smx_spectral_eval64(const smx_spectral64* sp, const double* x, int64_t P, int64_t ldx, double* y,
+                                   void* stream) {
+  const char* who = "smx_spectral_eval64";
+  SMX_REQUIRE(sp != nullptr, "smx_spectral_eval64: null plan");
+  SMX_REQUIRE(sp->fam && sp->fam_a && sp->fam_b && sp->node && sp->node_c && sp->n_nodes >= 1 &&
+                  (sp->n_hot_dims == 0 || (sp->hot_dim && sp->hot_deg && sp->hot_soff)),
+              "smx_spectral_eval64: incomplete plan");
+  if (sp->max_depth > 8) return smx::set_error(SMX_ERR_UNSUPPORTED, std::string(who) + ": hot nodes deeper than 8");
+  const int need = (sp->n_hb + sp->n_vp + 3) / 4 * 4;
+  SMX_REQUIRE(sp->n_vp >= 1 && sp->row % 2 == 0 && sp->row >= need, "smx_spectral_eval64: bad row");
+  for (int i = 0; i < kSeg; ++i)
+    SMX_REQUIRE(sp->node_seg[i] <= sp->node_seg[i + 1] && sp->cold_seg[i] <= sp->cold_seg[i + 1] &&
+                    sp->block_seg[i] <= sp->block_seg[i + 1],
+                "smx_spectral_eval64: segments not ordered");
+  SMX_REQUIRE(sp->node_seg[0] == 0 && sp->node_seg[kSeg] == sp->n_nodes && sp->cold_seg[0] == 0 &&
+                  sp->cold_seg[kSeg] == sp->n_cold_groups && sp->block_seg[0] == 0 &&
+                  sp->block_seg[kSeg] == sp->n_cold_blocks,
+              "smx_spectral_eval64: segments do not cover the plan");
+  SMX_REQUIRE(!sp->n_cold_groups || (sp->cold && sp->cold_ab), "smx_spectral_eval64: cold groups without tables");
+  SMX_REQUIRE(!sp->n_cold_blocks || (sp->blk_dims && sp->blk_run && sp->blk_ab),
+              "smx_spectral_eval64: cold blocks without tables");
+  SMX_REQUIRE(!sp->coef || aligned(sp->coef, 32), "smx_spectral_eval64: coefficients not 32-byte aligned");
+  SMX_REQUIRE(P >= 0 && ldx >= sp->d_in, "smx_spectral_eval64: bad sizes");
+  const size_t smem = (size_t(sp->row) + kSeg) * kTP * sizeof(double);
+  if (smem > kSmemMax)
+    return smx::set_error(SMX_ERR_UNSUPPORTED, std::string(who) + ": per-point row too large for shared memory");
+  if (P == 0) return SMX_OK;
+  SMX_REQUIRE(x && y, "smx_spectral_eval64: null pointer");
+  int rc = upload_consts64();
+  if (rc) return rc;
+  Spec64Args a;
+  a.d_in = sp->d_in;
+  a.row = sp->row;
+  a.n_hb = sp->n_hb;
+  a.n_vp = sp->n_vp;
+  a.n_hot_dims = sp->n_hot_dims;
+  for (int i = 0; i <= kSeg; ++i) {
+    a.node_seg[i] = sp->node_seg[i];
+    a.cold_seg[i] = sp->cold_seg[i];
+    a.block_seg[i] = sp->block_seg[i];
+  }
+  a.hot_dim = sp->hot_dim;
+  a.hot_deg = sp->hot_deg;
+  a.hot_soff = sp->hot_soff;
+  a.node = reinterpret_cast<const int4*>(sp->node);
+  a.node_c = sp->node_c;
+  a.cold = reinterpret_cast<const int4*>(sp->cold);
+  a.cold_ab = reinterpret_cast<const double2*>(sp->cold_ab);
+  a.blk_dims = reinterpret_cast<const int4*>(sp->blk_dims);
+  a.blk_run = reinterpret_cast<const int4*>(sp->blk_run);
+  a.blk_ab = reinterpret_cast<const double2*>(sp->blk_ab);
+  a.run = reinterpret_cast<const int4*>(sp->run);
+  a.coef = sp->coef;
+  a.fam_a = sp->fam_a;
+  a.fam_b = sp->fam_b;
+  a.fam = sp->fam;
+  a.c0 = sp->c0;
+  static bool attr_set = false;
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(spectral_eval64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemMax)) !=
+        cudaSuccess)
+      return smx::set_error(SMX_ERR_CUDA, "smx_spectral_eval64: shared-memory attribute");
+    attr_set = true;
+  }
+  spectral_eval64_kernel<<<smx::grid_for(P, kTP), kThreads, smem, smx::as_stream(stream)>>>(a, x, P, ldx, y);
+  SMX_LAUNCH_CHECK("smx_spectral_eval64");
+  return SMX_OK;
+}

@@ -26,6 +26,14 @@ of different interpolants and batch sizes:
 
   Launches of different kinds run on different streams, so their work
   overlaps on the device;
+* priorities -- a launch whose estimated work (multiply-adds: points x
+  |Lambda| x d_out, x3 for gradients) is at most ``fast_work`` runs on one of
+  ``n_fast_streams`` streams of the device's highest priority, the others on
+  ``n_streams`` normal streams.  The block scheduler then starts the blocks of
+  a small launch as soon as blocks of a running large launch retire, instead
+  of after all of the large launch's blocks, and a small request that finds
+  every normal stream busy is still admitted (the scan of the FIFO queue
+  passes requests whose class has no free stream);
 * staging   -- inputs are copied from the request's numpy array into a pinned
   host arena allocated once (no page-locking per request), then to the device
   without blocking the host; results come back into the arena the same way.
@@ -162,7 +170,8 @@ class Server:
     ``memory_budget`` (GiB) bounds the device memory of the requests in
     flight; ``staging`` (GiB) is the size of the pinned host arena."""
 
-    def __init__(self, interpolants: dict, memory_budget: float = 8.0, n_streams: int = 8, staging: float = 1.0):
+    def __init__(self, interpolants: dict, memory_budget: float = 8.0, n_streams: int = 8, staging: float = 1.0,
+                 n_fast_streams: int = 4, fast_work: float = 5e9):
         self.dev = torch.device("cuda", torch.cuda.current_device())
         self.sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
         self.ips = dict(interpolants)
@@ -176,6 +185,11 @@ class Server:
         self.arena = PinnedArena(int(staging * 1024**3))
         self.streams = [torch.cuda.Stream(device=self.dev) for _ in range(n_streams)]
         self.free_streams = collections.deque(self.streams)
+        # highest priority of the device (out-of-range values map to it)
+        self.fast_streams = [torch.cuda.Stream(device=self.dev, priority=-100) for _ in range(n_fast_streams)]
+        self.free_fast = collections.deque(self.fast_streams)
+        self.fast_work = float(fast_work)
+        self.fast_launches = 0
         self.waiting = collections.deque()
         self.inflight = []
         self.lock = threading.Lock()
@@ -244,48 +258,69 @@ class Server:
                 b += self.sms * 2 * 16 * 128 * 4 + 4 * self.sms
         return int(b)
 
+    def work(self, req):
+        """Estimated multiply-adds of a request: points x |Lambda| x d_out (the
+        orthogonal form's terms), x3 for a gradient (panel, contraction and
+        its transpose), or the combination sum's entries x d_out for an FP64
+        evaluation that runs it."""
+        ip = self.ips[req.name]
+        per = float(ip._tree.size) * ip.d_out
+        if req.op == "grad":
+            per *= 3.0
+        elif req.precision == "fp64" and ip._fp64_orthogonal() is None:
+            per = float(ip._plan.c.n_entries) * ip.d_out
+        return req.points * per
+
     def _kind(self, req):
-        """Launch kind: 'blocked' / 'stream' (persistent multi-plan launches), or
-        ('plan', name, op, precision[, id]) for requests evaluated by one call
-        per interpolant."""
+        """Launch kind: (fast, 'blocked' / 'stream') for the persistent
+        multi-plan launches, or (fast, 'plan', name, op, precision[, id]) for
+        requests evaluated by one call per interpolant; ``fast`` selects the
+        high-priority streams."""
         sp = self.spec[req.name]
+        fast = self.work(req) <= self.fast_work
         if req.op == "eval" and req.precision == "fp32" and sp.tc is None:
             if sp.blocked is None:
-                return "stream"
+                return (fast, "stream")
             if req.points <= 128 * self.sms:
-                return "blocked"
+                return (fast, "blocked")
             # a blocked request of a full round of tiles or more fills the GPU
             # alone and is evaluated exactly as alone (last-round split)
-            return ("plan", req.name, req.op, req.precision, req.id)
-        return ("plan", req.name, req.op, req.precision)
+            return (fast, "plan", req.name, req.op, req.precision, req.id)
+        return (fast, "plan", req.name, req.op, req.precision)
 
     # ------------------------------------------------------------------ admission
     def _admit(self):
         batches = {}
         with self.lock:
-            avail = len(self.free_streams)  # streams not yet promised in this step
+            # streams not yet promised in this step, per class (normal, fast)
+            avail = {False: len(self.free_streams), True: len(self.free_fast)}
+            kept = collections.deque()
             while self.waiting:
-                req = self.waiting[0]
+                req = self.waiting.popleft()
                 nb = self.request_bytes(req)
                 if nb > self.budget:
-                    self.waiting.popleft()
                     req.error = "request needs %d bytes, more than the server's budget" % nb
                     req.t_done = time.perf_counter()
                     req.done.set()
                     self.rejected.append(req)
                     continue
                 if self.in_use + nb > self.budget:
+                    kept.append(req)
                     break
                 kind = self._kind(req)
                 if kind not in batches:
-                    if avail < 1:
-                        break
-                    avail -= 1  # one stream per launch
-                self.waiting.popleft()
+                    if avail[kind[0]] < 1:
+                        kept.append(req)  # no stream of its class: later requests may still go
+                        if not avail[True] and not avail[False]:
+                            break
+                        continue
+                    avail[kind[0]] -= 1  # one stream per launch
                 batches.setdefault(kind, []).append((req, nb))
                 self.in_use += nb
                 self.admitted += 1
-            streams = {kind: self.free_streams.popleft() for kind in batches}
+            kept.extend(self.waiting)
+            self.waiting = kept
+            streams = {kind: (self.free_fast if kind[0] else self.free_streams).popleft() for kind in batches}
         now = time.perf_counter()
         for kind, batch in batches.items():
             try:
@@ -309,7 +344,7 @@ class Server:
                 self._building = None
             self.failed.extend(r for r, _ in batch)
             self.in_use -= sum(nb for _, nb in batch)
-            self.free_streams.append(stream)
+            self._release_stream(stream, kind[0])
 
     # ------------------------------------------------------------------ staging
     def _stage(self, g, nbytes):
@@ -340,21 +375,26 @@ class Server:
     # ------------------------------------------------------------------ launches
     def _launch_batch(self, kind, batch, stream, now):
         g = _Group(stream, [r for r, _ in batch], sum(nb for _, nb in batch))
+        g.fast = kind[0]
         self._building = g
         with torch.cuda.stream(stream):
             for req, _ in batch:
                 req.t_admit = now
-            if kind in ("blocked", "stream"):
-                self._launch_multiplan(kind, batch, g)
+            if kind[1] in ("blocked", "stream"):
+                self._launch_multiplan(kind[1], batch, g)
                 self.batch_launches += 1
             else:
-                self._launch_plan(kind, batch, g)
+                self._launch_plan(kind[1:], batch, g)
                 if len(batch) > 1:
                     self.batch_launches += 1
             g.event.record(stream)
         self._building = None
         self.launches += 1
+        self.fast_launches += int(kind[0])
         self.inflight.append(g)
+
+    def _release_stream(self, stream, fast):
+        (self.free_fast if fast else self.free_streams).append(stream)
 
     def _launch_multiplan(self, kind, batch, g):
         plan_idx, plans = {}, []
@@ -432,7 +472,7 @@ class Server:
                 for off in g.staged:
                     self.arena.free(off)
                 self.in_use -= g.nbytes
-                self.free_streams.append(g.stream)
+                self._release_stream(g.stream, g.fast)
 
     # ------------------------------------------------------------------ statistics
     def stats(self):
@@ -440,7 +480,8 @@ class Server:
         evals = sum(r.points * self.ips[r.name].d_out for r in self.completed if r.op == "eval")
         return dict(
             completed=len(self.completed), rejected=len(self.rejected), failed=len(self.failed),
-            launches=self.launches, batch_launches=self.batch_launches, staging_spills=self.spilled,
+            launches=self.launches, batch_launches=self.batch_launches, fast_launches=self.fast_launches,
+            staging_spills=self.spilled,
             p50_ms=float(np.percentile(lat, 50) * 1e3), p99_ms=float(np.percentile(lat, 99) * 1e3), evals=int(evals),
         )
 

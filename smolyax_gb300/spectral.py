@@ -172,6 +172,7 @@ class SpectralPlan:
         if d_out >= TC_MIN_DOUT or not stream_fits:
             self._build_tc(*self._fwd_args)
         self.memory_limit = ip._memory_limit
+        self._f64 = None
         self.blocked = None
         self.blocked_tc = None
         if d_out == 1 and self.tc is None:
@@ -394,6 +395,55 @@ class SpectralPlan:
         call("smx_spectral_eval", self.ref(), ptr(x), int(x.shape[0]), int(x.shape[1]), ptr(y), st)
         return y
 
+    def fp64_form(self):
+        """FP64 tables of the orthogonal form for ``csrc/spectral64.cu`` (one
+        output), built on first use from the same tree and the FP64
+        coefficients; None where that evaluator does not apply (more outputs,
+        hot nodes deeper than 8, or a per-point row beyond shared memory)."""
+        if self._f64 is None:
+            self._f64 = False
+            tr, _, maxdeg, fam, fa, fb, T, _ = self._fwd_args
+            d = int(self.c.d_in)
+            if self.c.d_out == 1:
+                lay = build_layout(tr, self.C64.cpu().numpy(), maxdeg, d, 1, fam, fa, fb, dtype=np.float64)
+                row = int(lay["row"])
+                if (row + 4) * 128 * 8 <= 227 * 1024 and int(lay["max_depth"]) <= 8:
+                    k = {}
+                    for name in ("hot_dim", "hot_deg", "hot_soff", "node", "cold", "run", "blk_dims", "blk_run"):
+                        k[name] = T(lay[name], torch.int32)
+                    for name in ("node_c", "coef", "cold_ab", "blk_ab"):
+                        k[name] = T(lay[name], torch.float64)
+                    st = capi.SmxSpectral64()
+                    st.d_in, st.row = d, row
+                    for name in ("n_hb", "n_vp", "n_hot_dims", "n_nodes", "n_cold_groups", "max_depth",
+                                 "n_cold_blocks"):
+                        setattr(st, name, int(lay[name]))
+                    for i in range(5):
+                        st.node_seg[i] = int(lay["node_seg"][i])
+                        st.cold_seg[i] = int(lay["cold_seg"][i])
+                        st.block_seg[i] = int(lay["block_seg"][i])
+                    for name, t in k.items():
+                        setattr(st, name, t.data_ptr() if t.numel() else None)
+                    st.fam_a, st.fam_b, st.fam = self.fa64.data_ptr(), self.fb64.data_ptr(), self.fam.data_ptr()
+                    st.c0 = float(self.C64[0, 0].item())
+                    self._f64 = (st, k)
+        return self._f64 or None
+
+    def evaluate64(self, x, y):
+        """y[P] (FP64, contiguous) at x[P, d_in] (FP64, rows contiguous, on the
+        device) through the FP64 evaluator of the orthogonal form."""
+        import ctypes
+
+        form = self.fp64_form()
+        if form is None:
+            raise ValueError("the plan has no FP64 orthogonal form (one output and a per-point row within shared memory)")
+        if x.dim() != 2 or (x.shape[0] > 1 and x.stride(1) != 1):
+            x = x.contiguous()
+        ldx = int(x.stride(0)) if x.shape[0] > 1 else int(x.shape[1])  # a one-row tensor may carry any row stride
+        call("smx_spectral_eval64", ctypes.byref(form[0]), ptr(x), int(x.shape[0]), ldx, ptr(y),
+             capi.stream_ptr(torch.cuda.current_stream()))
+        return y
+
     def _tc_step(self, P):
         """Points per panel chunk (the hi/lo panel of one chunk fits the memory limit)."""
         step = max(128, int(self.memory_limit * 1024**3 // (8 * ((self.tc["K"] + 31) // 32 * 32))) // 128 * 128)
@@ -532,8 +582,9 @@ def _round32(v):
 class _Runs:
     """Accumulates runs (4-aligned slot ranges with contiguous coefficients)."""
 
-    def __init__(self, dstride):
+    def __init__(self, dstride, dtype=np.float32):
         self.dstride = dstride
+        self.dtype = dtype
         self.tab = []
         self.coef = []
         self.ncoef = 0
@@ -551,7 +602,7 @@ class _Runs:
             while j < n and slots[j] - slots[j - 1] <= max_gap and slots[j] - a0 < max_len:
                 j += 1
             length = _round4(int(slots[j - 1]) + 1 - a0)
-            blk = np.zeros((length, self.dstride), dtype=np.float32)
+            blk = np.zeros((length, self.dstride), dtype=self.dtype)
             blk[np.asarray(slots[i:j]) - a0, : coefs.shape[1]] = coefs[i:j]
             self.tab.append((a0, length, self.ncoef, degree))
             self.coef.append(blk.ravel())
@@ -560,11 +611,13 @@ class _Runs:
         return r0, len(self.tab)
 
 
-def build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb, nseg=4):
-    """Layout of the FP32 evaluator (see ``csrc/spectral.cu``) from the index-set
+def build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb, nseg=4, dtype=np.float32):
+    """Layout of the per-point evaluators (``csrc/spectral.cu``, FP32, and
+    ``csrc/spectral64.cu``, FP64 with ``dtype=np.float64``) from the index-set
     tree (host arrays: parent, dim, deg, level, pre-order rank, remaining budget)
-    and the FP32 coefficients C[entry, d_out]; fam/fa/fb are the per-dimension
-    polynomial family and affine map to its variable."""
+    and the coefficients C[entry, d_out]; fam/fa/fb are the per-dimension
+    polynomial family and affine map to its variable.  The tables' structure
+    depends on the tree alone; coefficients and maps are stored in ``dtype``."""
     parent, dim, deg, level, rank, rem = (tr[key] for key in ("parent", "dim", "deg", "level", "rank", "rem"))
     n = parent.shape[0]
     dstride = 1 if d_out == 1 else _round4(d_out)
@@ -603,9 +656,12 @@ def build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb, nseg=4):
     vp_row[S] = n_hb + 1 + np.arange(S.size)
     n_vp = 1 + S.size
     row = _round4(n_hb + n_vp)
-    while row % 32 != 4:
-        row += 4
-    runs = _Runs(dstride)
+    if np.dtype(dtype).itemsize == 8:
+        row += 2  # doubles: 2 mod 4 keeps the 16-byte row reads of 8 consecutive points conflict-free
+    else:
+        while row % 32 != 4:
+            row += 4
+    runs = _Runs(dstride, dtype)
     # leaf children of each node, sorted by slot
     leaf_e = hot_e[~node_mask[hot_e]]
     order = np.lexsort((slot[leaf_e], parent[leaf_e]))
@@ -614,7 +670,7 @@ def build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb, nseg=4):
     starts = np.searchsorted(lp, nodes, side="left")
     ends = np.searchsorted(lp, nodes, side="right")
     node_tab = np.zeros((nodes.size, 4), dtype=np.int64)
-    node_c = np.zeros((nodes.size, dstride), dtype=np.float32)
+    node_c = np.zeros((nodes.size, dstride), dtype=dtype)
     cost_nodes = np.zeros(nodes.size)
     max_depth = int(level[nodes].max()) if nodes.size else 0
     for i, e in enumerate(nodes):
@@ -646,11 +702,11 @@ def build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb, nseg=4):
         slots = np.unique(np.concatenate([vp_row[parent[ce[b0:b1]]] for b0, b1 in part]))
         a0 = int(slots[0]) & ~3
         n4 = (_round4(int(slots[-1]) + 1) - a0) // 4
-        blk = np.zeros((n4 * 4, 4), dtype=np.float32)  # [slot][dim]
+        blk = np.zeros((n4 * 4, 4), dtype=dtype)  # [slot][dim]
         for jj, (b0, b1) in enumerate(part):
             e = ce[b0:b1]
             blk[vp_row[parent[e]] - a0, jj] = C[e, 0]
-        ab = np.zeros((2, 4), dtype=np.float32)
+        ab = np.zeros((2, 4), dtype=dtype)
         for jj, dd in enumerate(dims4):
             ab[0, jj] = alpha0[dd] * fa[dd]
             ab[1, jj] = alpha0[dd] * fb[dd]
@@ -704,12 +760,12 @@ def build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb, nseg=4):
         n_cold_blocks=len(blk_dims), block_seg=block_seg,
         blk_dims=as_i32(blk_dims, 4) if blk_dims else np.zeros((0, 4), np.int32),
         blk_run=as_i32(blk_run, 4) if blk_run else np.zeros((0, 4), np.int32),
-        blk_ab=np.asarray(blk_ab, dtype=np.float32).reshape(-1, 8),
-        cold_ab=np.asarray(cold_ab, dtype=np.float32).reshape(-1, 2),
+        blk_ab=np.asarray(blk_ab, dtype=dtype).reshape(-1, 8),
+        cold_ab=np.asarray(cold_ab, dtype=dtype).reshape(-1, 2),
         hot_dim=hot_dims.astype(np.int32), hot_deg=hot_deg.astype(np.int32), hot_soff=hot_soff.astype(np.int32),
         node=as_i32(node_tab, 4), node_c=node_c, cold=as_i32(cold_tab, 4) if cold_tab else np.zeros((0, 4), np.int32),
         run=as_i32(runs.tab, 4) if runs.tab else np.zeros((0, 4), np.int32),
-        coef=np.concatenate(runs.coef) if runs.coef else np.zeros(4, np.float32),
+        coef=np.concatenate(runs.coef) if runs.coef else np.zeros(4, dtype),
         cost=dict(nodes=float(cost_nodes.sum()), cold=float(np.sum(cost_cold)), blocks=float(np.sum(cost_blk)),
                   runs=len(runs.tab), coef_floats=int(runs.ncoef), node_seg=node_seg, cold_seg=cold_seg,
                   block_seg=block_seg),

@@ -1,5 +1,8 @@
 """FP64 path on the GPU against the reference's outputs (golden vectors).
 
+Both FP64 evaluators are checked: the default ("fp64": the orthogonal form in
+FP64 for one-output Leja / Gauss-Hermite plans, ``csrc/spectral64.cu``) and
+the reference's combination sum ("fp64_barycentric", ``csrc/eval64.cu``).
 Small cases: 1e-12 relative against the reference's values; gradients 1e-10
 relative with an absolute floor, NaN exactly where the reference has NaN.
 Benchmark workloads: the contract of ``gpu_helpers.check_fp64`` -- at least as
@@ -26,13 +29,14 @@ def _interp(**kw):
     return SmolyakBarycentricInterpolator(**kw)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp64_barycentric"])
 @pytest.mark.parametrize("name", [str(n) for n in INTERP["names"]])
-def test_small_cases(name):
+def test_small_cases(name, precision):
     z = INTERP
     spec, k, t, d_out, f = gio.small_case(z, name)
     ip = _interp(node_gen=product_generator(spec, len(k)), k=k, t=t, d_out=d_out, f=f)
     x = z[name + "/x"]
-    y = ip(x).cpu().numpy()
+    y = ip(x, precision=precision).cpu().numpy()
     np.testing.assert_allclose(y, z[name + "/y"], rtol=1e-12, atol=1e-13)
     g = ip.gradient(x[:-1]).cpu().numpy()
     assert_close_nan(g, z[name + "/grad"], rtol=1e-10, atol=1e-11)
@@ -40,20 +44,22 @@ def test_small_cases(name):
     assert (ip.n_f_evals, ip.n_f_evals_new) == tuple(int(v) for v in z[name + "/n_f_evals"])
 
 
-def test_config1_full():
+@pytest.mark.parametrize("precision", ["fp64", "fp64_barycentric"])
+def test_config1_full(precision):
     from smolyax_gb300 import nodes
 
     d = 10
     k = np.log((2 + np.arange(d)) / np.log(2))
     ip = _interp(node_gen=nodes.Leja(dim=d), k=k, t=8.831421, d_out=1, f=fns.rational(d, seed=0))
     x = np.random.default_rng(1).uniform(-1, 1, (10000, d))
-    check_fp64(ip(x).cpu().numpy(), CFG["cfg1/y"], EXACT["cfg1/y"])
+    check_fp64(ip(x, precision=precision).cpu().numpy(), CFG["cfg1/y"], EXACT["cfg1/y"])
     check_fp64_grad(ip.gradient(x[:64]).cpu().numpy(), CFG["cfg1/grad"], EXACT["cfg1/grad"])
     check_fp64(ip.integral().cpu().numpy(), CFG["cfg1/integral"], EXACT["cfg1/integral"], what="integral")
     assert (ip.n_f_evals, ip.n_f_evals_new) == tuple(int(v) for v in CFG["cfg1/n_f_evals"])
 
 
-def test_config2_subset():
+@pytest.mark.parametrize("precision", ["fp64", "fp64_barycentric"])
+def test_config2_subset(precision):
     from smolyax_gb300 import nodes
 
     d = 1000
@@ -61,7 +67,7 @@ def test_config2_subset():
     ip = _interp(node_gen=nodes.Leja(dim=d), k=k, t=8.224520, d_out=1, f=fns.rational(d, seed=0))
     x = np.random.default_rng(1).uniform(-1, 1, (256, d))
     np.testing.assert_allclose([x.sum(), (x * x).sum()], CFG["cfg2/x_checksum"], rtol=1e-14)
-    check_fp64(ip(x).cpu().numpy(), CFG["cfg2/y"], EXACT["cfg2/y"])
+    check_fp64(ip(x, precision=precision).cpu().numpy(), CFG["cfg2/y"], EXACT["cfg2/y"])
     check_fp64_grad(ip.gradient(x[:4]).cpu().numpy(), CFG["cfg2/grad"], EXACT["cfg2/grad"])
     check_fp64(ip.integral().cpu().numpy(), CFG["cfg2/integral"], EXACT["cfg2/integral"], what="integral")
     assert (ip.n_f_evals, ip.n_f_evals_new) == tuple(int(v) for v in CFG["cfg2/n_f_evals"])
@@ -129,5 +135,7 @@ def test_constant_only_and_chunking():
     a = _interp(node_gen=nodes.Leja(dim=d), k=k, t=6.0, d_out=1, f=f)
     b = _interp(node_gen=nodes.Leja(dim=d), k=k, t=6.0, d_out=1, f=f, memory_limit=1e-6)
     x = np.random.default_rng(2).uniform(-1, 1, (999, d))
+    bary = "fp64_barycentric"  # the evaluator that chunks by the memory limit
+    np.testing.assert_array_equal(a(x, precision=bary).cpu().numpy(), b(x, precision=bary).cpu().numpy())
     np.testing.assert_array_equal(a(x).cpu().numpy(), b(x).cpu().numpy())
     np.testing.assert_array_equal(a(x).cpu().numpy(), a(x).cpu().numpy())

@@ -104,7 +104,8 @@ def test_merged_gradients_tensor_core_and_fp64_equal_alone(fleet):
         reqs.append(Request("d", rng.uniform(-0.9, 0.9, (P, fleet["d"].d_in))))
     for P in (3, 90, 400):
         reqs.append(Request("b", rng.uniform(-0.9, 0.9, (P, fleet["b"].d_in)), precision="fp64"))
-    server = Server(fleet, memory_budget=4.0, n_streams=8, staging=1e-5)  # 10 KiB arena
+    # one stream class (fast_work = 0: no launch is small), so that each group is one launch
+    server = Server(fleet, memory_budget=4.0, n_streams=8, staging=1e-5, fast_work=0)  # 10 KiB arena
     for r in reqs:
         server.submit(r)
     server.drain()

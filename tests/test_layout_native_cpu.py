@@ -67,6 +67,28 @@ def test_perpoint_tables_equal(d, t, d_out, fam_id):
         assert nat[name] == float(py[name]), name
 
 
+@pytest.mark.parametrize("d,t,fam_id", [(1, 3.0, 0), (6, 5.0, 1), (40, 5.5, 0), (200, 6.5, 0), (1000, 8.22452, 0)])
+def test_perpoint_fp64_tables_equal(d, t, fam_id):
+    """The FP64 per-point layout (one output): FP64 coefficients and maps, the
+    FP64 row (n_hb + n_vp rounded up to 4, plus 2), the same structure as the
+    FP32 layout."""
+    tr, C, maxdeg, fam, fa, fb = _case(d, t, 1, fam_id, d + 1)
+    C = C.astype(np.float64) * (1 + 1e-9 * np.arange(C.size).reshape(C.shape))  # values not representable in FP32
+    py = build_layout(tr, C, maxdeg, d, 1, fam, fa, fb, dtype=np.float64)
+    nat = _capi.host_layout("perpoint", tr, C, 1, maxdeg, fam, fa, fb, PP_I32, PP_F32, PP_SCALARS, fp64=True)
+    for name in PP_I32:
+        np.testing.assert_array_equal(nat[name], np.asarray(py[name], dtype=np.int32).ravel(), err_msg=name)
+    for name in PP_F32:
+        assert py[name].dtype == np.float64, name
+        np.testing.assert_array_equal(nat[name], py[name].ravel(), err_msg=name)
+    for name in PP_SCALARS:
+        assert nat[name] == float(py[name]), name
+    assert nat["row"] == (int(py["n_hb"]) + int(py["n_vp"]) + 3) // 4 * 4 + 2
+    f32 = build_layout(tr, C.astype(np.float32), maxdeg, d, 1, fam, fa, fb)
+    for name in PP_I32:
+        np.testing.assert_array_equal(np.asarray(f32[name]), np.asarray(py[name]), err_msg=name)
+
+
 @pytest.mark.parametrize("d,t", [(1, 3.0), (12, 6.0), (200, 6.5), (1000, 8.22452)])
 def test_tape_equal(d, t):
     tr, C, maxdeg, fam, fa, fb = _case(d, t, 1, 0, 1)

@@ -13,11 +13,14 @@ class _Scheduler(serving.Server):
     """Server state without CUDA: request sizes and launch kinds are given,
     launches are recorded instead of run."""
 
-    def __init__(self, budget, n_streams, kinds, bytes_per_point, failing=()):
+    def __init__(self, budget, n_streams, kinds, bytes_per_point, failing=(), n_fast=0, fast=()):
         self.budget = budget
         self.in_use = 0
         self.streams = ["s%d" % i for i in range(n_streams)]
         self.free_streams = collections.deque(self.streams)
+        self.fast_streams = ["f%d" % i for i in range(n_fast)]
+        self.free_fast = collections.deque(self.fast_streams)
+        self._fast = set(fast)
         self.waiting = collections.deque()
         self.inflight = []
         self.lock = threading.Lock()
@@ -31,7 +34,7 @@ class _Scheduler(serving.Server):
         return self._bpp[req.name] * req.points
 
     def _kind(self, req):
-        return self._kinds[req.name]
+        return (req.name in self._fast, self._kinds[req.name])
 
     def _launch_batch(self, kind, batch, stream, now):
         if any(r.name in self._failing for r, _ in batch):
@@ -68,9 +71,25 @@ def test_merged_launch_per_kind_and_stream_limit():
     r = [s.submit(_req(n, 10)) for n in ("b", "b", "t", "b", "c")]
     s._admit()
     # two streams: one merged launch of the three 'b' requests, one of 't'; 'c' waits for a stream
-    kinds = {k: ids for k, ids, _ in s.launched}
+    kinds = {k[1]: ids for k, ids, _ in s.launched}
     assert kinds == {"blocked": [r[0].id, r[1].id, r[3].id], "stream": [r[2].id]}
     assert list(s.waiting) == [r[4]] and not s.free_streams
+
+
+def test_small_requests_take_the_high_priority_streams():
+    """Small launches go to the fast streams; when every normal stream is
+    busy, a small request behind a waiting large one is still admitted, and
+    the large one keeps its place at the head of the queue."""
+    s = _Scheduler(budget=10**6, n_streams=1, kinds={"a": None, "b": "x", "f": "blocked"},
+                   bytes_per_point={"a": 1, "b": 1, "f": 1}, n_fast=1, fast={"f"})
+    a1, b1, f1, f2 = (s.submit(_req(n, 10)) for n in ("a", "b", "f", "f"))
+    s._admit()
+    got = {k: (ids, st) for k, ids, st in s.launched}
+    assert got == {(False, None): ([a1.id], "s0"), (True, "blocked"): ([f1.id, f2.id], "f0")}
+    assert list(s.waiting) == [b1] and not s.free_streams and not s.free_fast
+    s._release_stream("s0", False)
+    s._admit()
+    assert s.launched[-1] == ((False, "x"), [b1.id], "s0") and not s.waiting
 
 
 def test_failed_launch_returns_its_stream_and_memory():
