@@ -480,6 +480,62 @@ def backward_workload(steps, warmup, points=None):
     return line
 
 
+def fp64_workload(steps, warmup, points=None):
+    """FP64 evaluation at the headline configuration (Leja d_in=1000, d_out=1,
+    |Lambda|=9999, rational f): the default FP64 evaluator of this plan (the
+    orthogonal form, csrc/spectral64.cu) and the reference's combination sum
+    (precision="fp64_barycentric"), one JSON line."""
+    import torch
+
+    from smolyax_gb300 import SmolyakBarycentricInterpolator, nodes
+
+    P = points or POINTS
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    k = np.log((2 + np.arange(D_IN)) / np.log(2))
+    ip = SmolyakBarycentricInterpolator(node_gen=nodes.Leja(dim=D_IN), k=k, t=T_THR, d_out=D_OUT, f=target(D_IN))
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1)
+    x = torch.rand(P, D_IN, dtype=torch.float64, device=dev, generator=gen) * 2 - 1
+    stream = torch.cuda.current_stream()
+
+    def timed(prec, n):
+        for _ in range(max(3, warmup)):
+            ip(x, precision=prec)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        for a, b in ev:
+            a.record(stream)
+            ip(x, precision=prec)
+            b.record(stream)
+        torch.cuda.synchronize()
+        return statistics.mean(a.elapsed_time(b) for a, b in ev)
+
+    with ClockSampler(0) as clk:
+        ms = timed("fp64", steps)
+        ms_b = timed("fp64_barycentric", min(steps, 3))
+    y, yb = ip(x), ip(x, precision="fp64_barycentric")
+    diff = float(((y - yb).abs() / yb.abs()).max())
+    terms = int(ip._tree.size)  # one FP64 multiply-add per entry of Lambda and point (the algorithmic work)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    peak = sms * 2 * 2.07e9  # GB300: 2 FP64 multiply-adds per SM and clock (ncu peak_sustained), 2070 MHz
+    line = {
+        "metric": METRIC, "workload": "fp64", "value": P * D_OUT / (ms * 1e-3), "unit": "evals/s", "n_gpus": 1,
+        "steps": steps, "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": "fp64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD + ", FP64 evaluation", "points": P, "d_in": D_IN, "d_out": D_OUT,
+                   "lambda": int(ip._tree.size)},
+        "form": "orthogonal polynomials in FP64 (csrc/spectral64.cu)",
+        "barycentric_ms": ms_b, "max_rel_diff_vs_barycentric": diff,
+        "roofline": {"bound": "fp64", "achieved": P * terms / (ms * 1e-3), "peak": peak, "unit": "DFMA/s",
+                     "frac": P * terms / (ms * 1e-3) / peak, "peak_kind": "nominal (2 per SM clock at 2070 MHz)"},
+        "clocks": clk.summary(),
+    }
+    del ip, x, y, yb
+    torch.cuda.empty_cache()
+    return line
+
+
 def quadrature_workload(max_samples=1 << 26):
     """The reference's quadrature study (notebooks/smolyak_quadrature.ipynb) on
     the GPU: Gauss-Hermite d_in=100, k_j = log((j+2)^2 / 0.1), f(x) = 1/(1 + 0.1
@@ -560,7 +616,7 @@ def serving_workload(n_req, rate):
         ips["ip%02d" % i] = SmolyakBarycentricInterpolator(node_gen=gen, k=k, t=t, d_out=d_out,
                                                             f=_vec_target_device(kind, d, d_out, i),
                                                             memory_limit=2.0)
-    server = Server(ips, memory_budget=48.0, n_streams=8)
+    server = Server(ips, memory_budget=48.0, n_streams=8, fast_work=2e11)
     setup_s = time.perf_counter() - t0
     rng = np.random.default_rng(1)
     pools = {}
@@ -568,8 +624,16 @@ def serving_workload(n_req, rate):
         kind = "leja" if isinstance(ip._node_gen, nodes.Leja) else "gh"
         xs = rng.uniform(-1, 1, (65536, ip.d_in)) if kind == "leja" else rng.normal(size=(65536, ip.d_in)) / np.sqrt(2)
         pools[name] = xs
-    reqs, arrivals = [], np.cumsum(rng.exponential(1.0 / rate, n_req))
+    # warm-up (not measured): each interpolant's evaluation and gradient at the
+    # largest batch, so that the allocator's blocks and the lazily built
+    # operands exist before the measured stream arrives
     names = sorted(ips)
+    warm = [Request(name, pools[name], op=op, precision="fp32") for name in names for op in ("eval", "grad")]
+    for r in warm:
+        server.submit(r)
+    server.drain()
+    server.reset_stats()
+    reqs, arrivals = [], np.cumsum(rng.exponential(1.0 / rate, n_req))
     for j in range(n_req):
         name = names[rng.integers(len(names))]
         P = int(np.exp(rng.uniform(0, np.log(65536))))
@@ -583,12 +647,15 @@ def serving_workload(n_req, rate):
     lat_e = np.array([r.latency for r in ev]) * 1e3
     lat_g = np.array([r.latency for r in reqs if r.op == "grad" and r.error is None]) * 1e3
     lat_s = np.array([r.latency for r in ev if r.points <= 4096]) * 1e3
+    lat_f = np.array([r.latency for r in ev if server.work(r) <= server.fast_work]) * 1e3
+    slow = sorted((r for r in reqs if r.error is None), key=lambda r: -r.latency)[:6]
     wait = np.array([r.t_admit - r.t_submit for r in reqs if r.error is None and r.t_admit is not None]) * 1e3
     line = {
         "metric": METRIC, "workload": "serving", "value": evals / wall, "unit": "evals/s", "n_gpus": 1,
         "higher_is_better": True, "dtype": "fp32", "data": "synthetic",
         "config": {"workload": "16 resident interpolants (d_in 4-1000, d_out 1-1024, |Lambda| 1e2-1e5, Leja/GH, seed 0);"
-                               " Poisson stream, 80% eval / 20% gradient, batch log-uniform [1, 65536]",
+                               " Poisson stream, 80% eval / 20% gradient, batch log-uniform [1, 65536];"
+                               " after one warm-up eval and gradient per interpolant at 65536 points",
                    "requests": n_req, "rate_per_s": rate},
         "latency_ms": {"p50": float(np.percentile(lat_e, 50)), "p99": float(np.percentile(lat_e, 99)),
                        "grad_p50": float(np.percentile(lat_g, 50)) if lat_g.size else None,
@@ -598,13 +665,19 @@ def serving_workload(n_req, rate):
                        "small_p50": float(np.percentile(lat_s, 50)) if lat_s.size else None,
                        "small_p99": float(np.percentile(lat_s, 99)) if lat_s.size else None,
                        "admit_wait_p50": float(np.percentile(wait, 50)),
-                       "admit_wait_p99": float(np.percentile(wait, 99))},
+                       "admit_wait_p99": float(np.percentile(wait, 99)),
+                       # evaluations on the high-priority streams (estimated work <= fast_work)
+                       "fast_p50": float(np.percentile(lat_f, 50)) if lat_f.size else None,
+                       "fast_p99": float(np.percentile(lat_f, 99)) if lat_f.size else None},
+        "slowest": [dict(ms=r.latency * 1e3, plan=r.name, points=r.points, op=r.op, gmac=server.work(r) / 1e9,
+                         wait_ms=(r.t_admit - r.t_submit) * 1e3) for r in slow],
         "wall_s": wall, "setup_s": setup_s, "launches": st["launches"], "merged_launches": st["batch_launches"],
         "high_priority_launches": st["fast_launches"],
         "completed": st["completed"], "rejected": st["rejected"], "clocks": clk.summary(),
         "fleet": [dict(d_in=d, d_out=o, lam=l, kind=kd, K=int(ips["ip%02d" % i]._tree.size),
                        tensor=ips["ip%02d" % i].spectral_plan().tc is not None) for i, d, o, l, kd in fleet],
     }
+    server.close()
     del server, ips
     torch.cuda.empty_cache()
     return line
@@ -764,7 +837,7 @@ def main():
     ap.add_argument("--points", type=int, default=POINTS)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="leja1000",
-                    choices=["leja1000", "serving", "leja64bwd", "quadrature"] + sorted(WORKLOADS))
+                    choices=["leja1000", "serving", "leja64bwd", "quadrature", "fp64"] + sorted(WORKLOADS))
     ap.add_argument("--requests", type=int, default=300)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--no-extras", action="store_true", help="headline only (skip the other configurations)")
@@ -778,6 +851,9 @@ def main():
         return 0
     if args.workload == "leja64bwd":
         return run_backward_workload(args)
+    if args.workload == "fp64":
+        print(json.dumps(fp64_workload(args.steps, args.warmup, args.points if args.points != POINTS else None)))
+        return 0
     if args.workload != "leja1000":
         return run_tensor_workload(args)
     return run_ours(args)

@@ -250,7 +250,7 @@ typedef struct smx_spectral {
   const int32_t* hot_soff;  /* [n_hot_dims] first basis slot                      */
   const int32_t* node;      /* [n_nodes][4] slot | depth << 16, prefix slot or -1, run range */
   const float* node_c;      /* [n_nodes][dstride] own coefficient                  */
-  const int32_t* cold;      /* [n_cold_groups][4] dim, run range, max degree | fam << 8 */
+  const int32_t* cold;      /* [n_cold_groups][4] dim, run range, max degree | fam << 16 */
   const float* cold_ab;     /* [n_cold_groups][2] affine map z = a x + b of the group */
   const int32_t* blk_dims;  /* [n_cold_blocks][4] the block's dimensions                */
   const int32_t* blk_run;   /* [n_cold_blocks][4] first slot, slot quads, coefficient offset, 0;
@@ -269,36 +269,41 @@ int smx_spectral_eval(const smx_spectral* plan_host, const double* x, int64_t P,
                       void* stream);
 
 /* FP64 evaluation of the orthogonal form, one output (the FP64 counterpart of
- * interpolation.py:264-304 for d_out = 1).  The same layout as smx_spectral
- * (built from the same index-set tree) with FP64 coefficients and affine maps;
- * `row` is the per-point row in doubles (even, >= n_hb + n_vp rounded up to
- * 4; 2 mod 4 keeps the 16-byte row reads free of bank conflicts), and the
- * block needs (row + 4) * 128 * 8 bytes of shared memory (<= 227 KB).  With
- * coefficients from smx_spectral_coefficients (compensated sums) the result is
- * within ~1e-14 relative of the exact value of the interpolant, where the
- * barycentric combination sum in FP64 cancels to 1e-13 .. 1e-10.  Non-finite
- * coordinates of active dimensions give NaN. */
+ * interpolation.py:264-304 for d_out = 1).  The per-point structure of
+ * smx_spectral -- hot basis values and the prefix products of the cold
+ * entries' parents in a row of `row` doubles per point (row >= n_hb + n_vp;
+ * odd keeps 8-byte reads of consecutive points on distinct banks; a block of
+ * 64 points needs (row + 4) * 64 * 8 bytes of shared memory, <= 227 KB) -- but every
+ * entry of Lambda is exactly one term (row slot, FP64 coefficient), without
+ * padding: at GB300's FP64 rate each term is a multiply-add that counts.
+ *   node[n_nodes][4]  slot | depth << 16, prefix slot or -1, term range of the
+ *                     hot leaf children (hot nodes in DFS pre-order, root first)
+ *   cold[G][4]        dimension, run range, max degree | family << 16 | unit << 20
+ *                     (unit: the map z = a x + b is the identity)
+ *   run[R][4]         term range, degree, 0 (runs of a group by degree)
+ *   terms[T][2]       slot (integer bits of the first double), coefficient
+ * With coefficients from smx_spectral_coefficients (compensated sums) the
+ * result is within ~1e-14 relative of the exact value of the interpolant,
+ * where the barycentric combination sum in FP64 cancels to 1e-13 .. 1e-10.
+ * Non-finite coordinates of active dimensions give NaN. */
 typedef struct smx_spectral64 {
   int32_t d_in;
   int32_t row;           /* doubles per point row                                  */
-  int32_t n_hb, n_vp, n_hot_dims, n_nodes, n_cold_groups, max_depth, n_cold_blocks;
-  int32_t node_seg[5], cold_seg[5], block_seg[5];
+  int32_t n_hb, n_vp, n_hot_dims, n_nodes, n_cold_groups, max_depth, n_terms;
+  int32_t node_seg[5], cold_seg[5];  /* the 4 work segments over nodes and cold groups */
   const int32_t* hot_dim;
   const int32_t* hot_deg;
   const int32_t* hot_soff;
-  const int32_t* node;      /* as smx_spectral                                       */
-  const double* node_c;     /* [n_nodes]                                             */
+  const int32_t* node;
+  const double* node_c;     /* [n_nodes] own coefficient (0 for the root)           */
   const int32_t* cold;
-  const double* cold_ab;    /* [n_cold_groups][2]                                    */
-  const int32_t* blk_dims;
-  const int32_t* blk_run;
-  const double* blk_ab;     /* [n_cold_blocks][2][4]                                 */
+  const double* cold_ab;    /* [G][2] a, b                                          */
   const int32_t* run;
-  const double* coef;       /* run coefficients (offsets multiples of 4)             */
-  const double* fam_a;      /* [d_in]                                                */
-  const double* fam_b;      /* [d_in]                                                */
-  const int32_t* fam;       /* [d_in]                                                */
-  double c0;                /* coefficient of the constant                           */
+  const double* terms;      /* [n_terms][2]                                         */
+  const double* fam_a;      /* [d_in]                                               */
+  const double* fam_b;      /* [d_in]                                               */
+  const int32_t* fam;       /* [d_in]                                               */
+  double c0;                /* coefficient of the constant                          */
 } smx_spectral64;
 
 /* y[P] (FP64) = the interpolant at the P rows of x (FP64, leading dimension ldx). */
@@ -554,10 +559,10 @@ int smx_layout_build(int kind, int64_t n, const int32_t* parent_host, const int3
                      const double* rem_host, const float* C_host, int d_out, const int64_t* maxdeg_host, int d,
                      const int32_t* fam_host, const double* fam_a_host, const double* fam_b_host,
                      smx_host_tables** out);
-/* The per-point layout with FP64 coefficients C[n][d_out] for the FP64
- * evaluator (smx_spectral64): kind SMX_LAYOUT_PERPOINT only; the coefficient
- * and map tables ("node_c", "coef", "cold_ab", "blk_ab") are read with
- * smx_layout_f64, "row" is the FP64 row. */
+/* The layout of the FP64 evaluator (smx_spectral64) from FP64 coefficients
+ * C[n] (one output): kind SMX_LAYOUT_PERPOINT only (its FP64 form); tables
+ * "node_c", "cold_ab", "terms" are read with smx_layout_f64, the others with
+ * smx_layout_i32 and smx_layout_scalar. */
 int smx_layout_build_f64(int kind, int64_t n, const int32_t* parent_host, const int32_t* dim_host,
                          const int32_t* deg_host, const int32_t* level_host, const int64_t* rank_host,
                          const double* rem_host, const double* C_host, int d_out, const int64_t* maxdeg_host, int d,

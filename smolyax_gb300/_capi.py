@@ -116,10 +116,9 @@ class SmxSpectral64(C.Structure):
         ("n_nodes", _i32),
         ("n_cold_groups", _i32),
         ("max_depth", _i32),
-        ("n_cold_blocks", _i32),
+        ("n_terms", _i32),
         ("node_seg", _i32 * 5),
         ("cold_seg", _i32 * 5),
-        ("block_seg", _i32 * 5),
         ("hot_dim", _p),
         ("hot_deg", _p),
         ("hot_soff", _p),
@@ -127,11 +126,8 @@ class SmxSpectral64(C.Structure):
         ("node_c", _p),
         ("cold", _p),
         ("cold_ab", _p),
-        ("blk_dims", _p),
-        ("blk_run", _p),
-        ("blk_ab", _p),
         ("run", _p),
-        ("coef", _p),
+        ("terms", _p),
         ("fam_a", _p),
         ("fam_b", _p),
         ("fam", _p),

@@ -388,16 +388,16 @@ extern "C" int smx_fp32_plan_create(const smx_plan* pl, const smx_tree* tree, co
     if (cudaStreamSynchronize(st) != cudaSuccess)  // the staging buffers go out of scope
       return smx::set_error(SMX_ERR_CUDA, "smx_fp32_plan_create: sync failed");
   }
-  // FP64 per-point tables (one output): the FP64 evaluator of the orthogonal form
+  // FP64 tables (one output): the FP64 evaluator of the orthogonal form
   if (dout == 1) {
     smx::layout::Tables p64;
-    if (smx::layout::build_perpoint(tr, C64_h.data(), 1, maxdeg.data(), d, fam_v.data(), fa_v.data(), fb_v.data(),
-                                    p64) &&
-        (int64_t(p64.scalar["row"]) + 4) * 128 * 8 <= 227 * 1024 && p64.scalar["max_depth"] <= 8) {
+    if (smx::layout::build_perpoint64(tr, C64_h.data(), maxdeg.data(), d, fam_v.data(), fa_v.data(), fb_v.data(),
+                                      p64) &&
+        (int64_t(p64.scalar["row"]) + 4) * 64 * 8 <= 227 * 1024 && p64.scalar["max_depth"] <= 8) {
       Pack<int32_t> pi;
       Pack<double> pf;
-      const char* names_i[] = {"hot_dim", "hot_deg", "hot_soff", "node", "cold", "run", "blk_dims", "blk_run"};
-      const char* names_f[] = {"node_c", "coef", "cold_ab", "blk_ab"};
+      const char* names_i[] = {"hot_dim", "hot_deg", "hot_soff", "node", "cold", "run"};
+      const char* names_f[] = {"node_c", "cold_ab", "terms"};
       for (const char* nm : names_i) pi.add(nm, p64.i32[nm]);
       for (const char* nm : names_f) pf.add(nm, p64.f64[nm]);
       if ((rc = h->ti64.upload(pi.v, st)) || (rc = h->tf64.upload(pf.v, st)) || (rc = h->fa64.upload(fa_v, st)) ||
@@ -412,11 +412,10 @@ extern "C" int smx_fp32_plan_create(const smx_plan* pl, const smx_tree* tree, co
       s.n_nodes = int(p64.scalar["n_nodes"]);
       s.n_cold_groups = int(p64.scalar["n_cold_groups"]);
       s.max_depth = int(p64.scalar["max_depth"]);
-      s.n_cold_blocks = int(p64.scalar["n_cold_blocks"]);
+      s.n_terms = int(p64.scalar["n_terms"]);
       for (int i = 0; i < 5; ++i) {
         s.node_seg[i] = p64.i32["node_seg"][i];
         s.cold_seg[i] = p64.i32["cold_seg"][i];
-        s.block_seg[i] = p64.i32["block_seg"][i];
       }
       auto ia = [&](const char* nm) { return pi.at(h->ti64.p, nm, p64.i32[nm]); };
       auto fa = [&](const char* nm) { return pf.at(h->tf64.p, nm, p64.f64[nm]); };
@@ -426,12 +425,9 @@ extern "C" int smx_fp32_plan_create(const smx_plan* pl, const smx_tree* tree, co
       s.node = ia("node");
       s.cold = ia("cold");
       s.run = ia("run");
-      s.blk_dims = ia("blk_dims");
-      s.blk_run = ia("blk_run");
       s.node_c = fa("node_c");
-      s.coef = fa("coef");
       s.cold_ab = fa("cold_ab");
-      s.blk_ab = fa("blk_ab");
+      s.terms = fa("terms");
       s.fam_a = h->fa64.p;
       s.fam_b = h->fb64.p;
       s.fam = h->fam.p;

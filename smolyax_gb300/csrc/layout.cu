@@ -57,19 +57,17 @@ int argmin(const double* v, int n) {
 }
 
 // Runs of the per-point evaluator (spectral.py _Runs): 4-aligned slot ranges
-// of at most 32 slots, gaps of at most 4, coefficients [length][dstride] of
-// type V (float for the FP32 evaluator, double for the FP64 one).
-template <typename V>
+// of at most 32 slots, gaps of at most 4, coefficients [length][dstride].
 struct Runs {
   int64_t dstride;
   std::vector<int32_t> tab;  // [n][4] start, length, coefficient offset, degree
-  std::vector<V> coef;
+  std::vector<float> coef;
   struct Range {
     int64_t first, second;
   };
   int64_t n() const { return int64_t(tab.size() / 4); }
   // slots increasing; coefs(i, o) = coefficient o of slot i
-  Range add(const std::vector<int64_t>& slots, const std::function<V(size_t, int)>& coefs, int d_out, int degree) {
+  Range add(const std::vector<int64_t>& slots, const std::function<float(size_t, int)>& coefs, int d_out, int degree) {
     const int64_t r0 = n();
     const size_t N = slots.size();
     for (size_t i = 0; i < N;) {
@@ -78,7 +76,7 @@ struct Runs {
       while (j < N && slots[j] - slots[j - 1] <= 4 && slots[j] - a0 < 32) ++j;
       const int64_t length = round4(slots[j - 1] + 1 - a0);
       const size_t base = coef.size();
-      coef.resize(base + size_t(length * dstride), V(0));
+      coef.resize(base + size_t(length * dstride), 0.f);
       for (size_t q = i; q < j; ++q)
         for (int o = 0; o < d_out; ++o) coef[base + size_t((slots[q] - a0) * dstride + o)] = coefs(q, o);
       tab.insert(tab.end(), {int32_t(a0), int32_t(length), int32_t(base), int32_t(degree)});
@@ -552,82 +550,100 @@ bool build_blocked_tc(const Tree& tr, const float* C, const int64_t* maxdeg, int
   return true;
 }
 
-static void put(Tables& t, const char* name, std::vector<float> v) { t.f32[name] = std::move(v); }
-static void put(Tables& t, const char* name, std::vector<double> v) { t.f64[name] = std::move(v); }
+// The structure shared by the per-point layouts (spectral.py _layout_front):
+// hot dimensions and basis slots, hot nodes in DFS pre-order, prefix slots of
+// the cold entries' parents by remaining budget (descending), hot leaves
+// sorted by (parent, slot) with each node's range.
+struct Front {
+  std::vector<int32_t> hot_dims, hot_deg, hot_soff;
+  int64_t n_hb = 0, n_vp = 0;
+  int max_depth = 0;
+  std::vector<int64_t> slot, vp_row, nodes, leaf, cold, starts, ends;
+};
 
-// Port of spectral.py build_layout (4 segments); coefficients and maps of type V.
-template <typename V>
-bool build_perpoint_t(const Tree& tr, const V* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
-                      const double* fa, const double* fb, Tables& out) {
-  constexpr int nseg = 4;
+Front front(const Tree& tr, const int64_t* maxdeg, int d) {
+  Front f;
   const int64_t n = tr.n;
-  const int64_t dstride = d_out == 1 ? 1 : round4(d_out);
-  auto Cv = [&](int64_t e, int o) { return C[e * d_out + o]; };
   std::vector<char> hot(d, 0);
   for (int64_t e = 1; e < n; ++e)
     if (tr.parent[e] > 0) hot[tr.dim[tr.parent[e]]] = 1;
-  std::vector<int32_t> hot_dims, hot_deg, hot_soff;
   std::vector<int64_t> hidx(d, -1);
-  int64_t n_hb = 0;
   for (int j = 0; j < d; ++j)
     if (hot[j]) {
-      hidx[j] = int64_t(hot_dims.size());
-      hot_dims.push_back(j);
-      hot_deg.push_back(int32_t(maxdeg[j]));
-      hot_soff.push_back(int32_t(n_hb));
-      n_hb += maxdeg[j];
+      hidx[j] = int64_t(f.hot_dims.size());
+      f.hot_dims.push_back(j);
+      f.hot_deg.push_back(int32_t(maxdeg[j]));
+      f.hot_soff.push_back(int32_t(f.n_hb));
+      f.n_hb += maxdeg[j];
     }
   std::vector<char> is_hot(n, 0);
   is_hot[0] = 1;
-  std::vector<int64_t> hot_e, cold_e;
+  std::vector<int64_t> hot_e;
   for (int64_t e = 1; e < n; ++e) {
     is_hot[e] = hot[tr.dim[e]];
-    (is_hot[e] ? hot_e : cold_e).push_back(e);
+    (is_hot[e] ? hot_e : f.cold).push_back(e);
   }
-  std::vector<int64_t> slot(n, -1);
-  for (int64_t e : hot_e) slot[e] = hot_soff[hidx[tr.dim[e]]] + tr.deg[e] - 1;
+  f.slot.assign(n, -1);
+  for (int64_t e : hot_e) f.slot[e] = f.hot_soff[hidx[tr.dim[e]]] + tr.deg[e] - 1;
   std::vector<char> hhc(n, 0), hcc(n, 0);
   for (int64_t e : hot_e) hhc[tr.parent[e]] = 1;
-  for (int64_t e : cold_e) hcc[tr.parent[e]] = 1;
+  for (int64_t e : f.cold) hcc[tr.parent[e]] = 1;
   std::vector<char> node_mask(n, 0);
   for (int64_t e = 0; e < n; ++e) node_mask[e] = is_hot[e] && (hhc[e] || hcc[e]);
   node_mask[0] = 1;
-  std::vector<int64_t> nodes;
   for (int64_t e = 0; e < n; ++e)
-    if (node_mask[e]) nodes.push_back(e);
-  std::stable_sort(nodes.begin(), nodes.end(), [&](int64_t a, int64_t b) { return tr.rank[a] < tr.rank[b]; });
+    if (node_mask[e]) f.nodes.push_back(e);
+  std::stable_sort(f.nodes.begin(), f.nodes.end(), [&](int64_t a, int64_t b) { return tr.rank[a] < tr.rank[b]; });
   std::vector<int64_t> S;
   for (int64_t e = 1; e < n; ++e)
     if (hcc[e]) S.push_back(e);
   std::stable_sort(S.begin(), S.end(), [&](int64_t a, int64_t b) { return -tr.rem[a] < -tr.rem[b]; });
-  std::vector<int64_t> vp_row(n, -1);
-  vp_row[0] = n_hb;
-  for (size_t i = 0; i < S.size(); ++i) vp_row[S[i]] = n_hb + 1 + int64_t(i);
-  const int64_t n_vp = 1 + int64_t(S.size());
-  int64_t row = round4(n_hb + n_vp);
-  if (sizeof(V) == 8)
-    row += 2;  // doubles: 2 mod 4 keeps the 16-byte row reads of 8 consecutive points conflict-free
-  else
-    while (row % 32 != 4) row += 4;
-  Runs<V> runs{dstride, {}, {}};
-  // leaf children of each node, sorted by (parent, slot)
-  std::vector<int64_t> leaf;
+  f.vp_row.assign(n, -1);
+  f.vp_row[0] = f.n_hb;
+  for (size_t i = 0; i < S.size(); ++i) f.vp_row[S[i]] = f.n_hb + 1 + int64_t(i);
+  f.n_vp = 1 + int64_t(S.size());
   for (int64_t e : hot_e)
-    if (!node_mask[e]) leaf.push_back(e);
-  std::stable_sort(leaf.begin(), leaf.end(), [&](int64_t a, int64_t b) {
-    return std::make_pair(tr.parent[a], slot[a]) < std::make_pair(tr.parent[b], slot[b]);
+    if (!node_mask[e]) f.leaf.push_back(e);
+  const std::vector<int64_t>& sl = f.slot;
+  std::stable_sort(f.leaf.begin(), f.leaf.end(), [&](int64_t a, int64_t b) {
+    return std::make_pair(tr.parent[a], sl[a]) < std::make_pair(tr.parent[b], sl[b]);
   });
+  for (int64_t e : f.nodes) {
+    f.max_depth = std::max(f.max_depth, int(tr.level[e]));
+    auto lo = std::lower_bound(f.leaf.begin(), f.leaf.end(), e, [&](int64_t v, int64_t key) { return tr.parent[v] < key; });
+    auto hi = std::upper_bound(f.leaf.begin(), f.leaf.end(), e, [&](int64_t key, int64_t v) { return key < tr.parent[v]; });
+    f.starts.push_back(int64_t(lo - f.leaf.begin()));
+    f.ends.push_back(int64_t(hi - f.leaf.begin()));
+  }
+  return f;
+}
+
+// Port of spectral.py build_layout (4 segments).
+bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
+                    const double* fa, const double* fb, Tables& out) {
+  constexpr int nseg = 4;
+  const int64_t dstride = d_out == 1 ? 1 : round4(d_out);
+  auto Cv = [&](int64_t e, int o) { return C[e * d_out + o]; };
+  Front f = front(tr, maxdeg, d);
+  const std::vector<int32_t>& hot_dims = f.hot_dims;
+  const std::vector<int32_t>& hot_deg = f.hot_deg;
+  const std::vector<int32_t>& hot_soff = f.hot_soff;
+  const std::vector<int64_t>& slot = f.slot;
+  const std::vector<int64_t>& vp_row = f.vp_row;
+  const std::vector<int64_t>& nodes = f.nodes;
+  const std::vector<int64_t>& cold_e = f.cold;
+  const int64_t n_hb = f.n_hb, n_vp = f.n_vp;
+  const int max_depth = f.max_depth;
+  int64_t row = round4(n_hb + n_vp);
+  while (row % 32 != 4) row += 4;
+  Runs runs{dstride, {}, {}};
   const int64_t NN = int64_t(nodes.size());
   std::vector<int32_t> node_tab(NN * 4);
-  std::vector<V> node_c(NN * dstride, V(0));
+  std::vector<float> node_c(NN * dstride, 0.f);
   std::vector<double> cost_nodes(NN);
-  int max_depth = 0;
-  for (int64_t e : nodes) max_depth = std::max(max_depth, int(tr.level[e]));
   for (int64_t i = 0; i < NN; ++i) {
     const int64_t e = nodes[i];
-    auto lo = std::lower_bound(leaf.begin(), leaf.end(), e, [&](int64_t v, int64_t key) { return tr.parent[v] < key; });
-    auto hi = std::upper_bound(leaf.begin(), leaf.end(), e, [&](int64_t key, int64_t v) { return key < tr.parent[v]; });
-    std::vector<int64_t> le(lo, hi), sl;
+    std::vector<int64_t> le(f.leaf.begin() + f.starts[i], f.leaf.begin() + f.ends[i]), sl;
     for (int64_t v : le) sl.push_back(slot[v]);
     const auto rr = runs.add(sl, [&](size_t q, int o) { return Cv(le[q], o); }, d_out, 0);
     const int64_t s0 = e != 0 ? slot[e] : 0;
@@ -661,7 +677,7 @@ bool build_perpoint_t(const Tree& tr, const V* C, int d_out, const int64_t* maxd
   }
   auto alpha0 = [&](int dd) { return fam[dd] == 0 ? 1.0 : sqrt(2.0); };
   std::vector<int32_t> blk_dims, blk_run;
-  std::vector<V> blk_ab;
+  std::vector<float> blk_ab;
   std::vector<double> cost_blk;
   for (size_t q = 0; q < simple.size(); q += 4) {
     const size_t np = std::min<size_t>(4, simple.size() - q);
@@ -675,17 +691,17 @@ bool build_perpoint_t(const Tree& tr, const V* C, int d_out, const int64_t* maxd
     sl.erase(std::unique(sl.begin(), sl.end()), sl.end());
     const int64_t a0 = sl.front() & ~int64_t(3);
     const int64_t n4 = (round4(sl.back() + 1) - a0) / 4;
-    std::vector<V> blk(size_t(n4 * 16), V(0));  // [slot][dimension]
+    std::vector<float> blk(size_t(n4 * 16), 0.f);  // [slot][dimension]
     for (size_t jj = 0; jj < np; ++jj)
       for (size_t r = simple[q + jj].first; r < simple[q + jj].second; ++r) {
         const int64_t v = ce[r];
         blk[size_t((vp_row[tr.parent[v]] - a0) * 4 + int64_t(jj))] = Cv(v, 0);
       }
-    V ab[8] = {0};
+    float ab[8] = {0};
     for (size_t jj = 0; jj < np; ++jj) {
       const int dd = dims4[jj];
-      ab[jj] = V(alpha0(dd) * fa[dd]);
-      ab[4 + jj] = V(alpha0(dd) * fb[dd]);
+      ab[jj] = float(alpha0(dd) * fa[dd]);
+      ab[4 + jj] = float(alpha0(dd) * fb[dd]);
     }
     while (dims4.size() < 4) dims4.push_back(dims4[0]);
     blk_dims.insert(blk_dims.end(), dims4.begin(), dims4.end());
@@ -695,7 +711,7 @@ bool build_perpoint_t(const Tree& tr, const V* C, int d_out, const int64_t* maxd
     cost_blk.push_back(16.0 + 9.0 * double(n4));
   }
   std::vector<int32_t> cold_tab;
-  std::vector<V> cold_ab;
+  std::vector<float> cold_ab;
   std::vector<double> cost_cold;
   for (const auto& b : general) {
     const int dd = tr.dim[ce[b.first]];
@@ -713,9 +729,9 @@ bool build_perpoint_t(const Tree& tr, const V* C, int d_out, const int64_t* maxd
       gmax = std::max(gmax, g);
       q = q2;
     }
-    cold_tab.insert(cold_tab.end(), {dd, int32_t(r_first), int32_t(runs.n()), int32_t(gmax | (fam[dd] << 8))});
-    cold_ab.push_back(V(fa[dd]));
-    cold_ab.push_back(V(fb[dd]));
+    cold_tab.insert(cold_tab.end(), {dd, int32_t(r_first), int32_t(runs.n()), int32_t(gmax | (fam[dd] << 16))});
+    cold_ab.push_back(float(fa[dd]));
+    cold_ab.push_back(float(fb[dd]));
     cost_cold.push_back(c);
   }
   std::vector<int64_t> allowed_nodes, all_cold, all_blk;
@@ -728,17 +744,17 @@ bool build_perpoint_t(const Tree& tr, const V* C, int d_out, const int64_t* maxd
   out.i32["block_seg"] = cuts(cost_blk, all_blk, nseg);
   out.i32["blk_dims"] = blk_dims;
   out.i32["blk_run"] = blk_run;
-  put(out, "blk_ab", std::move(blk_ab));
-  put(out, "cold_ab", std::move(cold_ab));
+  out.f32["blk_ab"] = blk_ab;
+  out.f32["cold_ab"] = cold_ab;
   out.i32["hot_dim"] = hot_dims;
   out.i32["hot_deg"] = hot_deg;
   out.i32["hot_soff"] = hot_soff;
   out.i32["node"] = node_tab;
-  put(out, "node_c", std::move(node_c));
+  out.f32["node_c"] = node_c;
   out.i32["cold"] = cold_tab;
   out.i32["run"] = runs.tab;
-  if (runs.coef.empty()) runs.coef.assign(4, V(0));
-  put(out, "coef", std::move(runs.coef));
+  if (runs.coef.empty()) runs.coef.assign(4, 0.f);
+  out.f32["coef"] = runs.coef;
   out.scalar["dstride"] = double(dstride);
   out.scalar["row"] = double(row);
   out.scalar["n_hb"] = double(n_hb);
@@ -751,14 +767,97 @@ bool build_perpoint_t(const Tree& tr, const V* C, int d_out, const int64_t* maxd
   return true;
 }
 
-bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
-                    const double* fa, const double* fb, Tables& out) {
-  return build_perpoint_t(tr, C, d_out, maxdeg, d, fam, fa, fb, out);
-}
-
-bool build_perpoint(const Tree& tr, const double* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
-                    const double* fa, const double* fb, Tables& out) {
-  return build_perpoint_t(tr, C, d_out, maxdeg, d, fam, fa, fb, out);
+// Port of spectral.py build_layout64: the FP64 evaluator's layout, every
+// entry of Lambda one term (slot, coefficient), no padding.
+bool build_perpoint64(const Tree& tr, const double* C, const int64_t* maxdeg, int d, const int32_t* fam,
+                      const double* fa, const double* fb, Tables& out) {
+  constexpr int nseg = 4;
+  const int64_t n = tr.n;
+  Front f = front(tr, maxdeg, d);
+  const int64_t row = (f.n_hb + f.n_vp) | 1;  // odd: 8-byte row reads of 16 consecutive points on distinct banks
+  std::vector<int64_t> t_slot;
+  std::vector<double> t_coef;
+  const int64_t NN = int64_t(f.nodes.size());
+  std::vector<int32_t> node_tab(NN * 4);
+  std::vector<double> node_c(NN, 0.0), cost_nodes(NN);
+  for (int64_t i = 0; i < NN; ++i) {
+    const int64_t e = f.nodes[i];
+    const int64_t t0 = int64_t(t_slot.size());
+    for (int64_t q = f.starts[i]; q < f.ends[i]; ++q) {
+      t_slot.push_back(f.slot[f.leaf[q]]);
+      t_coef.push_back(C[f.leaf[q]]);
+    }
+    node_tab[i * 4 + 0] = int32_t((e != 0 ? f.slot[e] : 0) | (int64_t(tr.level[e]) << 16));
+    node_tab[i * 4 + 1] = int32_t(e != 0 && f.vp_row[e] >= 0 ? f.vp_row[e] : -1);
+    node_tab[i * 4 + 2] = int32_t(t0);
+    node_tab[i * 4 + 3] = int32_t(t_slot.size());
+    if (e != 0) node_c[i] = C[e];
+    cost_nodes[i] = 4.0 + double(f.ends[i] - f.starts[i]);
+  }
+  std::vector<int64_t> ce = f.cold;
+  std::stable_sort(ce.begin(), ce.end(), [&](int64_t a, int64_t b) {
+    return std::make_tuple(tr.dim[a], tr.deg[a], f.vp_row[tr.parent[a]]) <
+           std::make_tuple(tr.dim[b], tr.deg[b], f.vp_row[tr.parent[b]]);
+  });
+  std::vector<int32_t> cold_tab, runs;
+  std::vector<double> cold_ab, cost_cold;
+  for (size_t i = 0; i < ce.size();) {
+    size_t j = i;
+    while (j < ce.size() && tr.dim[ce[j]] == tr.dim[ce[i]]) ++j;
+    const int dd = tr.dim[ce[i]];
+    const int32_t r_first = int32_t(runs.size() / 4);
+    int gmax = 0;
+    for (size_t q = i; q < j;) {
+      const int g = tr.deg[ce[q]];
+      size_t q2 = q;
+      while (q2 < j && tr.deg[ce[q2]] == g) ++q2;
+      const int64_t t0 = int64_t(t_slot.size());
+      for (size_t r = q; r < q2; ++r) {
+        t_slot.push_back(f.vp_row[tr.parent[ce[r]]]);
+        t_coef.push_back(C[ce[r]]);
+      }
+      runs.insert(runs.end(), {int32_t(t0), int32_t(t_slot.size()), g, 0});
+      gmax = std::max(gmax, g);
+      q = q2;
+    }
+    const int unit = fa[dd] == 1.0 && fb[dd] == 0.0 ? 1 : 0;
+    cold_tab.insert(cold_tab.end(), {dd, r_first, int32_t(runs.size() / 4), gmax | (fam[dd] << 16) | (unit << 20)});
+    cold_ab.push_back(fa[dd]);
+    cold_ab.push_back(fb[dd]);
+    cost_cold.push_back(3.0 + double(j - i) + 3.0 * gmax);
+    i = j;
+  }
+  std::vector<int64_t> allowed_nodes, all_cold;
+  for (int64_t i = 0; i <= NN; ++i)
+    if (i == NN || tr.level[f.nodes[i]] <= 1) allowed_nodes.push_back(i);
+  for (int64_t i = 0; i <= int64_t(cost_cold.size()); ++i) all_cold.push_back(i);
+  std::vector<double> terms(std::max<size_t>(t_slot.size(), 1) * 2, 0.0);
+  for (size_t q = 0; q < t_slot.size(); ++q) {
+    const int64_t bits = t_slot[q];
+    memcpy(&terms[2 * q], &bits, sizeof(bits));
+    terms[2 * q + 1] = t_coef[q];
+  }
+  out.i32["node_seg"] = cuts(cost_nodes, allowed_nodes, nseg);
+  out.i32["cold_seg"] = cuts(cost_cold, all_cold, nseg);
+  out.i32["hot_dim"] = f.hot_dims;
+  out.i32["hot_deg"] = f.hot_deg;
+  out.i32["hot_soff"] = f.hot_soff;
+  out.i32["node"] = node_tab;
+  out.i32["cold"] = cold_tab;
+  out.i32["run"] = runs;
+  out.f64["node_c"] = node_c;
+  out.f64["cold_ab"] = cold_ab;
+  out.f64["terms"] = terms;
+  out.scalar["row"] = double(row);
+  out.scalar["n_hb"] = double(f.n_hb);
+  out.scalar["n_vp"] = double(f.n_vp);
+  out.scalar["n_hot_dims"] = double(f.hot_dims.size());
+  out.scalar["n_nodes"] = double(NN);
+  out.scalar["n_cold_groups"] = double(cost_cold.size());
+  out.scalar["max_depth"] = double(f.max_depth);
+  out.scalar["n_terms"] = double(t_slot.size());
+  (void)n;
+  return true;
 }
 
 // Tape of the tensor-core panel (spectral.py build_tape): non-root entries in
@@ -848,10 +947,11 @@ extern "C" int smx_layout_build_f64(int kind, int64_t n, const int32_t* parent, 
                   fa && fb && C,
               "smx_layout_build_f64: bad arguments");
   SMX_REQUIRE(kind == SMX_LAYOUT_PERPOINT, "smx_layout_build_f64: only the per-point layout has an FP64 form");
+  SMX_REQUIRE(d_out == 1, "smx_layout_build_f64: the FP64 evaluator has one output");
   *out = nullptr;
   smx::layout::Tree tr{n, parent, dim, deg, level, rank, rem};
   auto h = std::make_unique<smx_host_tables>();
-  if (!smx::layout::build_perpoint(tr, C, d_out, maxdeg, d, fam, fa, fb, h->t))
+  if (!smx::layout::build_perpoint64(tr, C, maxdeg, d, fam, fa, fb, h->t))
     return smx::set_error(SMX_ERR_UNSUPPORTED, "smx_layout_build_f64: the plan is outside this evaluator's limits");
   *out = h.release();
   return SMX_OK;

@@ -519,7 +519,7 @@ __device__ __forceinline__ void spectral_eval_tile(const SpecArgs& a, const doub
   }
 
   // phase 2: cold groups of this segment.  Group descriptor: (dim, first
-  // run, end run, max degree | family << 8), affine map (a, b); runs carry
+  // run, end run, max degree | family << 16), affine map (a, b); runs carry
   // their degree in .w and are sorted by it.  The x column of group gi + 16
   // is prefetched into L2, the one of group gi + 1 into registers.
   {
@@ -541,7 +541,7 @@ __device__ __forceinline__ void spectral_eval_tile(const SpecArgs& a, const doub
         cg = __ldg(a.cold + gi + 1);
         xn = xp[cg.x];
       }
-      const int fm = cur.w >> 8;
+      const int fm = cur.w >> 16;
       const float z = fmaf(ab.x, x32(xv), ab.y);
       float pm1 = 0.f, pc = 1.f;
       int gcur = 0;

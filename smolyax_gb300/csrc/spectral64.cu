@@ -12,12 +12,14 @@
 // SM clock, the work per point is the bound: this evaluator does one DFMA per
 // term plus ~3 per hot basis value.
 //
-// Organisation as the FP32 per-point evaluator (spectral.cu): 128 points per
-// block, 16 warps = 4 point groups x 4 work segments; a row of `row` doubles
+// Organisation as the FP32 per-point evaluator (spectral.cu), with 64 points
+// per block: 8 warps = 2 point groups x 4 work segments; a row of `row` doubles
 // per point holds the hot basis values and the products of the hot prefixes
 // that cold entries extend; hot nodes are visited in DFS pre-order with the
-// path products on a register stack; cold blocks (4 degree-1 cold dimensions
-// over one run of prefix slots) and cold groups read their x column once.
+// path products on a register stack; each cold dimension reads its x column
+// once.  Unlike the FP32 layout, every entry of Lambda is exactly one term
+// (slot, coefficient) with no padding: a multiply-add per entry, with the
+// slot read from the term (a uniform 16-byte load), then the row value.
 #include <math.h>
 
 #include "common.cuh"
@@ -26,7 +28,8 @@
 namespace {
 
 constexpr int kSeg = 4;
-constexpr int kTP = 128;
+constexpr int kTP = 64;  // points per block: two blocks per SM when the row is <= ~215 doubles, so that
+                         // one block's load-bound basis phase overlaps the other's multiply-adds
 constexpr int kThreads = kSeg * kTP;
 constexpr int kMaxRec = 512;
 constexpr size_t kSmemMax = 227 * 1024;
@@ -35,7 +38,6 @@ struct Spec64Args {
   int d_in, row, n_hb, n_vp, n_hot_dims;
   int node_seg[kSeg + 1];
   int cold_seg[kSeg + 1];
-  int block_seg[kSeg + 1];
   const int32_t* hot_dim;
   const int32_t* hot_deg;
   const int32_t* hot_soff;
@@ -43,11 +45,8 @@ struct Spec64Args {
   const double* node_c;
   const int4* cold;
   const double2* cold_ab;
-  const int4* blk_dims;
-  const int4* blk_run;
-  const double2* blk_ab;  // per block: (a0, a1), (a2, a3), (b0, b1), (b2, b3)
   const int4* run;
-  const double* coef;
+  const double2* terms;  // (slot bits, coefficient)
   const double* fam_a;
   const double* fam_b;
   const int32_t* fam;
@@ -64,24 +63,18 @@ __device__ __forceinline__ double xin(double v) {
   return (b & 0x7fffffffffffffffll) == 0x7ff0000000000000ll ? __longlong_as_double(0x7ff8000000000000ll) : v;
 }
 
-// sum over a run's slots of coefficient * row value (length a multiple of 4,
-// start 4-aligned, coefficients 32-byte aligned): two chains of double2 pairs.
-__device__ __forceinline__ double dot_run64(const double* __restrict__ Rw, const double* __restrict__ coef, int4 r) {
-  const double2* T = reinterpret_cast<const double2*>(Rw + r.x);
-  const double2* Cq = reinterpret_cast<const double2*>(coef + r.z);
-  const int n2 = r.y >> 1;
-  double s0 = 0.0, s1 = 0.0;
-#pragma unroll 2
-  for (int k = 0; k < n2; ++k) {
-    const double2 t = T[k];
-    const double2 c = __ldg(Cq + k);
-    s0 = fma(c.x, t.x, s0);
-    s1 = fma(c.y, t.y, s1);
+// s + sum over the terms [t0, t1) of coefficient * row value
+__device__ __forceinline__ double sum_terms(const double* __restrict__ Rw, const double2* __restrict__ terms, int t0,
+                                            int t1, double s) {
+#pragma unroll 4
+  for (int t = t0; t < t1; ++t) {
+    const double2 tc = __ldg(terms + t);
+    s = fma(tc.y, Rw[__double2loint(tc.x)], s);
   }
-  return s0 + s1;
+  return s;
 }
 
-__global__ void __launch_bounds__(kThreads, 1) spectral_eval64_kernel(Spec64Args a, const double* __restrict__ x,
+__global__ void __launch_bounds__(kThreads, 2) spectral_eval64_kernel(Spec64Args a, const double* __restrict__ x,
                                                                       int64_t P, int64_t ldx,
                                                                       double* __restrict__ y) {
   extern __shared__ __align__(16) double sm64[];
@@ -95,9 +88,7 @@ __global__ void __launch_bounds__(kThreads, 1) spectral_eval64_kernel(Spec64Args
   double* Rw = sm64 + size_t(pl) * a.row;
 
   // phase 0: hot basis values phi_1..phi_g of every hot dimension; the empty
-  // prefix (= 1); zeros in the other prefix slots (phase 1 writes them, and
-  // the last run of hot leaves may extend into them with zero coefficients,
-  // which must not meet stale shared memory) and in the padding
+  // prefix (= 1); zeros in the other prefix slots and the padding
   for (int h = seg; h < a.n_hot_dims; h += kSeg) {
     const int dim = __ldg(a.hot_dim + h), g = __ldg(a.hot_deg + h), so = __ldg(a.hot_soff + h);
     const int fm = __ldg(a.fam + dim);
@@ -118,7 +109,7 @@ __global__ void __launch_bounds__(kThreads, 1) spectral_eval64_kernel(Spec64Args
 
   double acc = 0.0;
 
-  // phase 1: hot nodes of this segment: v_node * (c_node + sum of the runs of
+  // phase 1: hot nodes of this segment: v_node * (c_node + sum of the terms of
   // its leaf children); the node's product is stored for the cold entries
   {
     double st1 = 1.0, st2 = 1.0, st3 = 1.0, st4 = 1.0, st5 = 1.0, st6 = 1.0, st7 = 1.0, st8 = 1.0;
@@ -143,69 +134,22 @@ __global__ void __launch_bounds__(kThreads, 1) spectral_eval64_kernel(Spec64Args
         }
       }
       if (nd.y >= 0) Rw[nd.y] = v;
-      double s = __ldg(a.node_c + i);
-      for (int r = nd.z; r < nd.w; ++r) s += dot_run64(Rw, a.coef, __ldg(a.run + r));
-      acc = fma(v, s, acc);
+      acc = fma(v, sum_terms(Rw, a.terms, nd.z, nd.w, __ldg(a.node_c + i)), acc);
     }
   }
   __syncthreads();  // prefix products complete
 
-  // phase 2a: cold blocks: sum_j phi_1(z_j) * sum_s c[s][j] * prefix[s] over
-  // one run of prefix slots shared by the block's 4 dimensions (coefficients
-  // [slot][dimension], 16 per quad of slots)
-  {
-    const int b0 = a.block_seg[seg], b1 = a.block_seg[seg + 1];
-    int4 dn = b0 < b1 ? __ldg(a.blk_dims + b0) : make_int4(0, 0, 0, 0);
-    double xn0 = xp[dn.x], xn1 = xp[dn.y], xn2 = xp[dn.z], xn3 = xp[dn.w];
-    for (int bi = b0; bi < b1; ++bi) {
-      const double x0 = xn0, x1 = xn1, x2 = xn2, x3 = xn3;
-      if (bi + 8 < b1) {
-        const int4 pd = __ldg(a.blk_dims + bi + 8);
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(xp + pd.x));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(xp + pd.w));
-      }
-      if (bi + 1 < b1) {
-        dn = __ldg(a.blk_dims + bi + 1);
-        xn0 = xp[dn.x];
-        xn1 = xp[dn.y];
-        xn2 = xp[dn.z];
-        xn3 = xp[dn.w];
-      }
-      const int4 rr = __ldg(a.blk_run + bi);
-      const double2* T = reinterpret_cast<const double2*>(Rw + rr.x);
-      const double2* Cq = reinterpret_cast<const double2*>(a.coef + rr.z);
-      double u0 = 0.0, u1 = 0.0, u2 = 0.0, u3 = 0.0;
-      for (int k = 0; k < rr.y; ++k) {
-        const double2 t01 = T[2 * k], t23 = T[2 * k + 1];
-        const double ts[4] = {t01.x, t01.y, t23.x, t23.y};
-#pragma unroll
-        for (int s = 0; s < 4; ++s) {
-          const double2 clo = __ldg(Cq + 8 * k + 2 * s), chi = __ldg(Cq + 8 * k + 2 * s + 1);
-          u0 = fma(clo.x, ts[s], u0);
-          u1 = fma(clo.y, ts[s], u1);
-          u2 = fma(chi.x, ts[s], u2);
-          u3 = fma(chi.y, ts[s], u3);
-        }
-      }
-      const double2 a01 = __ldg(a.blk_ab + 4 * bi), a23 = __ldg(a.blk_ab + 4 * bi + 1);
-      const double2 f01 = __ldg(a.blk_ab + 4 * bi + 2), f23 = __ldg(a.blk_ab + 4 * bi + 3);
-      double v = fma(a01.x, xin(x0), f01.x) * u0;
-      v = fma(fma(a01.y, xin(x1), f01.y), u1, v);
-      v = fma(fma(a23.x, xin(x2), f23.x), u2, v);
-      v = fma(fma(a23.y, xin(x3), f23.y), u3, v);
-      acc += v;
-    }
-  }
-
-  // phase 2: cold groups: one cold dimension, runs sorted by degree
+  // phase 2: cold dimensions of this segment: per degree g (runs sorted by
+  // degree) phi_g(z) * sum of the terms over the prefix slots; the x column
+  // of group gi + 16 is prefetched into L2, the one of group gi + 1 into
+  // registers
   {
     const int g0 = a.cold_seg[seg], g1 = a.cold_seg[seg + 1];
     int4 cg = g0 < g1 ? __ldg(a.cold + g0) : make_int4(0, 0, 0, 0);
     double xn = g0 < g1 ? xp[cg.x] : 0.0;
     for (int gi = g0; gi < g1; ++gi) {
       const int4 cur = cg;
-      const double xv = xn;
-      const double2 ab = __ldg(a.cold_ab + gi);
+      const double xv = xin(xn);
       if (gi + 16 < g1) {
         const double* pf = xp + __ldg(&a.cold[gi + 16].x);
         asm volatile("prefetch.global.L2 [%0];" ::"l"(pf));
@@ -214,19 +158,24 @@ __global__ void __launch_bounds__(kThreads, 1) spectral_eval64_kernel(Spec64Args
         cg = __ldg(a.cold + gi + 1);
         xn = xp[cg.x];
       }
-      const int fm = cur.w >> 8;
-      const double z = fma(ab.x, xin(xv), ab.y);
-      double pm1 = 0.0, pc = 1.0;
-      int gcur = 0;
+      const int fm = (cur.w >> 16) & 0xf;
+      double z = xv;
+      if (!((cur.w >> 20) & 1)) {
+        const double2 ab = __ldg(a.cold_ab + gi);
+        z = fma(ab.x, xv, ab.y);
+      }
+      // phi_1 = alpha_0 z (alpha_0 = 1 for Legendre), then the recurrence
+      double pm1 = 1.0, pc = fm == 0 ? z : c_alpha64[fm][0] * z;
+      int gcur = 1;
       for (int r = cur.y; r < cur.z; ++r) {
         const int4 rr = __ldg(a.run + r);
-        while (gcur < rr.w) {
+        while (gcur < rr.z) {
           const double pn = fma(c_alpha64[fm][gcur] * z, pc, -c_beta64[fm][gcur] * pm1);
           pm1 = pc;
           pc = pn;
           ++gcur;
         }
-        acc = fma(pc, dot_run64(Rw, a.coef, rr), acc);
+        acc = fma(pc, sum_terms(Rw, a.terms, rr.x, rr.y, 0.0), acc);
       }
     }
   }
@@ -265,23 +214,18 @@ extern "C" int smx_spectral_eval64(const smx_spectral64* sp, const double* x, in
   const char* who = "smx_spectral_eval64";
   SMX_REQUIRE(sp != nullptr, "smx_spectral_eval64: null plan");
   SMX_REQUIRE(sp->fam && sp->fam_a && sp->fam_b && sp->node && sp->node_c && sp->n_nodes >= 1 &&
-                  (sp->n_hot_dims == 0 || (sp->hot_dim && sp->hot_deg && sp->hot_soff)),
+                  (sp->n_hot_dims == 0 || (sp->hot_dim && sp->hot_deg && sp->hot_soff)) &&
+                  (sp->n_terms == 0 || sp->terms) && (sp->n_cold_groups == 0 || (sp->cold && sp->cold_ab && sp->run)),
               "smx_spectral_eval64: incomplete plan");
   if (sp->max_depth > 8) return smx::set_error(SMX_ERR_UNSUPPORTED, std::string(who) + ": hot nodes deeper than 8");
-  const int need = (sp->n_hb + sp->n_vp + 3) / 4 * 4;
-  SMX_REQUIRE(sp->n_vp >= 1 && sp->row % 2 == 0 && sp->row >= need, "smx_spectral_eval64: bad row");
+  SMX_REQUIRE(sp->n_vp >= 1 && sp->row >= sp->n_hb + sp->n_vp, "smx_spectral_eval64: bad row");
   for (int i = 0; i < kSeg; ++i)
-    SMX_REQUIRE(sp->node_seg[i] <= sp->node_seg[i + 1] && sp->cold_seg[i] <= sp->cold_seg[i + 1] &&
-                    sp->block_seg[i] <= sp->block_seg[i + 1],
+    SMX_REQUIRE(sp->node_seg[i] <= sp->node_seg[i + 1] && sp->cold_seg[i] <= sp->cold_seg[i + 1],
                 "smx_spectral_eval64: segments not ordered");
   SMX_REQUIRE(sp->node_seg[0] == 0 && sp->node_seg[kSeg] == sp->n_nodes && sp->cold_seg[0] == 0 &&
-                  sp->cold_seg[kSeg] == sp->n_cold_groups && sp->block_seg[0] == 0 &&
-                  sp->block_seg[kSeg] == sp->n_cold_blocks,
+                  sp->cold_seg[kSeg] == sp->n_cold_groups,
               "smx_spectral_eval64: segments do not cover the plan");
-  SMX_REQUIRE(!sp->n_cold_groups || (sp->cold && sp->cold_ab), "smx_spectral_eval64: cold groups without tables");
-  SMX_REQUIRE(!sp->n_cold_blocks || (sp->blk_dims && sp->blk_run && sp->blk_ab),
-              "smx_spectral_eval64: cold blocks without tables");
-  SMX_REQUIRE(!sp->coef || aligned(sp->coef, 32), "smx_spectral_eval64: coefficients not 32-byte aligned");
+  SMX_REQUIRE(!sp->terms || aligned(sp->terms, 16), "smx_spectral_eval64: terms not 16-byte aligned");
   SMX_REQUIRE(P >= 0 && ldx >= sp->d_in, "smx_spectral_eval64: bad sizes");
   const size_t smem = (size_t(sp->row) + kSeg) * kTP * sizeof(double);
   if (smem > kSmemMax)
@@ -299,7 +243,6 @@ extern "C" int smx_spectral_eval64(const smx_spectral64* sp, const double* x, in
   for (int i = 0; i <= kSeg; ++i) {
     a.node_seg[i] = sp->node_seg[i];
     a.cold_seg[i] = sp->cold_seg[i];
-    a.block_seg[i] = sp->block_seg[i];
   }
   a.hot_dim = sp->hot_dim;
   a.hot_deg = sp->hot_deg;
@@ -308,11 +251,8 @@ extern "C" int smx_spectral_eval64(const smx_spectral64* sp, const double* x, in
   a.node_c = sp->node_c;
   a.cold = reinterpret_cast<const int4*>(sp->cold);
   a.cold_ab = reinterpret_cast<const double2*>(sp->cold_ab);
-  a.blk_dims = reinterpret_cast<const int4*>(sp->blk_dims);
-  a.blk_run = reinterpret_cast<const int4*>(sp->blk_run);
-  a.blk_ab = reinterpret_cast<const double2*>(sp->blk_ab);
   a.run = reinterpret_cast<const int4*>(sp->run);
-  a.coef = sp->coef;
+  a.terms = reinterpret_cast<const double2*>(sp->terms);
   a.fam_a = sp->fam_a;
   a.fam_b = sp->fam_b;
   a.fam = sp->fam;

@@ -35,13 +35,19 @@ of different interpolants and batch sizes:
   every normal stream busy is still admitted (the scan of the FIFO queue
   passes requests whose class has no free stream);
 * staging   -- inputs are copied from the request's numpy array into a pinned
-  host arena allocated once (no page-locking per request), then to the device
-  without blocking the host; results come back into the arena the same way.
+  host arena allocated once (no page-locking per request; the host copies run
+  on torch's intra-op threads), then to the device without blocking the host;
+  results come back into the arena the same way.
   When the arena is full, a launch takes a one-off pinned buffer instead
   (counted in ``stats()["staging_spills"]``);
 * completion -- each launch records a CUDA event; the loop polls the events,
   hands results to the requests, frees device memory, stream and staging
-  space, and admits requests that arrived meanwhile.  A launch that fails
+  space, and admits requests that arrived meanwhile.
+* host threads -- with ``host_threads`` > 0 the preparation of a launch
+  (staging copies, kernel launches) and the hand-back of its results run on a
+  pool of host threads, so that the copies of a large request do not hold up
+  the scheduling of the others (the copies and the CUDA calls release the
+  interpreter lock); with 0 everything runs on the caller's thread.  A launch that fails
   (an error raised while it is prepared) fails its requests with the message
   and gives back everything it took.
 
@@ -56,6 +62,7 @@ import collections
 import itertools
 import threading
 import time
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 import torch
@@ -171,7 +178,7 @@ class Server:
     flight; ``staging`` (GiB) is the size of the pinned host arena."""
 
     def __init__(self, interpolants: dict, memory_budget: float = 8.0, n_streams: int = 8, staging: float = 1.0,
-                 n_fast_streams: int = 4, fast_work: float = 5e9):
+                 n_fast_streams: int = 4, fast_work: float = 5e9, host_threads: int = 4):
         self.dev = torch.device("cuda", torch.cuda.current_device())
         self.sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
         self.ips = dict(interpolants)
@@ -200,6 +207,32 @@ class Server:
         self.launches = 0
         self.admitted = 0
         self.spilled = 0
+        self.pending = 0  # launches and completions handed to the host threads, not yet finished
+        self._building = {}  # stream -> group of a launch being prepared
+        self.pool = ThreadPoolExecutor(max_workers=host_threads) if host_threads > 0 else None
+
+    def close(self):
+        """Stop the host threads (after ``drain``)."""
+        if getattr(self, "pool", None) is not None:
+            self.pool.shutdown(wait=True)
+            self.pool = None
+
+    def _run(self, fn, *args):
+        """fn(*args) on a host thread of the pool, or here without one."""
+        if getattr(self, "pool", None) is None:
+            fn(*args)
+            return
+        with self.lock:
+            self.pending += 1
+
+        def task():
+            try:
+                fn(*args)
+            finally:
+                with self.lock:
+                    self.pending -= 1
+
+        self.pool.submit(task)
 
     # ------------------------------------------------------------------ interface
     def submit(self, req: Request) -> Request:
@@ -214,7 +247,7 @@ class Server:
 
     def idle(self):
         with self.lock:
-            return not self.waiting and not self.inflight
+            return not self.waiting and not self.inflight and not getattr(self, "pending", 0)
 
     def step(self):
         """One scheduling step: complete finished launches, then admit and launch."""
@@ -244,6 +277,8 @@ class Server:
             step = min(P, max(128, int(sp.memory_limit * 1024**3 // (8 * ldk)) // 128 * 128))
             b += P * d_out * 4 + 3 * P * ldo * 4 + P * d_in * 8  # cotangent, its TF32 split, dL/dx
             b += step * (ldk + 31) // 32 * 32 * 4 + capi.size("smx_spectral_vjp_x_workspace", bwd["n_slots"], step)
+        elif req.precision == "fp64" and ip._fp64_orthogonal() is not None:
+            b += P * d_out * 8  # the FP64 orthogonal evaluator takes no scratch
         elif req.precision == "fp64":
             per_point = capi.size("smx_eval_workspace", ip._plan.ref(), 1, 64)
             b += P * d_out * 8 + capi.size("smx_eval_workspace", ip._plan.ref(), min(P, max(1, ip._chunk(per_point))),
@@ -323,10 +358,13 @@ class Server:
             streams = {kind: (self.free_fast if kind[0] else self.free_streams).popleft() for kind in batches}
         now = time.perf_counter()
         for kind, batch in batches.items():
-            try:
-                self._launch_batch(kind, batch, streams[kind], now)
-            except Exception as e:  # the launch could not be prepared: fail its requests, give back what it took
-                self._fail(kind, batch, streams[kind], e)
+            self._run(self._prepare, kind, batch, streams[kind], now)
+
+    def _prepare(self, kind, batch, stream, now):
+        try:
+            self._launch_batch(kind, batch, stream, now)
+        except Exception as e:  # the launch could not be prepared: fail its requests, give back what it took
+            self._fail(kind, batch, stream, e)
 
     def _fail(self, kind, batch, stream, exc):
         msg = "%s: %s" % (type(exc).__name__, exc)
@@ -334,14 +372,14 @@ class Server:
             req.error = msg
             req.t_done = time.perf_counter()
             req.done.set()
-        g = getattr(self, "_building", None)
-        if g is not None and g.stream is stream and g.staged:
+        with self.lock:
+            g = getattr(self, "_building", {}).pop(stream, None)
+        if g is not None and g.staged:
             stream.synchronize()  # copies already queued from or into its staging ranges have finished
         with self.lock:
-            if g is not None and g.stream is stream:
+            if g is not None:
                 for off in g.staged:
                     self.arena.free(off)
-                self._building = None
             self.failed.extend(r for r, _ in batch)
             self.in_use -= sum(nb for _, nb in batch)
             self._release_stream(stream, kind[0])
@@ -357,14 +395,15 @@ class Server:
             return lambda shape, dtype: self.arena.view(off, shape, dtype)
         t = torch.empty(_staged_bytes(nbytes), dtype=torch.uint8, pin_memory=True)
         g.spill.append(t)
-        self.spilled += 1
+        with self.lock:
+            self.spilled += 1
         return lambda shape, dtype: t[: int(np.prod(shape)) * torch.tensor([], dtype=dtype).element_size()].view(
             dtype).view(*shape)
 
     def _h2d_into(self, g, req, dst):
         """Copy the request's input into the device rows dst (stream-ordered)."""
         view = self._stage(g, req.x.nbytes)(req.x.shape, torch.float64)
-        view.numpy()[...] = req.x
+        view.copy_(torch.from_numpy(req.x))  # host copy on torch's intra-op threads
         dst.copy_(view, non_blocking=True)
 
     def _d2h(self, g, y):
@@ -376,22 +415,22 @@ class Server:
     def _launch_batch(self, kind, batch, stream, now):
         g = _Group(stream, [r for r, _ in batch], sum(nb for _, nb in batch))
         g.fast = kind[0]
-        self._building = g
-        with torch.cuda.stream(stream):
+        with self.lock:
+            self._building[stream] = g
+        with torch.cuda.device(self.dev), torch.cuda.stream(stream):
             for req, _ in batch:
                 req.t_admit = now
             if kind[1] in ("blocked", "stream"):
                 self._launch_multiplan(kind[1], batch, g)
-                self.batch_launches += 1
             else:
                 self._launch_plan(kind[1:], batch, g)
-                if len(batch) > 1:
-                    self.batch_launches += 1
             g.event.record(stream)
-        self._building = None
-        self.launches += 1
-        self.fast_launches += int(kind[0])
-        self.inflight.append(g)
+        with self.lock:
+            self._building.pop(stream, None)
+            self.launches += 1
+            self.fast_launches += int(kind[0])
+            self.batch_launches += int(kind[1] in ("blocked", "stream") or len(batch) > 1)
+            self.inflight.append(g)
 
     def _release_stream(self, stream, fast):
         (self.free_fast if fast else self.free_streams).append(stream)
@@ -457,24 +496,38 @@ class Server:
 
     # ------------------------------------------------------------------ completion
     def _poll(self):
-        done = [g for g in self.inflight if g.event.query()]
-        if not done:
-            return
-        now = time.perf_counter()
+        with self.lock:
+            done = [g for g in self.inflight if g.event.query()]
+            for g in done:
+                self.inflight.remove(g)
         for g in done:
-            self.inflight.remove(g)
-            for req, h in zip(g.reqs, g.host):
-                req.result = h.numpy().copy()
-                req.t_done = now
-                req.done.set()
-                self.completed.append(req)
-            with self.lock:
-                for off in g.staged:
-                    self.arena.free(off)
-                self.in_use -= g.nbytes
-                self._release_stream(g.stream, g.fast)
+            self._run(self._complete, g)
+
+    def _complete(self, g):
+        """Hand a finished launch's results to its requests (a request is done
+        when its result is in its own host array) and give back the launch's
+        staging space, memory and stream."""
+        for req, h in zip(g.reqs, g.host):
+            out = torch.empty(tuple(h.shape), dtype=h.dtype)
+            out.copy_(h)  # out of the staging arena, on torch's intra-op threads
+            req.result = out.numpy()
+            req.t_done = time.perf_counter()
+            req.done.set()
+        with self.lock:
+            self.completed.extend(g.reqs)
+            for off in g.staged:
+                self.arena.free(off)
+            self.in_use -= g.nbytes
+            self._release_stream(g.stream, g.fast)
 
     # ------------------------------------------------------------------ statistics
+    def reset_stats(self):
+        """Forget completed, rejected and failed requests and zero the launch
+        counters (e.g. after a warm-up); requests in flight are unaffected."""
+        with self.lock:
+            self.completed, self.rejected, self.failed = [], [], []
+            self.batch_launches = self.launches = self.fast_launches = self.admitted = self.spilled = 0
+
     def stats(self):
         lat = np.array([r.latency for r in self.completed]) if self.completed else np.zeros(1)
         evals = sum(r.points * self.ips[r.name].d_out for r in self.completed if r.op == "eval")

@@ -405,23 +405,21 @@ class SpectralPlan:
             tr, _, maxdeg, fam, fa, fb, T, _ = self._fwd_args
             d = int(self.c.d_in)
             if self.c.d_out == 1:
-                lay = build_layout(tr, self.C64.cpu().numpy(), maxdeg, d, 1, fam, fa, fb, dtype=np.float64)
+                lay = build_layout64(tr, self.C64.cpu().numpy(), maxdeg, d, fam, fa, fb)
                 row = int(lay["row"])
-                if (row + 4) * 128 * 8 <= 227 * 1024 and int(lay["max_depth"]) <= 8:
+                if (row + 4) * 64 * 8 <= 227 * 1024 and int(lay["max_depth"]) <= 8:
                     k = {}
-                    for name in ("hot_dim", "hot_deg", "hot_soff", "node", "cold", "run", "blk_dims", "blk_run"):
+                    for name in ("hot_dim", "hot_deg", "hot_soff", "node", "cold", "run"):
                         k[name] = T(lay[name], torch.int32)
-                    for name in ("node_c", "coef", "cold_ab", "blk_ab"):
+                    for name in ("node_c", "cold_ab", "terms"):
                         k[name] = T(lay[name], torch.float64)
                     st = capi.SmxSpectral64()
                     st.d_in, st.row = d, row
-                    for name in ("n_hb", "n_vp", "n_hot_dims", "n_nodes", "n_cold_groups", "max_depth",
-                                 "n_cold_blocks"):
+                    for name in ("n_hb", "n_vp", "n_hot_dims", "n_nodes", "n_cold_groups", "max_depth", "n_terms"):
                         setattr(st, name, int(lay[name]))
                     for i in range(5):
                         st.node_seg[i] = int(lay["node_seg"][i])
                         st.cold_seg[i] = int(lay["cold_seg"][i])
-                        st.block_seg[i] = int(lay["block_seg"][i])
                     for name, t in k.items():
                         setattr(st, name, t.data_ptr() if t.numel() else None)
                     st.fam_a, st.fam_b, st.fam = self.fa64.data_ptr(), self.fb64.data_ptr(), self.fam.data_ptr()
@@ -582,9 +580,8 @@ def _round32(v):
 class _Runs:
     """Accumulates runs (4-aligned slot ranges with contiguous coefficients)."""
 
-    def __init__(self, dstride, dtype=np.float32):
+    def __init__(self, dstride):
         self.dstride = dstride
-        self.dtype = dtype
         self.tab = []
         self.coef = []
         self.ncoef = 0
@@ -602,7 +599,7 @@ class _Runs:
             while j < n and slots[j] - slots[j - 1] <= max_gap and slots[j] - a0 < max_len:
                 j += 1
             length = _round4(int(slots[j - 1]) + 1 - a0)
-            blk = np.zeros((length, self.dstride), dtype=self.dtype)
+            blk = np.zeros((length, self.dstride), dtype=np.float32)
             blk[np.asarray(slots[i:j]) - a0, : coefs.shape[1]] = coefs[i:j]
             self.tab.append((a0, length, self.ncoef, degree))
             self.coef.append(blk.ravel())
@@ -611,16 +608,14 @@ class _Runs:
         return r0, len(self.tab)
 
 
-def build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb, nseg=4, dtype=np.float32):
-    """Layout of the per-point evaluators (``csrc/spectral.cu``, FP32, and
-    ``csrc/spectral64.cu``, FP64 with ``dtype=np.float64``) from the index-set
-    tree (host arrays: parent, dim, deg, level, pre-order rank, remaining budget)
-    and the coefficients C[entry, d_out]; fam/fa/fb are the per-dimension
-    polynomial family and affine map to its variable.  The tables' structure
-    depends on the tree alone; coefficients and maps are stored in ``dtype``."""
+def _layout_front(tr, maxdeg, d):
+    """The structure shared by the per-point layouts (FP32 and FP64): hot
+    dimensions and their basis slots, hot nodes in DFS pre-order, the prefix
+    slots of the cold entries' parents (by remaining budget, descending: the
+    prefixes admissible for a cold pair are then (mostly) a leading range), and
+    each node's hot leaf children sorted by slot."""
     parent, dim, deg, level, rank, rem = (tr[key] for key in ("parent", "dim", "deg", "level", "rank", "rem"))
     n = parent.shape[0]
-    dstride = 1 if d_out == 1 else _round4(d_out)
     nonroot = np.arange(1, n)
     hot = np.zeros(d, dtype=bool)
     inner = nonroot[parent[nonroot] > 0]
@@ -646,33 +641,54 @@ def build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb, nseg=4, dtype=np.float32)
     node_mask[0] = True
     nodes = np.nonzero(node_mask)[0]
     nodes = nodes[np.argsort(rank[nodes], kind="stable")]
-    # prefix-product slots, ordered by remaining budget (descending): the
-    # prefixes admissible for a cold pair are then (mostly) a leading range
     S = np.nonzero(has_cold_child)[0]
     S = S[S != 0]
     S = S[np.argsort(-rem[S], kind="stable")]
     vp_row = np.full(n, -1, dtype=np.int64)
     vp_row[0] = n_hb
     vp_row[S] = n_hb + 1 + np.arange(S.size)
-    n_vp = 1 + S.size
-    row = _round4(n_hb + n_vp)
-    if np.dtype(dtype).itemsize == 8:
-        row += 2  # doubles: 2 mod 4 keeps the 16-byte row reads of 8 consecutive points conflict-free
-    else:
-        while row % 32 != 4:
-            row += 4
-    runs = _Runs(dstride, dtype)
-    # leaf children of each node, sorted by slot
     leaf_e = hot_e[~node_mask[hot_e]]
-    order = np.lexsort((slot[leaf_e], parent[leaf_e]))
-    leaf_e = leaf_e[order]
+    leaf_e = leaf_e[np.lexsort((slot[leaf_e], parent[leaf_e]))]
     lp = parent[leaf_e]
-    starts = np.searchsorted(lp, nodes, side="left")
-    ends = np.searchsorted(lp, nodes, side="right")
+    return dict(parent=parent, dim=dim, deg=deg, level=level, hot_dims=hot_dims, hot_deg=hot_deg, hot_soff=hot_soff,
+                n_hb=n_hb, cold_e=cold_e, slot=slot, nodes=nodes, vp_row=vp_row, n_vp=1 + S.size, leaf_e=leaf_e,
+                starts=np.searchsorted(lp, nodes, side="left"), ends=np.searchsorted(lp, nodes, side="right"),
+                max_depth=int(level[nodes].max()) if nodes.size else 0)
+
+
+def _cuts(cost, allowed, nseg):
+    """Segment boundaries: boundary k is the allowed index whose cumulative
+    cost is nearest k/nseg of the total (the first such, not before the
+    previous boundary)."""
+    tot = float(np.sum(cost))
+    cum = np.concatenate([[0.0], np.cumsum(cost)])
+    out = [0]
+    for k in range(1, nseg):
+        want = tot * k / nseg
+        cand = [a for a in allowed if a >= out[-1]]
+        out.append(min(cand, key=lambda a: abs(cum[a] - want)) if cand else out[-1])
+    out.append(len(cost))
+    return out
+
+
+def build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb, nseg=4):
+    """Layout of the FP32 per-point evaluator (see ``csrc/spectral.cu``) from
+    the index-set tree (host arrays: parent, dim, deg, level, pre-order rank,
+    remaining budget) and the FP32 coefficients C[entry, d_out]; fam/fa/fb are
+    the per-dimension polynomial family and affine map to its variable."""
+    fr = _layout_front(tr, maxdeg, d)
+    parent, dim, deg, level = fr["parent"], fr["dim"], fr["deg"], fr["level"]
+    hot_dims, hot_deg, hot_soff, n_hb = fr["hot_dims"], fr["hot_deg"], fr["hot_soff"], fr["n_hb"]
+    cold_e, slot, nodes, vp_row, n_vp = fr["cold_e"], fr["slot"], fr["nodes"], fr["vp_row"], fr["n_vp"]
+    leaf_e, starts, ends, max_depth = fr["leaf_e"], fr["starts"], fr["ends"], fr["max_depth"]
+    dstride = 1 if d_out == 1 else _round4(d_out)
+    row = _round4(n_hb + n_vp)
+    while row % 32 != 4:
+        row += 4
+    runs = _Runs(dstride)
     node_tab = np.zeros((nodes.size, 4), dtype=np.int64)
-    node_c = np.zeros((nodes.size, dstride), dtype=dtype)
+    node_c = np.zeros((nodes.size, dstride), dtype=np.float32)
     cost_nodes = np.zeros(nodes.size)
-    max_depth = int(level[nodes].max()) if nodes.size else 0
     for i, e in enumerate(nodes):
         le = leaf_e[starts[i] : ends[i]]
         r0, r1 = runs.add(slot[le], C[le])
@@ -702,11 +718,11 @@ def build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb, nseg=4, dtype=np.float32)
         slots = np.unique(np.concatenate([vp_row[parent[ce[b0:b1]]] for b0, b1 in part]))
         a0 = int(slots[0]) & ~3
         n4 = (_round4(int(slots[-1]) + 1) - a0) // 4
-        blk = np.zeros((n4 * 4, 4), dtype=dtype)  # [slot][dim]
+        blk = np.zeros((n4 * 4, 4), dtype=np.float32)  # [slot][dim]
         for jj, (b0, b1) in enumerate(part):
             e = ce[b0:b1]
             blk[vp_row[parent[e]] - a0, jj] = C[e, 0]
-        ab = np.zeros((2, 4), dtype=dtype)
+        ab = np.zeros((2, 4), dtype=np.float32)
         for jj, dd in enumerate(dims4):
             ab[0, jj] = alpha0[dd] * fa[dd]
             ab[1, jj] = alpha0[dd] * fb[dd]
@@ -734,25 +750,14 @@ def build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb, nseg=4, dtype=np.float32)
             r0, r1 = runs.add(vp_row[parent[grp]], C[grp], degree=int(g))
             c += sum(3 + t[1] / 4.0 * (1 + d_out) for t in runs.tab[r0:r1])
             q = q2
-        cold_tab.append((int(dd), r_first, len(runs.tab), int(deg[ce[i:j]].max()) | (int(fam[dd]) << 8)))
+        cold_tab.append((int(dd), r_first, len(runs.tab), int(deg[ce[i:j]].max()) | (int(fam[dd]) << 16)))
         cold_ab.append((fa[dd], fb[dd]))
         cost_cold.append(c)
 
-    def cuts(cost, allowed):
-        tot = float(np.sum(cost))
-        cum = np.concatenate([[0.0], np.cumsum(cost)])
-        out = [0]
-        for k in range(1, nseg):
-            want = tot * k / nseg
-            cand = [a for a in allowed if a >= out[-1]]
-            out.append(min(cand, key=lambda a: abs(cum[a] - want)) if cand else out[-1])
-        out.append(len(cost))
-        return out
-
     allowed_nodes = [i for i in range(nodes.size + 1) if i == nodes.size or level[nodes[i]] <= 1]
-    node_seg = cuts(cost_nodes, allowed_nodes)
-    cold_seg = cuts(np.asarray(cost_cold), list(range(len(cost_cold) + 1)))
-    block_seg = cuts(np.asarray(cost_blk), list(range(len(cost_blk) + 1)))
+    node_seg = _cuts(cost_nodes, allowed_nodes, nseg)
+    cold_seg = _cuts(np.asarray(cost_cold), list(range(len(cost_cold) + 1)), nseg)
+    block_seg = _cuts(np.asarray(cost_blk), list(range(len(cost_blk) + 1)), nseg)
     as_i32 = lambda v, w: np.asarray(v, dtype=np.int64).reshape(-1, w).astype(np.int32)
     return dict(
         dstride=dstride, row=row, n_hb=n_hb, n_vp=n_vp, n_hot_dims=int(hot_dims.size), n_nodes=int(nodes.size),
@@ -760,16 +765,121 @@ def build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb, nseg=4, dtype=np.float32)
         n_cold_blocks=len(blk_dims), block_seg=block_seg,
         blk_dims=as_i32(blk_dims, 4) if blk_dims else np.zeros((0, 4), np.int32),
         blk_run=as_i32(blk_run, 4) if blk_run else np.zeros((0, 4), np.int32),
-        blk_ab=np.asarray(blk_ab, dtype=dtype).reshape(-1, 8),
-        cold_ab=np.asarray(cold_ab, dtype=dtype).reshape(-1, 2),
+        blk_ab=np.asarray(blk_ab, dtype=np.float32).reshape(-1, 8),
+        cold_ab=np.asarray(cold_ab, dtype=np.float32).reshape(-1, 2),
         hot_dim=hot_dims.astype(np.int32), hot_deg=hot_deg.astype(np.int32), hot_soff=hot_soff.astype(np.int32),
         node=as_i32(node_tab, 4), node_c=node_c, cold=as_i32(cold_tab, 4) if cold_tab else np.zeros((0, 4), np.int32),
         run=as_i32(runs.tab, 4) if runs.tab else np.zeros((0, 4), np.int32),
-        coef=np.concatenate(runs.coef) if runs.coef else np.zeros(4, dtype),
+        coef=np.concatenate(runs.coef) if runs.coef else np.zeros(4, np.float32),
         cost=dict(nodes=float(cost_nodes.sum()), cold=float(np.sum(cost_cold)), blocks=float(np.sum(cost_blk)),
                   runs=len(runs.tab), coef_floats=int(runs.ncoef), node_seg=node_seg, cold_seg=cold_seg,
                   block_seg=block_seg),
     )
+
+
+def build_layout64(tr, C, maxdeg, d, fam, fa, fb, nseg=4):
+    """Layout of the FP64 evaluator of the orthogonal form (one output,
+    ``csrc/spectral64.cu``): the per-point structure of ``build_layout`` with
+    every entry of Lambda as exactly one term (row slot, FP64 coefficient) and
+    no padding -- at GB300's FP64 rate every term is a multiply-add that
+    counts.  Hot nodes (DFS pre-order) carry the terms of their hot leaf
+    children; each cold dimension is a group whose runs (one per degree) hold
+    the terms over the prefix slots.  ``terms`` is [n_terms, 2] FP64 with the
+    slot's integer bits in column 0.  C: FP64 coefficients of every entry."""
+    C = np.asarray(C, dtype=np.float64).reshape(-1)
+    fr = _layout_front(tr, maxdeg, d)
+    dim, deg, level, parent = fr["dim"], fr["deg"], fr["level"], fr["parent"]
+    n_hb, n_vp, nodes, slot, vp_row = fr["n_hb"], fr["n_vp"], fr["nodes"], fr["slot"], fr["vp_row"]
+    leaf_e, starts, ends, cold_e = fr["leaf_e"], fr["starts"], fr["ends"], fr["cold_e"]
+    row = (n_hb + n_vp) | 1  # odd: 8-byte row reads of 16 consecutive points fall on distinct banks
+    t_slot, t_coef = [], []
+    node_tab = np.zeros((nodes.size, 4), dtype=np.int64)
+    node_c = np.zeros(nodes.size)
+    cost_nodes = np.zeros(nodes.size)
+    for i, e in enumerate(nodes):
+        le = leaf_e[starts[i] : ends[i]]
+        t0 = len(t_slot)
+        t_slot.extend(slot[le].tolist())
+        t_coef.extend(C[le].tolist())
+        sl = int(slot[e]) if e != 0 else 0
+        node_tab[i] = (sl | (int(level[e]) << 16), int(vp_row[e]) if e != 0 and vp_row[e] >= 0 else -1, t0,
+                       len(t_slot))
+        if e != 0:  # the root's coefficient is c0
+            node_c[i] = C[e]
+        cost_nodes[i] = 4 + le.size
+    ce = cold_e[np.lexsort((vp_row[parent[cold_e]], deg[cold_e], dim[cold_e]))] if cold_e.size else cold_e
+    cold_tab, cold_ab, runs, cost_cold = [], [], [], []
+    i = 0
+    while i < ce.size:
+        j = i
+        while j < ce.size and dim[ce[j]] == dim[ce[i]]:
+            j += 1
+        dd = int(dim[ce[i]])
+        r_first = len(runs)
+        q = i
+        while q < j:
+            g = int(deg[ce[q]])
+            q2 = q
+            while q2 < j and deg[ce[q2]] == g:
+                q2 += 1
+            grp = ce[q:q2]
+            t0 = len(t_slot)
+            t_slot.extend(vp_row[parent[grp]].tolist())
+            t_coef.extend(C[grp].tolist())
+            runs.append((t0, len(t_slot), g, 0))
+            q = q2
+        gmax = int(deg[ce[i:j]].max())
+        unit = int(fa[dd] == 1.0 and fb[dd] == 0.0)
+        cold_tab.append((dd, r_first, len(runs), gmax | (int(fam[dd]) << 16) | (unit << 20)))
+        cold_ab.append((fa[dd], fb[dd]))
+        cost_cold.append(3.0 + (j - i) + 3.0 * gmax)
+        i = j
+    allowed_nodes = [q for q in range(nodes.size + 1) if q == nodes.size or level[nodes[q]] <= 1]
+    terms = np.zeros((max(len(t_slot), 1), 2))
+    terms[: len(t_slot), 0] = np.asarray(t_slot, dtype=np.int64).view(np.float64)
+    terms[: len(t_slot), 1] = t_coef
+    as_i32 = lambda v, w: np.asarray(v, dtype=np.int64).reshape(-1, w).astype(np.int32)
+    return dict(
+        row=row, n_hb=n_hb, n_vp=n_vp, n_hot_dims=int(fr["hot_dims"].size), n_nodes=int(nodes.size),
+        n_cold_groups=len(cold_tab), max_depth=fr["max_depth"], n_terms=len(t_slot),
+        node_seg=_cuts(cost_nodes, allowed_nodes, nseg), cold_seg=_cuts(np.asarray(cost_cold), list(range(len(cost_cold) + 1)), nseg),
+        hot_dim=fr["hot_dims"].astype(np.int32), hot_deg=fr["hot_deg"].astype(np.int32),
+        hot_soff=fr["hot_soff"].astype(np.int32), node=as_i32(node_tab, 4), node_c=node_c,
+        cold=as_i32(cold_tab, 4) if cold_tab else np.zeros((0, 4), np.int32),
+        cold_ab=np.asarray(cold_ab, dtype=np.float64).reshape(-1, 2),
+        run=as_i32(runs, 4) if runs else np.zeros((0, 4), np.int32), terms=terms,
+    )
+
+
+def evaluate_layout64(lay, x, fam, fa, fb, c0):
+    """Host FP64 replay of the FP64 evaluator's sums over a layout (tests)."""
+    P = x.shape[0]
+    R = np.zeros((P, lay["row"]))
+    hd, hg, ho = lay["hot_dim"], lay["hot_deg"], lay["hot_soff"]
+    for q in range(hd.size):
+        R[:, ho[q] : ho[q] + hg[q]] = _phi_table(int(fam[hd[q]]), fa[hd[q]] * x[:, hd[q]] + fb[hd[q]], int(hg[q]))[1:].T
+    R[:, lay["n_hb"]] = 1.0
+    slots = lay["terms"][: lay["n_terms"], 0].view(np.int64)
+    coef = lay["terms"][: lay["n_terms"], 1]
+    acc = np.full(P, float(c0))
+    stack = [np.ones(P)] * 9
+    for i, nd in enumerate(lay["node"]):
+        depth = int(nd[0]) >> 16
+        v = np.ones(P) if depth == 0 else (R[:, int(nd[0]) & 0xFFFF] if depth == 1 else stack[depth - 1] * R[:, int(nd[0]) & 0xFFFF])
+        stack[depth] = v
+        if nd[1] >= 0:
+            R[:, nd[1]] = v
+        s = lay["node_c"][i] + R[:, slots[nd[2] : nd[3]]] @ coef[nd[2] : nd[3]]
+        acc += v * s
+    for g, cg in enumerate(lay["cold"]):
+        dd, r0, r1, w = (int(v) for v in cg)
+        z = lay["cold_ab"][g, 0] * x[:, dd] + lay["cold_ab"][g, 1]
+        gmax = w & 0xFFFF
+        ph = _phi_table((w >> 16) & 0xF, z, gmax)
+        for r in range(r0, r1):
+            t0, t1, gg, _ = (int(v) for v in lay["run"][r])
+            acc += ph[gg] * (R[:, slots[t0:t1]] @ coef[t0:t1])
+    return acc
 
 
 def evaluate_layout(lay, x, fam, fa, fb, c0):

@@ -97,3 +97,42 @@ def test_layout_matches_direct_sum(d, t, d_out, fam_id):
     assert np.all(np.diff(lay["node_seg"]) >= 0) and np.all(np.diff(lay["cold_seg"]) >= 0)
     assert lay["max_depth"] <= 8
     assert lay["block_seg"][-1] == lay["n_cold_blocks"] and (d_out == 1 or lay["n_cold_blocks"] == 0)
+
+
+@pytest.mark.parametrize("d,t,fam_id,unit", [(1, 3.0, 0, False), (3, 4.5, 0, True), (6, 5.0, 1, False),
+                                             (12, 6.0, 0, True), (60, 5.8, 1, False), (200, 6.5, 0, True),
+                                             (1000, 8.22452, 0, True)])
+def test_fp64_layout_matches_direct_sum(d, t, fam_id, unit):
+    """The FP64 evaluator's layout (``build_layout64``): every entry of the
+    index set is exactly one term (no padding), the sums replayed in FP64 equal
+    the direct sum over the tree to rounding, and the row, term and segment
+    invariants the kernel relies on hold."""
+    from smolyax_gb300.spectral import build_layout64, evaluate_layout64
+
+    k = list(np.log((2 + np.arange(d)) / np.log(2)))
+    tr = python_tree(k, t)
+    n = tr["parent"].shape[0]
+    rng = np.random.default_rng(d + 7)
+    C = rng.normal(size=(n, 1))
+    maxdeg = np.zeros(d, dtype=np.int64)
+    for e in range(1, n):
+        maxdeg[tr["dim"][e]] = max(maxdeg[tr["dim"][e]], tr["deg"][e])
+    fam = np.full(d, fam_id)
+    fa, fb = (np.ones(d), np.zeros(d)) if unit else (np.full(d, 0.9), np.full(d, 0.05))
+    lay = build_layout64(tr, C, maxdeg, d, fam, fa, fb)
+    x = rng.uniform(-1, 1, (5, d))
+    ref = direct(tr, C, x, fam, fa, fb)[:, 0]
+    got = evaluate_layout64(lay, x, fam, fa, fb, C[0, 0])
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12 * np.max(np.abs(ref)))
+    # one term per entry: all entries but the root and the hot nodes
+    assert lay["n_terms"] == n - lay["n_nodes"]
+    slots = lay["terms"][: lay["n_terms"], 0].view(np.int64)
+    assert slots.min(initial=0) >= 0 and slots.max(initial=0) < lay["n_hb"] + lay["n_vp"] <= lay["row"]
+    assert lay["row"] % 2 == 1
+    node = lay["node"]
+    assert np.all(node[:, 2] <= node[:, 3]) and np.all(slots[np.concatenate(
+        [np.arange(a, b) for a, b in node[:, 2:4]] + [np.zeros(0, np.int64)]).astype(np.int64)] < lay["n_hb"])
+    assert lay["node_seg"][0] == 0 and lay["node_seg"][-1] == lay["n_nodes"]
+    assert lay["cold_seg"][0] == 0 and lay["cold_seg"][-1] == lay["n_cold_groups"]
+    assert np.all(np.diff(lay["node_seg"]) >= 0) and np.all(np.diff(lay["cold_seg"]) >= 0)
+    assert all((int(c[3]) >> 20) & 1 == int(unit) and (int(c[3]) >> 16) & 0xF == fam_id for c in lay["cold"])

@@ -67,26 +67,31 @@ def test_perpoint_tables_equal(d, t, d_out, fam_id):
         assert nat[name] == float(py[name]), name
 
 
-@pytest.mark.parametrize("d,t,fam_id", [(1, 3.0, 0), (6, 5.0, 1), (40, 5.5, 0), (200, 6.5, 0), (1000, 8.22452, 0)])
-def test_perpoint_fp64_tables_equal(d, t, fam_id):
-    """The FP64 per-point layout (one output): FP64 coefficients and maps, the
-    FP64 row (n_hb + n_vp rounded up to 4, plus 2), the same structure as the
-    FP32 layout."""
+P64_I32 = ("node_seg", "cold_seg", "hot_dim", "hot_deg", "hot_soff", "node", "cold", "run")
+P64_F64 = ("node_c", "cold_ab", "terms")
+P64_SCALARS = ("row", "n_hb", "n_vp", "n_hot_dims", "n_nodes", "n_cold_groups", "max_depth", "n_terms")
+
+
+@pytest.mark.parametrize("d,t,fam_id,unit", [(1, 3.0, 0, True), (6, 5.0, 1, False), (40, 5.5, 0, True),
+                                             (200, 6.5, 0, False), (1000, 8.22452, 0, True)])
+def test_fp64_tables_equal(d, t, fam_id, unit):
+    """The FP64 evaluator's layout (one term per entry): library and package
+    builders agree bit for bit, FP64 coefficients included."""
+    from smolyax_gb300.spectral import build_layout64
+
     tr, C, maxdeg, fam, fa, fb = _case(d, t, 1, fam_id, d + 1)
+    if unit:
+        fa, fb = np.ones(d), np.zeros(d)
     C = C.astype(np.float64) * (1 + 1e-9 * np.arange(C.size).reshape(C.shape))  # values not representable in FP32
-    py = build_layout(tr, C, maxdeg, d, 1, fam, fa, fb, dtype=np.float64)
-    nat = _capi.host_layout("perpoint", tr, C, 1, maxdeg, fam, fa, fb, PP_I32, PP_F32, PP_SCALARS, fp64=True)
-    for name in PP_I32:
+    py = build_layout64(tr, C, maxdeg, d, fam, fa, fb)
+    nat = _capi.host_layout("perpoint", tr, C, 1, maxdeg, fam, fa, fb, P64_I32, P64_F64, P64_SCALARS, fp64=True)
+    for name in P64_I32:
         np.testing.assert_array_equal(nat[name], np.asarray(py[name], dtype=np.int32).ravel(), err_msg=name)
-    for name in PP_F32:
-        assert py[name].dtype == np.float64, name
-        np.testing.assert_array_equal(nat[name], py[name].ravel(), err_msg=name)
-    for name in PP_SCALARS:
+    for name in P64_F64:
+        a = np.asarray(py[name], dtype=np.float64).ravel()
+        assert nat[name].view(np.int64).tolist() == a.view(np.int64).tolist(), name
+    for name in P64_SCALARS:
         assert nat[name] == float(py[name]), name
-    assert nat["row"] == (int(py["n_hb"]) + int(py["n_vp"]) + 3) // 4 * 4 + 2
-    f32 = build_layout(tr, C.astype(np.float32), maxdeg, d, 1, fam, fa, fb)
-    for name in PP_I32:
-        np.testing.assert_array_equal(np.asarray(f32[name]), np.asarray(py[name]), err_msg=name)
 
 
 @pytest.mark.parametrize("d,t", [(1, 3.0), (12, 6.0), (200, 6.5), (1000, 8.22452)])
