@@ -449,8 +449,13 @@ int smx_spectral_panel_bf16(int n_dims, const int32_t* dims, const int32_t* dmax
  *    contiguous, same columns as smx_spectral_panel_tf32) for dL/dC = A^T g;
  *    the basis values go through `ws` (smx_spectral_panel_t_workspace bytes);
  *  - smx_spectral_vjp_x: dL/dx[p][d] from G = g C^T ([P x ldg], columns in the
- *    panel's reversed order): reverse pass through the basis products; basis
- *    values in `ws` (smx_spectral_vjp_x_workspace bytes);
+ *    panel's reversed order): reverse pass through the basis products, one
+ *    warp per 32 points; with n_seg > 1 the tape is walked in the segments
+ *    seg[0..n_seg] (device int32 bounds, each but the last at a depth-1 entry,
+ *    as for smx_spectral_panel_tf32) by separate warps with their own
+ *    adjoint copies, which a last kernel sums (more parallelism for long
+ *    tapes; the result does not depend on the number of points); basis values
+ *    and adjoints in `ws` (smx_spectral_vjp_x_workspace bytes);
  *  - smx_spectral_coefficients_adjoint: adjoint of smx_spectral_coefficients,
  *    Fbar[r] = (A_1^T x ... x A_n^T) Cbar[ids] per summand (FP64). */
 size_t smx_spectral_panel_t_workspace(int n_slots, int64_t P);
@@ -458,11 +463,11 @@ int smx_spectral_panel_t_tf32(int n_dims, const int32_t* dims, const int32_t* dm
                               int n_slots, const int32_t* tape, int K, const float* fam_a, const float* fam_b,
                               const int32_t* fam, const double* x, int64_t P, int64_t ldx, float* AT_hi, float* AT_lo,
                               int64_t ldp, void* ws, size_t ws_bytes, void* stream);
-size_t smx_spectral_vjp_x_workspace(int n_slots, int64_t P);
+size_t smx_spectral_vjp_x_workspace(int n_slots, int n_seg, int64_t P);
 int smx_spectral_vjp_x(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff, int n_slots,
-                       const int32_t* tape, int K, const float* fam_a, const float* fam_b, const int32_t* fam,
-                       const double* x, int64_t P, int64_t ldx, const float* G, int64_t ldg, double* dx, int64_t lddx,
-                       void* ws, size_t ws_bytes, void* stream);
+                       const int32_t* tape, int K, const int32_t* seg, int n_seg, const float* fam_a,
+                       const float* fam_b, const int32_t* fam, const double* x, int64_t P, int64_t ldx, const float* G,
+                       int64_t ldg, double* dx, int64_t lddx, void* ws, size_t ws_bytes, void* stream);
 int smx_spectral_coefficients_adjoint(const smx_plan* plan_host, const int64_t* aoff, const double* A,
                                       const int32_t* ids, const double* Cbar, double* Fbar, void* stream);
 

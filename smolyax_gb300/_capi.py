@@ -253,9 +253,9 @@ SIGNATURES = {
     "smx_spectral_panel_t_workspace": (_sz, [_int, _i64]),
     "smx_spectral_panel_t_tf32": (_int, [_int, _p, _p, _p, _int, _p, _int, _p, _p, _p, _p, _i64, _i64, _p, _p,
                                           _i64, _p, _sz, _p]),
-    "smx_spectral_vjp_x_workspace": (_sz, [_int, _i64]),
-    "smx_spectral_vjp_x": (_int, [_int, _p, _p, _p, _int, _p, _int, _p, _p, _p, _p, _i64, _i64, _p, _i64, _p, _i64,
-                                   _p, _sz, _p]),
+    "smx_spectral_vjp_x_workspace": (_sz, [_int, _int, _i64]),
+    "smx_spectral_vjp_x": (_int, [_int, _p, _p, _p, _int, _p, _int, _p, _int, _p, _p, _p, _p, _i64, _i64, _p, _i64,
+                                   _p, _i64, _p, _sz, _p]),
     "smx_spectral_coefficients_adjoint": (_int, [_p, _p, _p, _p, _p, _p, _p]),
     "smx_split_tf32": (_int, [_p, _i64, _i64, _i64, _p, _p, _i64, _p]),
     "smx_layout_build": (_int, [_int, _i64, _p, _p, _p, _p, _p, _p, _p, _int, _p, _int, _p, _p, _p,

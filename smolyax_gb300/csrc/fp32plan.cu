@@ -129,6 +129,7 @@ struct smx_fp32_plan {
   DevBuf<float> Bh, Bl, bias, Rh, Rl;
   std::vector<int32_t> lvl1;
   std::vector<int> seg_off, seg_n;  // per wanted segment count: offset into segs, number of segments
+  int vjp_want = 1;                 // tape segments of the gradient walk (fixed per plan)
   // FP64 per-point tables of the orthogonal form (one output), when they fit
   bool have64 = false;
   DevBuf<int32_t> ti64;
@@ -385,6 +386,9 @@ extern "C" int smx_fp32_plan_create(const smx_plan* pl, const smx_tree* tree, co
       segs.insert(segs.end(), b.begin(), b.end());
     }
     if ((rc = h->segs.upload(segs, st))) return rc;
+    // gradient walk: one segment per 4096 tape entries, at most 32 and the
+    // depth-1 entries (spectral.py vjp_segment_count)
+    h->vjp_want = int(std::max<int64_t>(1, std::min<int64_t>({32, int64_t(h->K) / 4096, int64_t(h->lvl1.size())})));
     if (cudaStreamSynchronize(st) != cudaSuccess)  // the staging buffers go out of scope
       return smx::set_error(SMX_ERR_CUDA, "smx_fp32_plan_create: sync failed");
   }
@@ -621,7 +625,7 @@ VjpLayout vjp_layout(const smx_fp32_plan* h, int64_t P) {
   // the [K x d_out] product has few tiles and a long contraction over the points: split it over the SMs
   const int64_t tiles = ((h->K + 127) / 128) * ((h->d_out + 127) / 128);
   L.splits = int(std::max<int64_t>(1, std::min<int64_t>(64, (2 * int64_t(h->sms)) / std::max<int64_t>(tiles, 1))));
-  L.n_xws = smx_spectral_vjp_x_workspace(h->n_slots, m);
+  L.n_xws = smx_spectral_vjp_x_workspace(h->n_slots, h->vjp_want <= 1 ? 1 : h->seg_n[h->vjp_want], m);
   L.n_skws = smx_gemm_tf32x3_splitk_workspace(std::max(h->K, 1), h->d_out, int(m), L.splits);
   L.n_ptws = smx_spectral_panel_t_workspace(h->n_slots, m);
   size_t o = 0;
@@ -683,8 +687,10 @@ extern "C" int smx_vjp(const smx_fp32_plan* h, const double* x, int64_t P, int64
       if ((rc = smx_gemm_tf32x3(F(L.gh) + p0 * h->ldo, F(L.gl) + p0 * h->ldo, h->ldo, h->Rh.p, h->Rl.p, h->ldo,
                                 int(m), h->K, h->ldo, F(L.G), L.ldg, nullptr, 0, h->err.p, stream)) ||
           (rc = smx_spectral_vjp_x(h->n_dims, h->dims.p, h->dmax.p, h->dsoff.p, h->n_slots, h->tape.p, h->K,
-                                   h->fam_a.p, h->fam_b.p, h->fam.p, x + p0 * ldx, m, ldx, F(L.G), L.ldg,
-                                   dx + p0 * lddx, lddx, w + L.xws, L.n_xws, stream)))
+                                   h->vjp_want <= 1 ? nullptr : h->segs.p + h->seg_off[h->vjp_want],
+                                   h->vjp_want <= 1 ? 1 : h->seg_n[h->vjp_want], h->fam_a.p, h->fam_b.p, h->fam.p,
+                                   x + p0 * ldx, m, ldx, F(L.G), L.ldg, dx + p0 * lddx, lddx, w + L.xws, L.n_xws,
+                                   stream)))
         return rc;
     }
   }

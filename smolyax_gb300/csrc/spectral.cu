@@ -1212,35 +1212,21 @@ constexpr int kVjpTP = 32;
 // shared memory; GB = true (many basis slots, where that shared memory would
 // leave room for only a few warps per SM): they sit in a global scratch
 // [n_slots][rstride] beside the basis rows, read and updated through L1/L2.
-template <bool GB>
-__global__ void __launch_bounds__(kVjpTP) vjp_x_kernel(int n_dims, const int32_t* __restrict__ dims,
-                                                       const int32_t* __restrict__ dmax,
-                                                       const int32_t* __restrict__ dsoff, int n_slots,
-                                                       const int32_t* __restrict__ tape, int K,
-                                                       const float* __restrict__ fam_a,
-                                                       const float* __restrict__ fam_b,
-                                                       const int32_t* __restrict__ fam, const double* __restrict__ x,
-                                                       int64_t P, int64_t ldx, const float* __restrict__ G,
-                                                       int64_t ldg, double* __restrict__ dx, int64_t lddx,
-                                                       float* __restrict__ rowg, int64_t rstride,
-                                                       float* __restrict__ barg) {
-  extern __shared__ __align__(16) float sm[];
+// The reverse walk over the tape entries [j0, j1) for the 32 points of a
+// warp: every entry's G value times the products of the other factors of its
+// path goes to the adjoint of each factor's basis slot, bar[slot * BS + tid].
+// j0 must be the tape position of a depth-1 entry (or 0): the path state
+// starts empty there.
+__device__ __forceinline__ void vjp_walk(int j0, int j1, int K, const int32_t* __restrict__ tape,
+                                         const float* __restrict__ row, int64_t rstride, const float* __restrict__ G,
+                                         int64_t ldg, int64_t p0, int64_t P, float* tile, float* bar, int64_t BS,
+                                         int tid) {
   constexpr int TP = kVjpTP;
-  const int64_t BS = GB ? rstride : TP;              // slot stride of the adjoints
-  float* tile = GB ? sm : sm + size_t(n_slots) * TP;  // [32][TP + 1]
-  const int tid = threadIdx.x;
-  const int64_t p0 = blockIdx.x * int64_t(TP);
-  const int64_t p = p0 + tid;
-  float* bar = GB ? barg + p0 : sm;                  // bar[slot * BS + tid]
-  const double* xp = x + (p < P ? p : 0) * ldx;
-  float* row = rowg + p;
-  basis_row(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, xp, row, rstride, 0);
-  for (int s = 0; s < n_slots; ++s) bar[s * BS + tid] = 0.f;
   int64_t s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0, s6 = 0, s7 = 0, s8 = 0;
   float f1 = 1.f, f2 = 1.f, f3 = 1.f, f4 = 1.f, f5 = 1.f, f6 = 1.f, f7 = 1.f, f8 = 1.f;
   float q1 = 1.f, q2 = 1.f, q3 = 1.f, q4 = 1.f, q5 = 1.f, q6 = 1.f, q7 = 1.f;
-  for (int jb = 0; jb < K; jb += 32) {
-    const int jn = min(32, K - jb);
+  for (int jb = j0; jb < j1; jb += 32) {
+    const int jn = min(32, j1 - jb);
     __syncthreads();
     // tile[c][r] = G[p0 + r][K - 1 - (jb + c)]: coalesced over the 32 columns
     for (int idx = tid; idx < 32 * TP; idx += TP) {
@@ -1257,7 +1243,7 @@ __global__ void __launch_bounds__(kVjpTP) vjp_x_kernel(int n_dims, const int32_t
       for (int u = 0; u < 8; ++u) b[u] = row[int64_t(w[u] & 0xffff) * rstride];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        const int k = min(8, w[u] >> 16);  // 0: padding past the end of the tape
+        const int k = min(8, w[u] >> 16);  // 0: padding past the end of the range
         const int64_t sl = (w[u] & 0xffff) * BS + tid;
         switch (k) {
           case 1: s1 = sl; f1 = b[u]; q1 = b[u]; break;
@@ -1286,7 +1272,16 @@ __global__ void __launch_bounds__(kVjpTP) vjp_x_kernel(int n_dims, const int32_t
       }
     }
   }
-  if (p >= P) return;
+}
+
+// dL/dx[p][dim] = a_dim * sum_n bar(slot n of dim) * phi_n'(z) for the point
+// of thread tid, the adjoints summed over `nb` copies nbs floats apart.
+__device__ __forceinline__ void vjp_dx(int n_dims, const int32_t* __restrict__ dims,
+                                       const int32_t* __restrict__ dmax, const int32_t* __restrict__ dsoff,
+                                       const float* __restrict__ fam_a, const float* __restrict__ fam_b,
+                                       const int32_t* __restrict__ fam, const double* __restrict__ xp,
+                                       const float* bar, int64_t BS, int nb, int64_t nbs, int tid,
+                                       double* __restrict__ dxp) {
   for (int h = 0; h < n_dims; ++h) {
     const int dim = dims[h], g = dmax[h], so = dsoff[h];
     const int fm = fam[dim];
@@ -1300,14 +1295,89 @@ __global__ void __launch_bounds__(kVjpTP) vjp_x_kernel(int n_dims, const int32_t
       pc = pn;
       dm1 = dc;
       dc = dn;
-      acc = fmaf(bar[(so + n) * BS + tid], dc, acc);
+      float b = 0.f;
+      for (int q = 0; q < nb; ++q) b += bar[q * nbs + (so + n) * BS + tid];
+      acc = fmaf(b, dc, acc);
     }
-    dx[p * lddx + dim] = double(fam_a[dim]) * double(acc);
+    dxp[dim] = double(fam_a[dim]) * double(acc);
   }
 }
 
-// Adjoint of the coefficient transform: Gbar[r] = Cbar[ids[r]], then the
-// transposed mode products per summand: Fbar_s = (A_1^T x ... x A_n^T) Gbar_s.
+template <bool GB>
+__global__ void __launch_bounds__(kVjpTP) vjp_x_kernel(int n_dims, const int32_t* __restrict__ dims,
+                                                       const int32_t* __restrict__ dmax,
+                                                       const int32_t* __restrict__ dsoff, int n_slots,
+                                                       const int32_t* __restrict__ tape, int K,
+                                                       const float* __restrict__ fam_a,
+                                                       const float* __restrict__ fam_b,
+                                                       const int32_t* __restrict__ fam, const double* __restrict__ x,
+                                                       int64_t P, int64_t ldx, const float* __restrict__ G,
+                                                       int64_t ldg, double* __restrict__ dx, int64_t lddx,
+                                                       float* __restrict__ rowg, int64_t rstride,
+                                                       float* __restrict__ barg) {
+  extern __shared__ __align__(16) float sm[];
+  constexpr int TP = kVjpTP;
+  const int64_t BS = GB ? rstride : TP;              // slot stride of the adjoints
+  float* tile = GB ? sm : sm + size_t(n_slots) * TP;  // [32][TP + 1]
+  const int tid = threadIdx.x;
+  const int64_t p0 = blockIdx.x * int64_t(TP);
+  const int64_t p = p0 + tid;
+  float* bar = GB ? barg + p0 : sm;                  // bar[slot * BS + tid]
+  const double* xp = x + (p < P ? p : 0) * ldx;
+  float* row = rowg + p;
+  basis_row(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, xp, row, rstride, 0);
+  for (int s = 0; s < n_slots; ++s) bar[s * BS + tid] = 0.f;
+  vjp_walk(0, K, K, tape, row, rstride, G, ldg, p0, P, tile, bar, BS, tid);
+  if (p >= P) return;
+  vjp_dx(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, xp, bar, BS, 1, 0, tid, dx + p * lddx);
+}
+
+// Tape split into segments (each starting at a depth-1 entry) for more
+// parallelism when few points are walked: basis rows first (one thread per
+// point), then one warp per (32 points, segment) with its own adjoint copy in
+// global memory, then the sum over the copies.
+__global__ void __launch_bounds__(128) vjp_rows_kernel(int n_dims, const int32_t* __restrict__ dims,
+                                                       const int32_t* __restrict__ dmax,
+                                                       const int32_t* __restrict__ dsoff,
+                                                       const float* __restrict__ fam_a,
+                                                       const float* __restrict__ fam_b,
+                                                       const int32_t* __restrict__ fam, const double* __restrict__ x,
+                                                       int64_t P, int64_t ldx, float* __restrict__ rowg,
+                                                       int64_t rstride) {
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= rstride) return;
+  basis_row(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, x + (p < P ? p : 0) * ldx, rowg + p, rstride, 0);
+}
+
+__global__ void __launch_bounds__(kVjpTP) vjp_seg_kernel(int n_slots, const int32_t* __restrict__ tape, int K,
+                                                         const int32_t* __restrict__ seg, int64_t P,
+                                                         const float* __restrict__ G, int64_t ldg,
+                                                         const float* __restrict__ rowg, int64_t rstride,
+                                                         float* __restrict__ barg) {
+  __shared__ float tile[32 * (kVjpTP + 1)];
+  const int tid = threadIdx.x;
+  const int64_t p0 = blockIdx.x * int64_t(kVjpTP);
+  float* bar = barg + int64_t(blockIdx.y) * n_slots * rstride + p0;
+  for (int s = 0; s < n_slots; ++s) bar[s * rstride + tid] = 0.f;
+  vjp_walk(seg[blockIdx.y], seg[blockIdx.y + 1], K, tape, rowg + p0 + tid, rstride, G, ldg, p0, P, tile, bar, rstride,
+           tid);
+}
+
+__global__ void __launch_bounds__(128) vjp_sum_kernel(int n_dims, const int32_t* __restrict__ dims,
+                                                      const int32_t* __restrict__ dmax,
+                                                      const int32_t* __restrict__ dsoff,
+                                                      const float* __restrict__ fam_a,
+                                                      const float* __restrict__ fam_b,
+                                                      const int32_t* __restrict__ fam, const double* __restrict__ x,
+                                                      int64_t P, int64_t ldx, int n_slots, int n_seg,
+                                                      const float* __restrict__ barg, int64_t rstride,
+                                                      double* __restrict__ dx, int64_t lddx) {
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= P) return;
+  vjp_dx(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, x + p * ldx, barg + p, rstride, n_seg,
+         int64_t(n_slots) * rstride, 0, dx + p * lddx);
+}
+
 __global__ void coeff_adjoint_kernel(int n_sum, const int32_t* __restrict__ poff, const int32_t* __restrict__ pairs,
                                      const int64_t* __restrict__ eoff, const int32_t* __restrict__ pdeg,
                                      const int64_t* __restrict__ aoff, const double* __restrict__ A,
@@ -1375,37 +1445,54 @@ extern "C" int smx_spectral_panel_t_tf32(int n_dims, const int32_t* dims, const 
 // 32-point block (fewer than ~8 warps per SM).
 static bool vjp_global_bar(int n_slots) { return (size_t(n_slots) * kVjpTP + 32 * (kVjpTP + 1)) * 4 > 24 * 1024; }
 
-extern "C" size_t smx_spectral_vjp_x_workspace(int n_slots, int64_t P) {
-  if (n_slots < 0 || P < 0) return 0;
+extern "C" size_t smx_spectral_vjp_x_workspace(int n_slots, int n_seg, int64_t P) {
+  if (n_slots < 0 || P < 0 || n_seg < 0) return 0;
   const size_t rows = size_t(n_slots) * size_t((P + kVjpTP - 1) / kVjpTP * kVjpTP) * sizeof(float);
+  if (n_seg > 1) return (1 + size_t(n_seg)) * rows;
   return vjp_global_bar(n_slots) ? 2 * rows : rows;
 }
 
 extern "C" int smx_spectral_vjp_x(int n_dims, const int32_t* dims, const int32_t* dmax, const int32_t* dsoff,
-                                  int n_slots, const int32_t* tape, int K, const float* fam_a, const float* fam_b,
-                                  const int32_t* fam, const double* x, int64_t P, int64_t ldx, const float* G,
-                                  int64_t ldg, double* dx, int64_t lddx, void* ws, size_t ws_bytes, void* stream) {
+                                  int n_slots, const int32_t* tape, int K, const int32_t* seg, int n_seg,
+                                  const float* fam_a, const float* fam_b, const int32_t* fam, const double* x,
+                                  int64_t P, int64_t ldx, const float* G, int64_t ldg, double* dx, int64_t lddx,
+                                  void* ws, size_t ws_bytes, void* stream) {
   SMX_REQUIRE(n_dims >= 0 && n_slots >= 0 && K >= 0 && P >= 0 && ldg >= K, "smx_spectral_vjp_x: bad sizes");
+  if (n_seg < 1 || !seg) n_seg = 1;
+  SMX_REQUIRE(n_seg <= 65535, "smx_spectral_vjp_x: too many segments");
   if (P == 0) return SMX_OK;
   SMX_REQUIRE(dims && dmax && dsoff && tape && fam_a && fam_b && fam && x && G && dx, "smx_spectral_vjp_x: null");
-  SMX_REQUIRE(ws && ws_bytes >= smx_spectral_vjp_x_workspace(n_slots, P), "smx_spectral_vjp_x: workspace too small");
-  const bool gb = vjp_global_bar(n_slots);
-  const size_t smem = ((gb ? 0 : size_t(n_slots) * kVjpTP) + 32 * (kVjpTP + 1)) * sizeof(float);
+  SMX_REQUIRE(ws && ws_bytes >= smx_spectral_vjp_x_workspace(n_slots, n_seg, P),
+              "smx_spectral_vjp_x: workspace too small");
   int rc = upload_consts();
   if (rc) return rc;
+  const int64_t rstride = (P + kVjpTP - 1) / kVjpTP * kVjpTP;
+  float* rowg = static_cast<float*>(ws);
+  cudaStream_t st = smx::as_stream(stream);
+  if (n_seg > 1) {
+    float* barg = rowg + size_t(n_slots) * rstride;
+    vjp_rows_kernel<<<smx::grid_for(rstride, 128), 128, 0, st>>>(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, x, P,
+                                                                 ldx, rowg, rstride);
+    vjp_seg_kernel<<<dim3(unsigned(rstride / kVjpTP), unsigned(n_seg)), kVjpTP, 0, st>>>(n_slots, tape, K, seg, P, G,
+                                                                                         ldg, rowg, rstride, barg);
+    vjp_sum_kernel<<<smx::grid_for(P, 128), 128, 0, st>>>(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, x, P, ldx,
+                                                          n_slots, n_seg, barg, rstride, dx, lddx);
+    SMX_LAUNCH_CHECK("smx_spectral_vjp_x");
+    return SMX_OK;
+  }
+  const bool gb = vjp_global_bar(n_slots);
+  const size_t smem = ((gb ? 0 : size_t(n_slots) * kVjpTP) + 32 * (kVjpTP + 1)) * sizeof(float);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(vjp_x_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     attr = true;
   }
-  const int64_t rstride = (P + kVjpTP - 1) / kVjpTP * kVjpTP;
-  float* rowg = static_cast<float*>(ws);
   if (gb)
-    vjp_x_kernel<true><<<smx::grid_for(P, kVjpTP), kVjpTP, smem, smx::as_stream(stream)>>>(
+    vjp_x_kernel<true><<<smx::grid_for(P, kVjpTP), kVjpTP, smem, st>>>(
         n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, G, ldg, dx, lddx, rowg, rstride,
         rowg + size_t(n_slots) * rstride);
   else
-    vjp_x_kernel<false><<<smx::grid_for(P, kVjpTP), kVjpTP, smem, smx::as_stream(stream)>>>(
+    vjp_x_kernel<false><<<smx::grid_for(P, kVjpTP), kVjpTP, smem, st>>>(
         n_dims, dims, dmax, dsoff, n_slots, tape, K, fam_a, fam_b, fam, x, P, ldx, G, ldg, dx, lddx, rowg, rstride,
         nullptr);
   SMX_LAUNCH_CHECK("smx_spectral_vjp_x");

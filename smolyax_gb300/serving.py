@@ -276,7 +276,8 @@ class Server:
             ldo, ldk = bwd["ldo"], bwd["ldk"]
             step = min(P, max(128, int(sp.memory_limit * 1024**3 // (8 * ldk)) // 128 * 128))
             b += P * d_out * 4 + 3 * P * ldo * 4 + P * d_in * 8  # cotangent, its TF32 split, dL/dx
-            b += step * (ldk + 31) // 32 * 32 * 4 + capi.size("smx_spectral_vjp_x_workspace", bwd["n_slots"], step)
+            b += step * (ldk + 31) // 32 * 32 * 4 + capi.size("smx_spectral_vjp_x_workspace", bwd["n_slots"],
+                                                               bwd["vjp_seg"][1], step)
         elif req.precision == "fp64" and ip._fp64_orthogonal() is not None:
             b += P * d_out * 8  # the FP64 orthogonal evaluator takes no scratch
         elif req.precision == "fp64":

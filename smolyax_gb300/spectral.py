@@ -282,6 +282,14 @@ class SpectralPlan:
             Rh, Rl = torch.empty_like(Rd), torch.empty_like(Rd)
             call("smx_split_tf32", ptr(Rd), rows.shape[0], ldo, ldo, ptr(Rh), ptr(Rl), ldo, st)
             ops.update(Rh=Rh, Rl=Rl, ldo=ldo)
+            # tape segments of the gradient walk: fixed per plan (a point's dL/dx
+            # does not depend on the batch it comes in)
+            want = vjp_segment_count(K, ops["lvl1"].size)
+            if want > 1:
+                b = T(segment_bounds(ops["lvl1"], K, want), torch.int32)
+                ops["vjp_seg"] = (b, int(b.numel()) - 1)
+            else:
+                ops["vjp_seg"] = (None, 1)
             self._bwd = ops
         return self._bwd
 
@@ -298,6 +306,9 @@ class SpectralPlan:
         nd = int(ops["dims"].numel())
         common = (nd, ptr(ops["dims"]), ptr(ops["dmax"]), ptr(ops["dsoff"]), ops["n_slots"], ptr(ops["tape"]), K,
                   ptr(k["fam_a"]), ptr(k["fam_b"]), ptr(k["fam"]))
+        seg, n_seg = ops["vjp_seg"]
+        walk = (nd, ptr(ops["dims"]), ptr(ops["dmax"]), ptr(ops["dsoff"]), ops["n_slots"], ptr(ops["tape"]), K,
+                ptr(seg), n_seg, ptr(k["fam_a"]), ptr(k["fam_b"]), ptr(k["fam"]))
         g32 = torch.zeros(P, ldo, dtype=torch.float32, device=dev)
         g32[:, :d_out] = g.float()
         gh, gl = torch.empty_like(g32), torch.empty_like(g32)
@@ -309,13 +320,13 @@ class SpectralPlan:
             dx = torch.zeros(P, d, dtype=torch.float64, device=dev)
             ldg = _round32(K)  # 128-byte rows
             G = torch.empty(min(step, P), ldg, dtype=torch.float32, device=dev)
-            nws = capi.size("smx_spectral_vjp_x_workspace", ops["n_slots"], min(step, P))
+            nws = capi.size("smx_spectral_vjp_x_workspace", ops["n_slots"], n_seg, min(step, P))
             ws = torch.empty(max(nws, 1), dtype=torch.uint8, device=dev)
             for p0 in range(0, P, step):
                 p1 = min(P, p0 + step)
                 call("smx_gemm_tf32x3", ptr(gh[p0:p1]), ptr(gl[p0:p1]), ldo, ptr(ops["Rh"]), ptr(ops["Rl"]), ldo,
                      p1 - p0, K, ldo, ptr(G), ldg, None, 0, ptr(err), st)
-                call("smx_spectral_vjp_x", *common, ptr(x[p0:p1]), p1 - p0, d, ptr(G), ldg, ptr(dx[p0:p1]), d,
+                call("smx_spectral_vjp_x", *walk, ptr(x[p0:p1]), p1 - p0, d, ptr(G), ldg, ptr(dx[p0:p1]), d,
                      ptr(ws), nws, st)
         if need_coef:
             ldp = _round32(min(step, P))  # 128-byte rows
@@ -557,6 +568,12 @@ def segment_count(K, n_lvl1, n_points, sms):
     no more than there are depth-1 entries to start them."""
     n_pb = max(-(-int(n_points) // 128), 1)
     return max(1, min(32, -(-12 * int(sms) // n_pb), int(K) // 256, int(n_lvl1)))
+
+
+def vjp_segment_count(K, n_lvl1):
+    """Tape segments of the gradient walk: one per 4096 tape entries (at most
+    32 and the number of depth-1 entries), fixed per plan."""
+    return max(1, min(32, int(K) // 4096, int(n_lvl1)))
 
 
 def segment_bounds(lvl1, K, want):
