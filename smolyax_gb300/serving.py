@@ -508,14 +508,20 @@ class Server:
         """Hand a finished launch's results to its requests (a request is done
         when its result is in its own host array) and give back the launch's
         staging space, memory and stream."""
+        failed = []
         for req, h in zip(g.reqs, g.host):
-            out = torch.empty(tuple(h.shape), dtype=h.dtype)
-            out.copy_(h)  # out of the staging arena, on torch's intra-op threads
-            req.result = out.numpy()
+            try:
+                out = torch.empty(tuple(h.shape), dtype=h.dtype)
+                out.copy_(h)  # out of the staging arena, on torch's intra-op threads
+                req.result = out.numpy()
+            except Exception as e:  # the request fails; the launch's resources are still given back
+                req.error = "%s: %s" % (type(e).__name__, e)
+                failed.append(req)
             req.t_done = time.perf_counter()
             req.done.set()
         with self.lock:
-            self.completed.extend(g.reqs)
+            self.completed.extend(r for r in g.reqs if r not in failed)
+            self.failed.extend(failed)
             for off in g.staged:
                 self.arena.free(off)
             self.in_use -= g.nbytes

@@ -136,3 +136,28 @@ def test_pinned_arena_first_fit_and_merging():
     v = a.view(a.alloc(80), (10,), torch.float64)
     v[:] = 3.0
     assert float(v.sum()) == 30.0
+
+
+def test_launches_on_host_threads_give_back_what_failed_launches_took():
+    """With a pool of host threads, launches are prepared there; a launch that
+    raises fails its requests and returns its stream and memory, and the
+    server is idle once every task has finished."""
+    import time
+    from concurrent.futures import ThreadPoolExecutor
+
+    s = _Scheduler(budget=1000, n_streams=2, kinds={"f": "blocked", "a": None}, bytes_per_point={"f": 10, "a": 1},
+                   failing={"f"})
+    s.pool, s.pending, s._building = ThreadPoolExecutor(max_workers=2), 0, {}
+    try:
+        bad = [s.submit(_req("f", 10)) for _ in range(2)]
+        ok = s.submit(_req("a", 10))
+        s._admit()
+        t0 = time.perf_counter()
+        while not s.idle():
+            assert time.perf_counter() - t0 < 10
+            time.sleep(0.001)
+        assert all(r.error and r.done.is_set() for r in bad)
+        assert [ids for _, ids, _ in s.launched] == [[ok.id]]
+        assert s.in_use == 10 and len(s.free_streams) == 1
+    finally:
+        s.pool.shutdown(wait=True)
