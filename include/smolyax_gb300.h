@@ -268,26 +268,29 @@ typedef struct smx_spectral {
 int smx_spectral_eval(const smx_spectral* plan_host, const double* x, int64_t P, int64_t ldx, float* y,
                       void* stream);
 
-/* FP64 evaluation of the orthogonal form, one output (the FP64 counterpart of
- * interpolation.py:264-304 for d_out = 1).  The per-point structure of
- * smx_spectral -- hot basis values and the prefix products of the cold
- * entries' parents in a row of `row` doubles per point (row >= n_hb + n_vp;
- * odd keeps 8-byte reads of consecutive points on distinct banks; a block of
- * 64 points needs (row + 4) * 64 * 8 bytes of shared memory, <= 227 KB) -- but every
- * entry of Lambda is exactly one term (row slot, FP64 coefficient), without
- * padding: at GB300's FP64 rate each term is a multiply-add that counts.
+/* FP64 evaluation of the orthogonal form (the FP64 counterpart of
+ * interpolation.py:264-304).  The per-point structure of smx_spectral -- hot
+ * basis values and the prefix products of the cold entries' parents in a row
+ * of `row` doubles per point (row >= n_hb + n_vp; odd keeps 8-byte reads of
+ * consecutive points on distinct banks; a block of 64 points needs (row + 4 *
+ * (d_out == 1 ? 1 : 4)) * 64 * 8 bytes of shared memory, <= 227 KB) -- but
+ * every entry of Lambda is exactly one term (row slot, coefficients), without
+ * padding: at GB300's FP64 rate each term is a multiply-add that counts.  One
+ * output per pass (d_out = 1), else four (outputs o0..o0+3 per block row).
  *   node[n_nodes][4]  slot | depth << 16, prefix slot or -1, term range of the
  *                     hot leaf children (hot nodes in DFS pre-order, root first)
  *   cold[G][4]        dimension, run range, max degree | family << 16 | unit << 20
  *                     (unit: the map z = a x + b is the identity)
  *   run[R][4]         term range, degree, 0 (runs of a group by degree)
- *   terms[T][2]       slot (integer bits of the first double), coefficient
+ *   terms[T][2]       slot (integer bits of the first double), coefficient (d_out = 1)
+ *   coef[T][dstride]  coefficients (d_out > 1; dstride = d_out rounded up to 4)
  * With coefficients from smx_spectral_coefficients (compensated sums) the
  * result is within ~1e-14 relative of the exact value of the interpolant,
  * where the barycentric combination sum in FP64 cancels to 1e-13 .. 1e-10.
  * Non-finite coordinates of active dimensions give NaN. */
 typedef struct smx_spectral64 {
-  int32_t d_in;
+  int32_t d_in, d_out;
+  int32_t dstride;       /* 1 (d_out = 1) or d_out rounded up to 4                 */
   int32_t row;           /* doubles per point row                                  */
   int32_t n_hb, n_vp, n_hot_dims, n_nodes, n_cold_groups, max_depth, n_terms;
   int32_t node_seg[5], cold_seg[5];  /* the 4 work segments over nodes and cold groups */
@@ -295,18 +298,19 @@ typedef struct smx_spectral64 {
   const int32_t* hot_deg;
   const int32_t* hot_soff;
   const int32_t* node;
-  const double* node_c;     /* [n_nodes] own coefficient (0 for the root)           */
+  const double* node_c;     /* [n_nodes][dstride] own coefficients (0 for the root)  */
   const int32_t* cold;
   const double* cold_ab;    /* [G][2] a, b                                          */
   const int32_t* run;
   const double* terms;      /* [n_terms][2]                                         */
+  const double* coef;       /* [n_terms][dstride] (d_out > 1), else NULL            */
   const double* fam_a;      /* [d_in]                                               */
   const double* fam_b;      /* [d_in]                                               */
   const int32_t* fam;       /* [d_in]                                               */
-  double c0;                /* coefficient of the constant                          */
+  const double* c0;         /* [d_out] coefficients of the constant                 */
 } smx_spectral64;
 
-/* y[P] (FP64) = the interpolant at the P rows of x (FP64, leading dimension ldx). */
+/* y[P, d_out] (FP64) = the interpolant at the P rows of x (FP64, leading dimension ldx). */
 int smx_spectral_eval64(const smx_spectral64* plan_host, const double* x, int64_t P, int64_t ldx, double* y,
                         void* stream);
 
@@ -565,9 +569,9 @@ int smx_layout_build(int kind, int64_t n, const int32_t* parent_host, const int3
                      const int32_t* fam_host, const double* fam_a_host, const double* fam_b_host,
                      smx_host_tables** out);
 /* The layout of the FP64 evaluator (smx_spectral64) from FP64 coefficients
- * C[n] (one output): kind SMX_LAYOUT_PERPOINT only (its FP64 form); tables
- * "node_c", "cold_ab", "terms" are read with smx_layout_f64, the others with
- * smx_layout_i32 and smx_layout_scalar. */
+ * C[n][d_out]: kind SMX_LAYOUT_PERPOINT only (its FP64 form); tables
+ * "node_c", "cold_ab", "terms", "coef" are read with smx_layout_f64, the others
+ * with smx_layout_i32 and smx_layout_scalar. */
 int smx_layout_build_f64(int kind, int64_t n, const int32_t* parent_host, const int32_t* dim_host,
                          const int32_t* deg_host, const int32_t* level_host, const int64_t* rank_host,
                          const double* rem_host, const double* C_host, int d_out, const int64_t* maxdeg_host, int d,
@@ -621,9 +625,9 @@ int smx_fp32_eval(const smx_fp32_plan* fp32, const double* x, int64_t P, int64_t
 /* SMX_OK, or SMX_ERR_CUDA if a tensor-core pipeline wait of an earlier call
  * timed out (those results are invalid); resets the flag; synchronises. */
 int smx_fp32_plan_check(const smx_fp32_plan* fp32, void* stream);
-/* FP64 evaluation of the orthogonal form, y[P] (FP64), for one-output plans
- * whose per-point row fits the FP64 evaluator (smx_spectral64; the handle
- * builds those tables when it can): SMX_ERR_UNSUPPORTED otherwise.
+/* FP64 evaluation of the orthogonal form, y[P, d_out] (FP64), for plans whose
+ * per-point row fits the FP64 evaluator (smx_spectral64; the handle builds
+ * those tables when it can): SMX_ERR_UNSUPPORTED otherwise.
  * smx_eval(plan, 64, ...) evaluates through it when plan->fp32 is set and has
  * them, as the Python package does for precision "fp64". */
 int smx_fp32_plan_has_fp64(const smx_fp32_plan* fp32);

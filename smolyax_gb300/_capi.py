@@ -109,6 +109,8 @@ class SmxSpectral64(C.Structure):
 
     _fields_ = [
         ("d_in", _i32),
+        ("d_out", _i32),
+        ("dstride", _i32),
         ("row", _i32),
         ("n_hb", _i32),
         ("n_vp", _i32),
@@ -128,10 +130,11 @@ class SmxSpectral64(C.Structure):
         ("cold_ab", _p),
         ("run", _p),
         ("terms", _p),
+        ("coef", _p),
         ("fam_a", _p),
         ("fam_b", _p),
         ("fam", _p),
-        ("c0", C.c_double),
+        ("c0", _p),
     ]
 
 

@@ -392,16 +392,17 @@ extern "C" int smx_fp32_plan_create(const smx_plan* pl, const smx_tree* tree, co
     if (cudaStreamSynchronize(st) != cudaSuccess)  // the staging buffers go out of scope
       return smx::set_error(SMX_ERR_CUDA, "smx_fp32_plan_create: sync failed");
   }
-  // FP64 tables (one output): the FP64 evaluator of the orthogonal form
-  if (dout == 1) {
+  // FP64 tables: the FP64 evaluator of the orthogonal form
+  {
     smx::layout::Tables p64;
-    if (smx::layout::build_perpoint64(tr, C64_h.data(), maxdeg.data(), d, fam_v.data(), fa_v.data(), fb_v.data(),
-                                      p64) &&
-        (int64_t(p64.scalar["row"]) + 4) * 64 * 8 <= 227 * 1024 && p64.scalar["max_depth"] <= 8) {
+    const int64_t do_pass = dout == 1 ? 1 : 4;
+    if (smx::layout::build_perpoint64(tr, C64_h.data(), dout, maxdeg.data(), d, fam_v.data(), fa_v.data(),
+                                      fb_v.data(), p64) &&
+        (int64_t(p64.scalar["row"]) + 4 * do_pass) * 64 * 8 <= 227 * 1024 && p64.scalar["max_depth"] <= 8) {
       Pack<int32_t> pi;
       Pack<double> pf;
       const char* names_i[] = {"hot_dim", "hot_deg", "hot_soff", "node", "cold", "run"};
-      const char* names_f[] = {"node_c", "cold_ab", "terms"};
+      const char* names_f[] = {"node_c", "cold_ab", "terms", "coef"};
       for (const char* nm : names_i) pi.add(nm, p64.i32[nm]);
       for (const char* nm : names_f) pf.add(nm, p64.f64[nm]);
       if ((rc = h->ti64.upload(pi.v, st)) || (rc = h->tf64.upload(pf.v, st)) || (rc = h->fa64.upload(fa_v, st)) ||
@@ -409,6 +410,8 @@ extern "C" int smx_fp32_plan_create(const smx_plan* pl, const smx_tree* tree, co
         return rc;
       smx_spectral64& s = h->spectral64;
       s.d_in = d;
+      s.d_out = dout;
+      s.dstride = int(p64.scalar["dstride"]);
       s.row = int(p64.scalar["row"]);
       s.n_hb = int(p64.scalar["n_hb"]);
       s.n_vp = int(p64.scalar["n_vp"]);
@@ -432,10 +435,11 @@ extern "C" int smx_fp32_plan_create(const smx_plan* pl, const smx_tree* tree, co
       s.node_c = fa("node_c");
       s.cold_ab = fa("cold_ab");
       s.terms = fa("terms");
+      s.coef = fa("coef");
       s.fam_a = h->fa64.p;
       s.fam_b = h->fb64.p;
       s.fam = h->fam.p;
-      s.c0 = C64_h[0];
+      s.c0 = h->C64.p;  // row 0: the root's coefficients
       h->have64 = true;
       if (cudaStreamSynchronize(st) != cudaSuccess)  // the host blobs go out of scope
         return smx::set_error(SMX_ERR_CUDA, "smx_fp32_plan_create: sync failed");

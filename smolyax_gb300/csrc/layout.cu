@@ -769,29 +769,29 @@ bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* ma
 
 // Port of spectral.py build_layout64: the FP64 evaluator's layout, every
 // entry of Lambda one term (slot, coefficient), no padding.
-bool build_perpoint64(const Tree& tr, const double* C, const int64_t* maxdeg, int d, const int32_t* fam,
+bool build_perpoint64(const Tree& tr, const double* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
                       const double* fa, const double* fb, Tables& out) {
   constexpr int nseg = 4;
-  const int64_t n = tr.n;
+  const int64_t dstride = d_out == 1 ? 1 : round4(d_out);
   Front f = front(tr, maxdeg, d);
   const int64_t row = (f.n_hb + f.n_vp) | 1;  // odd: 8-byte row reads of 16 consecutive points on distinct banks
-  std::vector<int64_t> t_slot;
-  std::vector<double> t_coef;
+  std::vector<int64_t> t_slot, t_ent;
   const int64_t NN = int64_t(f.nodes.size());
   std::vector<int32_t> node_tab(NN * 4);
-  std::vector<double> node_c(NN, 0.0), cost_nodes(NN);
+  std::vector<double> node_c(size_t(NN * dstride), 0.0), cost_nodes(NN);
   for (int64_t i = 0; i < NN; ++i) {
     const int64_t e = f.nodes[i];
     const int64_t t0 = int64_t(t_slot.size());
     for (int64_t q = f.starts[i]; q < f.ends[i]; ++q) {
       t_slot.push_back(f.slot[f.leaf[q]]);
-      t_coef.push_back(C[f.leaf[q]]);
+      t_ent.push_back(f.leaf[q]);
     }
     node_tab[i * 4 + 0] = int32_t((e != 0 ? f.slot[e] : 0) | (int64_t(tr.level[e]) << 16));
     node_tab[i * 4 + 1] = int32_t(e != 0 && f.vp_row[e] >= 0 ? f.vp_row[e] : -1);
     node_tab[i * 4 + 2] = int32_t(t0);
     node_tab[i * 4 + 3] = int32_t(t_slot.size());
-    if (e != 0) node_c[i] = C[e];
+    if (e != 0)
+      for (int o = 0; o < d_out; ++o) node_c[size_t(i * dstride + o)] = C[e * d_out + o];
     cost_nodes[i] = 4.0 + double(f.ends[i] - f.starts[i]);
   }
   std::vector<int64_t> ce = f.cold;
@@ -814,7 +814,7 @@ bool build_perpoint64(const Tree& tr, const double* C, const int64_t* maxdeg, in
       const int64_t t0 = int64_t(t_slot.size());
       for (size_t r = q; r < q2; ++r) {
         t_slot.push_back(f.vp_row[tr.parent[ce[r]]]);
-        t_coef.push_back(C[ce[r]]);
+        t_ent.push_back(ce[r]);
       }
       runs.insert(runs.end(), {int32_t(t0), int32_t(t_slot.size()), g, 0});
       gmax = std::max(gmax, g);
@@ -831,11 +831,16 @@ bool build_perpoint64(const Tree& tr, const double* C, const int64_t* maxdeg, in
   for (int64_t i = 0; i <= NN; ++i)
     if (i == NN || tr.level[f.nodes[i]] <= 1) allowed_nodes.push_back(i);
   for (int64_t i = 0; i <= int64_t(cost_cold.size()); ++i) all_cold.push_back(i);
-  std::vector<double> terms(std::max<size_t>(t_slot.size(), 1) * 2, 0.0);
-  for (size_t q = 0; q < t_slot.size(); ++q) {
+  const size_t T = t_slot.size();
+  std::vector<double> terms(std::max<size_t>(T, 1) * 2, 0.0), coef;
+  if (d_out > 1) coef.assign(std::max<size_t>(T, 1) * size_t(dstride), 0.0);
+  for (size_t q = 0; q < T; ++q) {
     const int64_t bits = t_slot[q];
     memcpy(&terms[2 * q], &bits, sizeof(bits));
-    terms[2 * q + 1] = t_coef[q];
+    if (d_out == 1)
+      terms[2 * q + 1] = C[t_ent[q]];
+    else
+      for (int o = 0; o < d_out; ++o) coef[q * size_t(dstride) + o] = C[t_ent[q] * d_out + o];
   }
   out.i32["node_seg"] = cuts(cost_nodes, allowed_nodes, nseg);
   out.i32["cold_seg"] = cuts(cost_cold, all_cold, nseg);
@@ -848,6 +853,9 @@ bool build_perpoint64(const Tree& tr, const double* C, const int64_t* maxdeg, in
   out.f64["node_c"] = node_c;
   out.f64["cold_ab"] = cold_ab;
   out.f64["terms"] = terms;
+  out.f64["coef"] = coef;
+  out.scalar["d_out"] = double(d_out);
+  out.scalar["dstride"] = double(dstride);
   out.scalar["row"] = double(row);
   out.scalar["n_hb"] = double(f.n_hb);
   out.scalar["n_vp"] = double(f.n_vp);
@@ -855,8 +863,7 @@ bool build_perpoint64(const Tree& tr, const double* C, const int64_t* maxdeg, in
   out.scalar["n_nodes"] = double(NN);
   out.scalar["n_cold_groups"] = double(cost_cold.size());
   out.scalar["max_depth"] = double(f.max_depth);
-  out.scalar["n_terms"] = double(t_slot.size());
-  (void)n;
+  out.scalar["n_terms"] = double(T);
   return true;
 }
 
@@ -947,11 +954,10 @@ extern "C" int smx_layout_build_f64(int kind, int64_t n, const int32_t* parent, 
                   fa && fb && C,
               "smx_layout_build_f64: bad arguments");
   SMX_REQUIRE(kind == SMX_LAYOUT_PERPOINT, "smx_layout_build_f64: only the per-point layout has an FP64 form");
-  SMX_REQUIRE(d_out == 1, "smx_layout_build_f64: the FP64 evaluator has one output");
   *out = nullptr;
   smx::layout::Tree tr{n, parent, dim, deg, level, rank, rem};
   auto h = std::make_unique<smx_host_tables>();
-  if (!smx::layout::build_perpoint64(tr, C, maxdeg, d, fam, fa, fb, h->t))
+  if (!smx::layout::build_perpoint64(tr, C, d_out, maxdeg, d, fam, fa, fb, h->t))
     return smx::set_error(SMX_ERR_UNSUPPORTED, "smx_layout_build_f64: the plan is outside this evaluator's limits");
   *out = h.release();
   return SMX_OK;

@@ -38,9 +38,9 @@ bool build_blocked(const Tree& tr, const float* C, const int64_t* maxdeg, int d,
                    const double* fb, Tables& out);
 bool build_perpoint(const Tree& tr, const float* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
                     const double* fa, const double* fb, Tables& out);
-// The FP64 evaluator's layout (one output, FP64 coefficients C[n]): every
-// entry one term (slot, coefficient); FP64 tables in Tables::f64.
-bool build_perpoint64(const Tree& tr, const double* C, const int64_t* maxdeg, int d, const int32_t* fam,
+// The FP64 evaluator's layout (FP64 coefficients C[n][d_out]): every entry
+// one term (slot, coefficients); FP64 tables in Tables::f64.
+bool build_perpoint64(const Tree& tr, const double* C, int d_out, const int64_t* maxdeg, int d, const int32_t* fam,
                       const double* fa, const double* fb, Tables& out);
 bool build_tape(const Tree& tr, const int64_t* maxdeg, int d, Tables& out);
 bool build_blocked_tc(const Tree& tr, const float* C, const int64_t* maxdeg, int d, const int32_t* fam,

@@ -1,4 +1,4 @@
-// FP64 evaluation of the orthogonal form, one output.
+// FP64 evaluation of the orthogonal form (one output per pass, or four).
 //
 // The interpolant's combination sum (interpolation.py:264-304 over
 // barycentric.py:69-123) visits every tensor-product summand: ~6.6e4 FP64
@@ -35,22 +35,23 @@ constexpr int kMaxRec = 512;
 constexpr size_t kSmemMax = 227 * 1024;
 
 struct Spec64Args {
-  int d_in, row, n_hb, n_vp, n_hot_dims;
+  int d_in, d_out, dstride, row, n_hb, n_vp, n_hot_dims;
   int node_seg[kSeg + 1];
   int cold_seg[kSeg + 1];
   const int32_t* hot_dim;
   const int32_t* hot_deg;
   const int32_t* hot_soff;
   const int4* node;
-  const double* node_c;
+  const double* node_c;  // [n_nodes][dstride]
   const int4* cold;
   const double2* cold_ab;
   const int4* run;
-  const double2* terms;  // (slot bits, coefficient)
+  const double2* terms;  // (slot bits, coefficient when d_out = 1)
+  const double* coef;    // [n_terms][dstride] when d_out > 1
   const double* fam_a;
   const double* fam_b;
   const int32_t* fam;
-  double c0;
+  const double* c0;      // [d_out]
 };
 
 __constant__ double c_alpha64[2][kMaxRec];
@@ -63,22 +64,38 @@ __device__ __forceinline__ double xin(double v) {
   return (b & 0x7fffffffffffffffll) == 0x7ff0000000000000ll ? __longlong_as_double(0x7ff8000000000000ll) : v;
 }
 
-// s + sum over the terms [t0, t1) of coefficient * row value
-__device__ __forceinline__ double sum_terms(const double* __restrict__ Rw, const double2* __restrict__ terms, int t0,
-                                            int t1, double s) {
+// s[q] += sum over the terms [t0, t1) of coefficient (output o0 + q) * row
+// value: one output from the packed terms, or four from the coefficient rows.
+template <int DO>
+__device__ __forceinline__ void sum_terms(const double* __restrict__ Rw, const Spec64Args& a, int o0, int t0, int t1,
+                                          double (&s)[DO]) {
+  if constexpr (DO == 1) {
 #pragma unroll 4
-  for (int t = t0; t < t1; ++t) {
-    const double2 tc = __ldg(terms + t);
-    s = fma(tc.y, Rw[__double2loint(tc.x)], s);
+    for (int t = t0; t < t1; ++t) {
+      const double2 tc = __ldg(a.terms + t);
+      s[0] = fma(tc.y, Rw[__double2loint(tc.x)], s[0]);
+    }
+  } else {
+#pragma unroll 2
+    for (int t = t0; t < t1; ++t) {
+      const double r = Rw[__double2loint(__ldg(&a.terms[t].x))];
+      const double2* c = reinterpret_cast<const double2*>(a.coef + int64_t(t) * a.dstride + o0);
+      const double2 c01 = __ldg(c), c23 = __ldg(c + 1);
+      s[0] = fma(c01.x, r, s[0]);
+      s[1] = fma(c01.y, r, s[1]);
+      s[2] = fma(c23.x, r, s[2]);
+      s[3] = fma(c23.y, r, s[3]);
+    }
   }
-  return s;
 }
 
+template <int DO>
 __global__ void __launch_bounds__(kThreads, 2) spectral_eval64_kernel(Spec64Args a, const double* __restrict__ x,
                                                                       int64_t P, int64_t ldx,
                                                                       double* __restrict__ y) {
   extern __shared__ __align__(16) double sm64[];
-  double* RED = sm64 + size_t(a.row) * kTP;  // [kSeg][kTP]
+  double* RED = sm64 + size_t(a.row) * kTP;  // [kSeg][DO][kTP]
+  const int o0 = blockIdx.y * DO;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int seg = warp / (kTP / 32);
   const int pl = (warp % (kTP / 32)) * 32 + lane;
@@ -107,7 +124,9 @@ __global__ void __launch_bounds__(kThreads, 2) spectral_eval64_kernel(Spec64Args
   }
   __syncthreads();
 
-  double acc = 0.0;
+  double acc[DO];
+#pragma unroll
+  for (int q = 0; q < DO; ++q) acc[q] = 0.0;
 
   // phase 1: hot nodes of this segment: v_node * (c_node + sum of the terms of
   // its leaf children); the node's product is stored for the cold entries
@@ -134,7 +153,12 @@ __global__ void __launch_bounds__(kThreads, 2) spectral_eval64_kernel(Spec64Args
         }
       }
       if (nd.y >= 0) Rw[nd.y] = v;
-      acc = fma(v, sum_terms(Rw, a.terms, nd.z, nd.w, __ldg(a.node_c + i)), acc);
+      double sv[DO];
+#pragma unroll
+      for (int q = 0; q < DO; ++q) sv[q] = __ldg(a.node_c + int64_t(i) * a.dstride + o0 + q);
+      sum_terms<DO>(Rw, a, o0, nd.z, nd.w, sv);
+#pragma unroll
+      for (int q = 0; q < DO; ++q) acc[q] = fma(v, sv[q], acc[q]);
     }
   }
   __syncthreads();  // prefix products complete
@@ -175,19 +199,29 @@ __global__ void __launch_bounds__(kThreads, 2) spectral_eval64_kernel(Spec64Args
           pc = pn;
           ++gcur;
         }
-        acc = fma(pc, sum_terms(Rw, a.terms, rr.x, rr.y, 0.0), acc);
+        double sv[DO];
+#pragma unroll
+        for (int q = 0; q < DO; ++q) sv[q] = 0.0;
+        sum_terms<DO>(Rw, a, o0, rr.x, rr.y, sv);
+#pragma unroll
+        for (int q = 0; q < DO; ++q) acc[q] = fma(pc, sv[q], acc[q]);
       }
     }
   }
 
   // phase 3: the segments' sums, in a fixed order
-  RED[seg * kTP + pl] = acc;
+#pragma unroll
+  for (int q = 0; q < DO; ++q) RED[(seg * DO + q) * kTP + pl] = acc[q];
   __syncthreads();
   if (seg == 0 && live) {
-    double s = a.c0;
 #pragma unroll
-    for (int r = 0; r < kSeg; ++r) s += RED[r * kTP + pl];
-    y[p] = s;
+    for (int q = 0; q < DO; ++q) {
+      if (o0 + q >= a.d_out) continue;
+      double s = __ldg(a.c0 + o0 + q);
+#pragma unroll
+      for (int r = 0; r < kSeg; ++r) s += RED[(r * DO + q) * kTP + pl];
+      y[p * a.d_out + o0 + q] = s;
+    }
   }
 }
 
@@ -213,9 +247,12 @@ extern "C" int smx_spectral_eval64(const smx_spectral64* sp, const double* x, in
                                    void* stream) {
   const char* who = "smx_spectral_eval64";
   SMX_REQUIRE(sp != nullptr, "smx_spectral_eval64: null plan");
-  SMX_REQUIRE(sp->fam && sp->fam_a && sp->fam_b && sp->node && sp->node_c && sp->n_nodes >= 1 &&
+  SMX_REQUIRE(sp->d_out >= 1 && (sp->d_out == 1 ? sp->dstride == 1 : sp->dstride % 4 == 0 && sp->dstride >= sp->d_out),
+              "smx_spectral_eval64: bad output stride");
+  SMX_REQUIRE(sp->fam && sp->fam_a && sp->fam_b && sp->node && sp->node_c && sp->c0 && sp->n_nodes >= 1 &&
                   (sp->n_hot_dims == 0 || (sp->hot_dim && sp->hot_deg && sp->hot_soff)) &&
-                  (sp->n_terms == 0 || sp->terms) && (sp->n_cold_groups == 0 || (sp->cold && sp->cold_ab && sp->run)),
+                  (sp->n_terms == 0 || (sp->terms && (sp->d_out == 1 || sp->coef))) &&
+                  (sp->n_cold_groups == 0 || (sp->cold && sp->cold_ab && sp->run)),
               "smx_spectral_eval64: incomplete plan");
   if (sp->max_depth > 8) return smx::set_error(SMX_ERR_UNSUPPORTED, std::string(who) + ": hot nodes deeper than 8");
   SMX_REQUIRE(sp->n_vp >= 1 && sp->row >= sp->n_hb + sp->n_vp, "smx_spectral_eval64: bad row");
@@ -225,9 +262,12 @@ extern "C" int smx_spectral_eval64(const smx_spectral64* sp, const double* x, in
   SMX_REQUIRE(sp->node_seg[0] == 0 && sp->node_seg[kSeg] == sp->n_nodes && sp->cold_seg[0] == 0 &&
                   sp->cold_seg[kSeg] == sp->n_cold_groups,
               "smx_spectral_eval64: segments do not cover the plan");
-  SMX_REQUIRE(!sp->terms || aligned(sp->terms, 16), "smx_spectral_eval64: terms not 16-byte aligned");
+  SMX_REQUIRE((!sp->terms || aligned(sp->terms, 16)) && (!sp->coef || aligned(sp->coef, 32)) &&
+                  (sp->d_out == 1 || aligned(sp->node_c, 32)),
+              "smx_spectral_eval64: tables not aligned");
   SMX_REQUIRE(P >= 0 && ldx >= sp->d_in, "smx_spectral_eval64: bad sizes");
-  const size_t smem = (size_t(sp->row) + kSeg) * kTP * sizeof(double);
+  const int DO = sp->d_out == 1 ? 1 : 4;
+  const size_t smem = (size_t(sp->row) + size_t(kSeg) * DO) * kTP * sizeof(double);
   if (smem > kSmemMax)
     return smx::set_error(SMX_ERR_UNSUPPORTED, std::string(who) + ": per-point row too large for shared memory");
   if (P == 0) return SMX_OK;
@@ -236,6 +276,8 @@ extern "C" int smx_spectral_eval64(const smx_spectral64* sp, const double* x, in
   if (rc) return rc;
   Spec64Args a;
   a.d_in = sp->d_in;
+  a.d_out = sp->d_out;
+  a.dstride = sp->dstride;
   a.row = sp->row;
   a.n_hb = sp->n_hb;
   a.n_vp = sp->n_vp;
@@ -253,18 +295,32 @@ extern "C" int smx_spectral_eval64(const smx_spectral64* sp, const double* x, in
   a.cold_ab = reinterpret_cast<const double2*>(sp->cold_ab);
   a.run = reinterpret_cast<const int4*>(sp->run);
   a.terms = reinterpret_cast<const double2*>(sp->terms);
+  a.coef = sp->coef;
   a.fam_a = sp->fam_a;
   a.fam_b = sp->fam_b;
   a.fam = sp->fam;
   a.c0 = sp->c0;
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(spectral_eval64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemMax)) !=
-        cudaSuccess)
-      return smx::set_error(SMX_ERR_CUDA, "smx_spectral_eval64: shared-memory attribute");
-    attr_set = true;
+  static bool attr_set[2] = {false, false};
+  cudaStream_t st = smx::as_stream(stream);
+  const unsigned chunks = unsigned((sp->d_out + DO - 1) / DO);
+  SMX_REQUIRE(chunks <= 65535, "smx_spectral_eval64: too many outputs");
+  if (DO == 1) {
+    if (!attr_set[0]) {
+      if (cudaFuncSetAttribute(spectral_eval64_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               int(kSmemMax)) != cudaSuccess)
+        return smx::set_error(SMX_ERR_CUDA, "smx_spectral_eval64: shared-memory attribute");
+      attr_set[0] = true;
+    }
+    spectral_eval64_kernel<1><<<dim3(smx::grid_for(P, kTP), chunks), kThreads, smem, st>>>(a, x, P, ldx, y);
+  } else {
+    if (!attr_set[1]) {
+      if (cudaFuncSetAttribute(spectral_eval64_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               int(kSmemMax)) != cudaSuccess)
+        return smx::set_error(SMX_ERR_CUDA, "smx_spectral_eval64: shared-memory attribute");
+      attr_set[1] = true;
+    }
+    spectral_eval64_kernel<4><<<dim3(smx::grid_for(P, kTP), chunks), kThreads, smem, st>>>(a, x, P, ldx, y);
   }
-  spectral_eval64_kernel<<<smx::grid_for(P, kTP), kThreads, smem, smx::as_stream(stream)>>>(a, x, P, ldx, y);
   SMX_LAUNCH_CHECK("smx_spectral_eval64");
   return SMX_OK;
 }

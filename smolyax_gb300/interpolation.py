@@ -76,10 +76,10 @@ class SmolyakBarycentricInterpolator:
                  f: Callable = None, n_inputs: int = None, memory_limit: float = 4.0,
                  precision: str = "fp64") -> None:
         """Keyword arguments as in the reference (``interpolation.py:51-113``), plus
-        ``precision``: "fp64" (default) evaluates in FP64 -- one-output plans over
-        Leja / Gauss-Hermite rules in the orthogonal-polynomial form (coefficients
-        from compensated FP64 sums; ~1e-14 relative to the exact value, ~10x
-        faster), everything else as the reference's combination sum;
+        ``precision``: "fp64" (default) evaluates in FP64 -- plans over Leja /
+        Gauss-Hermite rules in the orthogonal-polynomial form (coefficients from
+        compensated FP64 sums; ~1e-14 relative to the exact value, ~10x faster),
+        other rules as the reference's combination sum;
         "fp64_barycentric" always evaluates the combination sum (the reference's
         algorithm, interpolation.py:264-304); "fp32" evaluates the orthogonal form
         in FP32 and returns FP32 values."""
@@ -522,14 +522,14 @@ class SmolyakBarycentricInterpolator:
         return y
 
     def _fp64_orthogonal(self):
-        """The orthogonal form that FP64 evaluation uses, or None: one output,
-        Leja or Gauss-Hermite rules in every dimension (their polynomial families
-        are the form's), degrees within the recurrence tables, and a per-point
-        row of the FP64 evaluator within shared memory."""
+        """The orthogonal form that FP64 evaluation uses, or None: Leja or
+        Gauss-Hermite rules in every dimension (their polynomial families are the
+        form's), degrees within the recurrence tables, and a per-point row of
+        the FP64 evaluator within shared memory."""
         if self._fp64_form_ok is None:
             from .spectral import MAX_DEGREE
 
-            self._fp64_form_ok = (self._d_out == 1 and int(np.max(self._maxdeg, initial=0)) < MAX_DEGREE
+            self._fp64_form_ok = (int(np.max(self._maxdeg, initial=0)) < MAX_DEGREE
                                   and all(isinstance(g, (_nodes.Leja1D, _nodes.GaussHermite1D))
                                           for g in self._node_gen)
                                   and self.spectral_plan().fp64_form() is not None)

@@ -407,45 +407,46 @@ class SpectralPlan:
         return y
 
     def fp64_form(self):
-        """FP64 tables of the orthogonal form for ``csrc/spectral64.cu`` (one
-        output), built on first use from the same tree and the FP64
-        coefficients; None where that evaluator does not apply (more outputs,
-        hot nodes deeper than 8, or a per-point row beyond shared memory)."""
+        """FP64 tables of the orthogonal form for ``csrc/spectral64.cu``, built on
+        first use from the same tree and the FP64 coefficients; None where that
+        evaluator does not apply (hot nodes deeper than 8, or a per-point row
+        beyond shared memory)."""
         if self._f64 is None:
             self._f64 = False
             tr, _, maxdeg, fam, fa, fb, T, _ = self._fwd_args
             d = int(self.c.d_in)
-            if self.c.d_out == 1:
-                lay = build_layout64(tr, self.C64.cpu().numpy(), maxdeg, d, fam, fa, fb)
-                row = int(lay["row"])
-                if (row + 4) * 64 * 8 <= 227 * 1024 and int(lay["max_depth"]) <= 8:
-                    k = {}
-                    for name in ("hot_dim", "hot_deg", "hot_soff", "node", "cold", "run"):
-                        k[name] = T(lay[name], torch.int32)
-                    for name in ("node_c", "cold_ab", "terms"):
-                        k[name] = T(lay[name], torch.float64)
-                    st = capi.SmxSpectral64()
-                    st.d_in, st.row = d, row
-                    for name in ("n_hb", "n_vp", "n_hot_dims", "n_nodes", "n_cold_groups", "max_depth", "n_terms"):
-                        setattr(st, name, int(lay[name]))
-                    for i in range(5):
-                        st.node_seg[i] = int(lay["node_seg"][i])
-                        st.cold_seg[i] = int(lay["cold_seg"][i])
-                    for name, t in k.items():
-                        setattr(st, name, t.data_ptr() if t.numel() else None)
-                    st.fam_a, st.fam_b, st.fam = self.fa64.data_ptr(), self.fb64.data_ptr(), self.fam.data_ptr()
-                    st.c0 = float(self.C64[0, 0].item())
-                    self._f64 = (st, k)
+            lay = build_layout64(tr, self.C64.cpu().numpy(), maxdeg, d, fam, fa, fb)
+            row = int(lay["row"])
+            DO = 1 if lay["d_out"] == 1 else 4
+            if (row + 4 * DO) * 64 * 8 <= 227 * 1024 and int(lay["max_depth"]) <= 8:
+                k = {}
+                for name in ("hot_dim", "hot_deg", "hot_soff", "node", "cold", "run"):
+                    k[name] = T(lay[name], torch.int32)
+                for name in ("node_c", "cold_ab", "terms", "coef"):
+                    k[name] = T(lay[name], torch.float64)
+                k["c0"] = self.C64[0].contiguous()
+                st = capi.SmxSpectral64()
+                st.d_in, st.row = d, row
+                for name in ("d_out", "dstride", "n_hb", "n_vp", "n_hot_dims", "n_nodes", "n_cold_groups", "max_depth",
+                             "n_terms"):
+                    setattr(st, name, int(lay[name]))
+                for i in range(5):
+                    st.node_seg[i] = int(lay["node_seg"][i])
+                    st.cold_seg[i] = int(lay["cold_seg"][i])
+                for name, t in k.items():
+                    setattr(st, name, t.data_ptr() if t.numel() else None)
+                st.fam_a, st.fam_b, st.fam = self.fa64.data_ptr(), self.fb64.data_ptr(), self.fam.data_ptr()
+                self._f64 = (st, k)
         return self._f64 or None
 
     def evaluate64(self, x, y):
-        """y[P] (FP64, contiguous) at x[P, d_in] (FP64, rows contiguous, on the
-        device) through the FP64 evaluator of the orthogonal form."""
+        """y[P, d_out] (FP64, contiguous) at x[P, d_in] (FP64, rows contiguous, on
+        the device) through the FP64 evaluator of the orthogonal form."""
         import ctypes
 
         form = self.fp64_form()
         if form is None:
-            raise ValueError("the plan has no FP64 orthogonal form (one output and a per-point row within shared memory)")
+            raise ValueError("the plan has no FP64 orthogonal form (a per-point row within shared memory)")
         if x.dim() != 2 or (x.shape[0] > 1 and x.stride(1) != 1):
             x = x.contiguous()
         ldx = int(x.stride(0)) if x.shape[0] > 1 else int(x.shape[1])  # a one-row tensor may carry any row stride
@@ -795,34 +796,39 @@ def build_layout(tr, C, maxdeg, d, d_out, fam, fa, fb, nseg=4):
 
 
 def build_layout64(tr, C, maxdeg, d, fam, fa, fb, nseg=4):
-    """Layout of the FP64 evaluator of the orthogonal form (one output,
-    ``csrc/spectral64.cu``): the per-point structure of ``build_layout`` with
-    every entry of Lambda as exactly one term (row slot, FP64 coefficient) and
-    no padding -- at GB300's FP64 rate every term is a multiply-add that
-    counts.  Hot nodes (DFS pre-order) carry the terms of their hot leaf
-    children; each cold dimension is a group whose runs (one per degree) hold
-    the terms over the prefix slots.  ``terms`` is [n_terms, 2] FP64 with the
-    slot's integer bits in column 0.  C: FP64 coefficients of every entry."""
-    C = np.asarray(C, dtype=np.float64).reshape(-1)
+    """Layout of the FP64 evaluator of the orthogonal form (``csrc/spectral64.cu``):
+    the per-point structure of ``build_layout`` with every entry of Lambda as
+    exactly one term (row slot, FP64 coefficients) and no padding -- at GB300's
+    FP64 rate every term is a multiply-add that counts.  Hot nodes (DFS
+    pre-order) carry the terms of their hot leaf children; each cold dimension
+    is a group whose runs (one per degree) hold the terms over the prefix
+    slots.  ``terms`` is [n_terms, 2] FP64 with the slot's integer bits in
+    column 0 and, for one output, the coefficient in column 1; with several
+    outputs the coefficients are ``coef`` [n_terms, dstride].  C: FP64
+    coefficients [entry] or [entry, d_out]."""
+    C = np.asarray(C, dtype=np.float64)
+    C = C.reshape(C.shape[0], -1)
+    d_out = C.shape[1]
+    dstride = 1 if d_out == 1 else _round4(d_out)
     fr = _layout_front(tr, maxdeg, d)
     dim, deg, level, parent = fr["dim"], fr["deg"], fr["level"], fr["parent"]
     n_hb, n_vp, nodes, slot, vp_row = fr["n_hb"], fr["n_vp"], fr["nodes"], fr["slot"], fr["vp_row"]
     leaf_e, starts, ends, cold_e = fr["leaf_e"], fr["starts"], fr["ends"], fr["cold_e"]
     row = (n_hb + n_vp) | 1  # odd: 8-byte row reads of 16 consecutive points fall on distinct banks
-    t_slot, t_coef = [], []
+    t_slot, t_ent = [], []
     node_tab = np.zeros((nodes.size, 4), dtype=np.int64)
-    node_c = np.zeros(nodes.size)
+    node_c = np.zeros((nodes.size, dstride))
     cost_nodes = np.zeros(nodes.size)
     for i, e in enumerate(nodes):
         le = leaf_e[starts[i] : ends[i]]
         t0 = len(t_slot)
         t_slot.extend(slot[le].tolist())
-        t_coef.extend(C[le].tolist())
+        t_ent.extend(le.tolist())
         sl = int(slot[e]) if e != 0 else 0
         node_tab[i] = (sl | (int(level[e]) << 16), int(vp_row[e]) if e != 0 and vp_row[e] >= 0 else -1, t0,
                        len(t_slot))
-        if e != 0:  # the root's coefficient is c0
-            node_c[i] = C[e]
+        if e != 0:  # the root's coefficients are c0
+            node_c[i, :d_out] = C[e]
         cost_nodes[i] = 4 + le.size
     ce = cold_e[np.lexsort((vp_row[parent[cold_e]], deg[cold_e], dim[cold_e]))] if cold_e.size else cold_e
     cold_tab, cold_ab, runs, cost_cold = [], [], [], []
@@ -842,7 +848,7 @@ def build_layout64(tr, C, maxdeg, d, fam, fa, fb, nseg=4):
             grp = ce[q:q2]
             t0 = len(t_slot)
             t_slot.extend(vp_row[parent[grp]].tolist())
-            t_coef.extend(C[grp].tolist())
+            t_ent.extend(grp.tolist())
             runs.append((t0, len(t_slot), g, 0))
             q = q2
         gmax = int(deg[ce[i:j]].max())
@@ -852,33 +858,43 @@ def build_layout64(tr, C, maxdeg, d, fam, fa, fb, nseg=4):
         cost_cold.append(3.0 + (j - i) + 3.0 * gmax)
         i = j
     allowed_nodes = [q for q in range(nodes.size + 1) if q == nodes.size or level[nodes[q]] <= 1]
-    terms = np.zeros((max(len(t_slot), 1), 2))
-    terms[: len(t_slot), 0] = np.asarray(t_slot, dtype=np.int64).view(np.float64)
-    terms[: len(t_slot), 1] = t_coef
+    T = len(t_slot)
+    terms = np.zeros((max(T, 1), 2))
+    terms[:T, 0] = np.asarray(t_slot, dtype=np.int64).view(np.float64)
+    coef = np.zeros((0, 1))
+    if d_out == 1:
+        terms[:T, 1] = C[t_ent, 0]
+    else:
+        coef = np.zeros((max(T, 1), dstride))
+        coef[:T, :d_out] = C[t_ent]
     as_i32 = lambda v, w: np.asarray(v, dtype=np.int64).reshape(-1, w).astype(np.int32)
     return dict(
-        row=row, n_hb=n_hb, n_vp=n_vp, n_hot_dims=int(fr["hot_dims"].size), n_nodes=int(nodes.size),
-        n_cold_groups=len(cold_tab), max_depth=fr["max_depth"], n_terms=len(t_slot),
-        node_seg=_cuts(cost_nodes, allowed_nodes, nseg), cold_seg=_cuts(np.asarray(cost_cold), list(range(len(cost_cold) + 1)), nseg),
+        d_out=d_out, dstride=dstride, row=row, n_hb=n_hb, n_vp=n_vp, n_hot_dims=int(fr["hot_dims"].size),
+        n_nodes=int(nodes.size), n_cold_groups=len(cold_tab), max_depth=fr["max_depth"], n_terms=T,
+        node_seg=_cuts(cost_nodes, allowed_nodes, nseg),
+        cold_seg=_cuts(np.asarray(cost_cold), list(range(len(cost_cold) + 1)), nseg),
         hot_dim=fr["hot_dims"].astype(np.int32), hot_deg=fr["hot_deg"].astype(np.int32),
         hot_soff=fr["hot_soff"].astype(np.int32), node=as_i32(node_tab, 4), node_c=node_c,
         cold=as_i32(cold_tab, 4) if cold_tab else np.zeros((0, 4), np.int32),
         cold_ab=np.asarray(cold_ab, dtype=np.float64).reshape(-1, 2),
-        run=as_i32(runs, 4) if runs else np.zeros((0, 4), np.int32), terms=terms,
+        run=as_i32(runs, 4) if runs else np.zeros((0, 4), np.int32), terms=terms, coef=coef,
     )
 
 
 def evaluate_layout64(lay, x, fam, fa, fb, c0):
-    """Host FP64 replay of the FP64 evaluator's sums over a layout (tests)."""
+    """Host FP64 replay of the FP64 evaluator's sums over a layout (tests):
+    [P, d_out]."""
     P = x.shape[0]
+    d_out = lay["d_out"]
     R = np.zeros((P, lay["row"]))
     hd, hg, ho = lay["hot_dim"], lay["hot_deg"], lay["hot_soff"]
     for q in range(hd.size):
         R[:, ho[q] : ho[q] + hg[q]] = _phi_table(int(fam[hd[q]]), fa[hd[q]] * x[:, hd[q]] + fb[hd[q]], int(hg[q]))[1:].T
     R[:, lay["n_hb"]] = 1.0
-    slots = lay["terms"][: lay["n_terms"], 0].view(np.int64)
-    coef = lay["terms"][: lay["n_terms"], 1]
-    acc = np.full(P, float(c0))
+    T = lay["n_terms"]
+    slots = lay["terms"][:T, 0].view(np.int64)
+    coef = lay["terms"][:T, 1:2] if d_out == 1 else lay["coef"][:T, :d_out]
+    acc = np.tile(np.asarray(c0, dtype=float).reshape(1, -1), (P, 1))
     stack = [np.ones(P)] * 9
     for i, nd in enumerate(lay["node"]):
         depth = int(nd[0]) >> 16
@@ -886,8 +902,8 @@ def evaluate_layout64(lay, x, fam, fa, fb, c0):
         stack[depth] = v
         if nd[1] >= 0:
             R[:, nd[1]] = v
-        s = lay["node_c"][i] + R[:, slots[nd[2] : nd[3]]] @ coef[nd[2] : nd[3]]
-        acc += v * s
+        s = lay["node_c"][i, :d_out][None, :] + R[:, slots[nd[2] : nd[3]]] @ coef[nd[2] : nd[3]]
+        acc += v[:, None] * s
     for g, cg in enumerate(lay["cold"]):
         dd, r0, r1, w = (int(v) for v in cg)
         z = lay["cold_ab"][g, 0] * x[:, dd] + lay["cold_ab"][g, 1]
@@ -895,7 +911,7 @@ def evaluate_layout64(lay, x, fam, fa, fb, c0):
         ph = _phi_table((w >> 16) & 0xF, z, gmax)
         for r in range(r0, r1):
             t0, t1, gg, _ = (int(v) for v in lay["run"][r])
-            acc += ph[gg] * (R[:, slots[t0:t1]] @ coef[t0:t1])
+            acc += ph[gg][:, None] * (R[:, slots[t0:t1]] @ coef[t0:t1])
     return acc
 
 

@@ -8,9 +8,9 @@ every call), checked bit for bit, and the same tables; its launch choices
 rules, so the values, dL/dx and dL/d(rows of F64) are compared with the
 package's at FP32 rounding (2^-20 of their scale), the two C entry points
 with each other bit for bit, and the values with the FP64 path at the 1e-6
-bound (element-wise: Leja cases).  For one output the handle also carries
-the FP64 tables of the orthogonal form: ``smx_eval(plan, 64, ...)`` then
-equals the package's precision "fp64" bit for bit."""
+bound (element-wise: Leja cases).  The handle also carries the FP64 tables
+of the orthogonal form: ``smx_eval(plan, 64, ...)`` then equals the
+package's precision "fp64" bit for bit."""
 import ctypes
 
 import numpy as np
@@ -95,11 +95,10 @@ def test_fp32_form_and_vjp_through_the_c_abi(kind, d, t, d_out, evaluator):
             assert float(((y1.double() - y64).abs() / y64.abs()).max()) < 1e-6
         # without the FP32 form, precision 32 is refused
         assert lib.smx_eval(ip._plan.ref(), 32, _capi.ptr(x), P, d, _capi.ptr(y1), None, 0, st) == -5
-        # FP64: one-output plans carry the FP64 tables of the orthogonal form, and
+        # FP64: the handle carries the FP64 tables of the orthogonal form, and
         # smx_eval(plan, 64, ...) with plan->fp32 set evaluates through them -- the
-        # same tables and kernel as the package's precision "fp64", bit for bit;
-        # other plans keep the combination sum
-        assert lib.smx_fp32_plan_has_fp64(h) == (1 if d_out == 1 else 0)
+        # same tables and kernel as the package's precision "fp64", bit for bit
+        assert lib.smx_fp32_plan_has_fp64(h) == 1
         y64c = torch.full((P, d_out), float("nan"), dtype=torch.float64, device="cuda")
         ip._plan.c.fp32 = h
         try:
@@ -108,13 +107,9 @@ def test_fp32_form_and_vjp_through_the_c_abi(kind, d, t, d_out, evaluator):
             _capi.call("smx_eval", ip._plan.ref(), 64, _capi.ptr(x), P, d, _capi.ptr(y64c), _capi.ptr(ws), nws, st)
         finally:
             ip._plan.c.fp32 = None
-        if d_out == 1:
-            assert ip._fp64_orthogonal() is not None
-            torch.cuda.synchronize()
-            assert torch.equal(y64c, y64)
-        else:
-            assert torch.equal(y64c, ip(x, precision="fp64_barycentric"))
-            assert lib.smx_fp32_eval64(h, _capi.ptr(x), P, d, _capi.ptr(y64c), st) == -5
+        assert ip._fp64_orthogonal() is not None
+        torch.cuda.synchronize()
+        assert torch.equal(y64c, y64)
         # vector-Jacobian products
         g = torch.as_tensor(rng.normal(size=(P, d_out)).astype(np.float32), device="cuda")
         R = int(ip._plan.c.n_entries)

@@ -1,9 +1,10 @@
 """FP64 path on the GPU against the reference's outputs (golden vectors).
 
 Both FP64 evaluators are checked: the default ("fp64": the orthogonal form in
-FP64 for one-output Leja / Gauss-Hermite plans, ``csrc/spectral64.cu``) and
+FP64 for Leja / Gauss-Hermite plans, ``csrc/spectral64.cu``) and
 the reference's combination sum ("fp64_barycentric", ``csrc/eval64.cu``).
-Small cases: 1e-12 relative against the reference's values; gradients 1e-10
+Small cases: 1e-12 relative against the reference's values (absolute floor
+1e-13, times the output scale for the orthogonal form); gradients 1e-10
 relative with an absolute floor, NaN exactly where the reference has NaN.
 Benchmark workloads: the contract of ``gpu_helpers.check_fp64`` -- at least as
 accurate as the reference against the extended-precision value of the same
@@ -37,7 +38,12 @@ def test_small_cases(name, precision):
     ip = _interp(node_gen=product_generator(spec, len(k)), k=k, t=t, d_out=d_out, f=f)
     x = z[name + "/x"]
     y = ip(x, precision=precision).cpu().numpy()
-    np.testing.assert_allclose(y, z[name + "/y"], rtol=1e-12, atol=1e-13)
+    # the absolute floor: 1e-13, times the output scale for the orthogonal form,
+    # which reproduces a nodal value (here an exact 0 at a grid point) to
+    # rounding instead of by the barycentric formula's one-hot
+    ref = np.asarray(z[name + "/y"], dtype=float)
+    floor = 1e-13 * (max(1.0, float(np.abs(ref).max())) if precision == "fp64" else 1.0)
+    np.testing.assert_allclose(y, ref, rtol=1e-12, atol=floor)
     g = ip.gradient(x[:-1]).cpu().numpy()
     assert_close_nan(g, z[name + "/grad"], rtol=1e-10, atol=1e-11)
     np.testing.assert_allclose(ip.integral().cpu().numpy(), z[name + "/integral"], rtol=1e-12, atol=1e-12)
@@ -73,27 +79,29 @@ def test_config2_subset(precision):
     assert (ip.n_f_evals, ip.n_f_evals_new) == tuple(int(v) for v in CFG["cfg2/n_f_evals"])
 
 
-def test_config4_subset():
+@pytest.mark.parametrize("precision", ["fp64", "fp64_barycentric"])
+def test_config4_subset(precision):
     from smolyax_gb300 import nodes
 
     d = 200
     k = np.log((2 + np.arange(d)) / np.log(2))
     ip = _interp(node_gen=nodes.Leja(dim=d), k=k, t=7.853604, d_out=64, f=fns.rational_vec(d, 64, seed=0))
     x = np.random.default_rng(1).uniform(-1, 1, (64, d))
-    check_fp64(ip(x).cpu().numpy(), CFG["cfg4/y"], EXACT["cfg4/y"])
+    check_fp64(ip(x, precision=precision).cpu().numpy(), CFG["cfg4/y"], EXACT["cfg4/y"])
     check_fp64_grad(ip.gradient(x[:3]).cpu().numpy(), CFG["cfg4/grad"], EXACT["cfg4/grad"])
     check_fp64(ip.integral().cpu().numpy(), CFG["cfg4/integral"], EXACT["cfg4/integral"], what="integral")
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp64_barycentric"])
 @pytest.mark.parametrize("tag,t", [("cfg3alt", 7.723434), ("cfg3", 9.464636)])
-def test_config3_gauss_hermite(tag, t):
+def test_config3_gauss_hermite(tag, t, precision):
     from smolyax_gb300 import nodes
 
     d = 100
     k = np.log((2 + np.arange(d)) / np.log(2))
     ip = _interp(node_gen=nodes.GaussHermite(dim=d), k=k, t=t, d_out=8, f=fns.exponential(d, 8, seed=0))
     x = np.random.default_rng(1).normal(size=(32, d))
-    check_fp64(ip(x).cpu().numpy(), CFG[tag + "/y"], EXACT[tag + "/y"])
+    check_fp64(ip(x, precision=precision).cpu().numpy(), CFG[tag + "/y"], EXACT[tag + "/y"])
     check_fp64(ip.integral().cpu().numpy(), CFG[tag + "/integral"], EXACT[tag + "/integral"], what="integral")
     assert (ip.n_f_evals, ip.n_f_evals_new) == tuple(int(v) for v in CFG[tag + "/n_f_evals"])
     if tag == "cfg3alt":

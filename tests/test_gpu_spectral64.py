@@ -1,6 +1,6 @@
 """FP64 evaluator of the orthogonal form (``csrc/spectral64.cu``).
 
-It is what ``ip(x)`` runs for one-output Leja / Gauss-Hermite plans.  Bounds:
+It is what ``ip(x)`` runs for Leja / Gauss-Hermite plans.  Bounds:
 against the extended-precision values of the benchmark workloads (cfg1,
 cfg2) 1e-13 element-wise relative -- tighter than the FP64 contract of
 ``gpu_helpers.check_fp64`` (1e-12, or the reference's own error), because the
@@ -9,7 +9,8 @@ is taken by compensated sums once, in the coefficients); against the
 barycentric FP64 evaluator 1e-12 element-wise on rules, domains, partial and
 multi-tile point counts.  Non-finite coordinates: NaN / Inf in an active
 dimension gives NaN for that point only; inactive dimensions are never read.
-The tables are checked to select this evaluator (``_fp64_orthogonal``).
+Plans with several outputs run four outputs per pass.  The tables are checked
+to select this evaluator (``_fp64_orthogonal``).
 """
 import numpy as np
 import pytest
@@ -152,8 +153,7 @@ def test_nodes_nonfinite_and_inactive():
 
 
 def test_device_input_strides_and_dispatch():
-    """Device FP64 inputs (contiguous or not) give the same values; plans with
-    more outputs keep the barycentric evaluator."""
+    """Device FP64 inputs (contiguous or not) give the same values."""
     from smolyax_gb300 import nodes
 
     d = 50
@@ -163,5 +163,28 @@ def test_device_input_strides_and_dispatch():
     y_host = ip(x).cpu().numpy()
     xd = torch.as_tensor(np.concatenate([x, x], axis=1), device="cuda")[:, :d]
     np.testing.assert_array_equal(ip(xd).cpu().numpy(), y_host)
-    two = _interp(node_gen=nodes.Leja(dim=d), k=k, t=6.0, d_out=2, f=fns.rational_vec(d, 2, seed=7))
-    assert two._fp64_orthogonal() is None
+
+
+@pytest.mark.parametrize("kind,d,t,d_out", [("leja", 30, 6.0, 2), ("leja", 60, 6.5, 7), ("gh", 40, 6.0, 9),
+                                            ("leja", 12, 7.0, 64)])
+def test_several_outputs(kind, d, t, d_out):
+    """Several outputs (four per pass, the last pass partial): against the
+    barycentric FP64 evaluator at 1e-12 element-wise for Leja plans, 1e-11 for
+    Gauss-Hermite ones, whose combination sum itself cancels to 1e-12 .. 1e-11
+    (measured against extended precision at the benchmark configurations)."""
+    from smolyax_gb300 import nodes
+
+    k = np.log((2 + np.arange(d)) / np.log(2))
+    rng = np.random.default_rng(d_out)
+    if kind == "leja":
+        gen, x, f = nodes.Leja(dim=d), rng.uniform(-1, 1, (333, d)), fns.rational_vec(d, d_out, seed=3)
+    else:
+        gen, x, f = nodes.GaussHermite(dim=d), rng.normal(size=(333, d)), fns.exponential(d, d_out, seed=3)
+    ip = _interp(node_gen=gen, k=k, t=t, d_out=d_out, f=f)
+    assert ip._fp64_orthogonal() is not None
+    y = ip(x).cpu().numpy()
+    yb = ip(x, precision=BARY).cpu().numpy()
+    err = rel_err(y, yb)
+    bound = 1e-12 if kind == "leja" else 1e-11
+    print("%s d=%d d_out=%d: orthogonal vs barycentric FP64 %.3e (bound %.0e)" % (kind, d, d_out, err, bound))
+    assert y.shape == (333, d_out) and err < bound

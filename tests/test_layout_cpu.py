@@ -99,10 +99,10 @@ def test_layout_matches_direct_sum(d, t, d_out, fam_id):
     assert lay["block_seg"][-1] == lay["n_cold_blocks"] and (d_out == 1 or lay["n_cold_blocks"] == 0)
 
 
-@pytest.mark.parametrize("d,t,fam_id,unit", [(1, 3.0, 0, False), (3, 4.5, 0, True), (6, 5.0, 1, False),
-                                             (12, 6.0, 0, True), (60, 5.8, 1, False), (200, 6.5, 0, True),
-                                             (1000, 8.22452, 0, True)])
-def test_fp64_layout_matches_direct_sum(d, t, fam_id, unit):
+@pytest.mark.parametrize("d,t,fam_id,unit,d_out", [(1, 3.0, 0, False, 1), (3, 4.5, 0, True, 1), (6, 5.0, 1, False, 3),
+                                                   (12, 6.0, 0, True, 1), (60, 5.8, 1, False, 1), (40, 5.5, 0, False, 6),
+                                                   (200, 6.5, 0, True, 1), (1000, 8.22452, 0, True, 1)])
+def test_fp64_layout_matches_direct_sum(d, t, fam_id, unit, d_out):
     """The FP64 evaluator's layout (``build_layout64``): every entry of the
     index set is exactly one term (no padding), the sums replayed in FP64 equal
     the direct sum over the tree to rounding, and the row, term and segment
@@ -113,7 +113,7 @@ def test_fp64_layout_matches_direct_sum(d, t, fam_id, unit):
     tr = python_tree(k, t)
     n = tr["parent"].shape[0]
     rng = np.random.default_rng(d + 7)
-    C = rng.normal(size=(n, 1))
+    C = rng.normal(size=(n, d_out))
     maxdeg = np.zeros(d, dtype=np.int64)
     for e in range(1, n):
         maxdeg[tr["dim"][e]] = max(maxdeg[tr["dim"][e]], tr["deg"][e])
@@ -121,8 +121,11 @@ def test_fp64_layout_matches_direct_sum(d, t, fam_id, unit):
     fa, fb = (np.ones(d), np.zeros(d)) if unit else (np.full(d, 0.9), np.full(d, 0.05))
     lay = build_layout64(tr, C, maxdeg, d, fam, fa, fb)
     x = rng.uniform(-1, 1, (5, d))
-    ref = direct(tr, C, x, fam, fa, fb)[:, 0]
-    got = evaluate_layout64(lay, x, fam, fa, fb, C[0, 0])
+    ref = direct(tr, C, x, fam, fa, fb)
+    got = evaluate_layout64(lay, x, fam, fa, fb, C[0])
+    assert lay["d_out"] == d_out and lay["dstride"] == (1 if d_out == 1 else (d_out + 3) // 4 * 4)
+    if d_out > 1:
+        assert lay["coef"].shape == (lay["n_terms"], lay["dstride"]) and np.all(lay["coef"][:, d_out:] == 0)
     np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12 * np.max(np.abs(ref)))
     # one term per entry: all entries but the root and the hot nodes
     assert lay["n_terms"] == n - lay["n_nodes"]

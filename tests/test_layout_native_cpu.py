@@ -68,23 +68,25 @@ def test_perpoint_tables_equal(d, t, d_out, fam_id):
 
 
 P64_I32 = ("node_seg", "cold_seg", "hot_dim", "hot_deg", "hot_soff", "node", "cold", "run")
-P64_F64 = ("node_c", "cold_ab", "terms")
-P64_SCALARS = ("row", "n_hb", "n_vp", "n_hot_dims", "n_nodes", "n_cold_groups", "max_depth", "n_terms")
+P64_F64 = ("node_c", "cold_ab", "terms", "coef")
+P64_SCALARS = ("d_out", "dstride", "row", "n_hb", "n_vp", "n_hot_dims", "n_nodes", "n_cold_groups", "max_depth",
+               "n_terms")
 
 
-@pytest.mark.parametrize("d,t,fam_id,unit", [(1, 3.0, 0, True), (6, 5.0, 1, False), (40, 5.5, 0, True),
-                                             (200, 6.5, 0, False), (1000, 8.22452, 0, True)])
-def test_fp64_tables_equal(d, t, fam_id, unit):
+@pytest.mark.parametrize("d,t,fam_id,unit,d_out", [(1, 3.0, 0, True, 1), (6, 5.0, 1, False, 1), (40, 5.5, 0, True, 1),
+                                                   (12, 6.0, 1, False, 5), (60, 5.8, 0, True, 8),
+                                                   (200, 6.5, 0, False, 1), (1000, 8.22452, 0, True, 1)])
+def test_fp64_tables_equal(d, t, fam_id, unit, d_out):
     """The FP64 evaluator's layout (one term per entry): library and package
     builders agree bit for bit, FP64 coefficients included."""
     from smolyax_gb300.spectral import build_layout64
 
-    tr, C, maxdeg, fam, fa, fb = _case(d, t, 1, fam_id, d + 1)
+    tr, C, maxdeg, fam, fa, fb = _case(d, t, d_out, fam_id, d + 1)
     if unit:
         fa, fb = np.ones(d), np.zeros(d)
     C = C.astype(np.float64) * (1 + 1e-9 * np.arange(C.size).reshape(C.shape))  # values not representable in FP32
     py = build_layout64(tr, C, maxdeg, d, fam, fa, fb)
-    nat = _capi.host_layout("perpoint", tr, C, 1, maxdeg, fam, fa, fb, P64_I32, P64_F64, P64_SCALARS, fp64=True)
+    nat = _capi.host_layout("perpoint", tr, C, d_out, maxdeg, fam, fa, fb, P64_I32, P64_F64, P64_SCALARS, fp64=True)
     for name in P64_I32:
         np.testing.assert_array_equal(nat[name], np.asarray(py[name], dtype=np.int32).ravel(), err_msg=name)
     for name in P64_F64:
