@@ -967,6 +967,7 @@ __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32
   // scratch [n_slots][gstride] read through L1
   const int64_t rstride = grow ? gstride : 128;
   float* tile = grow ? sm : sm + size_t(n_slots) * 128;  // [32][129]
+  float* stk = tile + 32 * 129;                          // [9][128] path products by depth
   const int tid = threadIdx.x;
   // blockIdx.x = segment (the segments of one block of points run side by side
   // and share its basis rows in cache), blockIdx.y strides over point blocks
@@ -991,59 +992,104 @@ __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32
     }
   }
   const int jbeg = seg ? seg[blockIdx.x] : 0, jend = seg ? seg[blockIdx.x + 1] : K;
-  float st1 = 1.f, st2 = 1.f, st3 = 1.f, st4 = 1.f, st5 = 1.f, st6 = 1.f, st7 = 1.f, st8 = 1.f;
+  // path products by depth: stk[d][tid] = product of the path's first d factors
+  // (stk[0] = 1), so an entry of depth d is stk[d - 1] * its basis value with no
+  // branch on d
+  stk[tid] = 1.f;
   // tiles of up to 32 entries, cut so that each covers one aligned group of 32
   // output columns (column K-1-j): full 128-byte lines of the FP32 rows
   for (int jb = jbeg, jn = 0; jb < jend; jb += jn) {
     jn = min(jend - jb, ((K - jb - 1) & 31) + 1);
     // 8 tape entries at a time: their basis values are loaded together (the
-    // loads are independent; only the stack updates are sequential)
+    // loads are independent; only the path products are sequential)
     for (int j = 0; j < jn; j += 8) {
       int w[8];
       float b[8];
 #pragma unroll
-      // past the tile: depth 8, whose stack slot no other depth reads
-      for (int u = 0; u < 8; ++u) w[u] = j + u < jn ? __ldg(tape + jb + j + u) : (8 << 16);
+      for (int u = 0; u < 8; ++u) w[u] = j + u < jn ? __ldg(tape + jb + j + u) : 0;
 #pragma unroll
       for (int u = 0; u < 8; ++u) b[u] = row[(w[u] & 0xffff) * rstride + tid];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        float v;
-        switch (w[u] >> 16) {
-          case 1: st1 = b[u]; v = st1; break;
-          case 2: st2 = st1 * b[u]; v = st2; break;
-          case 3: st3 = st2 * b[u]; v = st3; break;
-          case 4: st4 = st3 * b[u]; v = st4; break;
-          case 5: st5 = st4 * b[u]; v = st5; break;
-          case 6: st6 = st5 * b[u]; v = st6; break;
-          case 7: st7 = st6 * b[u]; v = st7; break;
-          default: st8 = st7 * b[u]; v = st8; break;
+        if (j + u < jn) {
+          const int d = min(max(w[u] >> 16, 1), 8);
+          const float v = stk[(d - 1) * 128 + tid] * b[u];
+          stk[d * 128 + tid] = v;
+          tile[(j + u) * 129 + tid] = v;
         }
-        if (j + u < jn) tile[(j + u) * 129 + tid] = v;
       }
     }
     __syncthreads();
-    // coalesced write-out: thread t -> column t % 32 of rows t / 32, t / 32 + 4, ...
-    const int c = tid & 31;
-    if (c < jn) {
-      for (int r = tid >> 5; r < 128; r += 4) {
-        if (p0 + r >= P) break;
-        const float v = tile[c * 129 + r];
-        // reversed column order: descendants (small coefficients) precede their
-        // ancestors, so the tensor-memory accumulator grows from small to large
-        const int col = K - 1 - (jb + c);
-        if constexpr (BF16) {
-          const __nv_bfloat16 h = __float2bfloat16_rn(v);
-          static_cast<__nv_bfloat16*>(Ahi)[(p0 + r) * lda + col] = h;
-          static_cast<__nv_bfloat16*>(Alo)[(p0 + r) * lda + col] = __float2bfloat16_rn(v - __bfloat162float(h));
-        } else {
-          uint32_t h;
-          asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
-          const float hf = __uint_as_float(h);
-          uint32_t l;
-          asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(v - hf));
-          static_cast<float*>(Ahi)[(p0 + r) * lda + col] = hf;
-          static_cast<float*>(Alo)[(p0 + r) * lda + col] = __uint_as_float(l);
+    // write-out: thread t -> 4 adjacent columns (quad t % 8 of the tile's
+    // 32-column group) of rows t / 8, t / 8 + 16, ...: a warp stores four whole
+    // 128-byte FP32 lines (four 64-byte BF16 half lines) per instruction
+    {
+      const int hi = (K - 1 - jb) & 31;  // group position of the tile's entry c = 0 (column K-1-jb)
+      const int lo = hi - jn + 1;        // ... and of its last entry
+      const int64_t colbase = int64_t(K - 1 - jb) - hi;
+      const int k0 = 4 * (tid & 7);
+      if (k0 + 3 >= lo && k0 <= hi) {
+        const bool full = k0 >= lo && k0 + 3 <= hi;
+        for (int r = tid >> 3; r < 128; r += 16) {
+          if (p0 + r >= P) break;
+          float v[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const int c = hi - (k0 + k);  // tile entry of group column k0 + k
+            v[k] = (c >= 0 && c < jn) ? tile[c * 129 + r] : 0.f;
+          }
+          // reversed column order: descendants (small coefficients) precede their
+          // ancestors, so the tensor-memory accumulator grows from small to large
+          const int64_t off = (p0 + r) * lda + colbase + k0;
+          if constexpr (BF16) {
+            __nv_bfloat16 h[4], l[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              h[k] = __float2bfloat16_rn(v[k]);
+              l[k] = __float2bfloat16_rn(v[k] - __bfloat162float(h[k]));
+            }
+            __nv_bfloat16* H = static_cast<__nv_bfloat16*>(Ahi) + off;
+            __nv_bfloat16* L = static_cast<__nv_bfloat16*>(Alo) + off;
+            if (full) {
+              uint2 hp, lp;
+              hp.x = uint32_t(__bfloat16_as_ushort(h[0])) | (uint32_t(__bfloat16_as_ushort(h[1])) << 16);
+              hp.y = uint32_t(__bfloat16_as_ushort(h[2])) | (uint32_t(__bfloat16_as_ushort(h[3])) << 16);
+              lp.x = uint32_t(__bfloat16_as_ushort(l[0])) | (uint32_t(__bfloat16_as_ushort(l[1])) << 16);
+              lp.y = uint32_t(__bfloat16_as_ushort(l[2])) | (uint32_t(__bfloat16_as_ushort(l[3])) << 16);
+              *reinterpret_cast<uint2*>(H) = hp;
+              *reinterpret_cast<uint2*>(L) = lp;
+            } else {
+#pragma unroll
+              for (int k = 0; k < 4; ++k)
+                if (k0 + k >= lo && k0 + k <= hi) {
+                  H[k] = h[k];
+                  L[k] = l[k];
+                }
+            }
+          } else {
+            float h[4], l[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              uint32_t hb, lb;
+              asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hb) : "f"(v[k]));
+              h[k] = __uint_as_float(hb);
+              asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lb) : "f"(v[k] - h[k]));
+              l[k] = __uint_as_float(lb);
+            }
+            float* H = static_cast<float*>(Ahi) + off;
+            float* L = static_cast<float*>(Alo) + off;
+            if (full) {
+              *reinterpret_cast<float4*>(H) = make_float4(h[0], h[1], h[2], h[3]);
+              *reinterpret_cast<float4*>(L) = make_float4(l[0], l[1], l[2], l[3]);
+            } else {
+#pragma unroll
+              for (int k = 0; k < 4; ++k)
+                if (k0 + k >= lo && k0 + k <= hi) {
+                  H[k] = h[k];
+                  L[k] = l[k];
+                }
+            }
+          }
         }
       }
     }
@@ -1060,7 +1106,7 @@ __global__ void __launch_bounds__(128) panel_tf32_kernel(int n_dims, const int32
 constexpr size_t kPanelSmemRows = 24 * 1024;
 
 extern "C" size_t smx_spectral_panel_workspace(int n_slots, int64_t P) {
-  const size_t smem = (size_t(n_slots) * 128 + 32 * 129) * sizeof(float);
+  const size_t smem = (size_t(n_slots) * 128 + 32 * 129 + 9 * 128) * sizeof(float);
   if (smem <= kPanelSmemRows) return 0;
   return size_t(n_slots) * size_t((P + 127) / 128 * 128) * sizeof(float);
 }
@@ -1080,7 +1126,7 @@ int panel_launch(int n_dims, const int32_t* dims, const int32_t* dmax, const int
   SMX_REQUIRE(ws_bytes >= need && (need == 0 || ws), what);
   float* grow = need ? static_cast<float*>(ws) : nullptr;
   const int64_t gstride = (P + 127) / 128 * 128;
-  const size_t smem = grow ? size_t(32 * 129) * sizeof(float) : (size_t(n_slots) * 128 + 32 * 129) * sizeof(float);
+  const size_t smem = (grow ? size_t(32 * 129 + 9 * 128) : size_t(n_slots) * 128 + 32 * 129 + 9 * 128) * sizeof(float);
   int rc = upload_consts();
   if (rc) return rc;
   static bool attr = false;
