@@ -616,7 +616,7 @@ def serving_workload(n_req, rate):
         ips["ip%02d" % i] = SmolyakBarycentricInterpolator(node_gen=gen, k=k, t=t, d_out=d_out,
                                                             f=_vec_target_device(kind, d, d_out, i),
                                                             memory_limit=2.0)
-    server = Server(ips, memory_budget=48.0, n_streams=8, fast_work=2e11)
+    server = Server(ips, memory_budget=48.0, n_streams=8)
     setup_s = time.perf_counter() - t0
     rng = np.random.default_rng(1)
     pools = {}

@@ -178,7 +178,7 @@ class Server:
     flight; ``staging`` (GiB) is the size of the pinned host arena."""
 
     def __init__(self, interpolants: dict, memory_budget: float = 8.0, n_streams: int = 8, staging: float = 1.0,
-                 n_fast_streams: int = 4, fast_work: float = 5e9, host_threads: int = 4):
+                 n_fast_streams: int = 4, fast_work: float = 2e11, host_threads: int = 4):
         self.dev = torch.device("cuda", torch.cuda.current_device())
         self.sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
         self.ips = dict(interpolants)
