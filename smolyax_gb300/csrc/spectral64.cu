@@ -8,9 +8,10 @@
 // entry of Lambda (9999 per point), with coefficients whose cancellation was
 // done once, by compensated sums, when they were computed; its terms are of
 // the size of the result (sum |term| / |y| ~ 2.4 at that workload), so plain
-// FP64 sums leave ~1e-14.  On GB300, whose FP64 rate is ~2 multiply-adds per
+// FP64 sums leave ~1e-14.  On GB300, whose FP64 rate is 2 multiply-adds per
 // SM clock, the work per point is the bound: this evaluator does one DFMA per
-// term plus ~3 per hot basis value.
+// term and output, plus a few per hot basis value, hot node and cold
+// dimension.
 //
 // Organisation as the FP32 per-point evaluator (spectral.cu), with 64 points
 // per block: 8 warps = 2 point groups x 4 work segments; a row of `row` doubles
@@ -18,8 +19,9 @@
 // that cold entries extend; hot nodes are visited in DFS pre-order with the
 // path products on a register stack; each cold dimension reads its x column
 // once.  Unlike the FP32 layout, every entry of Lambda is exactly one term
-// (slot, coefficient) with no padding: a multiply-add per entry, with the
-// slot read from the term (a uniform 16-byte load), then the row value.
+// (slot, coefficients) with no padding: per entry and output one multiply-add,
+// the slot read from the term (a uniform 16-byte load), then the row value.
+// With several outputs, block row blockIdx.y evaluates outputs 4y .. 4y+3.
 #include <math.h>
 
 #include "common.cuh"
