@@ -7,10 +7,12 @@ cfg2) 1e-13 element-wise relative -- tighter than the FP64 contract of
 form sums terms of the size of the result (the combination sum's cancellation
 is taken by compensated sums once, in the coefficients); against the
 barycentric FP64 evaluator 1e-12 element-wise on rules, domains, partial and
-multi-tile point counts.  Non-finite coordinates: NaN / Inf in an active
-dimension gives NaN for that point only; inactive dimensions are never read.
-Plans with several outputs run four outputs per pass.  The tables are checked
-to select this evaluator (``_fp64_orthogonal``).
+multi-tile point counts (1e-11 for Gauss-Hermite plans with several outputs,
+where the combination sum itself is off by up to that much).  Non-finite
+coordinates: NaN / Inf in an active dimension gives NaN for that point only;
+inactive dimensions are never read.  Plans with several outputs run four
+outputs per pass.  The tables are checked to select this evaluator
+(``_fp64_orthogonal``).
 """
 import numpy as np
 import pytest
