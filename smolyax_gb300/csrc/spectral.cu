@@ -1209,7 +1209,10 @@ __global__ void __launch_bounds__(128) panel_t_tf32_kernel(int n_dims, const int
   float* row = rowg + blockIdx.x * int64_t(128) + tid;
   basis_row(n_dims, dims, dmax, dsoff, fam_a, fam_b, fam, xp, row, rstride, 0);
   if (p >= P) return;
-  float st1 = 1.f, st2 = 1.f, st3 = 1.f, st4 = 1.f, st5 = 1.f, st6 = 1.f, st7 = 1.f, st8 = 1.f;
+  // path products by depth (stk[d][tid], stk[0] = 1): an entry of depth d is
+  // stk[d - 1] * its basis value, with no branch on d
+  __shared__ float stk[9 * 128];
+  stk[tid] = 1.f;
   for (int j = 0; j < K; j += 8) {
     int w[8];
     float bb[8];
@@ -1219,18 +1222,9 @@ __global__ void __launch_bounds__(128) panel_t_tf32_kernel(int n_dims, const int
     for (int u = 0; u < 8; ++u) bb[u] = row[int64_t(w[u] & 0xffff) * rstride];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
-      const float b = bb[u];
-      float v;
-      switch (w[u] >> 16) {
-        case 1: st1 = b; v = st1; break;
-        case 2: st2 = st1 * b; v = st2; break;
-        case 3: st3 = st2 * b; v = st3; break;
-        case 4: st4 = st3 * b; v = st4; break;
-        case 5: st5 = st4 * b; v = st5; break;
-        case 6: st6 = st5 * b; v = st6; break;
-        case 7: st7 = st6 * b; v = st7; break;
-        default: st8 = st7 * b; v = st8; break;
-      }
+      const int d = min(max(w[u] >> 16, 1), 8);
+      const float v = stk[(d - 1) * 128 + tid] * bb[u];
+      stk[d * 128 + tid] = v;
       if (j + u < K) {
         uint32_t h, l;
         asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
