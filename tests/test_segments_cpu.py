@@ -36,3 +36,21 @@ def test_segment_count():
     assert segment_count(20009, 205, 128, 152) == 32
     assert segment_count(300, 205, 128, 152) == 1  # short tapes are not split
     assert segment_count(20009, 3, 128, 152) == 3  # nor beyond their depth-1 entries
+
+
+def test_vjp_segment_count_and_bounds():
+    """Tape segments of the gradient walk: one per 4096 tape entries, at most
+    32 and at most the number of depth-1 entries; the bounds start at depth-1
+    entries and cover the tape (the same bounds as the panel's)."""
+    from smolyax_gb300.spectral import segment_bounds, vjp_segment_count
+
+    assert vjp_segment_count(5000, 300) == 1
+    assert vjp_segment_count(8192, 300) == 2
+    assert vjp_segment_count(63932, 400) == 15
+    assert vjp_segment_count(10**6, 400) == 32
+    assert vjp_segment_count(63932, 5) == 5
+    assert vjp_segment_count(0, 0) == 1
+    lvl1 = np.array([0, 10, 4000, 4100, 9000, 12000, 15000])
+    b = segment_bounds(lvl1, 16000, vjp_segment_count(16000, lvl1.size))
+    assert b[0] == 0 and b[-1] == 16000 and np.all(np.diff(b) > 0)
+    assert set(b[:-1].tolist()) <= set(lvl1.tolist())
