@@ -272,8 +272,10 @@ int smx_spectral_eval(const smx_spectral* plan_host, const double* x, int64_t P,
  * interpolation.py:264-304).  The per-point structure of smx_spectral -- hot
  * basis values and the prefix products of the cold entries' parents in a row
  * of `row` doubles per point (row >= n_hb + n_vp; odd keeps 8-byte reads of
- * consecutive points on distinct banks; a block of 64 points needs (row + 4 *
- * (d_out == 1 ? 1 : 4)) * 64 * 8 bytes of shared memory, <= 227 KB) -- but
+ * consecutive points on distinct banks; a block of B points needs (row + 4 *
+ * (d_out == 1 ? 1 : 4)) * B * 8 bytes of shared memory, <= 227 KB, with B =
+ * 64, 96 or 128 chosen per call for the fewest idle SM slots in the last
+ * wave) -- but
  * every entry of Lambda is exactly one term (row slot, coefficients), without
  * padding: at GB300's FP64 rate each term is a multiply-add that counts.  One
  * output per pass (d_out = 1), else four (outputs o0..o0+3 per block row).

@@ -24,15 +24,18 @@
 // With several outputs, block row blockIdx.y evaluates outputs 4y .. 4y+3.
 #include <math.h>
 
+#include <cmath>
+
 #include "common.cuh"
 #include "recurrence.cuh"
 
 namespace {
 
 constexpr int kSeg = 4;
-constexpr int kTP = 64;  // points per block: two blocks per SM when the row is <= ~215 doubles, so that
-                         // one block's load-bound basis phase overlaps the other's multiply-adds
-constexpr int kThreads = kSeg * kTP;
+// Points per block: 64, 96 or 128, picked per launch for the fewest idle SM
+// slots in the last wave (a point's arithmetic does not depend on the choice).
+// With 64, two blocks fit an SM when the row is <= ~215 doubles, so one
+// block's load-bound basis phase overlaps the other's multiply-adds.
 constexpr int kMaxRec = 512;
 constexpr size_t kSmemMax = 227 * 1024;
 
@@ -91,10 +94,10 @@ __device__ __forceinline__ void sum_terms(const double* __restrict__ Rw, const S
   }
 }
 
-template <int DO>
-__global__ void __launch_bounds__(kThreads, 2) spectral_eval64_kernel(Spec64Args a, const double* __restrict__ x,
-                                                                      int64_t P, int64_t ldx,
-                                                                      double* __restrict__ y) {
+template <int DO, int kTP>
+__global__ void __launch_bounds__(kSeg * kTP, kTP == 64 ? 2 : 1)
+    spectral_eval64_kernel(Spec64Args a, const double* __restrict__ x, int64_t P, int64_t ldx,
+                           double* __restrict__ y) {
   extern __shared__ __align__(16) double sm64[];
   double* RED = sm64 + size_t(a.row) * kTP;  // [kSeg][DO][kTP]
   const int o0 = blockIdx.y * DO;
@@ -243,7 +246,70 @@ int upload_consts64() {
 
 bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
 
+// Launch with the block size of the fewest idle SM slots in the last wave:
+// cost = waves * (resident blocks per SM * points per block), the points an SM
+// could have evaluated in that time, 15 % dearer with a single resident block
+// (measured at d_in = 1000: two blocks per SM overlap one block's load-bound
+// basis phase with the other's multiply-adds).
+template <int DO, int TP>
+int occupancy64(size_t smem, int* occ) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(spectral_eval64_kernel<DO, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(kSmemMax)) != cudaSuccess)
+      return smx::set_error(SMX_ERR_CUDA, "smx_spectral_eval64: shared-memory attribute");
+    attr_set = true;
+  }
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, spectral_eval64_kernel<DO, TP>, kSeg * TP, smem) !=
+      cudaSuccess)
+    return smx::set_error(SMX_ERR_CUDA, "smx_spectral_eval64: occupancy query");
+  return SMX_OK;
+}
+
+template <int DO>
+int launch64(const Spec64Args& a, const double* x, int64_t P, int64_t ldx, double* y, unsigned chunks,
+             size_t row_bytes, void* stream) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return smx::set_error(SMX_ERR_CUDA, "smx_spectral_eval64: no device");
+  }
+  const int tps[3] = {64, 96, 128};
+  int best = -1;
+  double best_cost = 0.0;
+  for (int i = 0; i < 3; ++i) {
+    const size_t smem = row_bytes * tps[i];
+    if (smem > kSmemMax) continue;
+    int occ = 0, rc;
+    if (i == 0) rc = occupancy64<DO, 64>(smem, &occ);
+    else if (i == 1) rc = occupancy64<DO, 96>(smem, &occ);
+    else rc = occupancy64<DO, 128>(smem, &occ);
+    if (rc) return rc;
+    if (occ < 1) continue;
+    const double blocks = double((P + tps[i] - 1) / tps[i]) * chunks;
+    const double slots = double(sms) * occ;
+    const double cost = std::ceil(blocks / slots) * occ * tps[i] * (occ >= 2 ? 1.0 : 1.15);
+    if (best < 0 || cost < best_cost) best = i, best_cost = cost;
+  }
+  if (best < 0) return smx::set_error(SMX_ERR_UNSUPPORTED, "smx_spectral_eval64: no block size fits");
+  cudaStream_t st = smx::as_stream(stream);
+  const int tp = tps[best];
+  const dim3 grid(smx::grid_for(P, tp), chunks);
+  const size_t smem = row_bytes * tp;
+  if (tp == 64)
+    spectral_eval64_kernel<DO, 64><<<grid, kSeg * 64, smem, st>>>(a, x, P, ldx, y);
+  else if (tp == 96)
+    spectral_eval64_kernel<DO, 96><<<grid, kSeg * 96, smem, st>>>(a, x, P, ldx, y);
+  else
+    spectral_eval64_kernel<DO, 128><<<grid, kSeg * 128, smem, st>>>(a, x, P, ldx, y);
+  SMX_LAUNCH_CHECK("smx_spectral_eval64");
+  return SMX_OK;
+}
+
 }  // namespace
+
 
 extern "C" int smx_spectral_eval64(const smx_spectral64* sp, const double* x, int64_t P, int64_t ldx, double* y,
                                    void* stream) {
@@ -269,8 +335,8 @@ extern "C" int smx_spectral_eval64(const smx_spectral64* sp, const double* x, in
               "smx_spectral_eval64: tables not aligned");
   SMX_REQUIRE(P >= 0 && ldx >= sp->d_in, "smx_spectral_eval64: bad sizes");
   const int DO = sp->d_out == 1 ? 1 : 4;
-  const size_t smem = (size_t(sp->row) + size_t(kSeg) * DO) * kTP * sizeof(double);
-  if (smem > kSmemMax)
+  const size_t row_bytes = (size_t(sp->row) + size_t(kSeg) * DO) * sizeof(double);  // per point of a block
+  if (row_bytes * 64 > kSmemMax)
     return smx::set_error(SMX_ERR_UNSUPPORTED, std::string(who) + ": per-point row too large for shared memory");
   if (P == 0) return SMX_OK;
   SMX_REQUIRE(x && y, "smx_spectral_eval64: null pointer");
@@ -302,27 +368,8 @@ extern "C" int smx_spectral_eval64(const smx_spectral64* sp, const double* x, in
   a.fam_b = sp->fam_b;
   a.fam = sp->fam;
   a.c0 = sp->c0;
-  static bool attr_set[2] = {false, false};
-  cudaStream_t st = smx::as_stream(stream);
   const unsigned chunks = unsigned((sp->d_out + DO - 1) / DO);
   SMX_REQUIRE(chunks <= 65535, "smx_spectral_eval64: too many outputs");
-  if (DO == 1) {
-    if (!attr_set[0]) {
-      if (cudaFuncSetAttribute(spectral_eval64_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               int(kSmemMax)) != cudaSuccess)
-        return smx::set_error(SMX_ERR_CUDA, "smx_spectral_eval64: shared-memory attribute");
-      attr_set[0] = true;
-    }
-    spectral_eval64_kernel<1><<<dim3(smx::grid_for(P, kTP), chunks), kThreads, smem, st>>>(a, x, P, ldx, y);
-  } else {
-    if (!attr_set[1]) {
-      if (cudaFuncSetAttribute(spectral_eval64_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               int(kSmemMax)) != cudaSuccess)
-        return smx::set_error(SMX_ERR_CUDA, "smx_spectral_eval64: shared-memory attribute");
-      attr_set[1] = true;
-    }
-    spectral_eval64_kernel<4><<<dim3(smx::grid_for(P, kTP), chunks), kThreads, smem, st>>>(a, x, P, ldx, y);
-  }
-  SMX_LAUNCH_CHECK("smx_spectral_eval64");
-  return SMX_OK;
+  return DO == 1 ? launch64<1>(a, x, P, ldx, y, chunks, row_bytes, stream)
+                 : launch64<4>(a, x, P, ldx, y, chunks, row_bytes, stream);
 }
