@@ -501,6 +501,37 @@ size_t smx_blocked_eval_batch_workspace(int n_plans, int n_items);
 int smx_blocked_eval_batch(const smx_blocked* plans_host, int n_plans, const smx_work* items_host, int n_items,
                            void* ws, size_t ws_bytes, void* stream);
 
+/* Serving queue: submit FP32 evaluation requests (plan, inputs, outputs) and
+ * poll for their completion, the continuous-batching loop of the serving path
+ * without a host runtime.  smx_serve_flush launches everything queued as one
+ * smx_blocked_eval_batch launch (blocked plans) and one
+ * smx_spectral_eval_batch launch (per-point plans, d_out <= 16) on the
+ * server's stream and records an event; a submit that finds its kind's queue
+ * full (max_items requests, or a new plan beyond max_plans distinct ones)
+ * flushes first.  Up to max_inflight flushes are outstanding; the next one
+ * waits for the oldest.  Results equal those of smx_blocked_eval /
+ * smx_spectral_eval on the same request.
+ *  - smx_serve_create: allocates the workspaces of max_inflight flushes (the
+ *    only allocation; submit / flush / poll allocate nothing);
+ *  - smx_serve_submit: `plan_host` is a host smx_blocked (kind
+ *    SMX_SERVE_BLOCKED) or smx_spectral (SMX_SERVE_SPECTRAL), identified by
+ *    its address until the request is flushed; x / y device, as for the batch
+ *    entry points.  Returns the ticket (>= 0, in submission order) or an
+ *    SMX_ERR_* code;
+ *  - smx_serve_poll: 1 if the ticket's outputs are written, 0 if it is queued
+ *    or running, or an SMX_ERR_* code (a failed launch);
+ *  - smx_serve_destroy: waits for the flushes in flight and frees the server.
+ * A server is used by one host thread at a time. */
+#define SMX_SERVE_BLOCKED 0
+#define SMX_SERVE_SPECTRAL 1
+typedef struct smx_server smx_server;
+int smx_serve_create(int max_items, int max_plans, int max_inflight, void* stream, smx_server** out);
+int64_t smx_serve_submit(smx_server* server, int kind, const void* plan_host, const double* x, int64_t P, int64_t ldx,
+                         float* y);
+int smx_serve_flush(smx_server* server);
+int smx_serve_poll(smx_server* server, int64_t ticket);
+void smx_serve_destroy(smx_server* server);
+
 
 /* ---- tensor-core contraction ---------------------------------------------------------
  * D[M x N] = A B^T (+ bias[n]) with tcgen05.mma kind::tf32 in 3xTF32 form:

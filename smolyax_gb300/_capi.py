@@ -13,6 +13,9 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libsmolyax_gb300.so")
 
 SMX_OK = 0
+SMX_ERR_ARG = -1
+SMX_SERVE_BLOCKED = 0
+SMX_SERVE_SPECTRAL = 1
 SMX_MODE_NONZERO = 0
 SMX_MODE_INDEXSET = 1
 SMX_MODE_ADDITIVE = 2
@@ -239,6 +242,11 @@ SIGNATURES = {
     "smx_blocked_eval_workspace": (_sz, [_p, _i64]),
     "smx_blocked_eval_batch_workspace": (_sz, [_int, _int]),
     "smx_blocked_eval_batch": (_int, [_p, _int, _p, _int, _p, _sz, _p]),
+    "smx_serve_create": (_int, [_int, _int, _int, _p, C.POINTER(_p)]),
+    "smx_serve_submit": (_i64, [_p, _int, _p, _p, _i64, _i64, _p]),
+    "smx_serve_flush": (_int, [_p]),
+    "smx_serve_poll": (_int, [_p, _i64]),
+    "smx_serve_destroy": (None, [_p]),
     "smx_eval_f64_noalloc": (_int, [_p, _p, _i64, _i64, _p, _p]),
     "smx_spectral_panel_workspace": (_sz, [_int, _i64]),
     "smx_spectral_panel_tf32": (_int, [_int, _p, _p, _p, _int, _p, _int, _p, _int, _p, _p, _p, _p, _i64, _i64, _p,

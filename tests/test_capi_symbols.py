@@ -11,7 +11,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def _declared():
     src = open(os.path.join(ROOT, "include", "smolyax_gb300.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = re.findall(r"^\s*(?:const\s+)?(?:int|void|size_t|char\s*\*|const char\s*\*)\s*\**\s*(smx_\w+)\s*\(", src, re.M)
+    names = re.findall(r"^\s*(?:const\s+)?(?:int64_t|int|void|size_t|char\s*\*|const char\s*\*)\s*\**\s*(smx_\w+)\s*\(", src, re.M)
     return sorted(set(names))
 
 
