@@ -551,6 +551,13 @@ int smx_gemm_tf32x3(const float* A_hi, const float* A_lo, int64_t lda, const flo
  * points); the slices' FP32 results go to `ws` and are added in slice order
  * (deterministic).  ws: smx_gemm_tf32x3_splitk_workspace bytes. */
 size_t smx_gemm_tf32x3_splitk_workspace(int M, int N, int K, int splits);
+/* Split count for the forward contraction of a plan whose panel chunks hold M
+ * points: enough K slices that the CTAs of one full chunk (128 x 128 tiles, or
+ * 128 x 256 for N > 192) fill the SMs once, at most 8 slices and at least 64
+ * K-tiles (2048 products) per slice; 1 where the tiles alone fill the GPU.  A
+ * function of (M, N, K) and the SM count only, so that for a fixed chunk size
+ * a point's result does not depend on the batch it is evaluated in. */
+int smx_gemm_tf32x3_splits(int64_t M, int N, int K);
 int smx_gemm_tf32x3_splitk(const float* A_hi, const float* A_lo, int64_t lda, const float* B_hi, const float* B_lo,
                            int64_t ldb, int M, int N, int K, float* D, int64_t ldd, const float* bias, int accumulate,
                            int splits, void* ws, size_t ws_bytes, int* err, void* stream);

@@ -259,6 +259,7 @@ SIGNATURES = {
     "smx_gemm_tf32x3_timeout_selftest": (_int, [_p, _p, _i64, _p, _p, _i64, _int, _int, _int, _p, _i64, _p,
                                                  C.c_uint64, _p]),
     "smx_gemm_tf32x3_splitk_workspace": (_sz, [_int, _int, _int, _int]),
+    "smx_gemm_tf32x3_splits": (_int, [_i64, _int, _int]),
     "smx_gemm_tf32x3_splitk": (_int, [_p, _p, _i64, _p, _p, _i64, _int, _int, _int, _p, _i64, _p, _int, _int, _p, _sz,
                                        _p, _p]),
     "smx_spectral_panel_t_workspace": (_sz, [_int, _i64]),

@@ -203,6 +203,12 @@ int64_t tc_step(const smx_fp32_plan* h, int64_t P) {
   return std::max<int64_t>(1, std::min(step, P));
 }
 
+// K slices of the forward contraction: fixed per plan (from its full chunk),
+// as in the package, so that both give the same values.
+int tc_splits(const smx_fp32_plan* h) {
+  return smx_gemm_tf32x3_splits(tc_step(h, int64_t(1) << 40), h->d_out, h->K);
+}
+
 // Segments of one panel launch over n points (spectral.py segment_count).
 int seg_want(const smx_fp32_plan* h, int64_t n) {
   const int64_t n_pb = std::max<int64_t>((n + 127) / 128, 1);
@@ -561,7 +567,8 @@ extern "C" size_t smx_fp32_workspace(const smx_fp32_plan* h, int64_t P) {
   if (h->evaluator != SMX_FP32_TENSOR) return 0;
   const int64_t step = tc_step(h, std::max<int64_t>(P, 1));
   const size_t lda = size_t(round32(std::max(h->K, 1)));
-  return 2 * up(size_t(step) * lda * sizeof(float)) + up(smx_spectral_panel_workspace(h->n_slots, step));
+  return 2 * up(size_t(step) * lda * sizeof(float)) + up(smx_spectral_panel_workspace(h->n_slots, step)) +
+         (tc_splits(h) > 1 ? up(smx_gemm_tf32x3_splitk_workspace(int(step), h->d_out, h->K, tc_splits(h))) : 0);
 }
 
 extern "C" int smx_fp32_eval(const smx_fp32_plan* h, const double* x, int64_t P, int64_t ldx, float* y, void* ws,
@@ -580,8 +587,11 @@ extern "C" int smx_fp32_eval(const smx_fp32_plan* h, const double* x, int64_t P,
   const size_t panel_bytes = up(size_t(step) * lda * sizeof(float));
   float* Ah = reinterpret_cast<float*>(w);
   float* Al = reinterpret_cast<float*>(w + panel_bytes);
-  void* pws = w + 2 * panel_bytes;
-  const size_t pws_bytes = ws_bytes - 2 * panel_bytes;
+  const int splits = tc_splits(h);
+  const size_t sk_bytes = splits > 1 ? up(smx_gemm_tf32x3_splitk_workspace(int(step), h->d_out, h->K, splits)) : 0;
+  void* skws = w + 2 * panel_bytes;
+  void* pws = w + 2 * panel_bytes + sk_bytes;
+  const size_t pws_bytes = ws_bytes - 2 * panel_bytes - sk_bytes;
   int rc;
   for (int64_t p0 = 0; p0 < P; p0 += step) {
     const int64_t m = std::min(step, P - p0);
@@ -591,8 +601,9 @@ extern "C" int smx_fp32_eval(const smx_fp32_plan* h, const double* x, int64_t P,
     if ((rc = smx_spectral_panel_tf32(h->n_dims, h->dims.p, h->dmax.p, h->dsoff.p, h->n_slots, h->tape.p, h->K, seg,
                                       n_seg, h->fam_a.p, h->fam_b.p, h->fam.p, x + p0 * ldx, m, ldx, Ah, Al, lda, pws,
                                       pws_bytes, stream)) ||
-        (rc = smx_gemm_tf32x3(Ah, Al, lda, h->Bh.p, h->Bl.p, h->ldk, int(m), h->d_out, h->K, y + p0 * h->d_out,
-                              h->d_out, h->bias.p, 0, h->err.p, stream)))
+        (rc = smx_gemm_tf32x3_splitk(Ah, Al, lda, h->Bh.p, h->Bl.p, h->ldk, int(m), h->d_out, h->K,
+                                     y + p0 * h->d_out, h->d_out, h->bias.p, 0, splits, skws, sk_bytes, h->err.p,
+                                     stream)))
       return rc;
   }
   return SMX_OK;

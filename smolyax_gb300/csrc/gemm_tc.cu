@@ -13,6 +13,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "common.cuh"
@@ -472,6 +473,19 @@ int splitk_slices(int K, int splits) {
   return (KT + per - 1) / per;
 }
 }  // namespace
+
+extern "C" int smx_gemm_tf32x3_splits(int64_t M, int N, int K) {
+  if (M <= 0 || N <= 0 || K <= 0) return 1;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  const int64_t ctas = (M + kBM - 1) / kBM * (N > 192 ? (N + 255) / 256 : (N + 127) / 128);
+  const int64_t k_tiles = (int64_t(K) + kBK - 1) / kBK;
+  const int64_t s = std::min<int64_t>(std::min<int64_t>(8, sms / ctas), k_tiles / 64);
+  return int(std::max<int64_t>(1, s));
+}
 
 extern "C" size_t smx_gemm_tf32x3_splitk_workspace(int M, int N, int K, int splits) {
   if (M <= 0 || N <= 0 || K <= 0 || splits < 1) return 0;

@@ -290,6 +290,8 @@ class Server:
                 step = sp._tc_step(P)
                 b += 2 * step * (sp.tc["K"] + 31) // 32 * 32 * 4 + capi.size("smx_spectral_panel_workspace",
                                                                                sp.tc["n_slots"], step)
+                if sp.tc_splits() > 1:
+                    b += capi.size("smx_gemm_tf32x3_splitk_workspace", step, d_out, sp.tc["K"], sp.tc_splits())
             elif sp.blocked is not None:
                 b += self.sms * 2 * 16 * 128 * 4 + 4 * self.sms
         return int(b)

@@ -459,6 +459,15 @@ class SpectralPlan:
         step = max(128, int(self.memory_limit * 1024**3 // (8 * ((self.tc["K"] + 31) // 32 * 32))) // 128 * 128)
         return max(1, min(step, P))
 
+    def tc_splits(self):
+        """K slices of the forward contraction (``smx_gemm_tf32x3_splits`` for a
+        full panel chunk): a plan constant, so a point's value does not depend
+        on the batch it arrives in."""
+        if "splits" not in self.tc:
+            self.tc["splits"] = capi.size("smx_gemm_tf32x3_splits", self._tc_step(1 << 40),
+                                          int(self.tc["Bd"].shape[0]), self.tc["K"])
+        return self.tc["splits"]
+
     def tc_chunks(self, P):
         """Number of panel chunks (each one panel and one GEMM launch) for P points."""
         return -(-int(P) // self._tc_step(P)) if P else 0
@@ -468,7 +477,7 @@ class SpectralPlan:
         panel (plus its basis-row kernel when the rows go to global scratch) and
         the GEMM."""
         scratch = capi.size("smx_spectral_panel_workspace", self.tc["n_slots"], 1) > 0
-        return self.tc_chunks(P) * (3 if scratch else 2)
+        return self.tc_chunks(P) * ((3 if scratch else 2) + (1 if self.tc_splits() > 1 else 0))
 
     def _segments(self, n):
         """Tape segments of one panel launch over n points (see segment_bounds).
@@ -528,6 +537,10 @@ class SpectralPlan:
         lda = (tc["K"] + 31) // 32 * 32  # 128-byte panel rows
         Ah = torch.empty(step, lda, dtype=torch.float32, device=x.device)
         Al = torch.empty_like(Ah)
+        splits = self.tc_splits()
+        if splits > 1:
+            nsk = capi.size("smx_gemm_tf32x3_splitk_workspace", step, d_out, tc["K"], splits)
+            skws = torch.empty(max(nsk, 1), dtype=torch.uint8, device=x.device)
         for p0 in range(0, P, step):
             p1 = min(P, p0 + step)
             nws = capi.size("smx_spectral_panel_workspace", tc["n_slots"], p1 - p0)
@@ -536,8 +549,13 @@ class SpectralPlan:
             call("smx_spectral_panel_tf32", int(tc["dims"].numel()), ptr(tc["dims"]), ptr(tc["dmax"]),
                  ptr(tc["dsoff"]), tc["n_slots"], ptr(tc["tape"]), tc["K"], ptr(seg), n_seg, ptr(k["fam_a"]),
                  ptr(k["fam_b"]), ptr(k["fam"]), ptr(x[p0:p1]), p1 - p0, d, ptr(Ah), ptr(Al), lda, ptr(ws), nws, st)
-            call("smx_gemm_tf32x3", ptr(Ah), ptr(Al), lda, ptr(tc["Bh"]), ptr(tc["Bl"]), ldk, p1 - p0, d_out,
-                 tc["K"], ptr(y[p0:p1]), d_out, ptr(tc["bias"]), 0, ptr(tc["err"]), st)
+            if splits > 1:
+                call("smx_gemm_tf32x3_splitk", ptr(Ah), ptr(Al), lda, ptr(tc["Bh"]), ptr(tc["Bl"]), ldk, p1 - p0,
+                     d_out, tc["K"], ptr(y[p0:p1]), d_out, ptr(tc["bias"]), 0, splits, ptr(skws), nsk, ptr(tc["err"]),
+                     st)
+            else:
+                call("smx_gemm_tf32x3", ptr(Ah), ptr(Al), lda, ptr(tc["Bh"]), ptr(tc["Bl"]), ldk, p1 - p0, d_out,
+                     tc["K"], ptr(y[p0:p1]), d_out, ptr(tc["bias"]), 0, ptr(tc["err"]), st)
         return y
 
 
