@@ -594,6 +594,66 @@ def serving_fleet(seed=0):
     return out
 
 
+def build_fleet(select=None):
+    """The serving fleet's interpolants (name -> interpolant), targets assembled
+    on the device; ``select(i, d_in, d_out, |Lambda|, rule)`` picks a subset."""
+    from smolyax_gb300 import SmolyakBarycentricInterpolator, indices, nodes
+
+    ips = {}
+    for i, d, d_out, lam, kind in serving_fleet(0):
+        if select is not None and not select(i, d, d_out, lam, kind):
+            continue
+        k = np.log((2 + np.arange(d)) / np.log(2))
+        t = indices.find_approximate_threshold(k, lam, nested=True, accuracy=0.01)
+        gen = nodes.Leja(dim=d) if kind == "leja" else nodes.GaussHermite(dim=d)
+        ips["ip%02d" % i] = SmolyakBarycentricInterpolator(node_gen=gen, k=k, t=t, d_out=d_out,
+                                                            f=_vec_target_device(kind, d, d_out, i),
+                                                            memory_limit=2.0)
+    return ips
+
+
+def fleet_workload(P, steps, warmup):
+    """Each tensor-core plan of the serving fleet with |Lambda| >= 1e4, alone:
+    FP32 evaluation of P points (inputs on the device, CUDA events over `steps`
+    calls after `warmup`), its K slices and its error against the FP64 path on
+    256 points.  One result dict."""
+    import torch
+
+    from smolyax_gb300 import nodes
+
+    torch.cuda.set_device(0)
+    ips = build_fleet(lambda i, d, d_out, lam, kind: d_out >= 16 and lam >= 10000)
+    rng = np.random.default_rng(0)
+    rows = []
+    for name, ip in ips.items():
+        sp = ip.spectral_plan()
+        if sp.tc is None:
+            continue
+        if isinstance(ip._node_gen, nodes.Leja):
+            x = torch.as_tensor(rng.uniform(-1, 1, (P, ip.d_in)), device="cuda")
+        else:
+            x = torch.as_tensor(rng.normal(size=(P, ip.d_in)) / np.sqrt(2), device="cuda")
+        for _ in range(warmup):
+            y = ip(x, precision="fp32")
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            y = ip(x, precision="fp32")
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        ref = ip(x[:256], precision="fp64").cpu().numpy()
+        err = float(np.max(np.abs(y[:256].cpu().numpy() - ref)) / np.max(np.abs(ref)))
+        rows.append(dict(plan=name, d_in=ip.d_in, d_out=ip.d_out, K=int(sp.tc["K"]), k_slices=sp.tc_splits(),
+                         chunk_points=sp._tc_step(1 << 40), ms=ms, evals_per_s=P * ip.d_out / (ms * 1e-3),
+                         max_rel_err_vs_fp64=err))
+    return {"workload": "fleet", "points": P, "steps": steps, "warmup": warmup, "unit": "ms", "data": "synthetic",
+            "config": {"workload": "tensor-core plans of the 16-interpolant serving fleet (seed 0) with |Lambda| >= "
+                                   "1e4, each alone, FP32 (3xTF32 contraction)"},
+            "plans": rows}
+
+
 def run_serving(args):
     print(json.dumps(serving_workload(args.requests, args.rate)))
     return 0
@@ -603,19 +663,12 @@ def serving_workload(n_req, rate):
     """Poisson stream of eval/gradient requests over the 16-interpolant fleet: one result dict."""
     import torch
 
-    from smolyax_gb300 import SmolyakBarycentricInterpolator, indices, nodes
+    from smolyax_gb300 import nodes
     from smolyax_gb300.serving import Request, Server, replay
 
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
-    ips, fleet = {}, serving_fleet(0)
-    for i, d, d_out, lam, kind in fleet:
-        k = np.log((2 + np.arange(d)) / np.log(2))
-        t = indices.find_approximate_threshold(k, lam, nested=True, accuracy=0.01)
-        gen = nodes.Leja(dim=d) if kind == "leja" else nodes.GaussHermite(dim=d)
-        ips["ip%02d" % i] = SmolyakBarycentricInterpolator(node_gen=gen, k=k, t=t, d_out=d_out,
-                                                            f=_vec_target_device(kind, d, d_out, i),
-                                                            memory_limit=2.0)
+    ips, fleet = build_fleet(), serving_fleet(0)
     server = Server(ips, memory_budget=48.0, n_streams=8)
     setup_s = time.perf_counter() - t0
     rng = np.random.default_rng(1)
@@ -838,7 +891,7 @@ def main():
     ap.add_argument("--points", type=int, default=POINTS)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="leja1000",
-                    choices=["leja1000", "serving", "leja64bwd", "quadrature", "fp64"] + sorted(WORKLOADS))
+                    choices=["leja1000", "serving", "leja64bwd", "quadrature", "fp64", "fleet"] + sorted(WORKLOADS))
     ap.add_argument("--requests", type=int, default=300)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--no-extras", action="store_true", help="headline only (skip the other configurations)")
@@ -854,6 +907,9 @@ def main():
         return run_backward_workload(args)
     if args.workload == "fp64":
         print(json.dumps(fp64_workload(args.steps, args.warmup, args.points if args.points != POINTS else None)))
+        return 0
+    if args.workload == "fleet":
+        print(json.dumps(fleet_workload(args.points if args.points != POINTS else 52192, min(args.steps, 3), 3)))
         return 0
     if args.workload != "leja1000":
         return run_tensor_workload(args)
