@@ -669,7 +669,9 @@ def serving_workload(n_req, rate):
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
     ips, fleet = build_fleet(), serving_fleet(0)
-    server = Server(ips, memory_budget=48.0, n_streams=8)
+    # 4 GB pinned staging arena: the stream's largest requests stage 0.1-0.4 GB
+    # each, and a request that finds the arena full pins a one-off host buffer
+    server = Server(ips, memory_budget=48.0, n_streams=8, staging=4.0)
     setup_s = time.perf_counter() - t0
     rng = np.random.default_rng(1)
     pools = {}
@@ -725,7 +727,7 @@ def serving_workload(n_req, rate):
         "slowest": [dict(ms=r.latency * 1e3, plan=r.name, points=r.points, op=r.op, gmac=server.work(r) / 1e9,
                          wait_ms=(r.t_admit - r.t_submit) * 1e3) for r in slow],
         "wall_s": wall, "setup_s": setup_s, "launches": st["launches"], "merged_launches": st["batch_launches"],
-        "high_priority_launches": st["fast_launches"],
+        "high_priority_launches": st["fast_launches"], "staging_spills": st["staging_spills"],
         "completed": st["completed"], "rejected": st["rejected"], "clocks": clk.summary(),
         "fleet": [dict(d_in=d, d_out=o, lam=l, kind=kd, K=int(ips["ip%02d" % i]._tree.size),
                        tensor=ips["ip%02d" % i].spectral_plan().tc is not None) for i, d, o, l, kd in fleet],
