@@ -175,7 +175,11 @@ class Server:
     """Request loop over resident interpolants (see the module docstring).
 
     ``memory_budget`` (GiB) bounds the device memory of the requests in
-    flight; ``staging`` (GiB) is the size of the pinned host arena."""
+    flight; ``staging`` (GiB) is the size of the pinned host arena: size it
+    for the inputs and outputs of the requests in flight, since a request that
+    finds it full pins a one-off host buffer, and pinning a new buffer of a
+    few hundred MB holds up every host thread's CUDA calls for tens of ms
+    (``stats()["staging_spills"]`` counts them)."""
 
     def __init__(self, interpolants: dict, memory_budget: float = 8.0, n_streams: int = 8, staging: float = 1.0,
                  n_fast_streams: int = 4, fast_work: float = 2e11, host_threads: int = 4):
