@@ -518,8 +518,11 @@ int smx_blocked_eval_batch(const smx_blocked* plans_host, int n_plans, const smx
  *    its address until the request is flushed; x / y device, as for the batch
  *    entry points.  Returns the ticket (>= 0, in submission order) or an
  *    SMX_ERR_* code;
+ *  - smx_serve_flush: a flush whose launch is refused (e.g. a per-point plan
+ *    beyond shared memory) or fails returns the error and fails all its
+ *    requests; the queue is then empty and takes new requests;
  *  - smx_serve_poll: 1 if the ticket's outputs are written, 0 if it is queued
- *    or running, or an SMX_ERR_* code (a failed launch);
+ *    or running, or the SMX_ERR_* code of its failed flush;
  *  - smx_serve_destroy: waits for the flushes in flight and frees the server.
  * A server is used by one host thread at a time. */
 #define SMX_SERVE_BLOCKED 0

@@ -25,6 +25,11 @@ struct Flight {
   cudaEvent_t event;
 };
 
+struct Failed {
+  int64_t begin, end;   // tickets of a flush whose launch was refused or failed
+  int rc;               // its error code, returned by smx_serve_poll
+};
+
 template <typename Plan>
 struct Queue {
   std::vector<Plan> plans;           // copies of the distinct plans
@@ -54,6 +59,7 @@ struct smx_server {
   std::vector<char> slot_busy;
   std::vector<cudaEvent_t> events;
   std::deque<Flight> flights;
+  std::vector<Failed> failed;
   Queue<smx_blocked> blocked;
   Queue<smx_spectral> spectral;
   int64_t next_ticket = 0;   // tickets issued
@@ -127,23 +133,25 @@ extern "C" int smx_serve_flush(smx_server* s) {
   }
   int slot = 0;
   while (s->slot_busy[slot]) ++slot;
-  if (!s->blocked.items.empty() &&
-      (rc = smx_blocked_eval_batch(s->blocked.plans.data(), int(s->blocked.plans.size()), s->blocked.items.data(),
-                                   int(s->blocked.items.size()), s->ws[2 * slot], s->ws_blocked, s->stream)))
-    return rc;
-  if (!s->spectral.items.empty() &&
-      (rc = smx_spectral_eval_batch(s->spectral.plans.data(), int(s->spectral.plans.size()),
-                                    s->spectral.items.data(), int(s->spectral.items.size()), s->ws[2 * slot + 1],
-                                    s->ws_spectral, s->stream)))
-    return rc;
-  if (cudaEventRecord(s->events[slot], s->stream) != cudaSuccess)
-    return smx::set_error(SMX_ERR_CUDA, "smx_serve_flush: event record failed");
-  s->slot_busy[slot] = 1;
-  s->flights.push_back(Flight{slot, s->next_ticket, s->events[slot]});
+  if (!s->blocked.items.empty())
+    rc = smx_blocked_eval_batch(s->blocked.plans.data(), int(s->blocked.plans.size()), s->blocked.items.data(),
+                                int(s->blocked.items.size()), s->ws[2 * slot], s->ws_blocked, s->stream);
+  if (!rc && !s->spectral.items.empty())
+    rc = smx_spectral_eval_batch(s->spectral.plans.data(), int(s->spectral.plans.size()), s->spectral.items.data(),
+                                 int(s->spectral.items.size()), s->ws[2 * slot + 1], s->ws_spectral, s->stream);
+  if (!rc && cudaEventRecord(s->events[slot], s->stream) != cudaSuccess)
+    rc = smx::set_error(SMX_ERR_CUDA, "smx_serve_flush: event record failed");
+  if (rc) {
+    // the whole flush fails: its tickets report rc, and the queue is free for new requests
+    s->failed.push_back(Failed{s->flushed_end, s->next_ticket, rc});
+  } else {
+    s->slot_busy[slot] = 1;
+    s->flights.push_back(Flight{slot, s->next_ticket, s->events[slot]});
+  }
   s->flushed_end = s->next_ticket;
   s->blocked.clear();
   s->spectral.clear();
-  return SMX_OK;
+  return rc;
 }
 
 extern "C" int64_t smx_serve_submit(smx_server* s, int kind, const void* plan_host, const double* x, int64_t P,
@@ -186,6 +194,8 @@ extern "C" int64_t smx_serve_submit(smx_server* s, int kind, const void* plan_ho
 
 extern "C" int smx_serve_poll(smx_server* s, int64_t ticket) {
   SMX_REQUIRE(s && ticket >= 0 && ticket < s->next_ticket, "smx_serve_poll: unknown ticket");
+  for (const Failed& f : s->failed)
+    if (ticket >= f.begin && ticket < f.end) return f.rc;
   if (ticket < s->retired_end) return 1;
   if (ticket >= s->flushed_end) return 0;  // queued, not launched yet
   const int rc = retire(s);

@@ -6,7 +6,8 @@ queue fills), polled to completion, and each output is compared BIT-EXACTLY
 with the package's FP32 evaluation of the same request alone (every tile of a
 merged launch is evaluated as alone).  Also: tickets in submission order, poll
 of a queued ticket returns 0 until its flush, argument errors are reported as
-SMX_ERR_ARG without touching the queue.
+SMX_ERR_ARG without touching the queue, and a flush refused on the host fails
+its own tickets only.
 """
 import ctypes as C
 import time
@@ -136,5 +137,35 @@ def test_argument_errors(plans):
         assert lib.smx_serve_flush(srv) == 0
         _wait(lib, srv, 0)
         torch.testing.assert_close(y, _alone(kind, plan, x, 1), rtol=0, atol=0)
+    finally:
+        lib.smx_serve_destroy(srv)
+
+
+def test_refused_flush_fails_its_tickets(plans):
+    """A flush whose launch is refused on the host (a per-point plan whose row
+    does not fit in shared memory: no launch happens) returns the error, its
+    tickets poll as that error, and the queue then serves new requests."""
+    from smolyax_gb300 import _capi as capi
+
+    lib = capi.load()
+    ip, kind, plan = next(p for p in plans if p[1] == capi.SMX_SERVE_SPECTRAL)
+    bad = type(plan).from_buffer_copy(plan)
+    bad.row = 4096  # (4096 + 32) * 128 * 4 bytes of shared memory: refused by the launcher
+    srv = C.c_void_p()
+    assert lib.smx_serve_create(8, 4, 2, None, C.byref(srv)) == 0
+    try:
+        x = torch.as_tensor(np.random.default_rng(3).uniform(-1, 1, (5, ip.d_in)), device="cuda")
+        y = torch.zeros(5, ip.d_out, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        args = (C.c_void_p(x.data_ptr()), 5, ip.d_in, C.c_void_p(y.data_ptr()))
+        assert lib.smx_serve_submit(srv, kind, C.byref(bad), *args) == 0
+        rc = lib.smx_serve_flush(srv)
+        assert rc < 0
+        assert lib.smx_serve_poll(srv, 0) == rc
+        assert lib.smx_serve_submit(srv, kind, C.byref(plan), *args) == 1
+        assert lib.smx_serve_flush(srv) == 0
+        _wait(lib, srv, 1)
+        assert lib.smx_serve_poll(srv, 0) == rc
+        torch.testing.assert_close(y, _alone(kind, plan, x, ip.d_out), rtol=0, atol=0)
     finally:
         lib.smx_serve_destroy(srv)
