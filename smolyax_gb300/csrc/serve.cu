@@ -113,7 +113,7 @@ extern "C" int smx_serve_create(int max_items, int max_plans, int max_inflight, 
 
 extern "C" void smx_serve_destroy(smx_server* s) {
   if (!s) return;
-  if (!s->flights.empty()) cudaStreamSynchronize(s->stream);
+  cudaStreamSynchronize(s->stream);  // launches in flight, including those of a flush that failed part-way
   for (void* p : s->ws)
     if (p) cudaFree(p);
   for (cudaEvent_t e : s->events)
